@@ -1,0 +1,447 @@
+"""Benchmark: GB300 edge assembly (+ Poisson solve) of the nalu-wind hot path.
+
+Contract (one JSON line from rank 0):
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+A step assembles the 128 x 128 x 64 stretched, jittered box (1,081,665
+nodes, 3,211,584 edges): the 3-dof momentum system (MomentumEdgeSolverAlg,
+67,543,497 nnz) and the continuity / pressure-Poisson system
+(ContinuityEdgeSolverAlg, 7,504,833 nnz), each zeroed then assembled through
+the C ABI. value = nnz assembled per second (Gnnz/s). Inputs are resident
+in HBM for `value`; `e2e` copies every input field from pinned host memory
+and reads both rhs vectors back inside the timed region.
+
+--poisson adds the pressure-Poisson solve on the 256 x 256 x 128 box
+(8,520,321 rows): ms to 1e-8 FP64 relative residual for plain FP64
+GMRES(50) + Jacobi and for the mixed-precision method.
+
+Multi-GPU (torchrun, N > 1): every rank runs an independent replica of the
+same workload (weak scaling); the timed region is bracketed by barriers and
+the max over ranks is reported. --impl reference times the CPU oracle (the
+restated reference path, OpenMP on all host cores) on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "nalu-wind_gb300"
+MOMENTUM_NNZ = 67_543_497
+CONTINUITY_NNZ = 7_504_833
+
+
+def _package():
+    if "nalu_wind_gb300" in sys.modules:
+        return sys.modules["nalu_wind_gb300"]
+    spec = importlib.util.spec_from_file_location(
+        "nalu_wind_gb300", PKG / "__init__.py", submodule_search_locations=[str(PKG)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["nalu_wind_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def algorithmic_bytes(kind: str, N: int, E: int, nnz: int) -> int:
+    """Compulsory bytes of one assembly: inputs read once, outputs written
+    once, 32-bit edge node ids; nnz is the 1-dof nnz (N + 2E)."""
+    if kind == "continuity":
+        return 32 * E + 96 * N + 8 * nnz + 8 * N
+    if kind == "momentum":
+        return 48 * E + 144 * N + 8 * 9 * nnz + 24 * N
+    if kind == "scalar":
+        return 40 * E + 96 * N + 8 * nnz + 8 * N
+    raise ValueError(kind)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def stop(self) -> dict:
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=6)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+def traffic_table() -> dict:
+    p = ROOT / "profiles" / "traffic.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def dist_setup(n_gpus: int):
+    rank, world = 0, 1
+    if n_gpus > 1 or "RANK" in os.environ:
+        import torch.distributed as dist
+        rank = int(os.environ.get("RANK", 0))
+        world = int(os.environ.get("WORLD_SIZE", 1))
+        if world > 1:
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            backend = "nccl"
+            try:
+                import torch
+                if not torch.cuda.is_available():
+                    backend = "gloo"
+            except Exception:
+                backend = "gloo"
+            dist.init_process_group(backend=backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------
+def build_inputs(nw, shape):
+    return nw.workload.lowmach_case(*shape, seed=2)
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    nw = _package()
+    nw.load()
+    nw.check(nw.load().nw_set_device(local))
+    case = build_inputs(nw, args.shape)
+    mesh = case.mesh
+    N, E = mesh.num_nodes, mesh.num_edges
+    stream = torch.cuda.current_stream()
+    nd = case.node
+    host = dict(coords=mesh.coords, velocity=nd["velocity"], dudx=nd["dudx"], viscosity=nd["viscosity"],
+                density=nd["density"], mask=nd["mask"], pressure=nd["pressure"], dpdx=nd["dpdx"],
+                udiag=nd["udiag"], area=mesh.area, mdot=case.edge["mdot"], pecfac=case.edge["pecfac"])
+    dev = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in host.items()}
+    pinned = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in host.items()}
+    lsm = nw.LinearSystem(3, stream=stream.cuda_stream)
+    lsm.build_edge_graph(N, mesh.edges)
+    lsm.finalize()
+    lsc = nw.LinearSystem(1, stream=stream.cuda_stream)
+    lsc.build_edge_graph(N, mesh.edges)
+    lsc.finalize()
+    nnz_m = lsm.sizes()[1]
+    nnz_c = lsc.sizes()[1]
+    nnz1 = nnz_c
+    mo, co = case.opts["momentum"], case.opts["continuity"]
+
+    def fields(d):
+        fm = nw.MomentumFields(*(d[k].data_ptr() for k in (
+            "coords", "velocity", "dudx", "viscosity", "density", "mask", "area", "mdot", "pecfac")))
+        fc = nw.ContinuityFields(*(d[k].data_ptr() for k in (
+            "coords", "velocity", "dpdx", "density", "pressure", "udiag", "area")))
+        return fm, fc
+
+    fm, fc = fields(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    mom_ms, con_ms = [], []
+
+    def step(timed_kernels=False):
+        if timed_kernels:
+            ev[0].record(stream)
+        lsm.zero_system()
+        lsm.assemble_momentum(fm, mo)
+        if timed_kernels:
+            ev[1].record(stream)
+        lsc.zero_system()
+        lsc.assemble_continuity(fc, co)
+        if timed_kernels:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    ms_total = t0.elapsed_time(t1)
+    # per-assembly kernel durations (separate pass, same stream)
+    for _ in range(args.steps):
+        step(timed_kernels=True)
+        torch.cuda.synchronize()
+        mom_ms.append(ev[0].elapsed_time(ev[1]))
+        con_ms.append(ev[1].elapsed_time(ev[2]))
+    # e2e: host inputs -> device -> assemble -> rhs back to host
+    rhs_m_host = torch.empty(3 * (lsm.sizes()[0] // 3), dtype=torch.float64).pin_memory()
+    rhs_c_host = torch.empty(lsc.sizes()[0], dtype=torch.float64).pin_memory()
+    _, rm_dev, _, _ = lsm.device_arrays()
+    _, rc_dev, _, _ = lsc.device_arrays()
+    h2d = sum(int(t.numel() * t.element_size()) for t in pinned.values())
+    d2h = int(rhs_m_host.numel() * 8 + rhs_c_host.numel() * 8)
+    import ctypes
+
+    def e2e_step():
+        for k, t in pinned.items():
+            dev[k].copy_(t, non_blocking=True)
+        step()
+        cudart_copy(rhs_m_host.data_ptr(), rm_dev, rhs_m_host.numel() * 8, stream.cuda_stream)
+        cudart_copy(rhs_c_host.data_ptr(), rc_dev, rhs_c_host.numel() * 8, stream.cuda_stream)
+
+    libcudart = _cudart()
+
+    def cudart_copy(dst, src, nbytes, s):
+        r = libcudart.cudaMemcpyAsync(ctypes.c_void_p(dst), ctypes.c_void_p(src), ctypes.c_size_t(nbytes),
+                                      ctypes.c_int(2), ctypes.c_void_p(s))
+        if r != 0:
+            raise RuntimeError(f"cudaMemcpyAsync failed {r}")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms_e2e = t0.elapsed_time(t1)
+    ms_total = max_over_ranks(ms_total, world)
+    ms_e2e = max_over_ranks(ms_e2e, world)
+    nnz_step = nnz_m + nnz_c
+    value = world * nnz_step * args.steps / (ms_total * 1e-3) / 1e9
+    e2e = world * nnz_step * args.steps / (ms_e2e * 1e-3) / 1e9
+    pk = peaks()
+    B_m = algorithmic_bytes("momentum", N, E, nnz1)
+    B_c = algorithmic_bytes("continuity", N, E, nnz1)
+    mom_avg = float(np.mean(mom_ms))
+    con_avg = float(np.mean(con_ms))
+    achieved = B_m / (mom_avg * 1e-3) / 1e9
+    tt = traffic_table().get("momentum_128x128x64")
+    out = {
+        "metric": "edge-assembly Gnnz/s", "value": round(value, 4), "unit": "Gnnz/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_total / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 128x128x64 stretched, jittered hex box; log-law velocity + noise)",
+        "config": {"workload": "lowmach 128x128x64: momentum (3-dof) + continuity edge assembly",
+                   "nodes": N, "edges": E, "nnz_momentum": nnz_m, "nnz_continuity": nnz_c,
+                   "l2": "inputs and outputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e, 4), "unit": "Gnnz/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"kernel": "momentum assembly (edge + row kernels)", "bound": "hbm",
+                     "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / pk["hbm_gbs"], 4), "peak_src": pk["src"],
+                     "algorithmic_bytes": B_m, "avg_ms": round(mom_avg, 4),
+                     "traffic": (tt["bytes_per_launch"] if tt else None)},
+        "continuity": {"avg_ms": round(con_avg, 4), "algorithmic_bytes": B_c,
+                       "achieved_gbs": round(B_c / (con_avg * 1e-3) / 1e9, 1),
+                       "gnnz_s": round(nnz_c / (con_avg * 1e-3) / 1e9, 4)},
+        "momentum": {"avg_ms": round(mom_avg, 4), "gnnz_s": round(nnz_m / (mom_avg * 1e-3) / 1e9, 4)},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clocks,
+    }
+    if args.poisson:
+        out["poisson"] = poisson_solves(nw, stream, args)
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(case, args)
+    return out
+
+
+def _cudart():
+    import ctypes
+    import torch
+    for name in ("libcudart.so", "libcudart.so.13", "libcudart.so.12"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    lib_dir = Path(torch.__file__).parent / "lib"
+    for p in sorted(lib_dir.glob("libcudart*.so*")):
+        return ctypes.CDLL(str(p))
+    import glob
+    for p in glob.glob(str(Path(sys.prefix) / "lib/python3*/site-packages/nvidia/cuda_runtime/lib/libcudart.so*")):
+        return ctypes.CDLL(p)
+    raise RuntimeError("libcudart not found")
+
+
+def poisson_solves(nw, stream, args) -> dict:
+    import torch
+    case = nw.workload.poisson_case(*args.poisson_shape, seed=3)
+    mesh = case.mesh
+    nd = case.node
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in dict(
+        coords=mesh.coords, velocity=nd["velocity"], dpdx=nd["dpdx"], density=nd["density"],
+        pressure=nd["pressure"], udiag=nd["udiag"], area=mesh.area).items()}
+    ls = nw.LinearSystem(1, stream=stream.cuda_stream)
+    ls.build_edge_graph(mesh.num_nodes, mesh.edges)
+    ls.finalize()
+    ls.zero_system()
+    ls.assemble_continuity(nw.ContinuityFields(*(d[k].data_ptr() for k in (
+        "coords", "velocity", "dpdx", "density", "pressure", "udiag", "area"))), case.opts["continuity"])
+    ls.from_host(rhs=case.extra["rhs"])
+    nr, nnz = ls.sizes()
+    res = {"workload": f"poisson {args.poisson_shape}", "rows": nr, "nnz": nnz, "tol": 1e-8}
+    for name, cfg in [
+        ("plain_fp64_gmres50_jacobi", nw.solver_cfg(kspace=50, max_iterations=20000, tolerance=1e-8)),
+        ("mixed_fp32_inner_jacobi", nw.solver_cfg(kspace=30, max_iterations=20000, tolerance=1e-8,
+                                                  precision=nw.PREC_MIXED, inner_kspace=30,
+                                                  inner_tolerance=1e-3)),
+    ]:
+        ls.set_solver_cfg(cfg)
+        x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+        t = time.perf_counter()
+        rep = ls.solve(x)
+        wall = (time.perf_counter() - t) * 1e3
+        res[name] = {"ms": round(rep.solve_ms, 2), "wall_ms": round(wall, 2), "iterations": rep.iterations,
+                     "outer": rep.outer_iterations, "rel_residual_fp64": rep.final_abs_residual / rep.rhs_norm,
+                     "converged": bool(rep.converged)}
+    return res
+
+
+def cpu_baseline(case, args, steps=1) -> dict:
+    """Oracle (restated reference path) on the host cores: per-edge kernels
+    plus the atomic sum_into, OpenMP on all cores, FP64."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import build as ob
+    ob.build()
+    from oracle import oracle as orc
+    mesh = case.mesh
+    nd = case.node
+    threads = os.cpu_count() or 1
+    rp1, ci1, lid1 = orc.build_graph(mesh.nalu_id, mesh.edges, 1)
+    rp3, ci3, lid3 = orc.build_graph(mesh.nalu_id, mesh.edges, 3)
+    mo, co = case.opts["momentum"], case.opts["continuity"]
+    omo = orc.MomentumOpts(*(getattr(mo, k) for k, _ in mo._fields_))
+    oco = orc.ContinuityOpts(*(getattr(co, k) for k, _ in co._fields_))
+    times = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        lhs, rhs = orc.momentum_local(mesh.edges, mesh.coords, nd["velocity"], nd["velocity"], nd["dudx"],
+                                      nd["viscosity"], nd["density"], nd["mask"], mesh.area, case.edge["mdot"],
+                                      case.edge["pecfac"], omo)
+        orc.sum_into(mesh.edges, 3, lhs, rhs, lid3, rp3, ci3, nthreads=threads, with_abs=False)
+        lhs, rhs = orc.continuity_local(mesh.edges, mesh.coords, nd["velocity"], nd["dpdx"], nd["density"],
+                                        nd["pressure"], nd["udiag"], mesh.area, oco)
+        orc.sum_into(mesh.edges, 1, lhs, rhs, lid1, rp1, ci1, nthreads=threads, with_abs=False)
+        times.append(time.perf_counter() - t)
+    nnz = int(ci3.shape[0] + ci1.shape[0])
+    sec = float(np.mean(times))
+    return {"value": round(nnz / sec / 1e9, 5), "unit": "Gnnz/s", "cores": threads, "kind": "port",
+            "sample": f"one full momentum + continuity assembly of the same workload ({nnz} nnz), "
+                      f"{steps} run(s), {sec:.2f} s each"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    nw = _package()
+    case = build_inputs(nw, args.shape)
+    # warm-up runs are discarded; each timed step is one full assembly
+    for _ in range(min(args.warmup, 1)):
+        cpu_baseline(case, args, steps=1)
+    cb = cpu_baseline(case, args, steps=max(1, min(args.steps, 3)))
+    return {"metric": "edge-assembly Gnnz/s", "value": cb["value"], "unit": "Gnnz/s", "n_gpus": world,
+            "steps": max(1, min(args.steps, 3)), "warmup": min(args.warmup, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic (same seeded workload)",
+            "config": {"workload": "lowmach 128x128x64: momentum (3-dof) + continuity edge assembly",
+                       "note": "CPU oracle restating the reference path; the reference build needs "
+                               "Trilinos/STK/Kokkos/MPI, absent here"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "Gnnz/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shape", type=int, nargs=3, default=[128, 128, 64])
+    ap.add_argument("--poisson", action="store_true")
+    ap.add_argument("--poisson-shape", type=int, nargs=3, default=[256, 256, 128])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.shape = tuple(args.shape)
+    args.poisson_shape = tuple(args.poisson_shape)
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    rank, world = dist_setup(args.gpus)
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        sys.path.insert(0, str(ROOT))
+        import __graft_entry__ as ge
+        ge.build()
+        out = run_ours(args, rank, world)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

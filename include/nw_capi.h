@@ -1,0 +1,266 @@
+/*
+ * nw_capi.h - C ABI of the GB300 edge-assembly + Krylov library
+ * (libnw_gb300.so).
+ *
+ * This is the drop-in boundary for nalu-wind's implicit hot path. Each entry
+ * point names the reference interface it replaces (paths are relative to
+ * the nalu-wind source tree). Plain pointers and sizes only; no C++ or torch
+ * types cross this boundary and no exception escapes it.
+ *
+ * Conventions
+ *  - Every function returns nw_status. On error, nw_last_error_string()
+ *    describes the failure (thread-local).
+ *  - A handle is used from one host thread. Device work is stream-ordered on
+ *    the handle's CUDA stream (nw_linsys_set_stream); pointers marked
+ *    "device" must be valid device memory for the duration of the call.
+ *  - Node indices are 0-based indices into the caller's node arrays. Node
+ *    ids (nalu_id) are the 1-based global ids that order the matrix rows.
+ *  - Node fields are interleaved per node (N x ncomp), as STK stores them.
+ */
+#ifndef NW_CAPI_H
+#define NW_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum nw_status {
+  NW_OK = 0,
+  NW_INVALID_ARG = 1,
+  NW_CUDA_ERROR = 2,
+  NW_NOT_FINALIZED = 3,
+  NW_NAN_DETECTED = 4,
+  NW_NOT_CONVERGED = 5,
+  NW_BREAKDOWN = 6,
+  NW_TIMEOUT = 7,
+  NW_NO_DEVICE = 8,
+  NW_INTERNAL = 9
+} nw_status;
+
+/* Krylov methods (the `method` strings passed to the Belos factory,
+ * src/LinearSolver.C:114) and preconditioners (src/LinearSolverConfig.C:
+ * 89-121). */
+enum { NW_GMRES = 0, NW_CG = 1, NW_FGMRES = 2 };
+enum {
+  NW_PC_NONE = 0,
+  NW_PC_JACOBI = 1, /* "jacobi" / "default": Ifpack2 Jacobi, 1 sweep */
+  NW_PC_SGS = 2,    /* "sgs": symmetric Gauss-Seidel, 1 sweep, multicolour order */
+  NW_PC_LEARNED = 3 /* learned edge message-passing preconditioner (FGMRES) */
+};
+/* Arithmetic of the solve. */
+enum {
+  NW_PREC_FP64 = 0,  /* FP64 Krylov, FP64 SpMV and preconditioner */
+  NW_PREC_MIXED = 1  /* FP32 inner Krylov inside FP64 iterative refinement */
+};
+
+/* TpetraLinearSolverConfig::load keys (src/LinearSolverConfig.C:37-140). */
+typedef struct nw_solver_cfg {
+  int method;             /* NW_GMRES, NW_CG, NW_FGMRES */
+  int preconditioner;     /* NW_PC_* */
+  int precision;          /* NW_PREC_* */
+  int kspace;             /* "kspace", default 50 */
+  int max_iterations;     /* "max_iterations", default 50 */
+  double tolerance;       /* "tolerance", default 1e-4 */
+  double final_tolerance; /* "final_tolerance", default = tolerance */
+  int inner_kspace;       /* mixed: inner restart length */
+  double inner_tolerance; /* mixed: relative reduction per inner solve */
+} nw_solver_cfg;
+
+/* Per-solve report: LinearSystem::linearSolveIterations / linearResidual /
+ * nonLinearResidual (include/LinearSystem.h:212-218). */
+typedef struct nw_solve_report {
+  int iterations;             /* total Krylov iterations */
+  int outer_iterations;       /* iterative-refinement steps (mixed) */
+  int status;                 /* nw_status of the solve */
+  int converged;
+  double final_rel_residual;  /* last tested relative residual */
+  double final_abs_residual;  /* explicit ||b - A x||_2 in FP64 */
+  double rhs_norm;            /* ||b||_2 (nonLinearResidual / l2Scaling) */
+  double solve_ms;            /* device time of the solve */
+} nw_solve_report;
+
+/* SolutionOptions numerics of ScalarEdgeSolverAlg::execute
+ * (src/edge_kernels/ScalarEdgeSolverAlg.C:61-69) and the Peclet function
+ * factory (include/EquationSystem.h:399-413). */
+typedef struct nw_scalar_opts {
+  double alpha, alpha_upw, upw_factor, relax, hybrid_factor;
+  int use_limiter;
+  int tanh_form; /* 0 classic Peclet function, 1 tanh */
+  double tanh_trans, tanh_width;
+} nw_scalar_opts;
+
+/* MomentumEdgeSolverAlg::execute options
+ * (src/edge_kernels/MomentumEdgeSolverAlg.C:76-88); VOF off. */
+typedef struct nw_momentum_opts {
+  double alpha, alpha_upw, upw_factor, relax, include_div_u;
+  int use_limiter;
+} nw_momentum_opts;
+
+/* ContinuityEdgeSolverAlg::execute options
+ * (src/edge_kernels/ContinuityEdgeSolverAlg.C:42-56); tau_scale = dt/gamma1. */
+typedef struct nw_continuity_opts {
+  double noc_fac, tau_scale, interp_together, solve_incompressible;
+} nw_continuity_opts;
+
+/* Device field pointers. Node fields are indexed by node index, edge fields
+ * by edge index in the order given to nw_linsys_build_edge_graph. */
+typedef struct nw_scalar_fields {
+  const double* coords;       /* N x 3 */
+  const double* velocity_rtm; /* N x 3 */
+  const double* q;            /* N */
+  const double* dqdx;         /* N x 3 */
+  const double* density;      /* N */
+  const double* diff_coeff;   /* N (diffFluxCoeff) */
+  const double* area;         /* E x 3 (edge_area_vector) */
+  const double* mdot;         /* E (mass_flow_rate) */
+} nw_scalar_fields;
+
+typedef struct nw_continuity_fields {
+  const double* coords;   /* N x 3 */
+  const double* velocity; /* N x 3 */
+  const double* dpdx;     /* N x 3 */
+  const double* density;  /* N */
+  const double* pressure; /* N */
+  const double* udiag;    /* N (momentum_diag) */
+  const double* area;     /* E x 3 */
+} nw_continuity_fields;
+
+typedef struct nw_momentum_fields {
+  const double* coords;    /* N x 3 */
+  const double* velocity;  /* N x 3 */
+  const double* dudx;      /* N x 9 */
+  const double* viscosity; /* N */
+  const double* density;   /* N */
+  const double* mask;      /* N (abl_wall_no_slip_wall_func_node_mask) */
+  const double* area;      /* E x 3 */
+  const double* mdot;      /* E */
+  const double* pecfac;    /* E (peclet_factor) */
+} nw_momentum_fields;
+
+typedef struct nw_linsys nw_linsys;
+
+/* ---- library ---- */
+const char* nw_last_error_string(void);
+int nw_version(void);
+/* Select the CUDA device used by handles created afterwards. */
+nw_status nw_set_device(int device);
+
+/* ---- construction: LinearSystem::create (src/LinearSystem.C:117-159) and
+ * the TpetraLinearSystem constructor; num_dof = LinearSystem::numDof. ---- */
+nw_status nw_linsys_create(int num_dof, const nw_solver_cfg* cfg,
+                           nw_linsys** out);
+nw_status nw_linsys_destroy(nw_linsys* ls);
+/* Stream for all device work of this handle (cudaStream_t; NULL = the
+ * legacy default stream). */
+nw_status nw_linsys_set_stream(nw_linsys* ls, void* stream);
+nw_status nw_linsys_set_solver_cfg(nw_linsys* ls, const nw_solver_cfg* cfg);
+
+/* ---- graph: LinearSystem::buildEdgeToNodeGraph
+ * (include/LinearSystem.h:114-117; src/TpetraLinearSystem.C:489-494) over a
+ * host edge list, then finalizeLinearSystem (src/TpetraLinearSystem.C:
+ * 1137-1272). Host arrays: global_id (N) is the STK identifier of each node
+ * (NULL: index + 1); nalu_id (N) is the naluGlobalId field, the id of each
+ * node's periodic master (NULL: no periodic slaves). Rows are the master
+ * nodes in ascending id, num_dof rows each. edge_nodes is E x 2 node
+ * indices. ---- */
+nw_status nw_linsys_build_edge_graph(nw_linsys* ls, int64_t num_nodes,
+                                     const int64_t* global_id,
+                                     const int64_t* nalu_id,
+                                     int64_t num_edges,
+                                     const int64_t* edge_nodes);
+nw_status nw_linsys_finalize(nw_linsys* ls);
+/* Graph export for parity checks (host arrays; pass NULL to query sizes). */
+nw_status nw_linsys_graph_sizes(const nw_linsys* ls, int64_t* nrows,
+                                int64_t* nnz);
+nw_status nw_linsys_get_graph(const nw_linsys* ls, int64_t* row_ptr,
+                              int32_t* col_idx);
+/* Row LID (first dof row) of every node: entityToLID. Host, N entries. */
+nw_status nw_linsys_get_node_lid(const nw_linsys* ls, int64_t* node_lid);
+
+/* ---- assembly: zeroSystem (src/TpetraLinearSystem.C:1274-1291) ---- */
+nw_status nw_linsys_zero(nw_linsys* ls);
+
+/* AssembleEdgeSolverAlgorithm::run_algorithm
+ * (include/AssembleEdgeSolverAlgorithm.h:47-100) with the per-edge physics
+ * of ScalarEdgeSolverAlg::execute (src/edge_kernels/
+ * ScalarEdgeSolverAlg.C:55-206) and the CoeffApplier sum into CSR
+ * (TpetraLinearSystem::sum_into, src/TpetraLinearSystem.C:1381-1459).
+ * Deterministic: no floating-point atomics. num_dof must be 1. */
+nw_status nw_assemble_scalar_edges(nw_linsys* ls, const nw_scalar_fields* f,
+                                   const nw_scalar_opts* o);
+/* ContinuityEdgeSolverAlg::execute (src/edge_kernels/
+ * ContinuityEdgeSolverAlg.C:37-195) + sum_into. num_dof must be 1. */
+nw_status nw_assemble_continuity_edges(nw_linsys* ls,
+                                       const nw_continuity_fields* f,
+                                       const nw_continuity_opts* o);
+/* MomentumEdgeSolverAlg::execute (src/edge_kernels/
+ * MomentumEdgeSolverAlg.C:70-313) + sum_into_row_vec_3
+ * (src/TpetraLinearSystem.C:1293-1335). num_dof must be 3. */
+nw_status nw_assemble_momentum_edges(nw_linsys* ls,
+                                     const nw_momentum_fields* f,
+                                     const nw_momentum_opts* o);
+
+/* LinearSystem::sumInto, host-vector overload (include/LinearSystem.h:
+ * 167-173): one entity block. nodes (host, n_ent) are node indices; rhs
+ * (host, n_ent*num_dof) and lhs (host, row-major square of that size). */
+nw_status nw_linsys_sum_into(nw_linsys* ls, int n_ent, const int64_t* nodes,
+                             const double* rhs, const double* lhs);
+
+/* applyDirichletBCs (src/TpetraLinearSystem.C:1686-1757): for each node in
+ * nodes (device, n), dof rows [begin, end) become identity rows and the rhs
+ * becomes bc - q. q and bc are device node fields (N x num_dof). */
+nw_status nw_linsys_apply_dirichlet(nw_linsys* ls, int64_t n,
+                                    const int64_t* nodes, int begin, int end,
+                                    const double* q, const double* bc);
+/* resetRows (src/TpetraLinearSystem.C:1759-1786). nodes: device. */
+nw_status nw_linsys_reset_rows(nw_linsys* ls, int64_t n, const int64_t* nodes,
+                               int begin, int end, double diag_value,
+                               double rhs_residual);
+/* loadComplete (src/TpetraLinearSystem.C:1788-1809): on one GPU there are
+ * no shared-not-owned rows; this only orders the stream. */
+nw_status nw_linsys_load_complete(nw_linsys* ls);
+
+/* Device views of the assembled system (owned by the handle). */
+nw_status nw_linsys_device_arrays(nw_linsys* ls, double** values,
+                                  double** rhs, const int64_t** row_ptr,
+                                  const int32_t** col_idx);
+/* Copy values (nnz) and rhs (nrows) to host arrays (either may be NULL). */
+nw_status nw_linsys_copy_to_host(nw_linsys* ls, double* values, double* rhs);
+/* Overwrite values / rhs from host arrays (either may be NULL). */
+nw_status nw_linsys_copy_from_host(nw_linsys* ls, const double* values,
+                                   const double* rhs);
+
+/* ---- solve: LinearSystem::solve (src/TpetraLinearSystem.C:1811-1881) ->
+ * TpetraLinearSolver::solve (src/LinearSolver.C:209-254). x (device, nrows)
+ * receives the solution from x0 = 0; final_iter selects final_tolerance. */
+nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
+                          nw_solve_report* rep);
+/* Residual history of the last solve (relative, first entry 1). */
+nw_status nw_linsys_residual_history(const nw_linsys* ls, double* hist,
+                                     int capacity, int* count);
+/* copy_tpetra_to_stk (src/TpetraLinearSystem.C:2183-2227): scatter a row
+ * vector (device, nrows) to a node field (device, N x num_dof); periodic
+ * slaves receive their master's value. */
+nw_status nw_linsys_rows_to_nodes(nw_linsys* ls, const double* x_rows,
+                                  double* x_nodes);
+
+/* ---- plain kernels on the assembled system (device vectors) ---- */
+nw_status nw_linsys_spmv(nw_linsys* ls, const double* x, double* y);
+nw_status nw_linsys_precond_apply(nw_linsys* ls, int preconditioner,
+                                  const double* x, double* y);
+/* Row order used by the multicolour SGS (host, nrows): rows of colour 0 in
+ * ascending order, then colour 1, ... */
+nw_status nw_linsys_sgs_order(nw_linsys* ls, int64_t* order, int* ncolors);
+
+/* ---- timing helpers (CUDA events on the handle's stream) ---- */
+nw_status nw_linsys_sync(nw_linsys* ls);
+/* Milliseconds of the last assembly call (edge + row phases). */
+nw_status nw_linsys_last_assembly_ms(const nw_linsys* ls, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NW_CAPI_H */

@@ -1,0 +1,357 @@
+"""Python bindings (ctypes) for libnw_gb300.so.
+
+The library is the product: a C ABI (include/nw_capi.h, include/nw_workload.h)
+over hand-written sm_103a kernels. This module only loads it and mirrors the
+reference's LinearSystem / LinearSolver surface (include/LinearSystem.h,
+src/LinearSolver.C) for tests and benchmarks. Device buffers are passed as
+integer device pointers (e.g. torch.Tensor.data_ptr()). There is no CPU
+fallback: every call fails loudly when the library or a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "libnw_gb300.so"
+
+# status codes (nw_status)
+NW_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "CUDA_ERROR", 3: "NOT_FINALIZED", 4: "NAN_DETECTED",
+                5: "NOT_CONVERGED", 6: "BREAKDOWN", 7: "TIMEOUT", 8: "NO_DEVICE", 9: "INTERNAL"}
+GMRES, CG, FGMRES = 0, 1, 2
+PC_NONE, PC_JACOBI, PC_SGS, PC_LEARNED = 0, 1, 2, 3
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class NwError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class SolverCfg(C.Structure):
+    _fields_ = [("method", C.c_int), ("preconditioner", C.c_int), ("precision", C.c_int),
+                ("kspace", C.c_int), ("max_iterations", C.c_int), ("tolerance", C.c_double),
+                ("final_tolerance", C.c_double), ("inner_kspace", C.c_int),
+                ("inner_tolerance", C.c_double)]
+
+
+class SolveReport(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("outer_iterations", C.c_int), ("status", C.c_int),
+                ("converged", C.c_int), ("final_rel_residual", C.c_double),
+                ("final_abs_residual", C.c_double), ("rhs_norm", C.c_double),
+                ("solve_ms", C.c_double)]
+
+
+class ScalarOpts(C.Structure):
+    _fields_ = [("alpha", C.c_double), ("alpha_upw", C.c_double), ("upw_factor", C.c_double),
+                ("relax", C.c_double), ("hybrid_factor", C.c_double), ("use_limiter", C.c_int),
+                ("tanh_form", C.c_int), ("tanh_trans", C.c_double), ("tanh_width", C.c_double)]
+
+
+class MomentumOpts(C.Structure):
+    _fields_ = [("alpha", C.c_double), ("alpha_upw", C.c_double), ("upw_factor", C.c_double),
+                ("relax", C.c_double), ("include_div_u", C.c_double), ("use_limiter", C.c_int)]
+
+
+class ContinuityOpts(C.Structure):
+    _fields_ = [("noc_fac", C.c_double), ("tau_scale", C.c_double),
+                ("interp_together", C.c_double), ("solve_incompressible", C.c_double)]
+
+
+_P = C.c_void_p
+
+
+class ScalarFields(C.Structure):
+    _fields_ = [(n, _P) for n in ("coords", "velocity_rtm", "q", "dqdx", "density", "diff_coeff",
+                                  "area", "mdot")]
+
+
+class ContinuityFields(C.Structure):
+    _fields_ = [(n, _P) for n in ("coords", "velocity", "dpdx", "density", "pressure", "udiag", "area")]
+
+
+class MomentumFields(C.Structure):
+    _fields_ = [(n, _P) for n in ("coords", "velocity", "dudx", "viscosity", "density", "mask",
+                                  "area", "mdot", "pecfac")]
+
+
+class BoxOpts(C.Structure):
+    _fields_ = [("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+                ("stretch_z", C.c_double), ("jitter", C.c_double), ("seed", C.c_uint64),
+                ("periodic_x", C.c_int), ("periodic_y", C.c_int), ("tets", C.c_int),
+                ("renumber", C.c_int), ("renumber_seed", C.c_uint64)]
+
+
+# every exported symbol with its argument types (checked by the CPU tests)
+_I64P = C.POINTER(C.c_int64)
+_I32P = C.POINTER(C.c_int32)
+_DP = C.POINTER(C.c_double)
+SIGNATURES = {
+    "nw_last_error_string": (C.c_char_p, []),
+    "nw_version": (C.c_int, []),
+    "nw_set_device": (C.c_int, [C.c_int]),
+    "nw_linsys_create": (C.c_int, [C.c_int, C.POINTER(SolverCfg), C.POINTER(C.c_void_p)]),
+    "nw_linsys_destroy": (C.c_int, [C.c_void_p]),
+    "nw_linsys_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "nw_linsys_set_solver_cfg": (C.c_int, [C.c_void_p, C.POINTER(SolverCfg)]),
+    "nw_linsys_build_edge_graph": (C.c_int, [C.c_void_p, C.c_int64, _I64P, _I64P, C.c_int64, _I64P]),
+    "nw_linsys_finalize": (C.c_int, [C.c_void_p]),
+    "nw_linsys_graph_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P]),
+    "nw_linsys_get_graph": (C.c_int, [C.c_void_p, _I64P, _I32P]),
+    "nw_linsys_get_node_lid": (C.c_int, [C.c_void_p, _I64P]),
+    "nw_linsys_zero": (C.c_int, [C.c_void_p]),
+    "nw_assemble_scalar_edges": (C.c_int, [C.c_void_p, C.POINTER(ScalarFields), C.POINTER(ScalarOpts)]),
+    "nw_assemble_continuity_edges": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
+                                               C.POINTER(ContinuityOpts)]),
+    "nw_assemble_momentum_edges": (C.c_int, [C.c_void_p, C.POINTER(MomentumFields), C.POINTER(MomentumOpts)]),
+    "nw_linsys_sum_into": (C.c_int, [C.c_void_p, C.c_int, _I64P, _DP, _DP]),
+    "nw_linsys_apply_dirichlet": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.c_int,
+                                            C.c_void_p, C.c_void_p]),
+    "nw_linsys_reset_rows": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.c_int,
+                                       C.c_double, C.c_double]),
+    "nw_linsys_load_complete": (C.c_int, [C.c_void_p]),
+    "nw_linsys_device_arrays": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                          C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "nw_linsys_copy_to_host": (C.c_int, [C.c_void_p, _DP, _DP]),
+    "nw_linsys_copy_from_host": (C.c_int, [C.c_void_p, _DP, _DP]),
+    "nw_linsys_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(SolveReport)]),
+    "nw_linsys_residual_history": (C.c_int, [C.c_void_p, _DP, C.c_int, C.POINTER(C.c_int)]),
+    "nw_linsys_rows_to_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "nw_linsys_spmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "nw_linsys_precond_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "nw_linsys_sgs_order": (C.c_int, [C.c_void_p, _I64P, C.POINTER(C.c_int)]),
+    "nw_linsys_sync": (C.c_int, [C.c_void_p]),
+    "nw_linsys_last_assembly_ms": (C.c_int, [C.c_void_p, _DP]),
+    "nw_mesh_box": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(BoxOpts), C.POINTER(C.c_void_p)]),
+    "nw_mesh_destroy": (C.c_int, [C.c_void_p]),
+    "nw_mesh_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P, _I64P, C.POINTER(C.c_int)]),
+    "nw_mesh_get": (C.c_int, [C.c_void_p, _DP, _I64P, _I64P, _I64P, _I64P, _DP, _DP, _DP]),
+}
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load libnw_gb300.so (in-tree). Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise NwError(9, f"{p} is not built; run nalu-wind_gb300/build.py")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != NW_OK:
+        msg = load().nw_last_error_string().decode()
+        raise NwError(status, msg)
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def dptr(x) -> int:
+    """Device pointer of a torch tensor (or an int already)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def solver_cfg(method=GMRES, preconditioner=PC_JACOBI, precision=PREC_FP64, kspace=50,
+               max_iterations=50, tolerance=1e-4, final_tolerance=None, inner_kspace=0,
+               inner_tolerance=0.0) -> SolverCfg:
+    """TpetraLinearSolverConfig::load defaults (src/LinearSolverConfig.C:37-52)."""
+    return SolverCfg(method, preconditioner, precision, kspace, max_iterations, tolerance,
+                     tolerance if final_tolerance is None else final_tolerance, inner_kspace,
+                     inner_tolerance)
+
+
+class LinearSystem:
+    """One GPU linear system: graph, assembly, Dirichlet rows and solve."""
+
+    def __init__(self, num_dof: int = 1, cfg: SolverCfg | None = None, stream: int | None = None):
+        self.lib = load()
+        self.num_dof = num_dof
+        h = C.c_void_p()
+        check(self.lib.nw_linsys_create(num_dof, C.byref(cfg) if cfg else None, C.byref(h)))
+        self.h = h
+        if stream is not None:
+            check(self.lib.nw_linsys_set_stream(self.h, C.c_void_p(stream)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nw_linsys_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream: int) -> None:
+        check(self.lib.nw_linsys_set_stream(self.h, C.c_void_p(stream)))
+
+    def set_solver_cfg(self, cfg: SolverCfg) -> None:
+        check(self.lib.nw_linsys_set_solver_cfg(self.h, C.byref(cfg)))
+
+    # -- graph (buildEdgeToNodeGraph + finalizeLinearSystem)
+    def build_edge_graph(self, num_nodes: int, edges: np.ndarray, global_id=None, nalu_id=None) -> None:
+        e = np.ascontiguousarray(edges, dtype=np.int64)
+        g = None if global_id is None else np.ascontiguousarray(global_id, dtype=np.int64)
+        n = None if nalu_id is None else np.ascontiguousarray(nalu_id, dtype=np.int64)
+        check(self.lib.nw_linsys_build_edge_graph(
+            self.h, num_nodes, None if g is None else _ptr(g, C.c_int64),
+            None if n is None else _ptr(n, C.c_int64), e.shape[0], _ptr(e, C.c_int64)))
+
+    def finalize(self) -> None:
+        check(self.lib.nw_linsys_finalize(self.h))
+
+    def sizes(self) -> tuple[int, int]:
+        nr, nz = C.c_int64(), C.c_int64()
+        check(self.lib.nw_linsys_graph_sizes(self.h, C.byref(nr), C.byref(nz)))
+        return nr.value, nz.value
+
+    def graph(self) -> tuple[np.ndarray, np.ndarray]:
+        nr, nz = self.sizes()
+        rp = np.zeros(nr + 1, np.int64)
+        ci = np.zeros(nz, np.int32)
+        check(self.lib.nw_linsys_get_graph(self.h, _ptr(rp, C.c_int64), _ptr(ci, C.c_int32)))
+        return rp, ci
+
+    def node_lid(self, num_nodes: int) -> np.ndarray:
+        out = np.zeros(num_nodes, np.int64)
+        check(self.lib.nw_linsys_get_node_lid(self.h, _ptr(out, C.c_int64)))
+        return out
+
+    # -- assembly
+    def zero_system(self) -> None:
+        check(self.lib.nw_linsys_zero(self.h))
+
+    def assemble_scalar(self, f: ScalarFields, o: ScalarOpts) -> None:
+        check(self.lib.nw_assemble_scalar_edges(self.h, C.byref(f), C.byref(o)))
+
+    def assemble_continuity(self, f: ContinuityFields, o: ContinuityOpts) -> None:
+        check(self.lib.nw_assemble_continuity_edges(self.h, C.byref(f), C.byref(o)))
+
+    def assemble_momentum(self, f: MomentumFields, o: MomentumOpts) -> None:
+        check(self.lib.nw_assemble_momentum_edges(self.h, C.byref(f), C.byref(o)))
+
+    def sum_into(self, nodes, rhs, lhs) -> None:
+        nodes = np.ascontiguousarray(nodes, np.int64)
+        rhs = np.ascontiguousarray(rhs, np.float64)
+        lhs = np.ascontiguousarray(lhs, np.float64)
+        check(self.lib.nw_linsys_sum_into(self.h, len(nodes), _ptr(nodes, C.c_int64),
+                                          _ptr(rhs, C.c_double), _ptr(lhs, C.c_double)))
+
+    def apply_dirichlet(self, n: int, nodes_dev, begin: int, end: int, q_dev, bc_dev) -> None:
+        check(self.lib.nw_linsys_apply_dirichlet(self.h, n, dptr(nodes_dev), begin, end,
+                                                 dptr(q_dev), dptr(bc_dev)))
+
+    def reset_rows(self, n: int, nodes_dev, begin: int, end: int, diag: float, rhs: float) -> None:
+        check(self.lib.nw_linsys_reset_rows(self.h, n, dptr(nodes_dev), begin, end, diag, rhs))
+
+    def load_complete(self) -> None:
+        check(self.lib.nw_linsys_load_complete(self.h))
+
+    def to_host(self) -> tuple[np.ndarray, np.ndarray]:
+        nr, nz = self.sizes()
+        v = np.zeros(nz)
+        r = np.zeros(nr)
+        check(self.lib.nw_linsys_copy_to_host(self.h, _ptr(v, C.c_double), _ptr(r, C.c_double)))
+        return v, r
+
+    def from_host(self, values=None, rhs=None) -> None:
+        v = None if values is None else np.ascontiguousarray(values, np.float64)
+        r = None if rhs is None else np.ascontiguousarray(rhs, np.float64)
+        check(self.lib.nw_linsys_copy_from_host(self.h, None if v is None else _ptr(v, C.c_double),
+                                                None if r is None else _ptr(r, C.c_double)))
+
+    def device_arrays(self):
+        v, r, rp, ci = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(self.lib.nw_linsys_device_arrays(self.h, C.byref(v), C.byref(r), C.byref(rp), C.byref(ci)))
+        return v.value, r.value, rp.value, ci.value
+
+    # -- solve
+    def solve(self, x_dev, final_iter: bool = False) -> SolveReport:
+        rep = SolveReport()
+        check(self.lib.nw_linsys_solve(self.h, dptr(x_dev), int(final_iter), C.byref(rep)))
+        return rep
+
+    def residual_history(self) -> np.ndarray:
+        cnt = C.c_int()
+        check(self.lib.nw_linsys_residual_history(self.h, None, 0, C.byref(cnt)))
+        out = np.zeros(cnt.value)
+        check(self.lib.nw_linsys_residual_history(self.h, _ptr(out, C.c_double), cnt.value, C.byref(cnt)))
+        return out
+
+    def spmv(self, x_dev, y_dev) -> None:
+        check(self.lib.nw_linsys_spmv(self.h, dptr(x_dev), dptr(y_dev)))
+
+    def precond_apply(self, kind: int, x_dev, y_dev) -> None:
+        check(self.lib.nw_linsys_precond_apply(self.h, kind, dptr(x_dev), dptr(y_dev)))
+
+    def sgs_order(self) -> tuple[np.ndarray, int]:
+        nr, _ = self.sizes()
+        order = np.zeros(nr, np.int64)
+        nc = C.c_int()
+        check(self.lib.nw_linsys_sgs_order(self.h, _ptr(order, C.c_int64), C.byref(nc)))
+        return order, nc.value
+
+    def sync(self) -> None:
+        check(self.lib.nw_linsys_sync(self.h))
+
+    def last_assembly_ms(self) -> float:
+        ms = C.c_double()
+        check(self.lib.nw_linsys_last_assembly_ms(self.h, C.byref(ms)))
+        return ms.value
+
+
+class Mesh:
+    """Synthetic block mesh (nw_workload.h): coordinates, ids, edges, geometry."""
+
+    def __init__(self, nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, stretch_z=1.0, jitter=0.0, seed=0,
+                 periodic_x=False, periodic_y=False, tets=False, renumber=0, renumber_seed=0):
+        lib = load()
+        o = BoxOpts(lx, ly, lz, stretch_z, jitter, seed, int(periodic_x), int(periodic_y), int(tets),
+                    renumber, renumber_seed)
+        h = C.c_void_p()
+        check(lib.nw_mesh_box(nx, ny, nz, C.byref(o), C.byref(h)))
+        try:
+            N, E, M, npe = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int()
+            check(lib.nw_mesh_sizes(h, C.byref(N), C.byref(E), C.byref(M), C.byref(npe)))
+            self.num_nodes, self.num_edges, self.num_elems, self.npe = N.value, E.value, M.value, npe.value
+            self.coords = np.zeros((self.num_nodes, 3))
+            self.global_id = np.zeros(self.num_nodes, np.int64)
+            self.nalu_id = np.zeros(self.num_nodes, np.int64)
+            self.edges = np.zeros((self.num_edges, 2), np.int64)
+            self.conn = np.zeros((self.num_elems, self.npe), np.int64)
+            self.area = np.zeros((self.num_edges, 3))
+            self.dualvol = np.zeros(self.num_nodes)
+            self.bnd_area = np.zeros((self.num_nodes, 3))
+            check(lib.nw_mesh_get(h, _ptr(self.coords, C.c_double), _ptr(self.global_id, C.c_int64),
+                                  _ptr(self.nalu_id, C.c_int64), _ptr(self.edges, C.c_int64),
+                                  _ptr(self.conn, C.c_int64), _ptr(self.area, C.c_double),
+                                  _ptr(self.dualvol, C.c_double), _ptr(self.bnd_area, C.c_double)))
+        finally:
+            lib.nw_mesh_destroy(h)
+        self.shape = (nx, ny, nz)
+        self.periodic = (bool(periodic_x), bool(periodic_y))
+
+
+from . import workload  # noqa: E402  (seeded synthetic inputs)

@@ -1,0 +1,46 @@
+// Launch wrappers of the edge-assembly kernels (assemble.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "nw_capi.h"
+
+namespace nw {
+
+using ScalarOpts = nw_scalar_opts;
+using ContinuityOpts = nw_continuity_opts;
+using MomentumOpts = nw_momentum_opts;
+
+// Coefficients written per edge by the edge phase (SoA arrays of E).
+constexpr int kScalarCoefs = 6;
+constexpr int kContinuityCoefs = 2;
+constexpr int kMomentumCoefs = 13;
+
+void launch_scalar_edges(cudaStream_t s, int64_t E, const int2* edges,
+                         const nw_scalar_fields& f, const ScalarOpts& o,
+                         double* buf);
+void launch_continuity_edges(cudaStream_t s, int64_t E, const int2* edges,
+                             const nw_continuity_fields& f,
+                             const ContinuityOpts& o, double* buf);
+void launch_momentum_edges(cudaStream_t s, int64_t E, const int2* edges,
+                           const nw_momentum_fields& f, const MomentumOpts& o,
+                           double* buf);
+// kind 0 scalar, 1 continuity, 2 momentum (3 dof)
+void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
+                 const uint32_t* inc, const int32_t* diag_pos,
+                 const int64_t* row_ptr, const double* buf, int64_t E,
+                 double relax, double* values, double* rhs, int accumulate);
+void launch_reset_rows(cudaStream_t s, int64_t n, const int64_t* nodes,
+                       const int64_t* node_lid, int num_dof, int begin,
+                       int end, const int64_t* row_ptr, const int32_t* col_idx,
+                       double* values, double* rhs, double diag_value,
+                       double rhs_value, const double* q, const double* bc,
+                       int64_t num_nodes, int* err);
+void launch_sum_into_block(cudaStream_t s, int n_ent, int num_dof,
+                           const int64_t* ent_lid, const double* lhs,
+                           const double* rhs_in, const int64_t* row_ptr,
+                           const int32_t* col_idx, double* values,
+                           double* rhs);
+
+}  // namespace nw

@@ -1,0 +1,92 @@
+// Krylov solver on the GPU: SpMV, deterministic reductions, Jacobi and
+// multicolour Gauss-Seidel relaxation, GMRES / FGMRES / CG, and the
+// mixed-precision iterative-refinement driver (krylov.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <functional>
+#include <vector>
+
+#include "nw_internal.h"
+
+namespace nw {
+
+// A CSR matrix resident on the device (FP64 values; optional FP32 copy).
+struct DevCsr {
+  int64_t n = 0;
+  int64_t nnz = 0;
+  const int64_t* row_ptr = nullptr;
+  const int32_t* col_idx = nullptr;
+  const double* values = nullptr;
+  int lanes = 8;  // sub-warp width per row for the SpMV
+};
+
+// Preconditioner applied inside the solver (right preconditioning).
+struct Precond {
+  int kind = NW_PC_JACOBI;
+  // multicolour SGS: rows grouped by colour
+  const int32_t* color_rows = nullptr;   // nrows, rows of colour 0, 1, ...
+  std::vector<int64_t> color_ptr;        // host, ncolors + 1
+  // user-supplied preconditioner (learned): y = M(x), FP64 device vectors
+  std::function<void(const double*, double*, cudaStream_t)> apply_fn;
+};
+
+struct SolveResult {
+  int iterations = 0;
+  int outer = 0;
+  int converged = 0;
+  nw_status status = NW_OK;
+  double final_rel = 0.0;
+  double final_abs = 0.0;
+  double bnorm = 0.0;
+  std::vector<double> history;
+};
+
+class KrylovSolver {
+ public:
+  KrylovSolver() = default;
+  ~KrylovSolver();
+  KrylovSolver(const KrylovSolver&) = delete;
+  KrylovSolver& operator=(const KrylovSolver&) = delete;
+
+  // Bind to a matrix; allocates work space for restart length m.
+  void setup(const DevCsr& A, int m, cudaStream_t s);
+  // Recompute diagonal-dependent data after the values changed.
+  void refresh(cudaStream_t s);
+
+  SolveResult solve(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                    const double* b, double* x, cudaStream_t s);
+
+  // Building blocks (device vectors of length n).
+  void spmv(const double* x, double* y, cudaStream_t s) const;
+  void apply_precond(const Precond& pc, const double* x, double* y,
+                     cudaStream_t s);
+  double dot(const double* a, const double* b, cudaStream_t s);
+
+ private:
+  SolveResult gmres(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                    const double* b, double* x, bool flexible,
+                    cudaStream_t s);
+  SolveResult cg(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                 const double* b, double* x, cudaStream_t s);
+  SolveResult mixed(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                    const double* b, double* x, cudaStream_t s);
+  void ensure_f32(cudaStream_t s);
+
+  DevCsr A_;
+  int m_ = 0;
+  DeviceArray<double> rdiag_;   // 1 / a_ii
+  DeviceArray<double> V_;       // (m+1) x n basis
+  DeviceArray<double> Z_;       // m x n (flexible)
+  DeviceArray<double> w_, z_, r_;
+  DeviceArray<double> partial_; // deterministic reduction partials
+  DeviceArray<double> scal_;    // small device scalars
+  double* h_pinned_ = nullptr;  // host mirror of scal_
+  // FP32 copies for the inner solve of the mixed method
+  DeviceArray<float> vals32_, rdiag32_, V32_, w32_, z32_, r32_;
+  bool f32_valid_ = false;
+  int red_blocks_ = 0;
+};
+
+}  // namespace nw

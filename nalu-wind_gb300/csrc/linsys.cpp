@@ -1,0 +1,641 @@
+// C ABI implementation: the LinearSystem / LinearSolver surface of
+// nalu-wind's Tpetra backend (include/LinearSystem.h:88-256,
+// src/TpetraLinearSystem.C, src/LinearSolver.C) on one GB300.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "assemble.h"
+#include "krylov.h"
+#include "nw_internal.h"
+
+namespace nw {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void fail(nw_status s, const std::string& msg) { throw Error{s, msg}; }
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    fail(NW_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+void set_last_error(const std::string& s) { g_last_error = s; }
+const char* last_error() { return g_last_error.c_str(); }
+
+}  // namespace nw
+
+using namespace nw;
+
+struct nw_linsys {
+  int num_dof = 1;
+  nw_solver_cfg cfg{};
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  bool built = false;
+  bool finalized = false;
+  bool pristine = false;  // zeroSystem issued, no values written since
+  HostGraph g;
+  DeviceArray<int64_t> row_ptr, node_lid;
+  DeviceArray<int32_t> col_idx, inc_ptr, diag_pos, color_rows;
+  DeviceArray<uint32_t> inc;
+  DeviceArray<int2> edges;
+  DeviceArray<double> values, rhs, buf;
+  DeviceArray<int> err;
+  DeviceArray<int64_t> scratch_lid;
+  DeviceArray<double> scratch_vals;
+  KrylovSolver solver;
+  Precond pc;
+  std::vector<int64_t> color_ptr;
+  std::vector<int32_t> color_rows_host;
+  std::vector<double> history;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool timed = false;
+};
+
+namespace {
+
+int g_device = 0;
+
+template <typename F>
+nw_status guard(F&& f) {
+  try {
+    f();
+    return NW_OK;
+  } catch (const Error& e) {
+    set_last_error(e.msg);
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    set_last_error("host allocation failed");
+    return NW_INTERNAL;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return NW_INTERNAL;
+  }
+}
+
+nw_solver_cfg default_cfg() {
+  nw_solver_cfg c{};
+  c.method = NW_GMRES;
+  c.preconditioner = NW_PC_JACOBI;
+  c.precision = NW_PREC_FP64;
+  c.kspace = 50;
+  c.max_iterations = 50;
+  c.tolerance = 1e-4;
+  c.final_tolerance = 1e-4;
+  c.inner_kspace = 0;
+  c.inner_tolerance = 0;
+  return c;
+}
+
+void check_cfg(const nw_solver_cfg& c) {
+  if (c.kspace < 1 || c.kspace > 1000) fail(NW_INVALID_ARG, "kspace out of range");
+  if (c.max_iterations < 0) fail(NW_INVALID_ARG, "max_iterations < 0");
+  if (!(c.tolerance >= 0.0)) fail(NW_INVALID_ARG, "tolerance < 0");
+  if (c.method < NW_GMRES || c.method > NW_FGMRES) fail(NW_INVALID_ARG, "bad method");
+  if (c.preconditioner < NW_PC_NONE || c.preconditioner > NW_PC_LEARNED)
+    fail(NW_INVALID_ARG, "bad preconditioner");
+}
+
+void need_finalized(const nw_linsys* ls) {
+  if (!ls) fail(NW_INVALID_ARG, "null handle");
+  if (!ls->finalized) fail(NW_NOT_FINALIZED, "linear system not finalized");
+}
+
+// materialise a pending zeroSystem before a partial update
+void materialize_zero(nw_linsys* ls) {
+  if (!ls->pristine) return;
+  NW_CUDA(cudaMemsetAsync(ls->values.p, 0, ls->values.n * sizeof(double), ls->stream));
+  NW_CUDA(cudaMemsetAsync(ls->rhs.p, 0, ls->rhs.n * sizeof(double), ls->stream));
+  ls->pristine = false;
+}
+
+void begin_timing(nw_linsys* ls) {
+  if (!ls->ev0) {
+    NW_CUDA(cudaEventCreate(&ls->ev0));
+    NW_CUDA(cudaEventCreate(&ls->ev1));
+  }
+  NW_CUDA(cudaEventRecord(ls->ev0, ls->stream));
+}
+void end_timing(nw_linsys* ls) {
+  NW_CUDA(cudaEventRecord(ls->ev1, ls->stream));
+  ls->timed = true;
+}
+
+void check_ptr(const void* p, const char* name) {
+  if (!p) fail(NW_INVALID_ARG, std::string("null field pointer: ") + name);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* nw_last_error_string(void) { return last_error(); }
+int nw_version(void) { return 1; }
+
+nw_status nw_set_device(int device) {
+  return guard([&] {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+      fail(NW_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= n) fail(NW_INVALID_ARG, "device out of range");
+    g_device = device;
+    NW_CUDA(cudaSetDevice(device));
+  });
+}
+
+nw_status nw_linsys_create(int num_dof, const nw_solver_cfg* cfg,
+                           nw_linsys** out) {
+  return guard([&] {
+    if (!out) fail(NW_INVALID_ARG, "null output");
+    *out = nullptr;
+    if (num_dof < 1 || num_dof > 3) fail(NW_INVALID_ARG, "num_dof must be 1..3");
+    // host-only until nw_linsys_finalize: graph construction needs no GPU
+    auto ls = std::make_unique<nw_linsys>();
+    ls->num_dof = num_dof;
+    ls->device = g_device;
+    ls->cfg = cfg ? *cfg : default_cfg();
+    check_cfg(ls->cfg);
+    *out = ls.release();
+  });
+}
+
+nw_status nw_linsys_destroy(nw_linsys* ls) {
+  return guard([&] {
+    if (!ls) return;
+    if (ls->ev0) cudaEventDestroy(ls->ev0);
+    if (ls->ev1) cudaEventDestroy(ls->ev1);
+    delete ls;
+  });
+}
+
+nw_status nw_linsys_set_stream(nw_linsys* ls, void* stream) {
+  return guard([&] {
+    if (!ls) fail(NW_INVALID_ARG, "null handle");
+    ls->stream = static_cast<cudaStream_t>(stream);
+  });
+}
+
+nw_status nw_linsys_set_solver_cfg(nw_linsys* ls, const nw_solver_cfg* cfg) {
+  return guard([&] {
+    if (!ls || !cfg) fail(NW_INVALID_ARG, "null argument");
+    check_cfg(*cfg);
+    const bool grow = ls->finalized && cfg->kspace > ls->cfg.kspace;
+    ls->cfg = *cfg;
+    if (grow) {
+      DevCsr A;
+      A.n = ls->g.nrows;
+      A.nnz = ls->g.nnz;
+      A.row_ptr = ls->row_ptr.p;
+      A.col_idx = ls->col_idx.p;
+      A.values = ls->values.p;
+      A.lanes = ls->num_dof == 1 ? 8 : 32;
+      ls->solver.setup(A, std::max(ls->cfg.kspace, ls->cfg.inner_kspace), ls->stream);
+    }
+  });
+}
+
+nw_status nw_linsys_build_edge_graph(nw_linsys* ls, int64_t num_nodes,
+                                     const int64_t* global_id,
+                                     const int64_t* nalu_id, int64_t num_edges,
+                                     const int64_t* edge_nodes) {
+  return guard([&] {
+    if (!ls) fail(NW_INVALID_ARG, "null handle");
+    if (num_edges > 0 && !edge_nodes) fail(NW_INVALID_ARG, "null edge list");
+    build_graph(ls->g, ls->num_dof, num_nodes, global_id, nalu_id, num_edges,
+                edge_nodes);
+    ls->built = true;
+    ls->finalized = false;
+  });
+}
+
+nw_status nw_linsys_finalize(nw_linsys* ls) {
+  return guard([&] {
+    if (!ls) fail(NW_INVALID_ARG, "null handle");
+    if (!ls->built) fail(NW_NOT_FINALIZED, "no graph built");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+      fail(NW_NO_DEVICE, "no CUDA device");
+    NW_CUDA(cudaSetDevice(ls->device));
+    ls->err.resize(1);
+    NW_CUDA(cudaMemset(ls->err.p, 0, sizeof(int)));
+    HostGraph& g = ls->g;
+    cudaStream_t s = ls->stream;
+    ls->row_ptr.upload(g.row_ptr, s);
+    ls->col_idx.upload(g.col_idx, s);
+    ls->node_lid.upload(g.node_lid, s);
+    ls->inc_ptr.upload(g.inc_ptr, s);
+    ls->inc.upload(g.inc, s);
+    ls->diag_pos.upload(g.diag_pos, s);
+    ls->edges.resize(g.num_edges);
+    if (g.num_edges)
+      NW_CUDA(cudaMemcpyAsync(ls->edges.p, g.edges.data(),
+                              g.num_edges * sizeof(int2),
+                              cudaMemcpyHostToDevice, s));
+    ls->values.resize(g.nnz);
+    ls->rhs.resize(g.nrows);
+    const int coefs = ls->num_dof == 3 ? kMomentumCoefs : kScalarCoefs;
+    ls->buf.resize(size_t(coefs) * std::max<int64_t>(g.num_edges, 1));
+    NW_CUDA(cudaMemsetAsync(ls->values.p, 0, g.nnz * sizeof(double), s));
+    NW_CUDA(cudaMemsetAsync(ls->rhs.p, 0, g.nrows * sizeof(double), s));
+    ls->pristine = false;
+    // multicolour order for Gauss-Seidel: node colours, dof rows interleaved
+    std::vector<int32_t> color;
+    const int nc = color_node_graph(g, color);
+    const int nd = ls->num_dof;
+    const int rc = nc * nd;
+    std::vector<int64_t> cnt(rc + 1, 0);
+    for (int64_t r = 0; r < g.node_rows; ++r)
+      for (int d = 0; d < nd; ++d) cnt[color[r] * nd + d + 1]++;
+    for (int c = 0; c < rc; ++c) cnt[c + 1] += cnt[c];
+    ls->color_ptr = cnt;
+    ls->color_rows_host.resize(g.nrows);
+    {
+      std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+      for (int64_t r = 0; r < g.node_rows; ++r)
+        for (int d = 0; d < nd; ++d)
+          ls->color_rows_host[pos[color[r] * nd + d]++] = int32_t(r * nd + d);
+    }
+    ls->color_rows.upload(ls->color_rows_host, s);
+    ls->pc.color_rows = ls->color_rows.p;
+    ls->pc.color_ptr = ls->color_ptr;
+    DevCsr A;
+    A.n = g.nrows;
+    A.nnz = g.nnz;
+    A.row_ptr = ls->row_ptr.p;
+    A.col_idx = ls->col_idx.p;
+    A.values = ls->values.p;
+    A.lanes = nd == 1 ? 8 : 32;
+    ls->solver.setup(A, std::max(ls->cfg.kspace, ls->cfg.inner_kspace), s);
+    NW_CUDA(cudaStreamSynchronize(s));
+    ls->finalized = true;
+  });
+}
+
+nw_status nw_linsys_graph_sizes(const nw_linsys* ls, int64_t* nrows,
+                                int64_t* nnz) {
+  return guard([&] {
+    if (!ls || !ls->built) fail(NW_NOT_FINALIZED, "no graph");
+    if (nrows) *nrows = ls->g.nrows;
+    if (nnz) *nnz = ls->g.nnz;
+  });
+}
+
+nw_status nw_linsys_get_graph(const nw_linsys* ls, int64_t* row_ptr,
+                              int32_t* col_idx) {
+  return guard([&] {
+    if (!ls || !ls->built) fail(NW_NOT_FINALIZED, "no graph");
+    if (row_ptr)
+      std::memcpy(row_ptr, ls->g.row_ptr.data(), ls->g.row_ptr.size() * sizeof(int64_t));
+    if (col_idx)
+      std::memcpy(col_idx, ls->g.col_idx.data(), ls->g.col_idx.size() * sizeof(int32_t));
+  });
+}
+
+nw_status nw_linsys_get_node_lid(const nw_linsys* ls, int64_t* node_lid) {
+  return guard([&] {
+    if (!ls || !ls->built) fail(NW_NOT_FINALIZED, "no graph");
+    if (!node_lid) fail(NW_INVALID_ARG, "null output");
+    std::memcpy(node_lid, ls->g.node_lid.data(), ls->g.node_lid.size() * sizeof(int64_t));
+  });
+}
+
+nw_status nw_linsys_zero(nw_linsys* ls) {
+  return guard([&] {
+    need_finalized(ls);
+    // zeroSystem is deferred: the next full assembly overwrites every slot
+    ls->pristine = true;
+  });
+}
+
+nw_status nw_assemble_scalar_edges(nw_linsys* ls, const nw_scalar_fields* f,
+                                   const nw_scalar_opts* o) {
+  return guard([&] {
+    need_finalized(ls);
+    if (ls->num_dof != 1) fail(NW_INVALID_ARG, "scalar assembly needs num_dof 1");
+    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+    check_ptr(f->coords, "coords");
+    check_ptr(f->velocity_rtm, "velocity_rtm");
+    check_ptr(f->q, "q");
+    check_ptr(f->dqdx, "dqdx");
+    check_ptr(f->density, "density");
+    check_ptr(f->diff_coeff, "diff_coeff");
+    check_ptr(f->area, "area");
+    check_ptr(f->mdot, "mdot");
+    if (!(o->relax != 0.0)) fail(NW_INVALID_ARG, "relaxation factor is zero");
+    begin_timing(ls);
+    const int64_t E = ls->g.num_edges;
+    launch_scalar_edges(ls->stream, E, ls->edges.p, *f, *o, ls->buf.p);
+    launch_rows(ls->stream, 0, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
+                ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, o->relax,
+                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1);
+    NW_CUDA(cudaGetLastError());
+    end_timing(ls);
+    ls->pristine = false;
+  });
+}
+
+nw_status nw_assemble_continuity_edges(nw_linsys* ls,
+                                       const nw_continuity_fields* f,
+                                       const nw_continuity_opts* o) {
+  return guard([&] {
+    need_finalized(ls);
+    if (ls->num_dof != 1) fail(NW_INVALID_ARG, "continuity assembly needs num_dof 1");
+    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+    check_ptr(f->coords, "coords");
+    check_ptr(f->velocity, "velocity");
+    check_ptr(f->dpdx, "dpdx");
+    check_ptr(f->density, "density");
+    check_ptr(f->pressure, "pressure");
+    check_ptr(f->udiag, "udiag");
+    check_ptr(f->area, "area");
+    if (!(o->tau_scale != 0.0)) fail(NW_INVALID_ARG, "tau_scale is zero");
+    begin_timing(ls);
+    const int64_t E = ls->g.num_edges;
+    launch_continuity_edges(ls->stream, E, ls->edges.p, *f, *o, ls->buf.p);
+    launch_rows(ls->stream, 1, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
+                ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, 1.0,
+                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1);
+    NW_CUDA(cudaGetLastError());
+    end_timing(ls);
+    ls->pristine = false;
+  });
+}
+
+nw_status nw_assemble_momentum_edges(nw_linsys* ls, const nw_momentum_fields* f,
+                                     const nw_momentum_opts* o) {
+  return guard([&] {
+    need_finalized(ls);
+    if (ls->num_dof != 3) fail(NW_INVALID_ARG, "momentum assembly needs num_dof 3");
+    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+    check_ptr(f->coords, "coords");
+    check_ptr(f->velocity, "velocity");
+    check_ptr(f->dudx, "dudx");
+    check_ptr(f->viscosity, "viscosity");
+    check_ptr(f->density, "density");
+    check_ptr(f->mask, "mask");
+    check_ptr(f->area, "area");
+    check_ptr(f->mdot, "mdot");
+    check_ptr(f->pecfac, "pecfac");
+    if (!(o->relax != 0.0)) fail(NW_INVALID_ARG, "relaxation factor is zero");
+    begin_timing(ls);
+    const int64_t E = ls->g.num_edges;
+    launch_momentum_edges(ls->stream, E, ls->edges.p, *f, *o, ls->buf.p);
+    launch_rows(ls->stream, 2, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
+                ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, o->relax,
+                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1);
+    NW_CUDA(cudaGetLastError());
+    end_timing(ls);
+    ls->pristine = false;
+  });
+}
+
+nw_status nw_linsys_sum_into(nw_linsys* ls, int n_ent, const int64_t* nodes,
+                             const double* rhs, const double* lhs) {
+  return guard([&] {
+    need_finalized(ls);
+    if (n_ent < 1 || n_ent * ls->num_dof > 128 || !nodes || !rhs || !lhs)
+      fail(NW_INVALID_ARG, "bad sum_into block");
+    materialize_zero(ls);
+    const int nd = ls->num_dof, nloc = n_ent * nd;
+    std::vector<int64_t> lid(n_ent);
+    for (int i = 0; i < n_ent; ++i) {
+      if (nodes[i] < 0 || nodes[i] >= ls->g.num_nodes)
+        fail(NW_INVALID_ARG, "node index out of range");
+      lid[i] = ls->g.node_lid[nodes[i]];
+    }
+    ls->scratch_lid.upload(lid, ls->stream);
+    std::vector<double> tmp(size_t(nloc) * nloc + nloc);
+    std::memcpy(tmp.data(), lhs, sizeof(double) * nloc * nloc);
+    std::memcpy(tmp.data() + size_t(nloc) * nloc, rhs, sizeof(double) * nloc);
+    ls->scratch_vals.upload(tmp, ls->stream);
+    launch_sum_into_block(ls->stream, n_ent, nd, ls->scratch_lid.p,
+                          ls->scratch_vals.p, ls->scratch_vals.p + size_t(nloc) * nloc,
+                          ls->row_ptr.p, ls->col_idx.p, ls->values.p, ls->rhs.p);
+    NW_CUDA(cudaGetLastError());
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+  });
+}
+
+nw_status nw_linsys_apply_dirichlet(nw_linsys* ls, int64_t n,
+                                    const int64_t* nodes, int begin, int end,
+                                    const double* q, const double* bc) {
+  return guard([&] {
+    need_finalized(ls);
+    if (n < 0 || (n > 0 && (!nodes || !q || !bc)) || begin < 0 ||
+        end > ls->num_dof || begin > end)
+      fail(NW_INVALID_ARG, "bad Dirichlet arguments");
+    materialize_zero(ls);
+    NW_CUDA(cudaMemsetAsync(ls->err.p, 0, sizeof(int), ls->stream));
+    launch_reset_rows(ls->stream, n, nodes, ls->node_lid.p, ls->num_dof, begin,
+                      end, ls->row_ptr.p, ls->col_idx.p, ls->values.p,
+                      ls->rhs.p, 1.0, 0.0, q, bc, ls->g.num_nodes, ls->err.p);
+    NW_CUDA(cudaGetLastError());
+    int herr = 0;
+    NW_CUDA(cudaMemcpyAsync(&herr, ls->err.p, sizeof(int), cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    if (herr) fail(NW_INVALID_ARG, "Dirichlet node index out of range");
+  });
+}
+
+nw_status nw_linsys_reset_rows(nw_linsys* ls, int64_t n, const int64_t* nodes,
+                               int begin, int end, double diag_value,
+                               double rhs_residual) {
+  return guard([&] {
+    need_finalized(ls);
+    if (n < 0 || (n > 0 && !nodes) || begin < 0 || end > ls->num_dof ||
+        begin > end)
+      fail(NW_INVALID_ARG, "bad resetRows arguments");
+    materialize_zero(ls);
+    NW_CUDA(cudaMemsetAsync(ls->err.p, 0, sizeof(int), ls->stream));
+    launch_reset_rows(ls->stream, n, nodes, ls->node_lid.p, ls->num_dof, begin,
+                      end, ls->row_ptr.p, ls->col_idx.p, ls->values.p,
+                      ls->rhs.p, diag_value, rhs_residual, nullptr, nullptr,
+                      ls->g.num_nodes, ls->err.p);
+    NW_CUDA(cudaGetLastError());
+    int herr = 0;
+    NW_CUDA(cudaMemcpyAsync(&herr, ls->err.p, sizeof(int), cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    if (herr) fail(NW_INVALID_ARG, "resetRows node index out of range");
+  });
+}
+
+nw_status nw_linsys_load_complete(nw_linsys* ls) {
+  return guard([&] {
+    need_finalized(ls);
+    materialize_zero(ls);
+  });
+}
+
+nw_status nw_linsys_device_arrays(nw_linsys* ls, double** values, double** rhs,
+                                  const int64_t** row_ptr,
+                                  const int32_t** col_idx) {
+  return guard([&] {
+    need_finalized(ls);
+    materialize_zero(ls);
+    if (values) *values = ls->values.p;
+    if (rhs) *rhs = ls->rhs.p;
+    if (row_ptr) *row_ptr = ls->row_ptr.p;
+    if (col_idx) *col_idx = ls->col_idx.p;
+  });
+}
+
+nw_status nw_linsys_copy_to_host(nw_linsys* ls, double* values, double* rhs) {
+  return guard([&] {
+    need_finalized(ls);
+    materialize_zero(ls);
+    if (values)
+      NW_CUDA(cudaMemcpyAsync(values, ls->values.p, ls->values.n * sizeof(double),
+                              cudaMemcpyDeviceToHost, ls->stream));
+    if (rhs)
+      NW_CUDA(cudaMemcpyAsync(rhs, ls->rhs.p, ls->rhs.n * sizeof(double),
+                              cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+  });
+}
+
+nw_status nw_linsys_copy_from_host(nw_linsys* ls, const double* values,
+                                   const double* rhs) {
+  return guard([&] {
+    need_finalized(ls);
+    materialize_zero(ls);
+    if (values)
+      NW_CUDA(cudaMemcpyAsync(ls->values.p, values, ls->values.n * sizeof(double),
+                              cudaMemcpyHostToDevice, ls->stream));
+    if (rhs)
+      NW_CUDA(cudaMemcpyAsync(ls->rhs.p, rhs, ls->rhs.n * sizeof(double),
+                              cudaMemcpyHostToDevice, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+  });
+}
+
+nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
+                          nw_solve_report* rep) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!x) fail(NW_INVALID_ARG, "null solution vector");
+    materialize_zero(ls);
+    ls->solver.refresh(ls->stream);
+    ls->pc.kind = ls->cfg.preconditioner;
+    const double tol = final_iter ? ls->cfg.final_tolerance : ls->cfg.tolerance;
+    cudaEvent_t a, b;
+    NW_CUDA(cudaEventCreate(&a));
+    NW_CUDA(cudaEventCreate(&b));
+    NW_CUDA(cudaEventRecord(a, ls->stream));
+    SolveResult r = ls->solver.solve(ls->cfg, tol, ls->pc, ls->rhs.p, x, ls->stream);
+    NW_CUDA(cudaEventRecord(b, ls->stream));
+    NW_CUDA(cudaEventSynchronize(b));
+    float ms = 0.f;
+    NW_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ls->history = r.history;
+    if (rep) {
+      rep->iterations = r.iterations;
+      rep->outer_iterations = r.outer;
+      rep->status = r.status;
+      rep->converged = r.converged;
+      rep->final_rel_residual = r.final_rel;
+      rep->final_abs_residual = r.final_abs;
+      rep->rhs_norm = r.bnorm;
+      rep->solve_ms = ms;
+    }
+    if (r.status == NW_NAN_DETECTED) fail(NW_NAN_DETECTED, "non-finite value in the solve");
+  });
+}
+
+nw_status nw_linsys_residual_history(const nw_linsys* ls, double* hist,
+                                     int capacity, int* count) {
+  return guard([&] {
+    if (!ls) fail(NW_INVALID_ARG, "null handle");
+    const int n = int(ls->history.size());
+    if (count) *count = n;
+    if (hist)
+      std::memcpy(hist, ls->history.data(), sizeof(double) * std::min(n, capacity));
+  });
+}
+
+nw_status nw_linsys_rows_to_nodes(nw_linsys* ls, const double* x_rows,
+                                  double* x_nodes) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!x_rows || !x_nodes) fail(NW_INVALID_ARG, "null vector");
+    // host-free gather: node_lid maps every node (slaves included) to rows
+    const int64_t N = ls->g.num_nodes;
+    const int nd = ls->num_dof;
+    std::vector<double> hr(ls->g.nrows), hn(size_t(N) * nd);
+    NW_CUDA(cudaMemcpyAsync(hr.data(), x_rows, hr.size() * sizeof(double),
+                            cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    for (int64_t n = 0; n < N; ++n)
+      for (int d = 0; d < nd; ++d) hn[n * nd + d] = hr[ls->g.node_lid[n] + d];
+    NW_CUDA(cudaMemcpyAsync(x_nodes, hn.data(), hn.size() * sizeof(double),
+                            cudaMemcpyHostToDevice, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+  });
+}
+
+nw_status nw_linsys_spmv(nw_linsys* ls, const double* x, double* y) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!x || !y) fail(NW_INVALID_ARG, "null vector");
+    materialize_zero(ls);
+    ls->solver.spmv(x, y, ls->stream);
+    NW_CUDA(cudaGetLastError());
+  });
+}
+
+nw_status nw_linsys_precond_apply(nw_linsys* ls, int preconditioner,
+                                  const double* x, double* y) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!x || !y) fail(NW_INVALID_ARG, "null vector");
+    if (preconditioner < NW_PC_NONE || preconditioner > NW_PC_SGS)
+      fail(NW_INVALID_ARG, "preconditioner must be none, jacobi or sgs");
+    materialize_zero(ls);
+    ls->solver.refresh(ls->stream);
+    Precond pc = ls->pc;
+    pc.kind = preconditioner;
+    ls->solver.apply_precond(pc, x, y, ls->stream);
+  });
+}
+
+nw_status nw_linsys_sgs_order(nw_linsys* ls, int64_t* order, int* ncolors) {
+  return guard([&] {
+    need_finalized(ls);
+    if (order)
+      for (size_t i = 0; i < ls->color_rows_host.size(); ++i)
+        order[i] = ls->color_rows_host[i];
+    if (ncolors) *ncolors = int(ls->color_ptr.size()) - 1;
+  });
+}
+
+nw_status nw_linsys_sync(nw_linsys* ls) {
+  return guard([&] {
+    if (!ls) fail(NW_INVALID_ARG, "null handle");
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+  });
+}
+
+nw_status nw_linsys_last_assembly_ms(const nw_linsys* ls, double* ms) {
+  return guard([&] {
+    if (!ls || !ms) fail(NW_INVALID_ARG, "null argument");
+    if (!ls->timed) fail(NW_INVALID_ARG, "no assembly timed yet");
+    NW_CUDA(cudaEventSynchronize(ls->ev1));
+    float f = 0.f;
+    NW_CUDA(cudaEventElapsedTime(&f, ls->ev0, ls->ev1));
+    *ms = f;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,561 @@
+// Synthetic mesh inputs (nw_workload.h): seeded hex / tet blocks with STK
+// generated-mesh numbering, periodic master ids, edges, and the edge area
+// vectors and dual volumes of the CVFEM sub-control surfaces/volumes.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <queue>
+#include <string>
+#include <vector>
+
+#include "nw_internal.h"
+#include "nw_workload.h"
+
+namespace nw {
+void set_last_error(const std::string& s);
+}
+
+struct nw_mesh {
+  int npe = 8;
+  int64_t N = 0, E = 0, M = 0;
+  std::vector<double> coords, area, dualvol, bnd;
+  std::vector<int64_t> gid, nid, edges, conn;
+};
+
+namespace {
+
+using nw::Error;
+using nw::fail;
+
+uint64_t splitmix64(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+double uniform01(uint64_t& s) { return double(splitmix64(s) >> 11) * 0x1.0p-53; }
+
+// Hex8 sub-control geometry, same construction as HexSCS::determinant_scs
+// and HexSCV::determinant_scv (src/master_element/Hex8CVFEM.C:363-389,
+// 565-591; include/master_element/Hex8GeometryFunctions.h).
+void hex_points(const double c[8][3], double v[27][3]) {
+  for (int n = 0; n < 8; ++n)
+    for (int d = 0; d < 3; ++d) v[n][d] = c[n][d];
+  for (int d = 0; d < 3; ++d) {
+    v[8][d] = 0.5 * (c[0][d] + c[1][d]);
+    v[9][d] = 0.5 * (c[1][d] + c[2][d]);
+    v[10][d] = 0.5 * (c[2][d] + c[3][d]);
+    v[11][d] = 0.5 * (c[3][d] + c[0][d]);
+    v[12][d] = 0.25 * (c[0][d] + c[1][d] + c[2][d] + c[3][d]);
+    v[13][d] = 0.5 * (c[4][d] + c[5][d]);
+    v[14][d] = 0.5 * (c[5][d] + c[6][d]);
+    v[15][d] = 0.5 * (c[6][d] + c[7][d]);
+    v[16][d] = 0.5 * (c[7][d] + c[4][d]);
+    v[17][d] = 0.25 * (c[4][d] + c[5][d] + c[6][d] + c[7][d]);
+    v[18][d] = 0.5 * (c[1][d] + c[5][d]);
+    v[19][d] = 0.5 * (c[0][d] + c[4][d]);
+    v[20][d] = 0.25 * (c[0][d] + c[1][d] + c[4][d] + c[5][d]);
+    v[21][d] = 0.5 * (c[3][d] + c[7][d]);
+    v[22][d] = 0.5 * (c[2][d] + c[6][d]);
+    v[23][d] = 0.25 * (c[2][d] + c[3][d] + c[6][d] + c[7][d]);
+    v[24][d] = 0.25 * (c[1][d] + c[2][d] + c[5][d] + c[6][d]);
+    v[25][d] = 0.25 * (c[0][d] + c[3][d] + c[4][d] + c[7][d]);
+    double s = 0.0;
+    for (int n = 0; n < 8; ++n) s += c[n][d];
+    v[26][d] = s * 0.125;
+  }
+}
+
+void quad_area(const double q[4][3], double a[3]) {
+  a[0] = a[1] = a[2] = 0.0;
+  double xm[3];
+  for (int d = 0; d < 3; ++d) xm[d] = 0.25 * (q[0][d] + q[1][d] + q[2][d] + q[3][d]);
+  double r1[3] = {q[0][0] - xm[0], q[0][1] - xm[1], q[0][2] - xm[2]};
+  for (int t = 0; t < 4; ++t) {
+    const int ti = (t + 1) % 4;
+    const double r2[3] = {q[ti][0] - xm[0], q[ti][1] - xm[1], q[ti][2] - xm[2]};
+    a[0] += r1[1] * r2[2] - r2[1] * r1[2];
+    a[1] += r1[2] * r2[0] - r2[2] * r1[0];
+    a[2] += r1[0] * r2[1] - r2[0] * r1[1];
+    for (int d = 0; d < 3; ++d) r1[d] = r2[d];
+  }
+  for (int d = 0; d < 3; ++d) a[d] *= 0.5;
+}
+
+double grandy(const double s[8][3]) {
+  double cv[14][3];
+  for (int n = 0; n < 8; ++n)
+    for (int d = 0; d < 3; ++d) cv[n][d] = s[n][d];
+  static const int fn[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                               {2, 3, 7, 6}, {1, 2, 6, 5}, {0, 4, 3, 7}};
+  for (int k = 0; k < 6; ++k)
+    for (int d = 0; d < 3; ++d)
+      cv[8 + k][d] = 0.25 * (cv[fn[k][0]][d] + cv[fn[k][1]][d] +
+                             cv[fn[k][2]][d] + cv[fn[k][3]][d]);
+  static const int tf[24][3] = {
+      {0, 8, 1},  {8, 2, 1},  {3, 2, 8},  {3, 8, 0},  {6, 9, 5},  {7, 9, 6},
+      {4, 9, 7},  {4, 5, 9},  {10, 0, 1}, {5, 10, 1}, {4, 10, 5}, {4, 0, 10},
+      {7, 6, 11}, {6, 2, 11}, {2, 3, 11}, {3, 7, 11}, {6, 12, 2}, {5, 12, 6},
+      {5, 1, 12}, {1, 2, 12}, {0, 4, 13}, {4, 7, 13}, {7, 3, 13}, {3, 0, 13}};
+  double vol = 0.0;
+  for (int k = 0; k < 24; ++k) {
+    const int p = tf[k][0], q = tf[k][1], r = tf[k][2];
+    double m[3], dx[3];
+    for (int d = 0; d < 3; ++d) m[d] = cv[p][d] + cv[q][d] + cv[r][d];
+    dx[0] = (cv[q][1] - cv[p][1]) * (cv[r][2] - cv[p][2]) -
+            (cv[r][1] - cv[p][1]) * (cv[q][2] - cv[p][2]);
+    dx[1] = (cv[r][0] - cv[p][0]) * (cv[q][2] - cv[p][2]) -
+            (cv[q][0] - cv[p][0]) * (cv[r][2] - cv[p][2]);
+    dx[2] = (cv[q][0] - cv[p][0]) * (cv[r][1] - cv[p][1]) -
+            (cv[r][0] - cv[p][0]) * (cv[q][1] - cv[p][1]);
+    vol += m[0] * dx[0] + m[1] * dx[1] + m[2] * dx[2];
+  }
+  return vol / 18.0;
+}
+
+void hex_geometry(const double c[8][3], double scs[12][3], double scv[8]) {
+  static const int facet[12][4] = {
+      {20, 8, 12, 26},  {24, 9, 12, 26},  {10, 12, 26, 23}, {11, 25, 26, 12},
+      {13, 20, 26, 17}, {17, 14, 24, 26}, {17, 15, 23, 26}, {16, 17, 26, 25},
+      {19, 20, 26, 25}, {20, 18, 24, 26}, {22, 23, 26, 24}, {21, 25, 26, 23}};
+  static const int sub[8][8] = {
+      {0, 8, 12, 11, 19, 20, 26, 25},  {8, 1, 9, 12, 20, 18, 24, 26},
+      {12, 9, 2, 10, 26, 24, 22, 23},  {11, 12, 10, 3, 25, 26, 23, 21},
+      {19, 20, 26, 25, 4, 13, 17, 16}, {20, 18, 24, 26, 13, 5, 14, 17},
+      {26, 24, 22, 23, 17, 14, 6, 15}, {25, 26, 23, 21, 16, 17, 15, 7}};
+  double v[27][3];
+  hex_points(c, v);
+  for (int ip = 0; ip < 12; ++ip) {
+    double q[4][3];
+    for (int k = 0; k < 4; ++k)
+      for (int d = 0; d < 3; ++d) q[k][d] = v[facet[ip][k]][d];
+    quad_area(q, scs[ip]);
+  }
+  for (int ip = 0; ip < 8; ++ip) {
+    double s[8][3];
+    for (int n = 0; n < 8; ++n)
+      for (int d = 0; d < 3; ++d) s[n][d] = v[sub[ip][n]][d];
+    scv[ip] = grandy(s);
+  }
+}
+
+// Tet4 sub-control geometry (TetSCS::determinant_scs / TetSCV::
+// determinant_scv, src/master_element/Tet4CVFEM.C:243-360, 522-620).
+void tet_geometry(const double c[4][3], double scs[6][3], double scv[4]) {
+  double p[15][3];
+  for (int j = 0; j < 4; ++j)
+    for (int d = 0; d < 3; ++d) p[j][d] = c[j][d];
+  const double h = 0.5, t = 1.0 / 3.0;
+  for (int d = 0; d < 3; ++d) {
+    p[4][d] = h * (c[0][d] + c[1][d]);
+    p[5][d] = h * (c[1][d] + c[2][d]);
+    p[6][d] = h * (c[2][d] + c[0][d]);
+    p[7][d] = t * (c[0][d] + c[1][d] + c[2][d]);
+    p[8][d] = h * (c[2][d] + c[3][d]);
+    p[9][d] = h * (c[3][d] + c[1][d]);
+    p[10][d] = t * (c[1][d] + c[2][d] + c[3][d]);
+    p[11][d] = h * (c[0][d] + c[3][d]);
+    p[12][d] = t * (c[0][d] + c[2][d] + c[3][d]);
+    p[13][d] = t * (c[0][d] + c[1][d] + c[3][d]);
+    p[14][d] = 0.0;
+    for (int j = 0; j < 4; ++j) p[14][d] += 0.25 * c[j][d];
+  }
+  static const int facet[6][4] = {{4, 7, 14, 13},  {7, 14, 10, 5},
+                                  {6, 12, 14, 7},  {11, 13, 14, 12},
+                                  {13, 9, 10, 14}, {10, 8, 12, 14}};
+  for (int ip = 0; ip < 6; ++ip) {
+    double q[4][3];
+    for (int k = 0; k < 4; ++k)
+      for (int d = 0; d < 3; ++d) q[k][d] = p[facet[ip][k]][d];
+    quad_area(q, scs[ip]);
+  }
+  static const int sub[4][8] = {{0, 4, 7, 6, 11, 13, 14, 12},
+                                {1, 5, 7, 4, 9, 10, 14, 13},
+                                {2, 6, 7, 5, 8, 12, 14, 10},
+                                {3, 9, 13, 11, 8, 10, 14, 12}};
+  for (int ip = 0; ip < 4; ++ip) {
+    double s[8][3];
+    for (int n = 0; n < 8; ++n)
+      for (int d = 0; d < 3; ++d) s[n][d] = p[sub[ip][n]][d];
+    scv[ip] = grandy(s);
+  }
+}
+
+const int kHexEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                             {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+const int kHexLr[12][2] = {{0, 1}, {1, 2}, {2, 3}, {0, 3}, {4, 5}, {5, 6},
+                           {6, 7}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+const int kTetEdge[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+const int kTetLr[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+// Kuhn split of a hex along the c0-c6 diagonal: conforming across blocks.
+const int kKuhn[6][4] = {{0, 1, 2, 6}, {0, 2, 3, 6}, {0, 3, 7, 6},
+                         {0, 7, 4, 6}, {0, 4, 5, 6}, {0, 5, 1, 6}};
+
+// reverse Cuthill-McKee of the node graph given as CSR adjacency
+std::vector<int64_t> rcm_order(int64_t N, const std::vector<int64_t>& ap,
+                               const std::vector<int64_t>& aj) {
+  std::vector<int64_t> order;
+  order.reserve(N);
+  std::vector<char> seen(N, 0);
+  std::vector<int64_t> deg(N);
+  for (int64_t i = 0; i < N; ++i) deg[i] = ap[i + 1] - ap[i];
+  std::vector<int64_t> byDeg(N);
+  std::iota(byDeg.begin(), byDeg.end(), 0);
+  std::stable_sort(byDeg.begin(), byDeg.end(),
+                   [&](int64_t a, int64_t b) { return deg[a] < deg[b]; });
+  std::vector<int64_t> nb;
+  for (int64_t s : byDeg) {
+    if (seen[s]) continue;
+    size_t head = order.size();
+    order.push_back(s);
+    seen[s] = 1;
+    while (head < order.size()) {
+      const int64_t u = order[head++];
+      nb.clear();
+      for (int64_t p = ap[u]; p < ap[u + 1]; ++p)
+        if (!seen[aj[p]]) {
+          seen[aj[p]] = 1;
+          nb.push_back(aj[p]);
+        }
+      std::sort(nb.begin(), nb.end(), [&](int64_t a, int64_t b) {
+        return deg[a] != deg[b] ? deg[a] < deg[b] : a < b;
+      });
+      order.insert(order.end(), nb.begin(), nb.end());
+    }
+  }
+  std::reverse(order.begin(), order.end());
+  return order;  // order[k] = old node placed at new position k
+}
+
+void build(nw_mesh& m, int nx, int ny, int nz, const nw_box_opts& o) {
+  if (nx < 1 || ny < 1 || nz < 1) fail(NW_INVALID_ARG, "box dimensions < 1");
+  if (!(o.lx > 0 && o.ly > 0 && o.lz > 0)) fail(NW_INVALID_ARG, "box lengths <= 0");
+  if (o.jitter < 0 || o.jitter >= 0.5) fail(NW_INVALID_ARG, "jitter must be in [0, 0.5)");
+  if (o.tets && (o.periodic_x || o.periodic_y))
+    fail(NW_INVALID_ARG, "periodic tet blocks are not supported");
+  if (o.renumber && (o.periodic_x || o.periodic_y))
+    fail(NW_INVALID_ARG, "renumbering of periodic blocks is not supported");
+  const int64_t NX = nx + 1, NY = ny + 1, NZ = nz + 1;
+  const int64_t N = NX * NY * NZ;
+  if (N >= (int64_t(1) << 31)) fail(NW_INVALID_ARG, "too many nodes");
+  auto nid = [&](int64_t i, int64_t j, int64_t k) { return i + NX * (j + NY * k); };
+  // z coordinates: geometric growth from z = 0
+  std::vector<double> zc(NZ);
+  const double r = o.stretch_z > 0 ? o.stretch_z : 1.0;
+  for (int64_t k = 0; k <= nz; ++k)
+    zc[k] = (std::abs(r - 1.0) < 1e-14) ? o.lz * double(k) / nz
+                                        : o.lz * (std::pow(r, double(k)) - 1.0) /
+                                              (std::pow(r, double(nz)) - 1.0);
+  std::vector<double> coords(3 * N);
+  uint64_t seed = o.seed;
+  for (int64_t k = 0; k < NZ; ++k)
+    for (int64_t j = 0; j < NY; ++j)
+      for (int64_t i = 0; i < NX; ++i) {
+        const int64_t n = nid(i, j, k);
+        double x = o.lx * double(i) / nx, y = o.ly * double(j) / ny, z = zc[k];
+        if (o.jitter > 0) {
+          const double ux = uniform01(seed), uy = uniform01(seed), uz = uniform01(seed);
+          if (i > 0 && i < nx && j > 0 && j < ny && k > 0 && k < nz) {
+            const double hz = std::min(zc[k + 1] - zc[k], zc[k] - zc[k - 1]);
+            x += o.jitter * (2 * ux - 1) * o.lx / nx;
+            y += o.jitter * (2 * uy - 1) * o.ly / ny;
+            z += o.jitter * (2 * uz - 1) * hz;
+          }
+        }
+        coords[3 * n] = x;
+        coords[3 * n + 1] = y;
+        coords[3 * n + 2] = z;
+      }
+  // periodic masters (low face is the master)
+  std::vector<int64_t> master(N);
+  for (int64_t k = 0; k < NZ; ++k)
+    for (int64_t j = 0; j < NY; ++j)
+      for (int64_t i = 0; i < NX; ++i) {
+        const int64_t mi = (o.periodic_x && i == nx) ? 0 : i;
+        const int64_t mj = (o.periodic_y && j == ny) ? 0 : j;
+        master[nid(i, j, k)] = nid(mi, mj, k);
+      }
+  // elements
+  const int npe = o.tets ? 4 : 8;
+  const int64_t H = int64_t(nx) * ny * nz;
+  const int64_t M = o.tets ? 6 * H : H;
+  std::vector<int64_t> conn(M * npe);
+  {
+    int64_t e = 0;
+    for (int64_t k = 0; k < nz; ++k)
+      for (int64_t j = 0; j < ny; ++j)
+        for (int64_t i = 0; i < nx; ++i) {
+          const int64_t c[8] = {nid(i, j, k),         nid(i + 1, j, k),
+                                nid(i + 1, j + 1, k), nid(i, j + 1, k),
+                                nid(i, j, k + 1),     nid(i + 1, j, k + 1),
+                                nid(i + 1, j + 1, k + 1), nid(i, j + 1, k + 1)};
+          if (o.tets) {
+            for (int t = 0; t < 6; ++t, ++e)
+              for (int q = 0; q < 4; ++q) conn[4 * e + q] = c[kKuhn[t][q]];
+          } else {
+            for (int q = 0; q < 8; ++q) conn[8 * e + q] = c[q];
+            ++e;
+          }
+        }
+  }
+  // renumbering (relabels ids and reorders node storage by new id)
+  if (o.renumber) {
+    std::vector<int64_t> perm(N);  // perm[new] = old
+    std::iota(perm.begin(), perm.end(), 0);
+    uint64_t rs = o.renumber_seed;
+    for (int64_t i = N - 1; i > 0; --i) {
+      const int64_t j = int64_t(splitmix64(rs) % uint64_t(i + 1));
+      std::swap(perm[i], perm[j]);
+    }
+    std::vector<int64_t> inv(N);
+    for (int64_t k = 0; k < N; ++k) inv[perm[k]] = k;
+    for (auto& c : conn) c = inv[c];
+    {
+      std::vector<double> nc(3 * N);
+      for (int64_t k = 0; k < N; ++k)
+        for (int d = 0; d < 3; ++d) nc[3 * k + d] = coords[3 * perm[k] + d];
+      coords.swap(nc);
+    }
+    for (int64_t k = 0; k < N; ++k) master[k] = k;
+    if (o.renumber == 2) {
+      // node adjacency from element edges
+      std::vector<std::vector<int64_t>> adj(N);
+      const int ne = o.tets ? 6 : 12;
+      for (int64_t e = 0; e < M; ++e)
+        for (int q = 0; q < ne; ++q) {
+          const int64_t a = conn[npe * e + (o.tets ? kTetEdge[q][0] : kHexEdge[q][0])];
+          const int64_t b = conn[npe * e + (o.tets ? kTetEdge[q][1] : kHexEdge[q][1])];
+          adj[a].push_back(b);
+          adj[b].push_back(a);
+        }
+      std::vector<int64_t> ap(N + 1, 0), aj;
+      for (int64_t i = 0; i < N; ++i) {
+        auto& v = adj[i];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        ap[i + 1] = ap[i] + int64_t(v.size());
+      }
+      aj.reserve(ap[N]);
+      for (auto& v : adj) aj.insert(aj.end(), v.begin(), v.end());
+      adj.clear();
+      adj.shrink_to_fit();
+      std::vector<int64_t> ord = rcm_order(N, ap, aj);
+      std::vector<int64_t> inv2(N);
+      for (int64_t k = 0; k < N; ++k) inv2[ord[k]] = k;
+      for (auto& c : conn) c = inv2[c];
+      std::vector<double> nc(3 * N);
+      for (int64_t k = 0; k < N; ++k)
+        for (int d = 0; d < 3; ++d) nc[3 * k + d] = coords[3 * ord[k] + d];
+      coords.swap(nc);
+    }
+  }
+  // edges: per-node sorted unique higher neighbours (node[0] = lower id)
+  const int ne = o.tets ? 6 : 12;
+  std::vector<int64_t> cnt(N + 1, 0);
+  for (int64_t e = 0; e < M; ++e)
+    for (int q = 0; q < ne; ++q) {
+      int64_t a = conn[npe * e + (o.tets ? kTetEdge[q][0] : kHexEdge[q][0])];
+      int64_t b = conn[npe * e + (o.tets ? kTetEdge[q][1] : kHexEdge[q][1])];
+      cnt[std::min(a, b) + 1]++;
+    }
+  for (int64_t i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int64_t> hi(cnt[N]);
+  {
+    std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+    for (int64_t e = 0; e < M; ++e)
+      for (int q = 0; q < ne; ++q) {
+        int64_t a = conn[npe * e + (o.tets ? kTetEdge[q][0] : kHexEdge[q][0])];
+        int64_t b = conn[npe * e + (o.tets ? kTetEdge[q][1] : kHexEdge[q][1])];
+        hi[pos[std::min(a, b)]++] = std::max(a, b);
+      }
+  }
+  std::vector<int64_t> eptr(N + 1, 0), ehi;
+  ehi.reserve(hi.size() / 2);
+  for (int64_t i = 0; i < N; ++i) {
+    auto b = hi.begin() + cnt[i], en = hi.begin() + cnt[i + 1];
+    std::sort(b, en);
+    auto u = std::unique(b, en);
+    ehi.insert(ehi.end(), b, u);
+    eptr[i + 1] = int64_t(ehi.size());
+  }
+  const int64_t E = int64_t(ehi.size());
+  std::vector<int64_t> edges(2 * E);
+  for (int64_t i = 0; i < N; ++i)
+    for (int64_t p = eptr[i]; p < eptr[i + 1]; ++p) {
+      edges[2 * p] = i;
+      edges[2 * p + 1] = ehi[p];
+    }
+  auto edge_of = [&](int64_t a, int64_t b) {
+    const int64_t lo = std::min(a, b), h = std::max(a, b);
+    auto it = std::lower_bound(ehi.begin() + eptr[lo], ehi.begin() + eptr[lo + 1], h);
+    return int64_t(it - ehi.begin());
+  };
+  // geometry: per-element sub-control surfaces and volumes, then gather
+  const int nscs = o.tets ? 6 : 12;
+  const int nscv = npe;
+  std::vector<double> escs(size_t(M) * nscs * 3), escv(size_t(M) * nscv);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < M; ++e) {
+    if (o.tets) {
+      double c[4][3], s[6][3], v[4];
+      for (int q = 0; q < 4; ++q)
+        for (int d = 0; d < 3; ++d) c[q][d] = coords[3 * conn[4 * e + q] + d];
+      tet_geometry(c, s, v);
+      for (int ip = 0; ip < 6; ++ip)
+        for (int d = 0; d < 3; ++d) escs[(size_t(e) * 6 + ip) * 3 + d] = s[ip][d];
+      for (int ip = 0; ip < 4; ++ip) escv[size_t(e) * 4 + ip] = v[ip];
+    } else {
+      double c[8][3], s[12][3], v[8];
+      for (int q = 0; q < 8; ++q)
+        for (int d = 0; d < 3; ++d) c[q][d] = coords[3 * conn[8 * e + q] + d];
+      hex_geometry(c, s, v);
+      for (int ip = 0; ip < 12; ++ip)
+        for (int d = 0; d < 3; ++d) escs[(size_t(e) * 12 + ip) * 3 + d] = s[ip][d];
+      for (int ip = 0; ip < 8; ++ip) escv[size_t(e) * 8 + ip] = v[ip];
+    }
+  }
+  std::vector<double> area(3 * E, 0.0), dualvol(N, 0.0);
+  for (int64_t e = 0; e < M; ++e) {
+    for (int ip = 0; ip < nscs; ++ip) {
+      const int la = o.tets ? kTetLr[ip][0] : kHexLr[ip][0];
+      const int lb = o.tets ? kTetLr[ip][1] : kHexLr[ip][1];
+      const int64_t a = conn[npe * e + la], b = conn[npe * e + lb];
+      const int64_t ed = edge_of(a, b);
+      // sign rule of GeometryInteriorAlg.C:209-213
+      const double sign = (a == edges[2 * ed]) ? 1.0 : -1.0;
+      for (int d = 0; d < 3; ++d)
+        area[3 * ed + d] += escs[(size_t(e) * nscs + ip) * 3 + d] * sign;
+    }
+    for (int ip = 0; ip < nscv; ++ip)
+      dualvol[conn[npe * e + ip]] += escv[size_t(e) * nscv + ip];
+  }
+  // lumped exposed area vectors on the non-periodic box faces; boundary
+  // nodes of the block are the ones on the original lattice boundary.
+  std::vector<double> bnd(3 * N, 0.0);
+  if (!o.renumber) {
+    auto addq = [&](int64_t n0, int64_t n1, int64_t n2, int64_t n3) {
+      // outward-oriented quad (n0..n3 counter-clockwise seen from outside)
+      double q[4][3];
+      const int64_t ns[4] = {n0, n1, n2, n3};
+      for (int k = 0; k < 4; ++k)
+        for (int d = 0; d < 3; ++d) q[k][d] = coords[3 * ns[k] + d];
+      double a[3];
+      quad_area(q, a);
+      for (int k = 0; k < 4; ++k)
+        for (int d = 0; d < 3; ++d) bnd[3 * ns[k] + d] += 0.25 * a[d];
+    };
+    for (int64_t j = 0; j < ny; ++j)
+      for (int64_t i = 0; i < nx; ++i) {
+        addq(nid(i, j, 0), nid(i, j + 1, 0), nid(i + 1, j + 1, 0), nid(i + 1, j, 0));
+        addq(nid(i, j, nz), nid(i + 1, j, nz), nid(i + 1, j + 1, nz), nid(i, j + 1, nz));
+      }
+    if (!o.periodic_x)
+      for (int64_t k = 0; k < nz; ++k)
+        for (int64_t j = 0; j < ny; ++j) {
+          addq(nid(0, j, k), nid(0, j, k + 1), nid(0, j + 1, k + 1), nid(0, j + 1, k));
+          addq(nid(nx, j, k), nid(nx, j + 1, k), nid(nx, j + 1, k + 1), nid(nx, j, k + 1));
+        }
+    if (!o.periodic_y)
+      for (int64_t k = 0; k < nz; ++k)
+        for (int64_t i = 0; i < nx; ++i) {
+          addq(nid(i, 0, k), nid(i + 1, 0, k), nid(i + 1, 0, k + 1), nid(i, 0, k + 1));
+          addq(nid(i, ny, k), nid(i, ny, k + 1), nid(i + 1, ny, k + 1), nid(i + 1, ny, k));
+        }
+  }
+  // periodic sums of nodal quantities: master and slaves hold the total
+  for (int64_t n = 0; n < N; ++n)
+    if (master[n] != n) {
+      dualvol[master[n]] += dualvol[n];
+      for (int d = 0; d < 3; ++d) bnd[3 * master[n] + d] += bnd[3 * n + d];
+    }
+  for (int64_t n = 0; n < N; ++n)
+    if (master[n] != n) {
+      dualvol[n] = dualvol[master[n]];
+      for (int d = 0; d < 3; ++d) bnd[3 * n + d] = bnd[3 * master[n] + d];
+    }
+  m.npe = npe;
+  m.N = N;
+  m.E = E;
+  m.M = M;
+  m.coords.swap(coords);
+  m.area.swap(area);
+  m.dualvol.swap(dualvol);
+  m.bnd.swap(bnd);
+  m.conn.swap(conn);
+  m.edges.swap(edges);
+  m.gid.resize(N);
+  m.nid.resize(N);
+  for (int64_t n = 0; n < N; ++n) {
+    m.gid[n] = n + 1;
+    m.nid[n] = master[n] + 1;
+  }
+}
+
+template <typename F>
+nw_status guard(F&& f) {
+  try {
+    f();
+    return NW_OK;
+  } catch (const Error& e) {
+    nw::set_last_error(e.msg);
+    return e.status;
+  } catch (const std::exception& e) {
+    nw::set_last_error(e.what());
+    return NW_INTERNAL;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+nw_status nw_mesh_box(int nx, int ny, int nz, const nw_box_opts* opts,
+                      nw_mesh** out) {
+  return guard([&] {
+    if (!opts || !out) fail(NW_INVALID_ARG, "null argument");
+    *out = nullptr;
+    auto m = std::make_unique<nw_mesh>();
+    build(*m, nx, ny, nz, *opts);
+    *out = m.release();
+  });
+}
+
+nw_status nw_mesh_destroy(nw_mesh* m) {
+  delete m;
+  return NW_OK;
+}
+
+nw_status nw_mesh_sizes(const nw_mesh* m, int64_t* num_nodes,
+                        int64_t* num_edges, int64_t* num_elems,
+                        int* nodes_per_elem) {
+  return guard([&] {
+    if (!m) fail(NW_INVALID_ARG, "null mesh");
+    if (num_nodes) *num_nodes = m->N;
+    if (num_edges) *num_edges = m->E;
+    if (num_elems) *num_elems = m->M;
+    if (nodes_per_elem) *nodes_per_elem = m->npe;
+  });
+}
+
+nw_status nw_mesh_get(const nw_mesh* m, double* coords, int64_t* global_id,
+                      int64_t* nalu_id, int64_t* edges, int64_t* conn,
+                      double* area, double* dualvol, double* bnd_area) {
+  return guard([&] {
+    if (!m) fail(NW_INVALID_ARG, "null mesh");
+    auto cp = [](auto* dst, const auto& src) {
+      if (dst) std::memcpy(dst, src.data(), src.size() * sizeof(src[0]));
+    };
+    cp(coords, m->coords);
+    cp(global_id, m->gid);
+    cp(nalu_id, m->nid);
+    cp(edges, m->edges);
+    cp(conn, m->conn);
+    cp(area, m->area);
+    cp(dualvol, m->dualvol);
+    cp(bnd_area, m->bnd);
+  });
+}
+
+}  // extern "C"

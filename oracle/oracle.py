@@ -1,0 +1,275 @@
+"""ctypes wrapper of the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the
+benchmark's CPU-baseline / reference arm. It is the checker, never the thing
+measured as the product. See oracle.h for the reference file:line each
+routine restates.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+
+I64 = C.POINTER(C.c_int64)
+I32 = C.POINTER(C.c_int32)
+DP = C.POINTER(C.c_double)
+
+
+class ScalarOpts(C.Structure):
+    _fields_ = [("alpha", C.c_double), ("alpha_upw", C.c_double), ("upw_factor", C.c_double),
+                ("relax", C.c_double), ("hybrid_factor", C.c_double), ("use_limiter", C.c_int),
+                ("tanh_form", C.c_int), ("tanh_trans", C.c_double), ("tanh_width", C.c_double)]
+
+
+class MomentumOpts(C.Structure):
+    _fields_ = [("alpha", C.c_double), ("alpha_upw", C.c_double), ("upw_factor", C.c_double),
+                ("relax", C.c_double), ("include_div_u", C.c_double), ("use_limiter", C.c_int)]
+
+
+class ContinuityOpts(C.Structure):
+    _fields_ = [("noc_fac", C.c_double), ("tau_scale", C.c_double),
+                ("interp_together", C.c_double), ("solve_incompressible", C.c_double)]
+
+
+class SolveReport(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("final_rel_implicit", C.c_double),
+                ("final_abs_explicit", C.c_double), ("rhs_norm", C.c_double)]
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            raise RuntimeError(f"{LIB} is not built; run oracle/build.py")
+        _lib = C.CDLL(str(LIB))
+        _lib.or_hex_box_num_nodes.restype = C.c_int64
+        _lib.or_hex_box_num_elems.restype = C.c_int64
+        _lib.or_hex8_edges.restype = C.c_int64
+        _lib.or_build_graph.restype = C.c_int64
+        _lib.or_peclet_classic.restype = C.c_double
+        _lib.or_peclet_classic.argtypes = [C.c_double, C.c_double]
+        _lib.or_peclet_tanh.restype = C.c_double
+        _lib.or_peclet_tanh.argtypes = [C.c_double, C.c_double, C.c_double]
+        _lib.or_solve.restype = C.c_int
+    return _lib
+
+
+def hex_box(nx, ny, nz):
+    L = lib()
+    N = L.or_hex_box_num_nodes(nx, ny, nz)
+    M = L.or_hex_box_num_elems(nx, ny, nz)
+    coords = np.zeros((N, 3))
+    conn = np.zeros((M, 8), np.int64)
+    L.or_hex_box(nx, ny, nz, _p(coords, C.c_double), _p(conn, C.c_int64))
+    return coords, conn
+
+
+def hex8_edges(conn, nnodes):
+    L = lib()
+    conn = _i64(conn)
+    M = conn.shape[0]
+    cap = 12 * M
+    edges = np.zeros((cap, 2), np.int64)
+    ee = np.zeros((M, 12), np.int64)
+    E = L.or_hex8_edges(C.c_int64(M), _p(conn, C.c_int64), C.c_int64(nnodes), C.c_int64(cap),
+                        _p(edges, C.c_int64), _p(ee, C.c_int64))
+    return edges[:E].copy(), ee
+
+
+def hex8_geometry(coords, conn, elem_edges, edges):
+    coords, conn, ee, edges = _f64(coords), _i64(conn), _i64(elem_edges), _i64(edges)
+    area = np.zeros((edges.shape[0], 3))
+    vol = np.zeros(coords.shape[0])
+    lib().or_hex8_geometry(C.c_int64(coords.shape[0]), _p(coords, C.c_double), C.c_int64(conn.shape[0]),
+                           _p(conn, C.c_int64), _p(ee, C.c_int64), C.c_int64(edges.shape[0]),
+                           _p(edges, C.c_int64), _p(area, C.c_double), _p(vol, C.c_double))
+    return area, vol
+
+
+def build_graph(nalu_id, edges, num_dof=1):
+    nalu_id, edges = _i64(nalu_id), _i64(edges)
+    N = nalu_id.shape[0]
+    nnz = C.c_int64()
+    L = lib()
+    nrows = L.or_build_graph(C.c_int64(N), _p(nalu_id, C.c_int64), C.c_int64(edges.shape[0]),
+                             _p(edges, C.c_int64), num_dof, C.byref(nnz), None, None, None)
+    rp = np.zeros(nrows + 1, np.int64)
+    ci = np.zeros(nnz.value, np.int32)
+    lid = np.zeros(N, np.int64)
+    L.or_build_graph(C.c_int64(N), _p(nalu_id, C.c_int64), C.c_int64(edges.shape[0]),
+                     _p(edges, C.c_int64), num_dof, C.byref(nnz), _p(rp, C.c_int64),
+                     _p(ci, C.c_int32), _p(lid, C.c_int64))
+    return rp, ci, lid
+
+
+def scalar_local(*args, mag=False, **kw):
+    return _scalar_local(*args, mag=mag, **kw)
+
+
+def _scalar_local(edges, coords, vrtm, q, dqdx, density, diff, area, mdot, opts: ScalarOpts, mag=False):
+    edges = _i64(edges)
+    E = edges.shape[0]
+    lhs = np.zeros((E, 4))
+    rhs = np.zeros((E, 2))
+    args = [_f64(a) for a in (coords, vrtm, q, dqdx, density, diff, area, mdot)]
+    fn = lib().or_scalar_edge_local_mag if mag else lib().or_scalar_edge_local
+    fn(C.c_int64(E), _p(edges, C.c_int64), *[_p(a, C.c_double) for a in args],
+                               C.byref(opts), _p(lhs, C.c_double), _p(rhs, C.c_double))
+    return lhs, rhs
+
+
+def continuity_local(*args, mag=False, **kw):
+    return _continuity_local(*args, mag=mag, **kw)
+
+
+def _continuity_local(edges, coords, vel, dpdx, density, pressure, udiag, area, opts: ContinuityOpts,
+                      mag=False):
+    edges = _i64(edges)
+    E = edges.shape[0]
+    lhs = np.zeros((E, 4))
+    rhs = np.zeros((E, 2))
+    args = [_f64(a) for a in (coords, vel, dpdx, density, pressure, udiag, area)]
+    fn = lib().or_continuity_edge_local_mag if mag else lib().or_continuity_edge_local
+    fn(C.c_int64(E), _p(edges, C.c_int64), *[_p(a, C.c_double) for a in args],
+                                   C.byref(opts), _p(lhs, C.c_double), _p(rhs, C.c_double))
+    return lhs, rhs
+
+
+def momentum_local(*args, mag=False, **kw):
+    return _momentum_local(*args, mag=mag, **kw)
+
+
+def _momentum_local(edges, coords, vrtm, vel, dudx, visc, density, mask, area, mdot, pecfac,
+                    opts: MomentumOpts, mag=False):
+    edges = _i64(edges)
+    E = edges.shape[0]
+    lhs = np.zeros((E, 36))
+    rhs = np.zeros((E, 6))
+    args = [_f64(a) for a in (coords, vrtm, vel, dudx, visc, density, mask, area, mdot, pecfac)]
+    fn = lib().or_momentum_edge_local_mag if mag else lib().or_momentum_edge_local
+    fn(C.c_int64(E), _p(edges, C.c_int64), *[_p(a, C.c_double) for a in args],
+                                 C.byref(opts), _p(lhs, C.c_double), _p(rhs, C.c_double))
+    return lhs, rhs
+
+
+def sum_into(edges, num_dof, lhs, rhs, node_lid, row_ptr, col_idx, nthreads=1, with_abs=True):
+    edges, lhs, rhs = _i64(edges), _f64(lhs), _f64(rhs)
+    node_lid, row_ptr = _i64(node_lid), _i64(row_ptr)
+    col_idx = np.ascontiguousarray(col_idx, np.int32)
+    nnz, nrows = col_idx.shape[0], row_ptr.shape[0] - 1
+    vals = np.zeros(nnz)
+    b = np.zeros(nrows)
+    va = np.zeros(nnz) if with_abs else None
+    ba = np.zeros(nrows) if with_abs else None
+    lib().or_sum_into_edges(C.c_int64(edges.shape[0]), _p(edges, C.c_int64), num_dof, _p(lhs, C.c_double),
+                            _p(rhs, C.c_double), _p(node_lid, C.c_int64), _p(row_ptr, C.c_int64),
+                            _p(col_idx, C.c_int32), _p(vals, C.c_double), _p(b, C.c_double),
+                            _p(va, C.c_double), _p(ba, C.c_double), nthreads)
+    return vals, b, va, ba
+
+
+def apply_dirichlet(nodes, num_dof, begin, end, q, bc, node_lid, row_ptr, col_idx, vals, rhs):
+    nodes, q, bc = _i64(nodes), _f64(q), _f64(bc)
+    lib().or_apply_dirichlet(C.c_int64(nodes.shape[0]), _p(nodes, C.c_int64), num_dof, begin, end,
+                             _p(q, C.c_double), _p(bc, C.c_double), _p(_i64(node_lid), C.c_int64),
+                             _p(_i64(row_ptr), C.c_int64),
+                             _p(np.ascontiguousarray(col_idx, np.int32), C.c_int32),
+                             _p(vals, C.c_double), _p(rhs, C.c_double))
+
+
+def reset_rows(nodes, begin, end, diag, rhs_value, node_lid, row_ptr, col_idx, vals, rhs):
+    nodes = _i64(nodes)
+    lib().or_reset_rows(C.c_int64(nodes.shape[0]), _p(nodes, C.c_int64), begin, end, C.c_double(diag),
+                        C.c_double(rhs_value), _p(_i64(node_lid), C.c_int64), _p(_i64(row_ptr), C.c_int64),
+                        _p(np.ascontiguousarray(col_idx, np.int32), C.c_int32), _p(vals, C.c_double),
+                        _p(rhs, C.c_double))
+
+
+def spmv(row_ptr, col_idx, vals, x, nthreads=1):
+    row_ptr, vals, x = _i64(row_ptr), _f64(vals), _f64(x)
+    col_idx = np.ascontiguousarray(col_idx, np.int32)
+    y = np.zeros(row_ptr.shape[0] - 1)
+    lib().or_spmv(C.c_int64(y.shape[0]), _p(row_ptr, C.c_int64), _p(col_idx, C.c_int32),
+                  _p(vals, C.c_double), _p(x, C.c_double), _p(y, C.c_double), nthreads)
+    return y
+
+
+def solve(row_ptr, col_idx, vals, b, method=0, precond=1, order=None, kspace=50, max_iters=50,
+          tol=1e-8, nthreads=1):
+    row_ptr, vals, b = _i64(row_ptr), _f64(vals), _f64(b)
+    col_idx = np.ascontiguousarray(col_idx, np.int32)
+    n = b.shape[0]
+    x = np.zeros(n)
+    hist = np.zeros(max_iters + 1)
+    rep = SolveReport()
+    od = None if order is None else _i64(order)
+    lib().or_solve(C.c_int64(n), _p(row_ptr, C.c_int64), _p(col_idx, C.c_int32), _p(vals, C.c_double),
+                   _p(b, C.c_double), _p(x, C.c_double), method, precond, _p(od, C.c_int64), kspace,
+                   max_iters, C.c_double(tol), _p(hist, C.c_double), C.byref(rep), nthreads)
+    return x, hist[:rep.iterations + 1].copy(), rep
+
+
+def precond_apply(row_ptr, col_idx, vals, kind, x, order=None):
+    row_ptr, vals, x = _i64(row_ptr), _f64(vals), _f64(x)
+    col_idx = np.ascontiguousarray(col_idx, np.int32)
+    y = np.zeros_like(x)
+    od = None if order is None else _i64(order)
+    lib().or_precond_apply(C.c_int64(x.shape[0]), _p(row_ptr, C.c_int64), _p(col_idx, C.c_int32),
+                           _p(vals, C.c_double), kind, _p(od, C.c_int64), _p(x, C.c_double),
+                           _p(y, C.c_double))
+    return y
+
+
+def mdot_unit_test(edges, vel, rho, area):
+    edges = _i64(edges)
+    out = np.zeros(edges.shape[0])
+    lib().or_mdot_unit_test(C.c_int64(edges.shape[0]), _p(edges, C.c_int64), _p(_f64(vel), C.c_double),
+                            _p(_f64(rho), C.c_double), _p(_f64(area), C.c_double), _p(out, C.c_double))
+    return out
+
+
+def mdot_edge(edges, coords, vel, dpdx, rho, p, udiag, area, noc=1.0, interp=1.0):
+    edges = _i64(edges)
+    out = np.zeros(edges.shape[0])
+    args = [_f64(a) for a in (coords, vel, dpdx, rho, p, udiag, area)]
+    lib().or_mdot_edge(C.c_int64(edges.shape[0]), _p(edges, C.c_int64), *[_p(a, C.c_double) for a in args],
+                       C.c_double(noc), C.c_double(interp), _p(out, C.c_double))
+    return out
+
+
+def nodal_grad_edge(edges, phi, area, dualvol, dim1=1):
+    edges = _i64(edges)
+    N = dualvol.shape[0]
+    grad = np.zeros((N, dim1 * 3))
+    lib().or_nodal_grad_edge(C.c_int64(edges.shape[0]), _p(edges, C.c_int64), dim1,
+                             _p(_f64(phi), C.c_double), _p(_f64(area), C.c_double),
+                             _p(_f64(dualvol), C.c_double), _p(grad, C.c_double))
+    return grad
+
+
+def peclet_classic(pe, hf):
+    return lib().or_peclet_classic(pe, hf)
+
+
+def peclet_tanh(x, c1, c2):
+    return lib().or_peclet_tanh(x, c1, c2)

@@ -1,0 +1,90 @@
+"""Extract the reference's known-answer golds for the edge-assembly path.
+
+Reads nalu-wind unit-test sources as text (no code from them is run) and
+writes tests/golden/reference_golds.json. Run in a checkout that has the
+reference tree:  python tests/golden/make_golden.py /path/to/nalu-wind
+The JSON is committed; tests never read the reference tree.
+
+Sources (paths within the nalu-wind tree):
+  unit_tests/edge_kernels/UnitTestScalarAdvDiffEdge.C   serial Tpetra CSR
+      graph, values and rhs (plain, FixPressureAtNode and Dirichlet)
+  unit_tests/edge_kernels/UnitTestContinuityAdvEdge.C   dense 8x8 LHS, rhs
+  unit_tests/edge_kernels/UnitTestMomentumAdvDiffEdge.C dense 24x24 LHS, rhs
+  unit_tests/UnitTestPecletFunction.C                   Peclet factors
+  unit_tests/ngp_algorithms/UnitTestGeometryAlg.C       dual volume, |A|^2
+  unit_tests/ngp_algorithms/UnitTestMdotAlg.C           mdot
+"""
+from __future__ import annotations
+
+import json
+import math
+import re
+import sys
+from pathlib import Path
+
+NUM = r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?"
+
+
+def _block(text: str, name: str) -> str:
+    """Body between the braces that follow `name` (first match)."""
+    i = text.index(name)
+    j = text.index("=", i)
+    k = text.index("{", j)
+    depth = 0
+    for p in range(k, len(text)):
+        if text[p] == "{":
+            depth += 1
+        elif text[p] == "}":
+            depth -= 1
+            if depth == 0:
+                return text[k + 1:p]
+    raise ValueError(name)
+
+
+def _nums(body: str) -> list[float]:
+    body = re.sub(r"//[^\n]*", "", body)
+    return [float(x) for x in re.findall(NUM, body)]
+
+
+def main(ref: Path, out: Path) -> None:
+    g: dict = {}
+    s = (ref / "unit_tests/edge_kernels/UnitTestScalarAdvDiffEdge.C").read_text()
+    sc = {}
+    for name in ["rowOffsets_serial", "cols_serial", "vals_serial", "fixed_vals_serial",
+                 "dirichlet_vals_serial", "rhs_serial", "fixed_rhs_serial", "dirichlet_rhs_serial"]:
+        vals = _nums(_block(s, f" {name} "))
+        sc[name] = [int(v) for v in vals] if name in ("rowOffsets_serial", "cols_serial") else vals
+    g["scalar_adv_diff_hex8"] = sc
+
+    c = (ref / "unit_tests/edge_kernels/UnitTestContinuityAdvEdge.C").read_text()
+    g["continuity_hex8"] = {"rhs": _nums(_block(c, "rhs[8]")), "lhs": _nums(_block(c, "lhs[8][8]"))}
+
+    m = (ref / "unit_tests/edge_kernels/UnitTestMomentumAdvDiffEdge.C").read_text()
+    g["momentum_hex8"] = {"rhs": _nums(_block(m, "rhs[24]")), "lhs": _nums(_block(m, "lhs[24][24]"))}
+
+    p = (ref / "unit_tests/UnitTestPecletFunction.C").read_text()
+    assert "std::sqrt(5.0)" in p and "1.0 / 6.0" in p
+    g["peclet_classic"] = {"A": 5.0, "hybrid_factor": 1.0,
+                           "peclet": [0.0, 1.0, math.sqrt(5.0), 1e5],
+                           "factor": [0.0, 1.0 / 6.0, 0.5, 1.0]}
+    assert "c1 = 5000.0" in p and "c2 = 200.0" in p
+    g["peclet_tanh"] = {"c1": 5000.0, "c2": 200.0,
+                        "x": [-5000.0 - 2000.0, 5000.0, 5000.0 + 2000.0], "factor": [0.0, 0.5, 1.0]}
+
+    geo = (ref / "unit_tests/ngp_algorithms/UnitTestGeometryAlg.C").read_text()
+    assert "EXPECT_NEAR(0.125, dVol[0], tol)" in geo and "0.25 * 0.25" in geo
+    g["geometry_hex8_unit_cube"] = {"dual_volume": 0.125, "area_mag_sq": 0.0625, "num_edges": 12}
+
+    md = (ref / "unit_tests/ngp_algorithms/UnitTestMdotAlg.C").read_text()
+    assert "EXPECT_NEAR(mdot[0], 2.5, tol)" in md and "field_fill(10.0, *velocity_)" in md
+    g["mdot_hex8_unit_cube"] = {"density": 1.0, "velocity": 10.0, "mdot": 2.5}
+
+    assert len(g["continuity_hex8"]["lhs"]) == 64 and len(g["momentum_hex8"]["lhs"]) == 576
+    assert len(g["momentum_hex8"]["rhs"]) == 24
+    out.write_text(json.dumps(g, indent=1))
+    print(f"wrote {out}")
+
+
+if __name__ == "__main__":
+    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(ref, Path(__file__).resolve().parent / "reference_golds.json")

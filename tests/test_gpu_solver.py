@@ -1,0 +1,158 @@
+"""GPU Krylov solves through the C ABI vs the oracle's restated solvers.
+
+Tolerances (FP64 plain method): residual histories agree per iteration to
+1e-10 relative (the GPU reductions sum in a different order, and GMRES
+amplifies that slightly over the iterations), solutions to 1e-9 relative.
+Mixed precision: the FP64 true residual reaches the tolerance, and the
+solution error against the FP64 oracle solve is reported and bounded.
+"""
+import numpy as np
+import pytest
+
+from gpu_util import dev, scalar_fields, to_dev_dict
+
+pytestmark = pytest.mark.gpu
+
+
+def _scalar_system(nw, n=32):
+    case = nw.workload.scalar_case(n, seed=1)
+    mesh = case.mesh
+    f = dict(coords=mesh.coords, velocity=case.node["velocity"], q=case.node["q"], dqdx=case.node["dqdx"],
+             density=case.node["density"], diff=case.node["diff_coeff"], area=mesh.area, mdot=case.edge["mdot"])
+    ls = nw.LinearSystem(1)
+    ls.build_edge_graph(mesh.num_nodes, mesh.edges, mesh.global_id, mesh.nalu_id)
+    ls.finalize()
+    d = to_dev_dict(f)
+    ls.zero_system()
+    ls.assemble_scalar(scalar_fields(nw, d), case.opts["scalar"])
+    nodes = case.extra["dirichlet_nodes"]
+    ls.apply_dirichlet(len(nodes), dev(nodes), 0, 1, d["q"], dev(case.node["bc"]))
+    ls.load_complete()
+    return ls, case, d
+
+
+def _poisson_system(nw, shape=(24, 24, 16)):
+    import torch
+    case = nw.workload.poisson_case(*shape, seed=3)
+    mesh = case.mesh
+    ls = nw.LinearSystem(1)
+    ls.build_edge_graph(mesh.num_nodes, mesh.edges)
+    ls.finalize()
+    nd = case.node
+    d = to_dev_dict(dict(coords=mesh.coords, velocity=nd["velocity"], dpdx=nd["dpdx"], density=nd["density"],
+                         pressure=nd["pressure"], udiag=nd["udiag"], area=mesh.area))
+    ls.zero_system()
+    ls.assemble_continuity(nw.ContinuityFields(*(d[k].data_ptr() for k in (
+        "coords", "velocity", "dpdx", "density", "pressure", "udiag", "area"))), case.opts["continuity"])
+    ls.from_host(rhs=case.extra["rhs"])
+    return ls, case
+
+
+@pytest.mark.parametrize("pc", [1, 2])
+def test_gmres_matches_oracle_history(nw, orc, pc):
+    import torch
+    ls, case, d = _scalar_system(nw)
+    cfg = nw.solver_cfg(method=nw.GMRES, preconditioner=pc, kspace=50, max_iterations=5000, tolerance=1e-8)
+    ls.set_solver_cfg(cfg)
+    nr, _ = ls.sizes()
+    x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    assert rep.converged == 1 and rep.status == 0
+    hist = ls.residual_history()
+    rp, ci = ls.graph()
+    vals, rhs = ls.to_host()
+    order = ls.sgs_order()[0] if pc == 2 else None
+    xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=0, precond=pc, order=order, kspace=50,
+                             max_iters=5000, tol=1e-8)
+    assert rep.iterations == orep.iterations
+    np.testing.assert_allclose(hist, ho, rtol=1e-10, atol=0)
+    xg = x.cpu().numpy()
+    assert np.linalg.norm(xg - xo) <= 1e-9 * np.linalg.norm(xo)
+    assert rep.final_abs_residual <= 1e-8 * rep.rhs_norm * 1.01
+
+
+def test_cg_and_gmres_on_poisson(nw, orc):
+    import torch
+    ls, case = _poisson_system(nw)
+    nr, _ = ls.sizes()
+    rp, ci = ls.graph()
+    vals, rhs = ls.to_host()
+    for method in (nw.CG, nw.GMRES):
+        ls.set_solver_cfg(nw.solver_cfg(method=method, preconditioner=nw.PC_JACOBI, kspace=30,
+                                        max_iterations=3000, tolerance=1e-8))
+        x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+        rep = ls.solve(x)
+        assert rep.converged == 1
+        xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=method, precond=1, kspace=30, max_iters=3000,
+                                 tol=1e-8)
+        assert abs(rep.iterations - orep.iterations) <= 1
+        k = min(len(ho), 40)
+        np.testing.assert_allclose(ls.residual_history()[:k], ho[:k], rtol=1e-9, atol=0)
+
+
+@pytest.mark.parametrize("pc", [1, 2])
+def test_mixed_precision_reaches_fp64_tolerance(nw, orc, pc):
+    import torch
+    ls, case = _poisson_system(nw)
+    nr, _ = ls.sizes()
+    ls.set_solver_cfg(nw.solver_cfg(method=nw.GMRES, preconditioner=pc, precision=nw.PREC_MIXED, kspace=30,
+                                    max_iterations=5000, tolerance=1e-10, inner_kspace=30,
+                                    inner_tolerance=1e-4))
+    x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    assert rep.converged == 1 and rep.outer_iterations >= 2
+    rp, ci = ls.graph()
+    vals, rhs = ls.to_host()
+    r = rhs - orc.spmv(rp, ci, vals, x.cpu().numpy())
+    assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(rhs) * 1.001
+    # error against the FP64 oracle solution (mean removed: the Neumann
+    # Laplacian fixes the solution up to a constant)
+    xo, _, _ = orc.solve(rp, ci, vals, rhs, method=0, precond=1, kspace=30, max_iters=20000, tol=1e-12)
+    xg = x.cpu().numpy()
+    e = (xg - xg.mean()) - (xo - xo.mean())
+    assert np.linalg.norm(e) <= 1e-6 * np.linalg.norm(xo - xo.mean())
+
+
+def test_spmv_and_preconditioners_match_oracle(nw, orc):
+    import torch
+    ls, case, d = _scalar_system(nw, 16)
+    rp, ci = ls.graph()
+    vals, rhs = ls.to_host()
+    rng = np.random.default_rng(3)
+    xv = rng.normal(size=rhs.shape[0])
+    y = torch.zeros(rhs.shape[0], dtype=torch.float64, device="cuda")
+    ls.spmv(dev(xv), y)
+    yo = orc.spmv(rp, ci, vals, xv)
+    np.testing.assert_allclose(y.cpu().numpy(), yo, rtol=1e-13, atol=1e-13 * np.abs(yo).max())
+    order, ncol = ls.sgs_order()
+    assert ncol >= 2
+    for kind in (0, 1, 2):
+        ls.precond_apply(kind, dev(xv), y)
+        yo = orc.precond_apply(rp, ci, vals, kind, xv, order if kind == 2 else None)
+        np.testing.assert_allclose(y.cpu().numpy(), yo, rtol=1e-12, atol=1e-12 * np.abs(yo).max())
+
+
+def test_nan_rhs_is_reported(nw):
+    """Fault injection on the input (a NaN in the rhs): the solve returns
+    NW_NAN_DETECTED instead of iterating on garbage."""
+    import torch
+    ls, case = _poisson_system(nw, (8, 8, 6))
+    rhs = case.extra["rhs"].copy()
+    rhs[5] = np.nan
+    ls.from_host(rhs=rhs)
+    ls.set_solver_cfg(nw.solver_cfg(max_iterations=50, tolerance=1e-8))
+    nr, _ = ls.sizes()
+    x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    with pytest.raises(nw.NwError) as e:
+        ls.solve(x)
+    assert e.value.status == 4
+
+
+def test_not_converged_status(nw):
+    import torch
+    ls, case = _poisson_system(nw, (12, 12, 8))
+    ls.set_solver_cfg(nw.solver_cfg(max_iterations=5, kspace=5, tolerance=1e-12))
+    nr, _ = ls.sizes()
+    x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    assert rep.converged == 0 and rep.status == 5 and rep.iterations == 5

@@ -1,0 +1,171 @@
+"""Pin the CPU oracle against the reference's own known-answer golds.
+
+Golds: tests/golden/reference_golds.json (extracted from the nalu-wind unit
+tests by tests/golden/make_golden.py). Tolerances are the reference tests'
+own: 1e-14 for the Tpetra CSR values, 1e-12 for the dense edge systems.
+"""
+import numpy as np
+import pytest
+
+import kat
+
+
+def scalar_system(orc, m):
+    o = orc.ScalarOpts(**m["opts"])
+    lhs, rhs = orc.scalar_local(m["edges"], m["coords"], m["velocity"], m["q"], m["dqdx"], m["density"],
+                                m["diff"], m["area"], m["mdot"], o)
+    rp, ci, lid = orc.build_graph(np.arange(1, 9), m["edges"], 1)
+    vals, b, _, _ = orc.sum_into(m["edges"], 1, lhs, rhs, lid, rp, ci)
+    return rp, ci, lid, vals, b
+
+
+def test_geometry_unit_cube(orc, golds):
+    m = kat.hex1(orc)
+    g = golds["geometry_hex8_unit_cube"]
+    assert m["edges"].shape[0] == g["num_edges"]
+    np.testing.assert_allclose(m["dualvol"], g["dual_volume"], rtol=0, atol=1e-16)
+    np.testing.assert_allclose((m["area"] ** 2).sum(1), g["area_mag_sq"], rtol=0, atol=1e-16)
+    # node[0] is the lower id on every edge
+    assert np.all(m["edges"][:, 0] < m["edges"][:, 1])
+
+
+def test_mdot_unit_cube(orc, golds):
+    m = kat.hex1(orc)
+    g = golds["mdot_hex8_unit_cube"]
+    v = np.full((8, 3), g["velocity"])
+    md = orc.mdot_edge(m["edges"], m["coords"], v, np.zeros((8, 3)), np.full(8, g["density"]), np.zeros(8),
+                       np.ones(8), m["area"])
+    np.testing.assert_allclose(md, g["mdot"], rtol=0, atol=1e-14)
+
+
+def test_peclet_functions(orc, golds):
+    g = golds["peclet_classic"]
+    for pe, f in zip(g["peclet"], g["factor"]):
+        assert abs(orc.peclet_classic(pe, g["hybrid_factor"]) - f) < 1e-8
+    g = golds["peclet_tanh"]
+    for x, f in zip(g["x"], g["factor"]):
+        assert abs(orc.peclet_tanh(x, g["c1"], g["c2"]) - f) < 1e-8
+
+
+def test_scalar_tpetra_graph_and_values(orc, golds):
+    m = kat.scalar_fixture(orc)
+    g = golds["scalar_adv_diff_hex8"]
+    rp, ci, lid, vals, b = scalar_system(orc, m)
+    assert rp.tolist() == g["rowOffsets_serial"]
+    assert ci.tolist() == g["cols_serial"]
+    np.testing.assert_allclose(vals, g["vals_serial"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(b, g["rhs_serial"], rtol=0, atol=1e-14)
+
+
+def test_scalar_fix_pressure_at_node(orc, golds):
+    """FixPressureAtNodeAlgorithm resets node id 1's row to (1, rhs = ref - p)
+    with p = density (UnitTestScalarAdvDiffEdge.C:229-293)."""
+    m = kat.scalar_fixture(orc)
+    g = golds["scalar_adv_diff_hex8"]
+    rp, ci, lid, vals, b = scalar_system(orc, m)
+    orc.reset_rows(np.array([0]), 0, 1, 1.0, 1.0 - m["density"][0], lid, rp, ci, vals, b)
+    np.testing.assert_allclose(vals, g["fixed_vals_serial"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(b, g["fixed_rhs_serial"], rtol=0, atol=1e-14)
+
+
+def test_scalar_dirichlet(orc, golds):
+    """applyDirichletBCs on every node with q = 2, bc = 0 except node 1 = 1
+    (UnitTestScalarAdvDiffEdge.C:295-381)."""
+    m = kat.scalar_fixture(orc)
+    g = golds["scalar_adv_diff_hex8"]
+    rp, ci, lid, vals, b = scalar_system(orc, m)
+    q = np.full(8, 2.0)
+    bc = np.zeros(8)
+    bc[0] = 1.0
+    orc.apply_dirichlet(np.arange(8), 1, 0, 1, q, bc, lid, rp, ci, vals, b)
+    np.testing.assert_allclose(vals, g["dirichlet_vals_serial"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(b, g["dirichlet_rhs_serial"], rtol=0, atol=1e-14)
+
+
+def test_continuity_dense(orc, golds):
+    m = kat.continuity_fixture(orc)
+    o = orc.ContinuityOpts(**m["opts"])
+    lhs, rhs = orc.continuity_local(m["edges"], m["coords"], m["velocity"], m["dpdx"], m["density"],
+                                    m["pressure"], m["udiag"], m["area"], o)
+    L, B = kat.dense_accumulate(m["edges"], lhs, rhs, 1, 8)
+    g = golds["continuity_hex8"]
+    np.testing.assert_allclose(L.ravel(), g["lhs"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(B, g["rhs"], rtol=0, atol=1e-12)
+
+
+def test_momentum_dense_same_dof(orc, golds):
+    m = kat.momentum_fixture(orc)
+    o = orc.MomentumOpts(**m["opts"])
+    lhs, rhs = orc.momentum_local(m["edges"], m["coords"], m["velocity"], m["velocity"], m["dudx"],
+                                  m["viscosity"], m["density"], m["mask"], m["area"], m["mdot"],
+                                  m["pecfac"], o)
+    L, B = kat.dense_accumulate(m["edges"], lhs, rhs, 3, 8, same_dof_only=True)
+    g = golds["momentum_hex8"]
+    np.testing.assert_allclose(L.ravel(), g["lhs"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(B, g["rhs"], rtol=0, atol=1e-12)
+
+
+def test_momentum_graph_block_structure(orc):
+    """numDof = 3: every dof row of a node shares the node's column list,
+    each column expanded to 3 consecutive columns
+    (fill_in_extra_dof_rows_per_node, src/TpetraLinearSystemHelpers.C:361-381)."""
+    m = kat.hex1(orc)
+    rp1, ci1, _ = orc.build_graph(np.arange(1, 9), m["edges"], 1)
+    rp3, ci3, lid3 = orc.build_graph(np.arange(1, 9), m["edges"], 3)
+    assert rp3[-1] == 9 * rp1[-1]
+    for r in range(8):
+        cols1 = ci1[rp1[r]:rp1[r + 1]]
+        expect = np.repeat(3 * cols1, 3) + np.tile(np.arange(3), len(cols1))
+        for d in range(3):
+            np.testing.assert_array_equal(ci3[rp3[3 * r + d]:rp3[3 * r + d + 1]], expect)
+    np.testing.assert_array_equal(lid3, 3 * np.arange(8))
+
+
+def test_threaded_sum_into_matches_serial(orc):
+    """The OpenMP (atomic) sum_into agrees with the serial order to rounding."""
+    m = kat.scalar_fixture(orc)
+    o = orc.ScalarOpts(**m["opts"])
+    lhs, rhs = orc.scalar_local(m["edges"], m["coords"], m["velocity"], m["q"], m["dqdx"], m["density"],
+                                m["diff"], m["area"], m["mdot"], o)
+    rp, ci, lid = orc.build_graph(np.arange(1, 9), m["edges"], 1)
+    v1, b1, va, _ = orc.sum_into(m["edges"], 1, lhs, rhs, lid, rp, ci, nthreads=1)
+    v4, b4, _, _ = orc.sum_into(m["edges"], 1, lhs, rhs, lid, rp, ci, nthreads=4)
+    assert np.all(np.abs(v1 - v4) <= 1e-15 * va + 1e-300)
+
+
+def test_oracle_gmres_solves_small_system(orc):
+    """Restated GMRES / CG reach the requested relative residual."""
+    m = kat.hex1(orc)
+    rp, ci, lid = orc.build_graph(np.arange(1, 9), m["edges"], 1)
+    # SPD Laplacian plus identity
+    vals = np.zeros(ci.shape[0])
+    for r in range(8):
+        for p in range(rp[r], rp[r + 1]):
+            vals[p] = 4.0 if ci[p] == r else -1.0
+    b = np.arange(1.0, 9.0)
+    for method in (0, 1):
+        for pc in (0, 1, 2):
+            x, hist, rep = orc.solve(rp, ci, vals, b, method=method, precond=pc, kspace=5, max_iters=60,
+                                     tol=1e-12)
+            assert rep.converged == 1
+            r = b - orc.spmv(rp, ci, vals, x)
+            assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(b)
+            assert hist[0] == 1.0 and hist[-1] <= 1e-12
+
+
+def test_oracle_sgs_is_forward_then_backward(orc):
+    """Symmetric Gauss-Seidel with zero start equals the explicit
+    (D + L)^-1 then (D + U)^-1 sweep pair."""
+    rng = np.random.default_rng(0)
+    n = 6
+    A = rng.normal(size=(n, n)) + 8 * np.eye(n)
+    rp = np.arange(0, n * n + 1, n, dtype=np.int64)
+    ci = np.tile(np.arange(n, dtype=np.int32), n)
+    x = rng.normal(size=n)
+    y = orc.precond_apply(rp, ci, A.ravel(), 2, x)
+    D = np.diag(np.diag(A))
+    y1 = np.linalg.solve(np.tril(A), x)
+    y2 = np.linalg.solve(np.triu(A), x - np.tril(A, -1) @ y1 - (np.triu(A, 1)) @ np.zeros(n))
+    # backward sweep solves (D + U) y = x - L y1
+    np.testing.assert_allclose(y, y2, rtol=1e-12, atol=1e-12)
+    del D
