@@ -109,6 +109,8 @@ SIGNATURES = {
     "nw_assemble_continuity_edges": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
                                                C.POINTER(ContinuityOpts)]),
     "nw_assemble_momentum_edges": (C.c_int, [C.c_void_p, C.POINTER(MomentumFields), C.POINTER(MomentumOpts)]),
+    "nw_assemble_continuity_edges_noalloc": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
+                                                       C.POINTER(ContinuityOpts), C.c_void_p, C.c_void_p]),
     "nw_linsys_sum_into": (C.c_int, [C.c_void_p, C.c_int, _I64P, _DP, _DP]),
     "nw_linsys_apply_dirichlet": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.c_int,
                                             C.c_void_p, C.c_void_p]),
@@ -248,6 +250,12 @@ class LinearSystem:
 
     def assemble_continuity(self, f: ContinuityFields, o: ContinuityOpts) -> None:
         check(self.lib.nw_assemble_continuity_edges(self.h, C.byref(f), C.byref(o)))
+
+    def assemble_continuity_noalloc(self, f: ContinuityFields, o: ContinuityOpts, values_dev, rhs_dev) -> None:
+        """Continuity assembly into caller-owned device arrays with no device
+        allocation (fixed in-library scratch; at most 524,288 edges)."""
+        check(self.lib.nw_assemble_continuity_edges_noalloc(self.h, C.byref(f), C.byref(o), dptr(values_dev),
+                                                            dptr(rhs_dev)))
 
     def assemble_momentum(self, f: MomentumFields, o: MomentumOpts) -> None:
         check(self.lib.nw_assemble_momentum_edges(self.h, C.byref(f), C.byref(o)))

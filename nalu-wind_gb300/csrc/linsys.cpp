@@ -639,3 +639,23 @@ nw_status nw_linsys_last_assembly_ms(const nw_linsys* ls, double* ms) {
 }
 
 }  // extern "C"
+
+namespace nw {
+PlanView plan_view(const nw_linsys* ls) {
+  need_finalized(ls);
+  PlanView v;
+  v.device = ls->device;
+  v.num_dof = ls->num_dof;
+  v.stream = ls->stream;
+  v.num_edges = ls->g.num_edges;
+  v.node_rows = ls->g.node_rows;
+  v.nrows = ls->g.nrows;
+  v.nnz = ls->g.nnz;
+  v.edges = ls->edges.p;
+  v.inc_ptr = ls->inc_ptr.p;
+  v.inc = ls->inc.p;
+  v.diag_pos = ls->diag_pos.p;
+  v.row_ptr = ls->row_ptr.p;
+  return v;
+}
+}  // namespace nw

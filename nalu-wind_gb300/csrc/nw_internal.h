@@ -85,3 +85,26 @@ void build_graph(HostGraph& g, int num_dof, int64_t num_nodes,
 int color_node_graph(const HostGraph& g, std::vector<int32_t>& color);
 
 }  // namespace nw
+
+namespace nw {
+// Read-only view of a finalized handle's assembly plan (device pointers),
+// for entry points that bring their own scratch and outputs.
+struct PlanView {
+  int device = 0;
+  int num_dof = 1;
+  cudaStream_t stream = nullptr;
+  int64_t num_edges = 0;
+  int64_t node_rows = 0;
+  int64_t nrows = 0;
+  int64_t nnz = 0;
+  const int2* edges = nullptr;
+  const int32_t* inc_ptr = nullptr;
+  const uint32_t* inc = nullptr;
+  const int32_t* diag_pos = nullptr;
+  const int64_t* row_ptr = nullptr;
+};
+// Throws Error unless the handle is finalized.
+PlanView plan_view(const nw_linsys* ls);
+[[noreturn]] void fail(nw_status s, const std::string& msg);
+void set_last_error(const std::string& s);
+}  // namespace nw
