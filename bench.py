@@ -299,7 +299,7 @@ def run_ours(args, rank, world):
                        "achieved_gbs": round(B_c / (con_avg * 1e-3) / 1e9, 1),
                        "gnnz_s": round(nnz_c / (con_avg * 1e-3) / 1e9, 4)},
         "momentum": {"avg_ms": round(mom_avg, 4), "gnnz_s": round(nnz_m / (mom_avg * 1e-3) / 1e9, 4)},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": 5 * args.steps,  # momentum: edge + row; continuity: node + edge + row
         "clocks": clocks,
     }
     if args.poisson:

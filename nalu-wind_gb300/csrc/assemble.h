@@ -23,14 +23,24 @@ void launch_scalar_edges(cudaStream_t s, int64_t E, const int2* edges,
 void launch_continuity_edges(cudaStream_t s, int64_t E, const int2* edges,
                              const nw_continuity_fields& f,
                              const ContinuityOpts& o, double* buf);
+// With a node buffer (N x 8 doubles) the reference-default options take the
+// node-phase + fast edge-phase route.
+void launch_continuity_edges(cudaStream_t s, int64_t E, int64_t N,
+                             const int2* edges, const nw_continuity_fields& f,
+                             const ContinuityOpts& o, double* buf,
+                             double* nodebuf);
+constexpr int kContinuityNodeStride = 8;
 void launch_momentum_edges(cudaStream_t s, int64_t E, const int2* edges,
                            const nw_momentum_fields& f, const MomentumOpts& o,
                            double* buf);
-// kind 0 scalar, 1 continuity, 2 momentum (3 dof)
+// kind 0 scalar, 1 continuity, 2 momentum (3 dof). smem_bytes: staging
+// size from row_stage_bytes (0 disables staging).
 void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
                  const uint32_t* inc, const int32_t* diag_pos,
                  const int64_t* row_ptr, const double* buf, int64_t E,
-                 double relax, double* values, double* rhs, int accumulate);
+                 double relax, double* values, double* rhs, int accumulate,
+                 int smem_bytes);
+int row_stage_bytes(int kind, const int64_t* row_ptr_host, int64_t R);
 void launch_reset_rows(cudaStream_t s, int64_t n, const int64_t* nodes,
                        const int64_t* node_lid, int num_dof, int begin,
                        int end, const int64_t* row_ptr, const int32_t* col_idx,

@@ -50,7 +50,8 @@ struct nw_linsys {
   DeviceArray<int32_t> col_idx, inc_ptr, diag_pos, color_rows;
   DeviceArray<uint32_t> inc;
   DeviceArray<int2> edges;
-  DeviceArray<double> values, rhs, buf;
+  DeviceArray<double> values, rhs, buf, nodebuf;
+  int stage_bytes[3] = {0, 0, 0};  // row-phase staging per kind
   DeviceArray<int> err;
   DeviceArray<int64_t> scratch_lid;
   DeviceArray<double> scratch_vals;
@@ -246,6 +247,13 @@ nw_status nw_linsys_finalize(nw_linsys* ls) {
     ls->rhs.resize(g.nrows);
     const int coefs = ls->num_dof == 3 ? kMomentumCoefs : kScalarCoefs;
     ls->buf.resize(size_t(coefs) * std::max<int64_t>(g.num_edges, 1));
+    if (ls->num_dof == 1) {
+      ls->nodebuf.resize(size_t(kContinuityNodeStride) * g.num_nodes);
+      ls->stage_bytes[0] = ls->stage_bytes[1] =
+          row_stage_bytes(0, g.row_ptr.data(), g.node_rows);
+    } else if (ls->num_dof == 3) {
+      ls->stage_bytes[2] = row_stage_bytes(2, g.row_ptr.data(), g.node_rows);
+    }
     NW_CUDA(cudaMemsetAsync(ls->values.p, 0, g.nnz * sizeof(double), s));
     NW_CUDA(cudaMemsetAsync(ls->rhs.p, 0, g.nrows * sizeof(double), s));
     ls->pristine = false;
@@ -338,7 +346,7 @@ nw_status nw_assemble_scalar_edges(nw_linsys* ls, const nw_scalar_fields* f,
     launch_scalar_edges(ls->stream, E, ls->edges.p, *f, *o, ls->buf.p);
     launch_rows(ls->stream, 0, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
                 ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, o->relax,
-                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1);
+                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[0]);
     NW_CUDA(cudaGetLastError());
     end_timing(ls);
     ls->pristine = false;
@@ -362,10 +370,11 @@ nw_status nw_assemble_continuity_edges(nw_linsys* ls,
     if (!(o->tau_scale != 0.0)) fail(NW_INVALID_ARG, "tau_scale is zero");
     begin_timing(ls);
     const int64_t E = ls->g.num_edges;
-    launch_continuity_edges(ls->stream, E, ls->edges.p, *f, *o, ls->buf.p);
+    launch_continuity_edges(ls->stream, E, ls->g.num_nodes, ls->edges.p, *f, *o,
+                            ls->buf.p, ls->nodebuf.p);
     launch_rows(ls->stream, 1, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
                 ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, 1.0,
-                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1);
+                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[1]);
     NW_CUDA(cudaGetLastError());
     end_timing(ls);
     ls->pristine = false;
@@ -393,7 +402,7 @@ nw_status nw_assemble_momentum_edges(nw_linsys* ls, const nw_momentum_fields* f,
     launch_momentum_edges(ls->stream, E, ls->edges.p, *f, *o, ls->buf.p);
     launch_rows(ls->stream, 2, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
                 ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, o->relax,
-                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1);
+                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[2]);
     NW_CUDA(cudaGetLastError());
     end_timing(ls);
     ls->pristine = false;

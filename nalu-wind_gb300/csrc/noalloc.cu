@@ -83,7 +83,7 @@ extern "C" nw_status nw_assemble_continuity_edges_noalloc(
     double* scratch = scratch_on(v.device);
     nw::launch_continuity_edges(v.stream, v.num_edges, v.edges, *f, *o, scratch);
     nw::launch_rows(v.stream, 1, v.node_rows, v.inc_ptr, v.inc, v.diag_pos,
-                    v.row_ptr, scratch, v.num_edges, 1.0, values, rhs, 0);
+                    v.row_ptr, scratch, v.num_edges, 1.0, values, rhs, 0, 0);
     NW_CUDA(cudaGetLastError());
     return NW_OK;
   } catch (const nw::Error& e) {
