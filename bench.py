@@ -343,12 +343,18 @@ def poisson_solves(nw, stream, args) -> dict:
     ls.from_host(rhs=case.extra["rhs"])
     nr, nnz = ls.sizes()
     res = {"workload": f"poisson {args.poisson_shape}", "rows": nr, "nnz": nnz, "tol": 1e-8}
-    for name, cfg in [
-        ("plain_fp64_gmres50_jacobi", nw.solver_cfg(kspace=50, max_iterations=20000, tolerance=1e-8)),
-        ("mixed_fp32_inner_jacobi", nw.solver_cfg(kspace=30, max_iterations=20000, tolerance=1e-8,
-                                                  precision=nw.PREC_MIXED, inner_kspace=30,
-                                                  inner_tolerance=1e-3)),
-    ]:
+    variants = [
+        ("plain_fp64_gmres50_jacobi", nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8)),
+        ("plain_fp64_gmres50_sgs", nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8,
+                                                 preconditioner=nw.PC_SGS)),
+        ("mixed_fp32_inner_jacobi", nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8,
+                                                  precision=nw.PREC_MIXED, inner_kspace=50,
+                                                  inner_tolerance=1e-4)),
+        ("mixed_fp32_inner_sgs", nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8,
+                                               precision=nw.PREC_MIXED, inner_kspace=50, inner_tolerance=1e-4,
+                                               preconditioner=nw.PC_SGS)),
+    ]
+    for name, cfg in variants:
         ls.set_solver_cfg(cfg)
         x = torch.zeros(nr, dtype=torch.float64, device="cuda")
         t = time.perf_counter()
@@ -422,6 +428,8 @@ def main():
     ap.add_argument("--shape", type=int, nargs=3, default=[128, 128, 64])
     ap.add_argument("--poisson", action="store_true")
     ap.add_argument("--poisson-shape", type=int, nargs=3, default=[256, 256, 128])
+    ap.add_argument("--poisson-maxit", type=int, default=20000)
+    ap.add_argument("--poisson-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.shape = tuple(args.shape)

@@ -83,25 +83,86 @@ void spmv_launch(int lanes, int64_t n, const int64_t* rp, const int32_t* ci,
 }
 
 // ---------------------------------------------------------------------------
+// Sliced-ELL SpMV: one warp per 32-row slice, lane = row; slot k of the
+// slice holds row entries k (padding: value 0, column = the row).
+template <typename VT, typename XT, typename ACC>
+__global__ void __launch_bounds__(kBlock)
+    sell_spmv_k(int64_t n, int64_t nslices, const int64_t* __restrict__ off,
+                const int32_t* __restrict__ cols, const VT* __restrict__ v,
+                const XT* __restrict__ x, const XT* __restrict__ b,
+                XT* __restrict__ y) {
+  const int64_t sl = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (sl >= nslices) return;
+  const int64_t o = off[sl];
+  const int len = int((off[sl + 1] - o) >> 5);
+  const int64_t row = (sl << 5) + lane;
+  ACC acc = 0;
+  const int32_t* c = cols + o + lane;
+  const VT* vv = v + o + lane;
+#pragma unroll 4
+  for (int k = 0; k < len; ++k) acc += ACC(vv[32 * k]) * ACC(x[c[32 * k]]);
+  if (row < n) y[row] = b ? XT(ACC(b[row]) - acc) : XT(acc);
+}
+
+// values in SELL order (FP64 and optionally FP32) from the CSR values
+__global__ void sell_gather_k(int64_t slots, const int32_t* __restrict__ map,
+                              const double* __restrict__ csr,
+                              double* __restrict__ out64, float* __restrict__ out32) {
+  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= slots) return;
+  const int32_t p = map[q];
+  const double v = p >= 0 ? csr[p] : 0.0;
+  out64[q] = v;
+  if (out32) out32[q] = float(v);
+}
+
+// ---------------------------------------------------------------------------
 // Deterministic multi-dot: out[k] = sum_i V[k][i] * w[i] for k < nv.
 // Stage 1 writes per-block partials (fixed grid); stage 2 sums them in a
 // fixed tree order.
+//
+// FP32 vectors: every product is formed exactly (p + e with e = fma(a, b,
+// -p)) and accumulated as a two-float sum (Knuth two-sum); warp reductions
+// combine the pairs on the FP32 pipes and only one value per warp is
+// widened to FP64. GB300's FP64 pipe is about 1/58 of its FP32 rate, so
+// per-thread FP64 work is kept out of these loops.
+struct F2 {
+  float s, c;
+};
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float x) {
+  const float t = s + x;
+  const float bp = t - s;
+  c += (s - (t - bp)) + (x - bp);
+  s = t;
+}
 __device__ __forceinline__ void acc_prod(double a, double b, double& s,
                                          double& c) {
   s = fma(a, b, s);
   (void)c;
 }
-// Exact FP32 product p + e, added to (s, c) with a two-sum; c collects the
-// rounding errors.
 __device__ __forceinline__ void acc_prod(float a, float b, float& s,
                                          float& c) {
   const float p = a * b;
-  const float e = fmaf(a, b, -p);
-  const float t = s + p;
-  const float bp = t - s;
-  const float err = (s - (t - bp)) + (p - bp);
-  s = t;
-  c += err + e;
+  c += fmaf(a, b, -p);
+  two_sum_acc(s, c, p);
+}
+// warp sum of (s, c); result valid in lane 0 as a double
+__device__ __forceinline__ double warp_sum(double s, double c) {
+  double v = s + c;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  return v;
+}
+__device__ __forceinline__ double warp_sum(float s, float c) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float os = __shfl_down_sync(0xffffffffu, s, off);
+    const float oc = __shfl_down_sync(0xffffffffu, c, off);
+    c += oc;
+    two_sum_acc(s, c, os);
+  }
+  return double(s) + double(c);
 }
 
 template <typename T>
@@ -110,26 +171,43 @@ __global__ void __launch_bounds__(kBlock)
            const T* __restrict__ w, double* __restrict__ partial) {
   __shared__ double red[kTile][kBlock / 32];
   const int G = gridDim.x;
+  const int64_t stride = int64_t(G) * blockDim.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int k0 = 0; k0 < nv; k0 += kTile) {
     const int kt = min(kTile, nv - k0);
     T s[kTile], c[kTile];
 #pragma unroll
     for (int k = 0; k < kTile; ++k) s[k] = c[k] = T(0);
-    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-         i += int64_t(G) * blockDim.x) {
-      const T wi = w[i];
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    // two elements per step for more loads in flight
+    for (; i + stride < n; i += 2 * stride) {
+      const T w0 = w[i], w1 = w[i + stride];
+      T a0[kTile], a1[kTile];
 #pragma unroll
       for (int k = 0; k < kTile; ++k)
-        if (k < kt) acc_prod(V[int64_t(k0 + k) * ld + i], wi, s[k], c[k]);
+        if (k < kt) {
+          a0[k] = V[int64_t(k0 + k) * ld + i];
+          a1[k] = V[int64_t(k0 + k) * ld + i + stride];
+        }
+#pragma unroll
+      for (int k = 0; k < kTile; ++k)
+        if (k < kt) {
+          acc_prod(a0[k], w0, s[k], c[k]);
+          acc_prod(a1[k], w1, s[k], c[k]);
+        }
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (i < n) {
+      const T w0 = w[i];
+#pragma unroll
+      for (int k = 0; k < kTile; ++k)
+        if (k < kt) acc_prod(V[int64_t(k0 + k) * ld + i], w0, s[k], c[k]);
+    }
 #pragma unroll
     for (int k = 0; k < kTile; ++k) {
-      double v = double(s[k]) + double(c[k]);
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1)
-        v += __shfl_down_sync(0xffffffffu, v, off);
-      if (lane == 0) red[k][warp] = v;
+      if (k < kt) {
+        const double v = warp_sum(s[k], c[k]);
+        if (lane == 0) red[k][warp] = v;
+      }
     }
     __syncthreads();
     if (threadIdx.x < kt) {
@@ -163,42 +241,85 @@ __global__ void reduce_partials_k(int G, const double* __restrict__ partial,
   }
 }
 
-// w -= sum_k h[k] V[k]  (h on the device, FP64)
+// w -= sum_k h[k] V[k]  (h on the device, FP64), one element per thread.
+// The coefficients are converted to the vector precision once per block
+// (FP64<->FP32 conversions issue on the narrow FP64 pipe). With
+// nrm_partial != nullptr each block also writes the partial ||w||^2 of its
+// elements to nrm_partial[blockIdx.x].
+constexpr int kMaxVecs = 1024;
+
 template <typename T>
 __global__ void __launch_bounds__(kBlock)
     maxpy_k(int64_t n, int nv, const T* __restrict__ V, int64_t ld,
-            const double* __restrict__ h, T* __restrict__ w) {
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  T acc = w[i];
-  for (int k = 0; k < nv; ++k) acc -= T(h[k]) * V[int64_t(k) * ld + i];
-  w[i] = acc;
-}
-
-// y = x / nrm[0] (y = 0 when the norm is zero). One FP64 reciprocal per
-// block, then a multiply per element in the vector's own precision.
-template <typename T>
-__global__ void scale_by_norm_k(int64_t n, const T* __restrict__ x,
-                                T* __restrict__ y,
-                                const double* __restrict__ nrm) {
-  __shared__ double inv;
-  if (threadIdx.x == 0) {
-    const double hn = nrm[0];
-    inv = hn != 0.0 ? 1.0 / hn : 0.0;
-  }
+            const double* __restrict__ h, T* __restrict__ w,
+            double* __restrict__ nrm_partial) {
+  __shared__ T hs[kMaxVecs];
+  __shared__ double red[kBlock / 32];
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) hs[k] = T(h[k]);
   __syncthreads();
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  y[i] = x[i] * T(inv);
+  T ss = T(0), cc = T(0);
+  if (i < n) {
+    T acc = w[i];
+    int k = 0;
+    for (; k + 8 <= nv; k += 8) {
+      T a[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) a[q] = V[int64_t(k + q) * ld + i];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc -= hs[k + q] * a[q];
+    }
+    for (; k < nv; ++k) acc -= hs[k] * V[int64_t(k) * ld + i];
+    w[i] = acc;
+    if (nrm_partial) acc_prod(acc, acc, ss, cc);
+  }
+  if (!nrm_partial) return;
+  const double v = warp_sum(ss, cc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < kBlock / 32; ++q) t += red[q];
+    nrm_partial[blockIdx.x] = t;
+  }
 }
 
 __global__ void sqrt_scalar_k(double* s) { s[0] = sqrt(s[0]); }
+
+// v32 = float(r / nrm[0]) (start of an inner FP32 cycle).
+__global__ void scale_to_f32_k(int64_t n, const double* __restrict__ r,
+                               float* __restrict__ v, const double* __restrict__ nrm) {
+  __shared__ double inv;
+  if (threadIdx.x == 0) inv = nrm[0] != 0.0 ? 1.0 / nrm[0] : 0.0;
+  __syncthreads();
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = float(r[i] * inv);
+}
 
 template <typename T>
 __global__ void jacobi_k(int64_t n, const T* __restrict__ rd,
                          const T* __restrict__ x, T* __restrict__ y) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) y[i] = x[i] * rd[i];
+}
+
+// v = w / nrm[0] and, when rd is given, z = rd * v (the Jacobi application
+// of the next Arnoldi step) in the same pass.
+template <typename T>
+__global__ void scale_jacobi_k(int64_t n, const T* __restrict__ w,
+                               T* __restrict__ v, const double* __restrict__ nrm,
+                               const T* __restrict__ rd, T* __restrict__ z) {
+  __shared__ T inv;
+  if (threadIdx.x == 0) {
+    const double hn = nrm[0];
+    inv = T(hn != 0.0 ? 1.0 / hn : 0.0);
+  }
+  __syncthreads();
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T vi = w[i] * inv;
+  v[i] = vi;
+  if (rd) z[i] = vi * rd[i];
 }
 
 // one colour of a Gauss-Seidel sweep: rows of this colour are mutually
@@ -264,16 +385,19 @@ __global__ void xpby_k(int64_t n, const double* __restrict__ z, double beta,
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) p[i] = z[i] + beta * p[i];
 }
-// y = sum_k c[k] V[k] (c on host -> passed in device scalar array)
+// y = sum_k c[k] V[k] (c in a device array), in the vector precision.
 template <typename T>
 __global__ void combine_k(int64_t n, int nv, const T* __restrict__ V,
                           int64_t ld, const double* __restrict__ c,
                           T* __restrict__ y) {
+  __shared__ T cs[kMaxVecs];
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) cs[k] = T(c[k]);
+  __syncthreads();
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double acc = 0.0;
-  for (int k = 0; k < nv; ++k) acc += c[k] * double(V[int64_t(k) * ld + i]);
-  y[i] = T(acc);
+  T acc = T(0);
+  for (int k = 0; k < nv; ++k) acc += cs[k] * V[int64_t(k) * ld + i];
+  y[i] = acc;
 }
 
 inline unsigned grid1(int64_t n) { return unsigned((n + kBlock - 1) / kBlock); }
@@ -293,16 +417,53 @@ void KrylovSolver::setup(const DevCsr& A, int m, cudaStream_t s) {
   NW_CUDA(cudaGetDevice(&dev));
   int sms = 0;
   NW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  red_blocks_ = int(std::max<int64_t>(1, std::min<int64_t>(4 * sms, (n + kBlock - 1) / kBlock)));
+  red_blocks_ = int(std::max<int64_t>(1, std::min<int64_t>(8 * sms, (n + 2 * kBlock - 1) / (2 * kBlock))));
   rdiag_.resize(n);
   V_.resize(size_t(m_ + 1) * n);
   Z_.release();
   w_.resize(n);
   z_.resize(n);
   r_.resize(n);
-  partial_.resize(size_t(m_ + 2) * red_blocks_);
+  partial_.resize(std::max<size_t>(size_t(m_ + 2) * red_blocks_, size_t(grid1(n))));
   scal_.resize(4 * (m_ + 4));
   if (!h_pinned_) NW_CUDA(cudaMallocHost(&h_pinned_, sizeof(double) * 4 * 1024));
+  // sliced-ELL layout from the host CSR
+  sell_slices_ = 0;
+  if (A.row_ptr_host && A.col_idx_host && n > 0) {
+    const int64_t ns = (n + 31) / 32;
+    std::vector<int64_t> off(ns + 1, 0);
+    for (int64_t sl = 0; sl < ns; ++sl) {
+      int64_t len = 0;
+      for (int64_t r = sl * 32; r < std::min(n, sl * 32 + 32); ++r)
+        len = std::max(len, A.row_ptr_host[r + 1] - A.row_ptr_host[r]);
+      off[sl + 1] = off[sl] + 32 * len;
+    }
+    if (off[ns] < (int64_t(1) << 31)) {
+      std::vector<int32_t> cols(off[ns]), map(off[ns]);
+      for (int64_t sl = 0; sl < ns; ++sl) {
+        const int64_t len = (off[sl + 1] - off[sl]) / 32;
+        for (int lane = 0; lane < 32; ++lane) {
+          const int64_t r = sl * 32 + lane;
+          for (int64_t k = 0; k < len; ++k) {
+            const int64_t q = off[sl] + 32 * k + lane;
+            const int64_t p = r < n ? A.row_ptr_host[r] + k : -1;
+            if (r < n && p < A.row_ptr_host[r + 1]) {
+              cols[q] = A.col_idx_host[p];
+              map[q] = int32_t(p);
+            } else {
+              cols[q] = int32_t(r < n ? r : 0);
+              map[q] = -1;
+            }
+          }
+        }
+      }
+      sell_off_.upload(off, s);
+      sell_cols_.upload(cols, s);
+      sell_map_.upload(map, s);
+      sell_vals_.resize(off[ns]);
+      sell_slices_ = ns;
+    }
+  }
   f32_valid_ = false;
   refresh(s);
 }
@@ -311,6 +472,9 @@ void KrylovSolver::refresh(cudaStream_t s) {
   if (A_.n == 0) return;
   rdiag_k<<<grid1(A_.n), kBlock, 0, s>>>(A_.n, A_.row_ptr, A_.col_idx,
                                           A_.values, rdiag_.p, nullptr);
+  if (sell_slices_)
+    sell_gather_k<<<grid1(int64_t(sell_vals_.n)), kBlock, 0, s>>>(
+        int64_t(sell_vals_.n), sell_map_.p, A_.values, sell_vals_.p, nullptr);
   NW_CUDA(cudaGetLastError());
   f32_valid_ = false;
 }
@@ -326,14 +490,43 @@ void KrylovSolver::ensure_f32(cudaStream_t s) {
   r32_.resize(n);
   convert_k<double, float><<<grid1(A_.nnz), kBlock, 0, s>>>(A_.nnz, A_.values,
                                                              vals32_.p);
+  if (sell_slices_) {
+    sell_vals32_.resize(sell_vals_.n);
+    sell_gather_k<<<grid1(int64_t(sell_vals_.n)), kBlock, 0, s>>>(
+        int64_t(sell_vals_.n), sell_map_.p, A_.values, sell_vals_.p, sell_vals32_.p);
+  }
   convert_k<double, float><<<grid1(n), kBlock, 0, s>>>(n, rdiag_.p, rdiag32_.p);
   NW_CUDA(cudaGetLastError());
   f32_valid_ = true;
 }
 
 void KrylovSolver::spmv(const double* x, double* y, cudaStream_t s) const {
-  spmv_launch<double, double, double>(A_.lanes, A_.n, A_.row_ptr, A_.col_idx,
-                                      A_.values, x, nullptr, y, s);
+  spmv64(x, nullptr, y, s);
+}
+
+// y = A x (b == nullptr) or y = b - A x, FP64
+void KrylovSolver::spmv64(const double* x, const double* b, double* y,
+                          cudaStream_t s) const {
+  if (sell_slices_) {
+    const int64_t threads = sell_slices_ * 32;
+    sell_spmv_k<double, double, double><<<unsigned((threads + kBlock - 1) / kBlock), kBlock, 0, s>>>(
+        A_.n, sell_slices_, sell_off_.p, sell_cols_.p, sell_vals_.p, x, b, y);
+  } else {
+    spmv_launch<double, double, double>(A_.lanes, A_.n, A_.row_ptr, A_.col_idx,
+                                        A_.values, x, b, y, s);
+  }
+}
+
+// FP32 SpMV of the mixed method (FP32 values and accumulation)
+void KrylovSolver::spmv32(const float* x, float* y, cudaStream_t s) const {
+  if (sell_slices_ && sell_vals32_.n) {
+    const int64_t threads = sell_slices_ * 32;
+    sell_spmv_k<float, float, float><<<unsigned((threads + kBlock - 1) / kBlock), kBlock, 0, s>>>(
+        A_.n, sell_slices_, sell_off_.p, sell_cols_.p, sell_vals32_.p, x, nullptr, y);
+  } else {
+    spmv_launch<float, float, float>(A_.lanes, A_.n, A_.row_ptr, A_.col_idx,
+                                     vals32_.p, x, nullptr, y, s);
+  }
 }
 
 double KrylovSolver::dot(const double* a, const double* b, cudaStream_t s) {
@@ -427,29 +620,35 @@ SolveResult KrylovSolver::gmres(const nw_solver_cfg& cfg, double tol,
   bool done = false;
   double* hs = scal_.p;             // h (m+1)
   double* h2 = scal_.p + (m_ + 2);  // second-pass h, then norm
+  // Jacobi fuses into the normalisation that produces each basis vector
+  const bool fuse_jacobi = pc.kind == NW_PC_JACOBI;
   while (!done && its < cfg.max_iterations) {
-    // V0 = r / beta
+    // V0 = r / beta (and z0 = D^-1 V0)
     NW_CUDA(cudaMemcpyAsync(h2, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
-    scale_by_norm_k<double><<<grid1(n), kBlock, 0, s>>>(n, r_.p, V, h2);
+    scale_jacobi_k<double><<<grid1(n), kBlock, 0, s>>>(
+        n, r_.p, V, h2, fuse_jacobi ? rdiag_.p : nullptr, flexible ? Z_.p : z_.p);
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int j = 0;
     for (; j < m && its < cfg.max_iterations; ++j) {
       double* vj = V + size_t(j) * n;
       double* zj = flexible ? Z_.p + size_t(j) * n : z_.p;
-      apply_precond(pc, vj, zj, s);
+      if (!fuse_jacobi) apply_precond(pc, vj, zj, s);
       spmv(zj, w_.p, s);
       // two classical Gram-Schmidt passes, coefficients kept on the device
       mdot_k<double><<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, n, w_.p, partial_.p);
       reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, hs, 0, nullptr);
-      maxpy_k<double><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, hs, w_.p);
+      maxpy_k<double><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, hs, w_.p, nullptr);
       mdot_k<double><<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, n, w_.p, partial_.p);
       reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, h2 + 1, 1, hs);
-      maxpy_k<double><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, h2 + 1, w_.p);
-      mdot_k<double><<<red_blocks_, kBlock, 0, s>>>(n, 1, w_.p, 0, w_.p, partial_.p);
-      reduce_partials_k<<<1, kBlock, 0, s>>>(red_blocks_, partial_.p, h2, 0, nullptr);
+      maxpy_k<double><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, h2 + 1, w_.p, partial_.p);
+      reduce_partials_k<<<1, kBlock, 0, s>>>(int(grid1(n)), partial_.p, h2, 0, nullptr);
       sqrt_scalar_k<<<1, 1, 0, s>>>(h2);
-      scale_by_norm_k<double><<<grid1(n), kBlock, 0, s>>>(n, w_.p, V + size_t(j + 1) * n, h2);
+      {
+        double* znext = (j + 1 < m) ? (flexible ? Z_.p + size_t(j + 1) * n : z_.p) : nullptr;
+        scale_jacobi_k<double><<<grid1(n), kBlock, 0, s>>>(
+            n, w_.p, V + size_t(j + 1) * n, h2, (fuse_jacobi && znext) ? rdiag_.p : nullptr, znext);
+      }
       NW_CUDA(cudaGetLastError());
       NW_CUDA(cudaMemcpyAsync(h_pinned_, hs, sizeof(double) * (j + 1),
                               cudaMemcpyDeviceToHost, s));
@@ -512,13 +711,11 @@ SolveResult KrylovSolver::gmres(const nw_solver_cfg& cfg, double tol,
       NW_CUDA(cudaGetLastError());
     }
     if (done || its >= cfg.max_iterations) break;
-    spmv_launch<double, double, double>(A_.lanes, n, A_.row_ptr, A_.col_idx,
-                                        A_.values, x, b, r_.p, s);
+    spmv64(x, b, r_.p, s);
     beta = std::sqrt(dot(r_.p, r_.p, s));
     if (beta == 0.0) break;
   }
-  spmv_launch<double, double, double>(A_.lanes, n, A_.row_ptr, A_.col_idx,
-                                      A_.values, x, b, r_.p, s);
+  spmv64(x, b, r_.p, s);
   res.final_abs = std::sqrt(dot(r_.p, r_.p, s));
   res.final_rel = rel;
   res.iterations = its;
@@ -575,8 +772,7 @@ SolveResult KrylovSolver::cg(const nw_solver_cfg& cfg, double tol,
     rz = rzn;
     xpby_k<<<grid1(n), kBlock, 0, s>>>(n, z, beta, p);
   }
-  spmv_launch<double, double, double>(A_.lanes, n, A_.row_ptr, A_.col_idx,
-                                      A_.values, x, b, r, s);
+  spmv64(x, b, r, s);
   res.final_abs = std::sqrt(dot(r, r, s));
   res.final_rel = rel;
   res.iterations = its;
@@ -611,6 +807,7 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
     return res;
   }
   std::vector<double> H(size_t(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+  const bool fuse_jacobi = pc.kind == NW_PC_JACOBI;
   float* V = V32_.p;
   double* hs = scal_.p;
   double* h2 = scal_.p + (m_ + 2);
@@ -621,28 +818,28 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
   while (its < cfg.max_iterations) {
     ++outer;
     // inner: solve A d = r (scaled) in FP32
-    convert_k<double, float><<<grid1(n), kBlock, 0, s>>>(n, r_.p, r32_.p);
     NW_CUDA(cudaMemcpyAsync(h2, &rnorm, sizeof(double), cudaMemcpyHostToDevice, s));
-    scale_by_norm_k<float><<<grid1(n), kBlock, 0, s>>>(n, r32_.p, V, h2);
+    scale_to_f32_k<<<grid1(n), kBlock, 0, s>>>(n, r_.p, V, h2);
+    if (fuse_jacobi) jacobi_k<float><<<grid1(n), kBlock, 0, s>>>(n, rdiag32_.p, V, z32_.p);
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = 1.0;  // inner system solved for r / ||r||
     int j = 0;
     for (; j < m && its < cfg.max_iterations; ++j) {
       float* vj = V + size_t(j) * n;
-      precond_apply_t<float, float>(pc, n, A_.row_ptr, A_.col_idx, vals32_.p,
-                                    rdiag32_.p, vj, z32_.p, s);
-      spmv_launch<float, float, float>(A_.lanes, n, A_.row_ptr, A_.col_idx,
-                                       vals32_.p, z32_.p, nullptr, w32_.p, s);
+      if (!fuse_jacobi)
+        precond_apply_t<float, float>(pc, n, A_.row_ptr, A_.col_idx, vals32_.p,
+                                      rdiag32_.p, vj, z32_.p, s);
+      spmv32(z32_.p, w32_.p, s);
       mdot_k<float><<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, n, w32_.p, partial_.p);
       reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, hs, 0, nullptr);
-      maxpy_k<float><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, hs, w32_.p);
+      maxpy_k<float><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, hs, w32_.p, nullptr);
       mdot_k<float><<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, n, w32_.p, partial_.p);
       reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, h2 + 1, 1, hs);
-      maxpy_k<float><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, h2 + 1, w32_.p);
-      mdot_k<float><<<red_blocks_, kBlock, 0, s>>>(n, 1, w32_.p, 0, w32_.p, partial_.p);
-      reduce_partials_k<<<1, kBlock, 0, s>>>(red_blocks_, partial_.p, h2, 0, nullptr);
+      maxpy_k<float><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, h2 + 1, w32_.p, partial_.p);
+      reduce_partials_k<<<1, kBlock, 0, s>>>(int(grid1(n)), partial_.p, h2, 0, nullptr);
       sqrt_scalar_k<<<1, 1, 0, s>>>(h2);
-      scale_by_norm_k<float><<<grid1(n), kBlock, 0, s>>>(n, w32_.p, V + size_t(j + 1) * n, h2);
+      scale_jacobi_k<float><<<grid1(n), kBlock, 0, s>>>(n, w32_.p, V + size_t(j + 1) * n, h2,
+                                                        fuse_jacobi ? rdiag32_.p : nullptr, z32_.p);
       NW_CUDA(cudaGetLastError());
       NW_CUDA(cudaMemcpyAsync(h_pinned_, hs, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
       NW_CUDA(cudaMemcpyAsync(h_pinned_ + (j + 1), h2, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -690,8 +887,7 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
       add_f32_k<<<grid1(n), kBlock, 0, s>>>(n, z32_.p, x);
     }
     // outer FP64 true residual
-    spmv_launch<double, double, double>(A_.lanes, n, A_.row_ptr, A_.col_idx,
-                                        A_.values, x, b, r_.p, s);
+    spmv64(x, b, r_.p, s);
     rnorm = std::sqrt(dot(r_.p, r_.p, s));
     rel = rnorm / bnorm;
     if (!std::isfinite(rel)) {

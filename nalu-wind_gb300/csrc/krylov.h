@@ -19,7 +19,10 @@ struct DevCsr {
   const int64_t* row_ptr = nullptr;
   const int32_t* col_idx = nullptr;
   const double* values = nullptr;
-  int lanes = 8;  // sub-warp width per row for the SpMV
+  int lanes = 8;  // sub-warp width per row for the CSR kernels
+  // host copies of the graph (setup only: builds the sliced-ELL layout)
+  const int64_t* row_ptr_host = nullptr;
+  const int32_t* col_idx_host = nullptr;
 };
 
 // Preconditioner applied inside the solver (right preconditioning).
@@ -60,6 +63,8 @@ class KrylovSolver {
 
   // Building blocks (device vectors of length n).
   void spmv(const double* x, double* y, cudaStream_t s) const;
+  void spmv64(const double* x, const double* b, double* y, cudaStream_t s) const;
+  void spmv32(const float* x, float* y, cudaStream_t s) const;
   void apply_precond(const Precond& pc, const double* x, double* y,
                      cudaStream_t s);
   double dot(const double* a, const double* b, cudaStream_t s);
@@ -83,6 +88,14 @@ class KrylovSolver {
   DeviceArray<double> partial_; // deterministic reduction partials
   DeviceArray<double> scal_;    // small device scalars
   double* h_pinned_ = nullptr;  // host mirror of scal_
+  // Sliced ELLPACK copy (slices of 32 rows, column-major within a slice)
+  // used by the solver's SpMV: coalesced value/column loads for short rows.
+  // sell_map_ holds the CSR index of every slot (-1 for padding).
+  DeviceArray<int64_t> sell_off_;
+  DeviceArray<int32_t> sell_cols_, sell_map_;
+  DeviceArray<double> sell_vals_;
+  DeviceArray<float> sell_vals32_;
+  int64_t sell_slices_ = 0;
   // FP32 copies for the inner solve of the mixed method
   DeviceArray<float> vals32_, rdiag32_, V32_, w32_, z32_, r32_;
   bool f32_valid_ = false;

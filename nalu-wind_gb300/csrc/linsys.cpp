@@ -201,6 +201,8 @@ nw_status nw_linsys_set_solver_cfg(nw_linsys* ls, const nw_solver_cfg* cfg) {
       A.col_idx = ls->col_idx.p;
       A.values = ls->values.p;
       A.lanes = ls->num_dof == 1 ? 8 : 32;
+      A.row_ptr_host = ls->g.row_ptr.data();
+      A.col_idx_host = ls->g.col_idx.data();
       ls->solver.setup(A, std::max(ls->cfg.kspace, ls->cfg.inner_kspace), ls->stream);
     }
   });
@@ -284,6 +286,8 @@ nw_status nw_linsys_finalize(nw_linsys* ls) {
     A.col_idx = ls->col_idx.p;
     A.values = ls->values.p;
     A.lanes = nd == 1 ? 8 : 32;
+    A.row_ptr_host = g.row_ptr.data();
+    A.col_idx_host = g.col_idx.data();
     ls->solver.setup(A, std::max(ls->cfg.kspace, ls->cfg.inner_kspace), s);
     NW_CUDA(cudaStreamSynchronize(s));
     ls->finalized = true;
@@ -599,6 +603,7 @@ nw_status nw_linsys_spmv(nw_linsys* ls, const double* x, double* y) {
     need_finalized(ls);
     if (!x || !y) fail(NW_INVALID_ARG, "null vector");
     materialize_zero(ls);
+    ls->solver.refresh(ls->stream);  // values may have changed since the last solve
     ls->solver.spmv(x, y, ls->stream);
     NW_CUDA(cudaGetLastError());
   });
