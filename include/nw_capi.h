@@ -80,6 +80,7 @@ typedef struct nw_solve_report {
   double final_abs_residual;  /* explicit ||b - A x||_2 in FP64 */
   double rhs_norm;            /* ||b||_2 (nonLinearResidual / l2Scaling) */
   double solve_ms;            /* device time of the solve */
+  int fallback;               /* learned preconditioner failed; SGS result */
 } nw_solve_report;
 
 /* SolutionOptions numerics of ScalarEdgeSolverAlg::execute
@@ -269,6 +270,66 @@ nw_status nw_linsys_precond_apply(nw_linsys* ls, int preconditioner,
 /* Row order used by the multicolour SGS (host, nrows): rows of colour 0 in
  * ascending order, then colour 1, ... */
 nw_status nw_linsys_sgs_order(nw_linsys* ls, int64_t* order, int* ncolors);
+
+/* ---- learned preconditioner (NW_PC_LEARNED). No counterpart in the
+ * reference: nalu-wind's preconditioners are Ifpack2 relaxations and MueLu
+ * (src/LinearSolverConfig.C:89-121). M(v) = z1 + P Net(R (v - A z1)) with
+ * z1 one multicolour SGS sweep, R / P over plain aggregates, and Net a
+ * 4-layer, 64-channel edge message-passing network (BF16, FP32
+ * accumulation) acting as the coarse solver; applied inside FGMRES, with
+ * SGS as fallback when the flexible solve fails. ---- */
+typedef struct nw_learned nw_learned;
+/* Network with seeded random weights (device resident). */
+nw_status nw_learned_create(uint64_t seed, nw_learned** out);
+nw_status nw_learned_destroy(nw_learned* net);
+/* Weight file: magic, shapes, Adam step, FP32 weights, FNV-1a checksum. */
+nw_status nw_learned_save(nw_learned* net, const char* path);
+nw_status nw_learned_load(nw_learned* net, const char* path);
+/* Host copy of the flat FP32 parameters (get when out != NULL, then set
+ * when in != NULL). n must equal nw_learned_num_params(). */
+int64_t nw_learned_num_params(void);
+nw_status nw_learned_params(nw_learned* net, float* out, const float* in,
+                            int64_t n);
+/* Build the aggregation / coarse level of this system's graph (num_dof 1)
+ * and use `net` for NW_PC_LEARNED solves of this handle. */
+nw_status nw_linsys_attach_learned(nw_linsys* ls, nw_learned* net);
+/* Coarse level of an attached handle, refreshed from the current values
+ * (host arrays; NULL entries skipped). */
+nw_status nw_linsys_coarse_sizes(nw_linsys* ls, int64_t* nc, int64_t* nnzc);
+nw_status nw_linsys_coarse_graph(nw_linsys* ls, int32_t* agg, int64_t* cptr,
+                                 int32_t* ccol, float* wgt, float* dinv);
+/* Harvest (residual, error) pairs from the handle's assembled system:
+ * x* from a tight mixed-precision solve, then `restarts` cycles of plain
+ * FP64 Jacobi-GMRES(kspace) from x0 = 0, one pair per restart. Stored on
+ * the device as the coarse residual R (r - A z1) with the energy norms
+ * ||e||_A^2 and ||e - z1||_A^2 of the error e = x* - x. */
+nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts,
+                             int kspace, int* total_pairs);
+nw_status nw_learned_clear_data(nw_learned* net);
+/* Adam training over the harvested pairs (`epochs` passes), on the graph
+ * of `ls`; loss = ||z1 + P e_c - e||_A^2 / ||e||_A^2 (the A-norm error
+ * left after the smoothing sweep and the coarse correction), mean over
+ * the last epoch in *loss. */
+nw_status nw_learned_train(nw_learned* net, nw_linsys* ls, int epochs,
+                           int batch, double lr, uint64_t shuffle_seed,
+                           double* loss);
+/* Mean loss over the harvested pairs, parameters unchanged. */
+nw_status nw_learned_evaluate(nw_learned* net, nw_linsys* ls, double* loss);
+/* One pair through forward and backward on the coarse level of `ls`
+ * (device rc of length nc, ea = ||e||_A^2, ca = ||e - z1||_A^2): the loss
+ * (e_c' Ac e_c - 2 e_c' rc + ca) / ea and its parameter gradient (host). */
+nw_status nw_learned_loss_grad(nw_learned* net, nw_linsys* ls, const float* rc,
+                               double ea, double ca, double* loss, float* grad);
+/* Coarse correction ec = Net(rc) (device vectors of length nc). */
+nw_status nw_learned_forward(nw_learned* net, nw_linsys* ls, const float* rc,
+                             float* ec);
+/* The network's BF16 tensor-core GEMMs on device buffers (testing):
+ * kind 0: out_bf16[m x 64] = relu(a_bf16[m x 128] b), b given transposed
+ *         (64 x 128); kind 1: out_f32[m x 128] = a_bf16[m x 64] b^T, b
+ *         row-major 128 x 64; kind 2: out_f32[128 x 64] = a_bf16[m x 128]^T
+ *         b_bf16[m x 64]. */
+nw_status nw_gemm_bf16(int kind, int64_t m, const void* a, const void* b,
+                       void* out);
 
 /* ---- timing helpers (CUDA events on the handle's stream) ---- */
 nw_status nw_linsys_sync(nw_linsys* ls);

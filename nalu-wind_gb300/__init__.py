@@ -44,7 +44,7 @@ class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int), ("outer_iterations", C.c_int), ("status", C.c_int),
                 ("converged", C.c_int), ("final_rel_residual", C.c_double),
                 ("final_abs_residual", C.c_double), ("rhs_norm", C.c_double),
-                ("solve_ms", C.c_double)]
+                ("solve_ms", C.c_double), ("fallback", C.c_int)]
 
 
 class ScalarOpts(C.Structure):
@@ -129,6 +129,25 @@ SIGNATURES = {
     "nw_linsys_sgs_order": (C.c_int, [C.c_void_p, _I64P, C.POINTER(C.c_int)]),
     "nw_linsys_sync": (C.c_int, [C.c_void_p]),
     "nw_linsys_last_assembly_ms": (C.c_int, [C.c_void_p, _DP]),
+    "nw_learned_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    "nw_learned_destroy": (C.c_int, [C.c_void_p]),
+    "nw_learned_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "nw_learned_load": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "nw_learned_num_params": (C.c_int64, []),
+    "nw_learned_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64]),
+    "nw_linsys_attach_learned": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "nw_linsys_coarse_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P]),
+    "nw_linsys_coarse_graph": (C.c_int, [C.c_void_p, _I32P, _I64P, _I32P, C.POINTER(C.c_float),
+                                         C.POINTER(C.c_float)]),
+    "nw_learned_harvest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "nw_learned_clear_data": (C.c_int, [C.c_void_p]),
+    "nw_learned_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_uint64,
+                                   C.POINTER(C.c_double)]),
+    "nw_learned_evaluate": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "nw_learned_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                       C.POINTER(C.c_double), C.POINTER(C.c_float)]),
+    "nw_learned_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "nw_gemm_bf16": (C.c_int, [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "nw_mesh_box": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(BoxOpts), C.POINTER(C.c_void_p)]),
     "nw_mesh_destroy": (C.c_int, [C.c_void_p]),
     "nw_mesh_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P, _I64P, C.POINTER(C.c_int)]),
@@ -324,10 +343,98 @@ class LinearSystem:
     def sync(self) -> None:
         check(self.lib.nw_linsys_sync(self.h))
 
+    # -- learned preconditioner
+    def attach_learned(self, net: "Learned") -> None:
+        check(self.lib.nw_linsys_attach_learned(self.h, net.h))
+        self._learned = net  # keep alive
+
+    def coarse_graph(self) -> dict:
+        nc, nnzc = C.c_int64(), C.c_int64()
+        check(self.lib.nw_linsys_coarse_sizes(self.h, C.byref(nc), C.byref(nnzc)))
+        nr, _ = self.sizes()
+        agg = np.zeros(nr, np.int32)
+        cptr = np.zeros(nc.value + 1, np.int64)
+        ccol = np.zeros(nnzc.value, np.int32)
+        wgt = np.zeros(nnzc.value, np.float32)
+        dinv = np.zeros(nc.value, np.float32)
+        check(self.lib.nw_linsys_coarse_graph(self.h, _ptr(agg, C.c_int32), _ptr(cptr, C.c_int64),
+                                              _ptr(ccol, C.c_int32), _ptr(wgt, C.c_float),
+                                              _ptr(dinv, C.c_float)))
+        return dict(nc=nc.value, agg=agg, cptr=cptr, ccol=ccol, wgt=wgt, dinv=dinv)
+
     def last_assembly_ms(self) -> float:
         ms = C.c_double()
         check(self.lib.nw_linsys_last_assembly_ms(self.h, C.byref(ms)))
         return ms.value
+
+
+class Learned:
+    """Learned two-level preconditioner network (NW_PC_LEARNED)."""
+
+    def __init__(self, seed: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.nw_learned_create(seed, C.byref(h)))
+        self.h = h
+        self.num_params = int(self.lib.nw_learned_num_params())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nw_learned_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        check(self.lib.nw_learned_params(self.h, _ptr(out, C.c_float), None, self.num_params))
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        check(self.lib.nw_learned_params(self.h, None, _ptr(p, C.c_float), self.num_params))
+
+    def save(self, path) -> None:
+        check(self.lib.nw_learned_save(self.h, str(path).encode()))
+
+    def load(self, path) -> None:
+        check(self.lib.nw_learned_load(self.h, str(path).encode()))
+
+    def harvest(self, ls: "LinearSystem", restarts: int, kspace: int = 30) -> int:
+        n = C.c_int()
+        check(self.lib.nw_learned_harvest(self.h, ls.h, restarts, kspace, C.byref(n)))
+        return n.value
+
+    def clear_data(self) -> None:
+        check(self.lib.nw_learned_clear_data(self.h))
+
+    def train(self, ls: "LinearSystem", epochs: int, batch: int = 8, lr: float = 1e-3, seed: int = 0) -> float:
+        loss = C.c_double()
+        check(self.lib.nw_learned_train(self.h, ls.h, epochs, batch, lr, seed, C.byref(loss)))
+        return loss.value
+
+    def evaluate(self, ls: "LinearSystem") -> float:
+        loss = C.c_double()
+        check(self.lib.nw_learned_evaluate(self.h, ls.h, C.byref(loss)))
+        return loss.value
+
+    def loss_grad(self, ls: "LinearSystem", rc_dev, ea: float, ca: float):
+        loss = C.c_double()
+        g = np.zeros(self.num_params, np.float32)
+        check(self.lib.nw_learned_loss_grad(self.h, ls.h, dptr(rc_dev), ea, ca, C.byref(loss),
+                                            _ptr(g, C.c_float)))
+        return loss.value, g
+
+    def forward(self, ls: "LinearSystem", rc_dev, ec_dev) -> None:
+        check(self.lib.nw_learned_forward(self.h, ls.h, dptr(rc_dev), dptr(ec_dev)))
+
+
+def gemm_bf16(kind: int, m: int, a_dev, b_dev, out_dev) -> None:
+    check(load().nw_gemm_bf16(kind, m, dptr(a_dev), dptr(b_dev), dptr(out_dev)))
 
 
 class Mesh:

@@ -30,6 +30,7 @@
 #include <cstring>
 
 #include "krylov.h"
+#include "learned.h"
 
 namespace nw {
 namespace {
@@ -367,6 +368,17 @@ __global__ void convert_k(int64_t n, const A* __restrict__ a, B* __restrict__ b)
   if (i < n) b[i] = B(a[i]);
 }
 
+// y = a - y (FP32)
+__global__ void rsub_f32_k(int64_t n, const float* __restrict__ a, float* __restrict__ y) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a[i] - y[i];
+}
+// y += a (FP32)
+__global__ void add32_k(int64_t n, const float* __restrict__ a, float* __restrict__ y) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += a[i];
+}
+
 // x += alpha * y (FP64)
 __global__ void axpy_k(int64_t n, double alpha, const double* __restrict__ y,
                        double* __restrict__ x) {
@@ -475,6 +487,7 @@ void KrylovSolver::refresh(cudaStream_t s) {
   if (sell_slices_)
     sell_gather_k<<<grid1(int64_t(sell_vals_.n)), kBlock, 0, s>>>(
         int64_t(sell_vals_.n), sell_map_.p, A_.values, sell_vals_.p, nullptr);
+  if (cl_) cl_->refresh(A_.values, s);
   NW_CUDA(cudaGetLastError());
   f32_valid_ = false;
 }
@@ -570,11 +583,54 @@ void precond_apply_t(const Precond& pc, int64_t n, const int64_t* rp,
 
 }  // namespace
 
+// FP32 preconditioner of the mixed method. Learned (two-level, symmetric
+// smoothing): z1 = SGS(x), r1 = x - A z1, z2 = z1 + P Net(R r1), then the
+// post-smoothing z = z2 + SGS(x - A z2).
+void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
+                             cudaStream_t s) {
+  const int64_t n = A_.n;
+  if (pc.kind != NW_PC_LEARNED) {
+    precond_apply_t<float, float>(pc, n, A_.row_ptr, A_.col_idx, vals32_.p,
+                                  rdiag32_.p, x, y, s);
+    return;
+  }
+  if (!has_learned()) fail(NW_INVALID_ARG, "no learned preconditioner attached");
+  Precond sgs = pc;
+  sgs.kind = NW_PC_SGS;
+  precond_apply_t<float, float>(sgs, n, A_.row_ptr, A_.col_idx, vals32_.p,
+                                rdiag32_.p, x, y, s);
+  tmp32_.resize(n);
+  rc32_.resize(cl_->nc);
+  ec32_.resize(cl_->nc);
+  spmv32(y, tmp32_.p, s);
+  rsub_f32_k<<<grid1(n), kBlock, 0, s>>>(n, x, tmp32_.p);
+  launch_restrict(*cl_, tmp32_.p, rc32_.p, s);
+  net_->forward(*cl_, cl_->wgt.p, cl_->dinv.p, rc32_.p, ec32_.p, s);
+  launch_prolong_add(*cl_, ec32_.p, y, s);
+  post32_.resize(n);
+  spmv32(y, tmp32_.p, s);
+  rsub_f32_k<<<grid1(n), kBlock, 0, s>>>(n, x, tmp32_.p);
+  precond_apply_t<float, float>(sgs, n, A_.row_ptr, A_.col_idx, vals32_.p,
+                                rdiag32_.p, tmp32_.p, post32_.p, s);
+  add32_k<<<grid1(n), kBlock, 0, s>>>(n, post32_.p, y);
+  NW_CUDA(cudaGetLastError());
+}
+
 void KrylovSolver::apply_precond(const Precond& pc, const double* x, double* y,
                                  cudaStream_t s) {
   if (pc.kind == NW_PC_LEARNED) {
-    if (!pc.apply_fn) fail(NW_INVALID_ARG, "learned preconditioner not set");
-    pc.apply_fn(x, y, s);
+    if (pc.apply_fn) {
+      pc.apply_fn(x, y, s);
+      return;
+    }
+    // FP64 interface around the FP32 learned preconditioner
+    ensure_f32(s);
+    const int64_t n = A_.n;
+    tmp32b_.resize(n);
+    convert_k<double, float><<<grid1(n), kBlock, 0, s>>>(n, x, tmp32b_.p);
+    z32_.resize(n);
+    precond32(pc, tmp32b_.p, z32_.p, s);
+    convert_k<float, double><<<grid1(n), kBlock, 0, s>>>(n, z32_.p, y);
     return;
   }
   precond_apply_t<double, double>(pc, A_.n, A_.row_ptr, A_.col_idx, A_.values,
@@ -584,10 +640,31 @@ void KrylovSolver::apply_precond(const Precond& pc, const double* x, double* y,
 SolveResult KrylovSolver::solve(const nw_solver_cfg& cfg, double tol,
                                 const Precond& pc, const double* b, double* x,
                                 cudaStream_t s) {
-  if (cfg.precision == NW_PREC_MIXED) return mixed(cfg, tol, pc, b, x, s);
-  if (cfg.method == NW_CG) return cg(cfg, tol, pc, b, x, s);
-  return gmres(cfg, tol, pc, b, x,
-               cfg.method == NW_FGMRES || pc.kind == NW_PC_LEARNED, s);
+  SolveResult r;
+  if (cfg.precision == NW_PREC_MIXED)
+    r = mixed(cfg, tol, pc, b, x, s);
+  else if (cfg.method == NW_CG && pc.kind != NW_PC_LEARNED)
+    r = cg(cfg, tol, pc, b, x, s);
+  else
+    r = gmres(cfg, tol, pc, b, x, cfg.method == NW_FGMRES || pc.kind == NW_PC_LEARNED, s);
+  // The learned preconditioner is judged by the FP64 residual: if the
+  // flexible solve fails (no convergence, breakdown, non-finite values)
+  // the same solve is repeated with plain symmetric Gauss-Seidel.
+  if (pc.kind == NW_PC_LEARNED && !r.converged && std::isfinite(r.bnorm)) {
+    Precond sgs = pc;
+    sgs.kind = NW_PC_SGS;
+    const SolveResult first = r;
+    r = cfg.precision == NW_PREC_MIXED ? mixed(cfg, tol, sgs, b, x, s)
+                                       : gmres(cfg, tol, sgs, b, x, false, s);
+    r.fallback = 1;
+    r.iterations += first.iterations;
+    r.outer += first.outer;
+    // history: the failed learned attempt, then the SGS solve
+    std::vector<double> h = first.history;
+    h.insert(h.end(), r.history.begin(), r.history.end());
+    r.history.swap(h);
+  }
+  return r;
 }
 
 // Restarted right-preconditioned GMRES(m) / FGMRES(m), FP64.
@@ -808,6 +885,8 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
   }
   std::vector<double> H(size_t(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
   const bool fuse_jacobi = pc.kind == NW_PC_JACOBI;
+  const bool flexible = pc.kind == NW_PC_LEARNED;
+  if (flexible && Z32_.n < size_t(m) * n) Z32_.resize(size_t(m) * n);
   float* V = V32_.p;
   double* hs = scal_.p;
   double* h2 = scal_.p + (m_ + 2);
@@ -826,10 +905,9 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
     int j = 0;
     for (; j < m && its < cfg.max_iterations; ++j) {
       float* vj = V + size_t(j) * n;
-      if (!fuse_jacobi)
-        precond_apply_t<float, float>(pc, n, A_.row_ptr, A_.col_idx, vals32_.p,
-                                      rdiag32_.p, vj, z32_.p, s);
-      spmv32(z32_.p, w32_.p, s);
+      float* zj = flexible ? Z32_.p + size_t(j) * n : z32_.p;
+      if (!fuse_jacobi) precond32(pc, vj, zj, s);
+      spmv32(zj, w32_.p, s);
       mdot_k<float><<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, n, w32_.p, partial_.p);
       reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, hs, 0, nullptr);
       maxpy_k<float><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, hs, w32_.p, nullptr);
@@ -881,9 +959,12 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
     if (kk > 0) {
       for (int i = 0; i < kk; ++i) y[i] *= rnorm;
       NW_CUDA(cudaMemcpyAsync(h2, y.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
-      combine_k<float><<<grid1(n), kBlock, 0, s>>>(n, kk, V, n, h2, w32_.p);
-      precond_apply_t<float, float>(pc, n, A_.row_ptr, A_.col_idx, vals32_.p,
-                                    rdiag32_.p, w32_.p, z32_.p, s);
+      if (flexible) {
+        combine_k<float><<<grid1(n), kBlock, 0, s>>>(n, kk, Z32_.p, n, h2, z32_.p);
+      } else {
+        combine_k<float><<<grid1(n), kBlock, 0, s>>>(n, kk, V, n, h2, w32_.p);
+        precond32(pc, w32_.p, z32_.p, s);
+      }
       add_f32_k<<<grid1(n), kBlock, 0, s>>>(n, z32_.p, x);
     }
     // outer FP64 true residual

@@ -12,6 +12,9 @@
 
 namespace nw {
 
+struct LearnedNet;
+struct CoarseLevel;
+
 // A CSR matrix resident on the device (FP64 values; optional FP32 copy).
 struct DevCsr {
   int64_t n = 0;
@@ -36,6 +39,7 @@ struct Precond {
 };
 
 struct SolveResult {
+  int fallback = 0;  // learned preconditioner replaced by SGS after failing
   int iterations = 0;
   int outer = 0;
   int converged = 0;
@@ -68,6 +72,18 @@ class KrylovSolver {
   void apply_precond(const Precond& pc, const double* x, double* y,
                      cudaStream_t s);
   double dot(const double* a, const double* b, cudaStream_t s);
+  // Learned two-level preconditioner (NW_PC_LEARNED); the coarse level is
+  // refreshed from the matrix values on every refresh().
+  void attach_learned(LearnedNet* net, CoarseLevel* cl) {
+    net_ = net;
+    cl_ = cl;
+  }
+  bool has_learned() const { return net_ && cl_; }
+  void ensure_f32(cudaStream_t s);
+  // FP32 preconditioner application (Jacobi, SGS or learned) of the mixed
+  // method; y and x must not alias.
+  void precond32(const Precond& pc, const float* x, float* y, cudaStream_t s);
+  const float* vals32() const { return vals32_.p; }
 
  private:
   SolveResult gmres(const nw_solver_cfg& cfg, double tol, const Precond& pc,
@@ -77,7 +93,9 @@ class KrylovSolver {
                  const double* b, double* x, cudaStream_t s);
   SolveResult mixed(const nw_solver_cfg& cfg, double tol, const Precond& pc,
                     const double* b, double* x, cudaStream_t s);
-  void ensure_f32(cudaStream_t s);
+  LearnedNet* net_ = nullptr;
+  CoarseLevel* cl_ = nullptr;
+  DeviceArray<float> Z32_, rc32_, ec32_, tmp32_, tmp32b_, post32_;
 
   DevCsr A_;
   int m_ = 0;

@@ -1,0 +1,118 @@
+// Learned two-level preconditioner (learned.cu).
+//
+// M(v) = z1 + P Net(R (v - A z1)),  z1 = one multicolour symmetric
+// Gauss-Seidel sweep of A z = v (FP32),
+// R / P = restriction (sum) / prolongation (copy) over plain aggregates of
+// the matrix graph, and Net = a 4-layer edge message-passing network with
+// 64 channels acting as the coarse solver on the aggregate graph. The coarse
+// operator Ac = R A P (Galerkin, summed in a fixed order) supplies the edge
+// weights w_IJ = -Ac_IJ / Ac_II and the Jacobi scaling 1 / Ac_II.
+//
+// Network (BF16 weights and activations, FP32 accumulation):
+//   u = D^-1 r_c, s = rms(u), x = u / s
+//   H0 = relu([x, W x] W0)                 W0: 2 x 64
+//   Hl = relu([H(l-1), W H(l-1)] Wl)       Wl: 128 x 64, l = 1..3
+//   e_c = s * (H3 wout)                    wout: 64
+// where (W h)_I = sum_J w_IJ h_J. Trained on the GPU (forward, backward
+// and Adam kernels in learned.cu; the dense layers use mma.sync BF16 tensor
+// core instructions) over (residual, error) pairs harvested at the restarts
+// of plain Jacobi-GMRES, minimising the energy norm of the error left after
+// the smoothing and the coarse correction,
+//   L = ||z1 + P e_c - e||_A^2 / ||e||_A^2
+//     = (e_c' Ac e_c - 2 e_c' r_c + cA) / eA,
+// with r_c = R (r - A z1) = P' A (e - z1), cA = ||e - z1||_A^2 and
+// eA = ||e||_A^2 = e' r. The minimiser is the exact Galerkin coarse solve
+// e_c = Ac^-1 r_c, so the network learns to approximate it. The form
+// assumes a symmetric operator (the pressure Poisson system is).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "nw_internal.h"
+
+namespace nw {
+
+constexpr int kHid = 64;
+constexpr int kIn2 = 2 * kHid;  // concatenated [h, W h]
+// flat parameter layout: W0 (2 x 64) | W1 | W2 | W3 (128 x 64 each) | wout
+constexpr int kOffW0 = 0;
+constexpr int kOffW1 = kOffW0 + 2 * kHid;
+constexpr int kOffW2 = kOffW1 + kIn2 * kHid;
+constexpr int kOffW3 = kOffW2 + kIn2 * kHid;
+constexpr int kOffWout = kOffW3 + kIn2 * kHid;
+constexpr int kNumParams = kOffWout + kHid;
+
+// Aggregation and Galerkin structures for one fine graph (1 dof).
+struct CoarseLevel {
+  int64_t nf = 0, nc = 0, nnzc = 0;
+  std::vector<int32_t> agg_h;              // fine row -> aggregate
+  std::vector<int64_t> cptr_h;             // coarse CSR
+  std::vector<int32_t> ccol_h, cdiag_h, rev_h;
+  DeviceArray<int32_t> agg, mrows, ccol, cdiag, rev, gfine;
+  DeviceArray<int64_t> mptr, cptr, gptr;
+  DeviceArray<double> ac;                  // Galerkin values
+  DeviceArray<float> wgt, dinv;            // edge weights, 1 / Ac_II
+  void setup(const HostGraph& g, cudaStream_t s);
+  void refresh(const double* fine_values, cudaStream_t s);
+};
+
+// Activations of one forward pass on a coarse graph (sized to nc).
+struct NetWork {
+  int64_t nc = 0;
+  DeviceArray<float> u, x, ax, y, dy, ec, scal, partial, part2;
+  DeviceArray<uint16_t> xc1, xc2, xc3, h3, dz;  // BF16
+  DeviceArray<float> dxc, dh;
+  void resize(int64_t n);
+};
+
+struct LearnedNet {
+  std::vector<float> params_h;           // host master copy (save/load)
+  DeviceArray<float> params, grads, adam_m, adam_v;
+  DeviceArray<uint16_t> wbf, wtbf;       // BF16 W1..W3 (row-major) and transposes
+  DeviceArray<float> wpartial;           // weight-gradient partials
+  int64_t adam_step = 0;
+  uint64_t seed = 0;
+  // training data (coarse vectors of one aggregation)
+  int64_t data_nc = 0, data_nnzc = 0;
+  int npairs = 0, nsystems = 0;
+  std::vector<int> pair_system;
+  std::vector<double> pair_ea, pair_ca;   // ||e||_A^2, ||e - z1||_A^2
+  std::vector<DeviceArray<float>*> sys_wgt, sys_dinv, pair_rc;
+  NetWork work;
+  ~LearnedNet();
+  void init(uint64_t seed, cudaStream_t s);
+  void sync_bf16(cudaStream_t s);  // BF16 copies from the FP32 masters
+  void upload(cudaStream_t s);
+  void download(cudaStream_t s);
+  void clear_data();
+  // forward: coarse residual -> coarse correction (FP32, device)
+  void forward(const CoarseLevel& cl, const float* wgt, const float* dinv,
+               const float* rc, float* ec, cudaStream_t s);
+  // loss and parameter gradients (accumulated into grads) for one pair;
+  // returns the loss (host sync). with_grad = false: loss only.
+  double forward_backward(const CoarseLevel& cl, const float* wgt,
+                          const float* dinv, const float* rc, double ea,
+                          double ca, cudaStream_t s, bool with_grad = true);
+  void adam(double lr, double scale, cudaStream_t s);
+};
+
+// Weight file with a header and an FNV-1a checksum.
+void save_params(const std::string& path, const std::vector<float>& p, uint64_t step);
+void load_params(const std::string& path, std::vector<float>& p);
+
+// Kernel launchers used by the tests through the C ABI.
+void launch_gemm_fwd(const uint16_t* a, const uint16_t* wt, uint16_t* out,
+                     int64_t m, int ldo, cudaStream_t s);
+void launch_gemm_dx(const uint16_t* dz, const uint16_t* w, float* dx, int64_t m,
+                    cudaStream_t s);
+void launch_gemm_wgrad(const uint16_t* xc, const uint16_t* dz, float* partial,
+                       float* dw, int64_t m, cudaStream_t s);
+
+// Two-level application helpers (FP32).
+void launch_restrict(const CoarseLevel& cl, const float* r, float* rc, cudaStream_t s);
+void launch_prolong_add(const CoarseLevel& cl, const float* ec, float* z, cudaStream_t s);
+
+}  // namespace nw

@@ -9,11 +9,13 @@
 #include <cstring>
 #include <memory>
 #include <new>
+#include <numeric>
 #include <string>
 #include <vector>
 
 #include "assemble.h"
 #include "krylov.h"
+#include "learned.h"
 #include "nw_internal.h"
 
 namespace nw {
@@ -62,6 +64,12 @@ struct nw_linsys {
   std::vector<double> history;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false;
+  nw_learned* learned = nullptr;
+  std::unique_ptr<CoarseLevel> coarse;
+};
+
+struct nw_learned {
+  LearnedNet net;
 };
 
 namespace {
@@ -538,6 +546,8 @@ nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
     need_finalized(ls);
     if (!x) fail(NW_INVALID_ARG, "null solution vector");
     materialize_zero(ls);
+    if (ls->cfg.preconditioner == NW_PC_LEARNED && !ls->coarse)
+      fail(NW_INVALID_ARG, "NW_PC_LEARNED needs nw_linsys_attach_learned");
     ls->solver.refresh(ls->stream);
     ls->pc.kind = ls->cfg.preconditioner;
     const double tol = final_iter ? ls->cfg.final_tolerance : ls->cfg.tolerance;
@@ -562,6 +572,7 @@ nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
       rep->final_abs_residual = r.final_abs;
       rep->rhs_norm = r.bnorm;
       rep->solve_ms = ms;
+      rep->fallback = r.fallback;
     }
     if (r.status == NW_NAN_DETECTED) fail(NW_NAN_DETECTED, "non-finite value in the solve");
   });
@@ -673,3 +684,361 @@ PlanView plan_view(const nw_linsys* ls) {
   return v;
 }
 }  // namespace nw
+
+// ---------------------------------------------------------------------------
+// Learned preconditioner entry points.
+namespace {
+
+void need_learned(const nw_linsys* ls) {
+  need_finalized(ls);
+  if (!ls->coarse || !ls->learned)
+    fail(NW_INVALID_ARG, "no learned preconditioner attached to this system");
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t nw_learned_num_params(void) { return kNumParams; }
+
+nw_status nw_learned_create(uint64_t seed, nw_learned** out) {
+  return guard([&] {
+    if (!out) fail(NW_INVALID_ARG, "null output");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) fail(NW_NO_DEVICE, "no CUDA device");
+    NW_CUDA(cudaSetDevice(g_device));
+    auto p = std::make_unique<nw_learned>();
+    p->net.init(seed, nullptr);
+    NW_CUDA(cudaStreamSynchronize(nullptr));
+    *out = p.release();
+  });
+}
+
+nw_status nw_learned_destroy(nw_learned* net) {
+  return guard([&] { delete net; });
+}
+
+nw_status nw_learned_save(nw_learned* net, const char* path) {
+  return guard([&] {
+    if (!net || !path) fail(NW_INVALID_ARG, "null argument");
+    net->net.download(nullptr);
+    save_params(path, net->net.params_h, uint64_t(net->net.adam_step));
+  });
+}
+
+nw_status nw_learned_load(nw_learned* net, const char* path) {
+  return guard([&] {
+    if (!net || !path) fail(NW_INVALID_ARG, "null argument");
+    std::vector<float> p;
+    load_params(path, p);
+    net->net.params_h = p;
+    net->net.upload(nullptr);
+    NW_CUDA(cudaStreamSynchronize(nullptr));
+  });
+}
+
+nw_status nw_learned_params(nw_learned* net, float* out, const float* in, int64_t n) {
+  return guard([&] {
+    if (!net || n != kNumParams) fail(NW_INVALID_ARG, "parameter count mismatch");
+    if (out) {
+      net->net.download(nullptr);
+      std::memcpy(out, net->net.params_h.data(), sizeof(float) * n);
+    }
+    if (in) {
+      net->net.params_h.assign(in, in + n);
+      net->net.upload(nullptr);
+      NW_CUDA(cudaStreamSynchronize(nullptr));
+    }
+  });
+}
+
+nw_status nw_linsys_attach_learned(nw_linsys* ls, nw_learned* net) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!net) fail(NW_INVALID_ARG, "null network");
+    if (ls->num_dof != 1) fail(NW_INVALID_ARG, "the learned preconditioner needs num_dof 1");
+    if (!ls->coarse) {
+      auto cl = std::make_unique<CoarseLevel>();
+      cl->setup(ls->g, ls->stream);
+      ls->coarse = std::move(cl);
+    }
+    ls->learned = net;
+    ls->solver.attach_learned(&net->net, ls->coarse.get());
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+  });
+}
+
+nw_status nw_linsys_coarse_sizes(nw_linsys* ls, int64_t* nc, int64_t* nnzc) {
+  return guard([&] {
+    need_learned(ls);
+    if (nc) *nc = ls->coarse->nc;
+    if (nnzc) *nnzc = ls->coarse->nnzc;
+  });
+}
+
+nw_status nw_linsys_coarse_graph(nw_linsys* ls, int32_t* agg, int64_t* cptr, int32_t* ccol,
+                                 float* wgt, float* dinv) {
+  return guard([&] {
+    need_learned(ls);
+    materialize_zero(ls);
+    CoarseLevel& cl = *ls->coarse;
+    cl.refresh(ls->values.p, ls->stream);
+    if (agg) std::memcpy(agg, cl.agg_h.data(), sizeof(int32_t) * cl.nf);
+    if (cptr) std::memcpy(cptr, cl.cptr_h.data(), sizeof(int64_t) * (cl.nc + 1));
+    if (ccol) std::memcpy(ccol, cl.ccol_h.data(), sizeof(int32_t) * cl.nnzc);
+    if (wgt) NW_CUDA(cudaMemcpyAsync(wgt, cl.wgt.p, sizeof(float) * cl.nnzc, cudaMemcpyDeviceToHost, ls->stream));
+    if (dinv) NW_CUDA(cudaMemcpyAsync(dinv, cl.dinv.p, sizeof(float) * cl.nc, cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+  });
+}
+
+nw_status nw_learned_clear_data(nw_learned* net) {
+  return guard([&] {
+    if (!net) fail(NW_INVALID_ARG, "null network");
+    net->net.clear_data();
+  });
+}
+
+nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int kspace,
+                             int* total_pairs) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!net || restarts < 1 || kspace < 1) fail(NW_INVALID_ARG, "bad harvest arguments");
+    if (ls->learned != net) {
+      const nw_status st = nw_linsys_attach_learned(ls, net);
+      if (st != NW_OK) fail(st, nw_last_error_string());
+    }
+    materialize_zero(ls);
+    LearnedNet& L = net->net;
+    CoarseLevel& cl = *ls->coarse;
+    cudaStream_t s = ls->stream;
+    const int64_t n = ls->g.nrows;
+    if (L.npairs > 0 && (L.data_nc != cl.nc || L.data_nnzc != cl.nnzc))
+      fail(NW_INVALID_ARG, "harvested pairs come from a different graph; clear them first");
+    L.data_nc = cl.nc;
+    L.data_nnzc = cl.nnzc;
+    KrylovSolver& ks = ls->solver;
+    ks.refresh(s);
+    ks.ensure_f32(s);
+    Precond pc = ls->pc;
+    // x*: tight mixed-precision solve with SGS
+    DeviceArray<double> xs, x, d, r;
+    xs.resize(n);
+    x.resize(n);
+    d.resize(n);
+    r.resize(n);
+    nw_solver_cfg tight = ls->cfg;
+    tight.precision = NW_PREC_MIXED;
+    tight.kspace = std::min(50, std::max(ls->cfg.kspace, 30));
+    tight.inner_kspace = tight.kspace;
+    tight.inner_tolerance = 1e-4;
+    tight.max_iterations = 100000;
+    pc.kind = NW_PC_SGS;
+    SolveResult sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
+    if (!sr.converged) fail(NW_NOT_CONVERGED, "harvest: reference solve did not converge");
+    // system coarse weights
+    const int sys = L.nsystems++;
+    auto* w = new DeviceArray<float>();
+    auto* dv = new DeviceArray<float>();
+    w->resize(cl.nnzc);
+    dv->resize(cl.nc);
+    NW_CUDA(cudaMemcpyAsync(w->p, cl.wgt.p, sizeof(float) * cl.nnzc, cudaMemcpyDeviceToDevice, s));
+    NW_CUDA(cudaMemcpyAsync(dv->p, cl.dinv.p, sizeof(float) * cl.nc, cudaMemcpyDeviceToDevice, s));
+    L.sys_wgt.push_back(w);
+    L.sys_dinv.push_back(dv);
+    // restarted Jacobi-GMRES(kspace), one pair per restart
+    nw_solver_cfg cyc = ls->cfg;
+    cyc.precision = NW_PREC_FP64;
+    cyc.method = NW_GMRES;
+    cyc.kspace = std::min(kspace, 1000);
+    cyc.max_iterations = kspace;
+    Precond jac = ls->pc;
+    jac.kind = NW_PC_JACOBI;
+    NW_CUDA(cudaMemsetAsync(x.p, 0, n * 8, s));
+    NW_CUDA(cudaMemcpyAsync(r.p, ls->rhs.p, n * 8, cudaMemcpyDeviceToDevice, s));
+    DeviceArray<float> r32, z1, e32;
+    r32.resize(n);
+    z1.resize(n);
+    e32.resize(n);
+    std::vector<double> hbuf(n);
+    std::vector<float> h32(n), hz(n);
+    for (int k = 0; k < restarts; ++k) {
+      // pair: r, e = x* - x
+      std::vector<double> hr(n), hx(n), hxs(n);
+      NW_CUDA(cudaMemcpyAsync(hr.data(), r.p, n * 8, cudaMemcpyDeviceToHost, s));
+      NW_CUDA(cudaMemcpyAsync(hx.data(), x.p, n * 8, cudaMemcpyDeviceToHost, s));
+      NW_CUDA(cudaMemcpyAsync(hxs.data(), xs.p, n * 8, cudaMemcpyDeviceToHost, s));
+      NW_CUDA(cudaStreamSynchronize(s));
+      double rn = 0.0;
+      for (int64_t i = 0; i < n; ++i) {
+        h32[i] = float(hr[i]);
+        rn += hr[i] * hr[i];
+      }
+      if (!(rn > 0.0)) break;
+      NW_CUDA(cudaMemcpyAsync(r32.p, h32.data(), n * 4, cudaMemcpyHostToDevice, s));
+      // z1 = SGS(r), r1 = r - A z1, rc = R r1
+      Precond sg = ls->pc;
+      sg.kind = NW_PC_SGS;
+      ks.precond32(sg, r32.p, z1.p, s);
+      auto* rc = new DeviceArray<float>();
+      rc->resize(cl.nc);
+      DeviceArray<float> az;
+      az.resize(n);
+      ks.spmv32(z1.p, az.p, s);
+      NW_CUDA(cudaMemcpyAsync(hz.data(), z1.p, n * 4, cudaMemcpyDeviceToHost, s));
+      std::vector<float> haz(n);
+      NW_CUDA(cudaMemcpyAsync(haz.data(), az.p, n * 4, cudaMemcpyDeviceToHost, s));
+      NW_CUDA(cudaStreamSynchronize(s));
+      // e = x* - x; eA = e' A e = e' r; cA = (e - z1)' A (e - z1) = (e - z1)' r1
+      std::vector<float> rcv(cl.nc, 0.f);
+      std::vector<double> racc(cl.nc, 0.0);
+      double ea = 0.0, ca = 0.0;
+      for (int64_t i = 0; i < n; ++i) {
+        const double e = hxs[i] - hx[i];
+        const double r1 = double(h32[i]) - double(haz[i]);
+        ea += e * hr[i];
+        ca += (e - double(hz[i])) * r1;
+        racc[cl.agg_h[i]] += r1;
+      }
+      for (int64_t I = 0; I < cl.nc; ++I) rcv[I] = float(racc[I]);
+      NW_CUDA(cudaMemcpyAsync(rc->p, rcv.data(), cl.nc * 4, cudaMemcpyHostToDevice, s));
+      NW_CUDA(cudaStreamSynchronize(s));
+      if (ea > 0.0 && std::isfinite(ea) && std::isfinite(ca)) {
+        L.pair_rc.push_back(rc);
+        L.pair_system.push_back(sys);
+        L.pair_ea.push_back(ea);
+        L.pair_ca.push_back(std::max(ca, 0.0));
+        L.npairs++;
+      } else {
+        delete rc;
+      }
+      // next restart: d = GMRES(kspace) on A d = r; x += d; r = b - A x
+      ks.solve(cyc, 1e-300, jac, r.p, d.p, s);
+      std::vector<double> hd(n);
+      NW_CUDA(cudaMemcpyAsync(hd.data(), d.p, n * 8, cudaMemcpyDeviceToHost, s));
+      NW_CUDA(cudaStreamSynchronize(s));
+      for (int64_t i = 0; i < n; ++i) hx[i] += hd[i];
+      NW_CUDA(cudaMemcpyAsync(x.p, hx.data(), n * 8, cudaMemcpyHostToDevice, s));
+      ks.spmv64(x.p, ls->rhs.p, r.p, s);
+    }
+    NW_CUDA(cudaStreamSynchronize(s));
+    if (total_pairs) *total_pairs = L.npairs;
+  });
+}
+
+nw_status nw_learned_train(nw_learned* net, nw_linsys* ls, int epochs, int batch, double lr,
+                           uint64_t shuffle_seed, double* loss) {
+  return guard([&] {
+    need_learned(ls);
+    if (!net || epochs < 1 || batch < 1 || !(lr > 0)) fail(NW_INVALID_ARG, "bad training arguments");
+    LearnedNet& L = net->net;
+    CoarseLevel& cl = *ls->coarse;
+    if (L.npairs == 0) fail(NW_INVALID_ARG, "no harvested pairs");
+    if (L.data_nc != cl.nc || L.data_nnzc != cl.nnzc)
+      fail(NW_INVALID_ARG, "pairs were harvested on a different graph");
+    cudaStream_t s = ls->stream;
+    std::vector<int> order(L.npairs);
+    std::iota(order.begin(), order.end(), 0);
+    uint64_t st = shuffle_seed * 0x9E3779B97F4A7C15ull + 7;
+    double last = 0.0;
+    for (int ep = 0; ep < epochs; ++ep) {
+      for (int i = L.npairs - 1; i > 0; --i) {
+        st ^= st << 13;
+        st ^= st >> 7;
+        st ^= st << 17;
+        std::swap(order[i], order[int(st % uint64_t(i + 1))]);
+      }
+      double sum = 0.0;
+      int inb = 0;
+      for (int k = 0; k < L.npairs; ++k) {
+        const int p = order[k];
+        const int sys = L.pair_system[p];
+        sum += L.forward_backward(cl, L.sys_wgt[sys]->p, L.sys_dinv[sys]->p, L.pair_rc[p]->p,
+                                  L.pair_ea[p], L.pair_ca[p], s);
+        if (++inb == batch || k + 1 == L.npairs) {
+          L.adam(lr, 1.0 / inb, s);
+          inb = 0;
+        }
+      }
+      last = sum / L.npairs;
+    }
+    NW_CUDA(cudaStreamSynchronize(s));
+    if (loss) *loss = last;
+  });
+}
+
+nw_status nw_learned_evaluate(nw_learned* net, nw_linsys* ls, double* loss) {
+  return guard([&] {
+    need_learned(ls);
+    if (!net || !loss) fail(NW_INVALID_ARG, "null argument");
+    LearnedNet& L = net->net;
+    CoarseLevel& cl = *ls->coarse;
+    if (L.npairs == 0) fail(NW_INVALID_ARG, "no harvested pairs");
+    if (L.data_nc != cl.nc || L.data_nnzc != cl.nnzc)
+      fail(NW_INVALID_ARG, "pairs were harvested on a different graph");
+    double sum = 0.0;
+    for (int p = 0; p < L.npairs; ++p) {
+      const int sys = L.pair_system[p];
+      sum += L.forward_backward(cl, L.sys_wgt[sys]->p, L.sys_dinv[sys]->p, L.pair_rc[p]->p,
+                                L.pair_ea[p], L.pair_ca[p], ls->stream, false);
+    }
+    *loss = sum / L.npairs;
+  });
+}
+
+nw_status nw_learned_loss_grad(nw_learned* net, nw_linsys* ls, const float* rc, double ea,
+                               double ca, double* loss, float* grad) {
+  return guard([&] {
+    need_learned(ls);
+    if (!net || !rc || !(ea > 0)) fail(NW_INVALID_ARG, "bad arguments");
+    materialize_zero(ls);
+    LearnedNet& L = net->net;
+    CoarseLevel& cl = *ls->coarse;
+    cl.refresh(ls->values.p, ls->stream);
+    NW_CUDA(cudaMemsetAsync(L.grads.p, 0, kNumParams * 4, ls->stream));
+    const double l = L.forward_backward(cl, cl.wgt.p, cl.dinv.p, rc, ea, ca, ls->stream);
+    if (loss) *loss = l;
+    if (grad) {
+      NW_CUDA(cudaMemcpyAsync(grad, L.grads.p, kNumParams * 4, cudaMemcpyDeviceToHost, ls->stream));
+      NW_CUDA(cudaStreamSynchronize(ls->stream));
+    }
+    NW_CUDA(cudaMemsetAsync(L.grads.p, 0, kNumParams * 4, ls->stream));
+  });
+}
+
+nw_status nw_learned_forward(nw_learned* net, nw_linsys* ls, const float* rc, float* ec) {
+  return guard([&] {
+    need_learned(ls);
+    if (!net || !rc || !ec) fail(NW_INVALID_ARG, "null vector");
+    materialize_zero(ls);
+    CoarseLevel& cl = *ls->coarse;
+    cl.refresh(ls->values.p, ls->stream);
+    net->net.forward(cl, cl.wgt.p, cl.dinv.p, rc, ec, ls->stream);
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+  });
+}
+
+nw_status nw_gemm_bf16(int kind, int64_t m, const void* a, const void* b, void* out) {
+  return guard([&] {
+    if (!a || !b || !out || m < 0) fail(NW_INVALID_ARG, "bad GEMM arguments");
+    const auto* ah = static_cast<const uint16_t*>(a);
+    const auto* bh = static_cast<const uint16_t*>(b);
+    if (kind == 0) {
+      launch_gemm_fwd(ah, bh, static_cast<uint16_t*>(out), m, 64, nullptr);
+    } else if (kind == 1) {
+      launch_gemm_dx(ah, bh, static_cast<float*>(out), m, nullptr);
+    } else if (kind == 2) {
+      DeviceArray<float> part;
+      part.resize(size_t(4 * 152) * 128 * 64);
+      NW_CUDA(cudaMemsetAsync(out, 0, 128 * 64 * 4, nullptr));
+      launch_gemm_wgrad(ah, bh, part.p, static_cast<float*>(out), m, nullptr);
+      NW_CUDA(cudaStreamSynchronize(nullptr));
+    } else {
+      fail(NW_INVALID_ARG, "GEMM kind must be 0, 1 or 2");
+    }
+    NW_CUDA(cudaGetLastError());
+    NW_CUDA(cudaStreamSynchronize(nullptr));
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,194 @@
+"""Learned two-level preconditioner on the GPU, through the C ABI.
+
+Tolerances, all written against the oracle (oracle/learned_oracle.py):
+* BF16 tensor-core GEMMs vs torch FP32 matmul of the same BF16 operands:
+  FP32 outputs within 1e-5 of the sum of |products| per entry; the BF16
+  output of the forward GEMM within 2^-7 relative (one BF16 rounding step
+  after a differently ordered FP32 sum) plus 1e-5 of the |product| sum.
+* Forward output and every parameter-gradient block vs the oracle with the
+  same BF16 rounding points: relative L2 error <= 5e-3 (what remains is
+  FP32 accumulation, which can move a value across a BF16 rounding
+  boundary). Vs the pure FP64 oracle: cosine >= 0.99 and relative L2
+  error <= 0.1 per block (BF16 keeps 8 significant bits).
+"""
+import numpy as np
+import pytest
+
+from gpu_util import dev
+
+from oracle import learned_oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_tensor(a):
+    import torch
+    return torch.from_numpy(np.asarray(a, np.float32)).to(torch.bfloat16).cuda()
+
+
+@pytest.mark.parametrize("m", [37, 5003])
+def test_bf16_gemms_match_torch(nw, m):
+    import torch
+    rng = np.random.default_rng(m)
+    a = _bf16_tensor(rng.normal(size=(m, 128)))
+    wt = _bf16_tensor(rng.normal(size=(64, 128)) * 0.1)
+    out = torch.empty((m, 64), dtype=torch.bfloat16, device="cuda")
+    nw.gemm_bf16(0, m, a, wt, out)
+    ref = (a.float() @ wt.float().T)
+    scale = (a.float().abs() @ wt.float().abs().T)
+    err = (out.float() - torch.relu(ref)).abs()
+    assert bool((err <= 2.0 ** -7 * ref.abs() + 1e-5 * scale).all())
+
+    dz = _bf16_tensor(rng.normal(size=(m, 64)))
+    w = _bf16_tensor(rng.normal(size=(128, 64)) * 0.1)
+    dx = torch.empty((m, 128), dtype=torch.float32, device="cuda")
+    nw.gemm_bf16(1, m, dz, w, dx)
+    ref = dz.float() @ w.float().T
+    assert bool(((dx - ref).abs() <= 1e-5 * (dz.float().abs() @ w.float().abs().T) + 1e-30).all())
+
+    dw = torch.empty((128, 64), dtype=torch.float32, device="cuda")
+    nw.gemm_bf16(2, m, a, dz, dw)
+    ref = a.float().T @ dz.float()
+    assert bool(((dw - ref).abs() <= 1e-5 * (a.float().abs().T @ dz.float().abs()) + 1e-30).all())
+
+
+def _poisson(nw, shape, seed=3, stretch=1.04, jitter=0.0, rhs_seed=None):
+    case = nw.workload.poisson_case(*shape, seed=seed, stretch=stretch, jitter=jitter)
+    mesh = case.mesh
+    ls = nw.LinearSystem(1)
+    ls.build_edge_graph(mesh.num_nodes, mesh.edges)
+    ls.finalize()
+    nd = case.node
+    d = {k: dev(v) for k, v in dict(coords=mesh.coords, velocity=nd["velocity"], dpdx=nd["dpdx"],
+                                     density=nd["density"], pressure=nd["pressure"], udiag=nd["udiag"],
+                                     area=mesh.area).items()}
+    ls.zero_system()
+    ls.assemble_continuity(nw.ContinuityFields(*(d[k].data_ptr() for k in (
+        "coords", "velocity", "dpdx", "density", "pressure", "udiag", "area"))), case.opts["continuity"])
+    rhs = case.extra["rhs"]
+    if rhs_seed is not None:
+        rhs = np.random.default_rng(rhs_seed).normal(size=rhs.shape)
+        rhs -= rhs.mean()
+    ls.from_host(rhs=rhs)
+    return ls
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _blocks(g):
+    H = lo.H
+    o = [0, 2 * H, 2 * H + 2 * H * H, 2 * H + 4 * H * H, 2 * H + 6 * H * H, len(g)]
+    return [g[o[i]:o[i + 1]] for i in range(5)]
+
+
+def test_forward_and_gradient_match_oracle(nw):
+    import torch
+    ls = _poisson(nw, (14, 12, 10))
+    net = nw.Learned(seed=5)
+    ls.attach_learned(net)
+    cg = ls.coarse_graph()
+    nc = cg["nc"]
+    rng = np.random.default_rng(11)
+    # a fresh network's output layer is zero (no gradient reaches the
+    # hidden layers): check with every layer random
+    H = lo.H
+    net.set_params(np.concatenate([rng.uniform(-1.7, 1.7, 2 * H), rng.uniform(-0.2, 0.2, 6 * H * H),
+                                   rng.uniform(-0.2, 0.2, H)]).astype(np.float32))
+    rc = rng.normal(size=nc).astype(np.float32)
+    ea, ca = 40.0, 25.0
+    rc_d = dev(rc)
+    ec_d = torch.zeros(nc, dtype=torch.float32, device="cuda")
+    net.forward(ls, rc_d, ec_d)
+    L, g = net.loss_grad(ls, rc_d, ea, ca)
+    p = net.params().astype(np.float64)
+    Lb, gb, ecb = lo.loss_and_grad(p, cg, rc, ea, ca, bf16_points=True)
+    Lf, gf, ecf = lo.loss_and_grad(p, cg, rc, ea, ca)
+    ec = ec_d.cpu().numpy().astype(np.float64)
+    assert _rel(ec, ecb) <= 5e-3
+    assert _rel(ec, ecf) <= 0.1
+    Ac = lo.coarse_operator(cg)
+    lscale = (np.abs(ecb) @ np.abs(Ac) @ np.abs(ecb) + 2 * np.abs(ecb) @ np.abs(rc) + ca) / ea
+    assert abs(L - Lb) <= 5e-3 * lscale
+    for blk, (a, b, f) in enumerate(zip(_blocks(g.astype(np.float64)), _blocks(gb), _blocks(gf))):
+        assert _rel(a, b) <= 5e-3, (blk, _rel(a, b))
+        cos = float(a @ f / (np.linalg.norm(a) * np.linalg.norm(f)))
+        assert cos >= 0.99 and _rel(a, f) <= 0.1, (blk, cos, _rel(a, f))
+
+
+def test_weight_file_roundtrip_and_corruption(nw, tmp_path):
+    net = nw.Learned(seed=1)
+    p = net.params()
+    path = tmp_path / "w.bin"
+    net.save(path)
+    other = nw.Learned(seed=2)
+    assert not np.array_equal(other.params(), p)
+    other.load(path)
+    np.testing.assert_array_equal(other.params(), p)
+    raw = bytearray(path.read_bytes())
+    bad = tmp_path / "bad.bin"
+    raw[100] ^= 0x40
+    bad.write_bytes(bytes(raw))
+    with pytest.raises(nw.NwError, match="checksum"):
+        other.load(bad)
+    bad.write_bytes(path.read_bytes()[:1000])
+    with pytest.raises(nw.NwError, match="truncated"):
+        other.load(bad)
+    bad.write_bytes(b"XXXXXXXX" + path.read_bytes()[8:])
+    with pytest.raises(nw.NwError, match="not a network weight file"):
+        other.load(bad)
+    np.testing.assert_array_equal(other.params(), p)  # failed loads change nothing
+
+
+def _solve(nw, ls, pc, method, tol=1e-8):
+    import torch
+    ls.set_solver_cfg(nw.solver_cfg(method=method, preconditioner=pc, precision=nw.PREC_MIXED, kspace=30,
+                                    inner_kspace=30, max_iterations=20000, tolerance=tol))
+    nr, _ = ls.sizes()
+    x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    # FP64-verified residual
+    vals, rhs = ls.to_host()
+    rp, ci = ls.graph()
+    xh = x.cpu().numpy()
+    ax = np.add.reduceat(vals * xh[ci], rp[:-1]) if len(vals) else np.zeros(nr)
+    true_rel = np.linalg.norm(rhs - ax) / np.linalg.norm(rhs)
+    return rep, true_rel
+
+
+def test_training_reduces_loss_and_speeds_up_the_solve(nw):
+    """Train on pairs from two systems, then solve a held-out system and
+    right-hand side. The method without the network is the same two-level
+    preconditioner with an untrained network (zero output layer: symmetric
+    SGS smoothing only); the trained network must cut the FGMRES iteration
+    count."""
+    net = nw.Learned(seed=0)
+    train_a = _poisson(nw, (40, 40, 24), seed=3, stretch=1.04)
+    train_b = _poisson(nw, (40, 40, 24), seed=4, stretch=1.10, jitter=0.05)
+    npairs = 0
+    for ls in (train_a, train_b):
+        ls.attach_learned(net)
+        npairs = net.harvest(ls, restarts=24, kspace=30)
+    assert npairs >= 40
+    before = net.evaluate(train_a)
+    net.train(train_a, epochs=30, batch=4, lr=2e-3, seed=1)
+    after = net.evaluate(train_a)
+    assert after < 0.9 * before, (before, after)
+    test = _poisson(nw, (40, 40, 24), seed=9, stretch=1.07, jitter=0.03, rhs_seed=99)
+    test.attach_learned(nw.Learned(seed=0))
+    rep_0, rel_0 = _solve(nw, test, nw.PC_LEARNED, nw.FGMRES)
+    test.attach_learned(net)
+    rep_l, rel_l = _solve(nw, test, nw.PC_LEARNED, nw.FGMRES)
+    assert rep_0.converged and rep_l.converged and rep_l.fallback == 0 and rep_0.fallback == 0
+    assert rel_0 <= 1.01e-8 and rel_l <= 1.01e-8
+    assert rep_l.iterations < rep_0.iterations, (rep_l.iterations, rep_0.iterations)
+
+
+def test_broken_network_falls_back_to_sgs(nw):
+    ls = _poisson(nw, (20, 20, 12))
+    net = nw.Learned(seed=0)
+    ls.attach_learned(net)
+    net.set_params(np.full(net.num_params, np.nan, np.float32))
+    rep, rel = _solve(nw, ls, nw.PC_LEARNED, nw.FGMRES)
+    assert rep.fallback == 1 and rep.converged == 1 and rel <= 1.01e-8
