@@ -273,11 +273,13 @@ nw_status nw_linsys_sgs_order(nw_linsys* ls, int64_t* order, int* ncolors);
 
 /* ---- learned preconditioner (NW_PC_LEARNED). No counterpart in the
  * reference: nalu-wind's preconditioners are Ifpack2 relaxations and MueLu
- * (src/LinearSolverConfig.C:89-121). M(v) = z1 + P Net(R (v - A z1)) with
- * z1 one multicolour SGS sweep, R / P over plain aggregates, and Net a
+ * (src/LinearSolverConfig.C:89-121). M(v) = z2 + SGS(v - A z2),
+ * z2 = z1 + alpha P Net(R (v - A z1)), z1 = SGS(v): one multicolour SGS
+ * sweep, a coarse correction over plain aggregates (R sums, P copies) by a
  * 4-layer, 64-channel edge message-passing network (BF16, FP32
- * accumulation) acting as the coarse solver; applied inside FGMRES, with
- * SGS as fallback when the flexible solve fails. ---- */
+ * accumulation) scaled by its energy-optimal factor alpha, and a second
+ * SGS sweep. Applied inside FGMRES; the solve is repeated with SGS when the
+ * flexible solve fails or stalls. ---- */
 typedef struct nw_learned nw_learned;
 /* Network with seeded random weights (device resident). */
 nw_status nw_learned_create(uint64_t seed, nw_learned** out);
@@ -290,6 +292,12 @@ nw_status nw_learned_load(nw_learned* net, const char* path);
 int64_t nw_learned_num_params(void);
 nw_status nw_learned_params(nw_learned* net, float* out, const float* in,
                             int64_t n);
+/* post_smooth 1 (default): M(v) ends with a second SGS sweep on
+ * v - A z (symmetric two-level cycle); 0: no post-smoothing.
+ * agg_passes (1..4, default 2): plain aggregation applied that many times
+ * (aggregates of aggregates) to build the coarse level; takes effect at
+ * the next nw_linsys_attach_learned. */
+nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes);
 /* Build the aggregation / coarse level of this system's graph (num_dof 1)
  * and use `net` for NW_PC_LEARNED solves of this handle. */
 nw_status nw_linsys_attach_learned(nw_linsys* ls, nw_learned* net);

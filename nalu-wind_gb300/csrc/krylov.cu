@@ -581,10 +581,21 @@ void precond_apply_t(const Precond& pc, int64_t n, const int64_t* rp,
   NW_CUDA(cudaGetLastError());
 }
 
+// The learned preconditioner is given up (and the solve repeated with
+// SGS) when kStallCycles restart cycles in a row each reduce the true
+// residual by less than a factor kStallRatio.
+constexpr int kStallCycles = 5;
+constexpr double kStallRatio = 0.99;
+bool stalled(int& stalls, double rnorm, double prev) {
+  stalls = rnorm > kStallRatio * prev ? stalls + 1 : 0;
+  return stalls >= kStallCycles;
+}
+
 }  // namespace
 
 // FP32 preconditioner of the mixed method. Learned (two-level, symmetric
-// smoothing): z1 = SGS(x), r1 = x - A z1, z2 = z1 + P Net(R r1), then the
+// smoothing): z1 = SGS(x), r1 = x - A z1, ec = Net(R r1),
+// z2 = z1 + alpha P ec with the energy-optimal alpha, then the
 // post-smoothing z = z2 + SGS(x - A z2).
 void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
                              cudaStream_t s) {
@@ -605,8 +616,9 @@ void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
   spmv32(y, tmp32_.p, s);
   rsub_f32_k<<<grid1(n), kBlock, 0, s>>>(n, x, tmp32_.p);
   launch_restrict(*cl_, tmp32_.p, rc32_.p, s);
-  net_->forward(*cl_, cl_->wgt.p, cl_->dinv.p, rc32_.p, ec32_.p, s);
-  launch_prolong_add(*cl_, ec32_.p, y, s);
+  net_->coarse_correction(*cl_, rc32_.p, ec32_.p, s);
+  launch_prolong_add(*cl_, ec32_.p, net_->alpha_dev(), y, s);
+  if (!net_->post_smooth) return;
   post32_.resize(n);
   spmv32(y, tmp32_.p, s);
   rsub_f32_k<<<grid1(n), kBlock, 0, s>>>(n, x, tmp32_.p);
@@ -693,7 +705,7 @@ SolveResult KrylovSolver::gmres(const nw_solver_cfg& cfg, double tol,
   NW_CUDA(cudaMemcpyAsync(r_.p, b, n * sizeof(double),
                           cudaMemcpyDeviceToDevice, s));
   double rel = 1.0;
-  int its = 0;
+  int its = 0, stalls = 0;
   bool done = false;
   double* hs = scal_.p;             // h (m+1)
   double* h2 = scal_.p + (m_ + 2);  // second-pass h, then norm
@@ -789,8 +801,13 @@ SolveResult KrylovSolver::gmres(const nw_solver_cfg& cfg, double tol,
     }
     if (done || its >= cfg.max_iterations) break;
     spmv64(x, b, r_.p, s);
+    const double prev = beta;
     beta = std::sqrt(dot(r_.p, r_.p, s));
     if (beta == 0.0) break;
+    if (pc.kind == NW_PC_LEARNED && stalled(stalls, beta, prev)) {
+      res.status = NW_NOT_CONVERGED;
+      break;
+    }
   }
   spmv64(x, b, r_.p, s);
   res.final_abs = std::sqrt(dot(r_.p, r_.p, s));
@@ -891,9 +908,9 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
   double* hs = scal_.p;
   double* h2 = scal_.p + (m_ + 2);
   double rel = 1.0;
-  int its = 0, outer = 0;
+  int its = 0, outer = 0, stalls = 0;
   NW_CUDA(cudaMemcpyAsync(r_.p, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  double rnorm = bnorm;
+  double rnorm = bnorm, prev_rnorm = bnorm;
   while (its < cfg.max_iterations) {
     ++outer;
     // inner: solve A d = r (scaled) in FP32
@@ -977,6 +994,11 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
     }
     res.history.back() = rel;
     if (rel <= tol || res.status != NW_OK) break;
+    if (flexible && stalled(stalls, rnorm, prev_rnorm)) {
+      res.status = NW_NOT_CONVERGED;
+      break;
+    }
+    prev_rnorm = rnorm;
   }
   res.final_abs = rnorm;
   res.final_rel = rel;

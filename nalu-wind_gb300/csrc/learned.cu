@@ -353,19 +353,18 @@ __global__ void __launch_bounds__(kB)
   }
 }
 
-// Energy-norm loss terms and dL/dy for one pair (thread per coarse row):
-//   (Ac ec)_I = (ec_I - sum_J w_IJ ec_J) / dinv_I    (Ac = D (I - W))
-//   L = (sum_I ec_I (Ac ec)_I - 2 ec_I rc_I + cA) / eA,  ec = s y
-//   dL/dy_I = s * 2 ((Ac ec)_I - rc_I) / eA           (Ac symmetric)
-__global__ void loss_k(int64_t nc, const int64_t* __restrict__ cptr,
-                       const int32_t* __restrict__ ccol, const int32_t* __restrict__ cdiag,
-                       const float* __restrict__ wgt, const float* __restrict__ dinv,
-                       const float* __restrict__ ec, const float* __restrict__ rc,
-                       const float* __restrict__ scal, float inv_ea,
-                       float* __restrict__ dy, float* __restrict__ partial) {
-  __shared__ float red[kB / 32];
+// Coarse operator applied to the network output, thread per coarse row:
+//   (Ac ec)_I = (ec_I - sum_J w_IJ ec_J) / dinv_I     (Ac = D (I - W))
+// with per-block partial sums of ec' rc and ec' Ac ec (two per block).
+__global__ void coarse_apply_k(int64_t nc, const int64_t* __restrict__ cptr,
+                               const int32_t* __restrict__ ccol,
+                               const int32_t* __restrict__ cdiag,
+                               const float* __restrict__ wgt, const float* __restrict__ dinv,
+                               const float* __restrict__ ec, const float* __restrict__ rc,
+                               float* __restrict__ aec, float* __restrict__ partial) {
+  __shared__ float red[2][kB / 32];
   const int64_t I = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  float l = 0.f;
+  float num = 0.f, den = 0.f;
   if (I < nc) {
     const float e = ec[I];
     float a = e;
@@ -373,18 +372,55 @@ __global__ void loss_k(int64_t nc, const int64_t* __restrict__ cptr,
     for (int64_t q = cptr[I]; q < cptr[I + 1]; ++q)
       if (q != dpos) a = fmaf(-wgt[q], ec[ccol[q]], a);
     const float d = dinv[I];
-    const float aec = d != 0.f ? a / d : 0.f;
-    l = e * aec - 2.f * e * rc[I];
-    dy[I] = scal[0] * 2.f * (aec - rc[I]) * inv_ea;
+    const float v = d != 0.f ? a / d : 0.f;
+    aec[I] = v;
+    num = e * rc[I];
+    den = e * v;
   }
-  for (int off = 16; off > 0; off >>= 1) l += __shfl_down_sync(0xffffffffu, l, off);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
+  for (int off = 16; off > 0; off >>= 1) {
+    num += __shfl_down_sync(0xffffffffu, num, off);
+    den += __shfl_down_sync(0xffffffffu, den, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = num;
+    red[1][threadIdx.x >> 5] = den;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    float t = 0.f;
-    for (int q = 0; q < kB / 32; ++q) t += red[q];
-    partial[blockIdx.x] = t;
+    float a = 0.f, b = 0.f;
+    for (int q = 0; q < kB / 32; ++q) {
+      a += red[0][q];
+      b += red[1][q];
+    }
+    partial[2 * blockIdx.x] = a;
+    partial[2 * blockIdx.x + 1] = b;
   }
+}
+
+// Energy-optimal scaling of the coarse correction, fixed-order sums:
+//   scal[2] = alpha = ec' rc / ec' Ac ec   (0 unless the denominator is > 0)
+//   scal[3] = (ec' rc)^2 / ec' Ac ec       (A-norm error energy removed)
+__global__ void alpha_k(int nblocks, const float* __restrict__ partial, float* __restrict__ scal) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double num = 0.0, den = 0.0;
+  for (int b = 0; b < nblocks; ++b) {
+    num += partial[2 * b];
+    den += partial[2 * b + 1];
+  }
+  const bool ok = den > 0.0 && isfinite(num) && isfinite(den);
+  scal[2] = ok ? float(num / den) : 0.f;
+  scal[3] = ok ? float(num * num / den) : 0.f;
+}
+
+// dL/dy for the scaled loss L = (cA - (ec' rc)^2 / ec' Ac ec) / eA:
+//   dL/dy_I = s * (2 / eA) (alpha^2 (Ac ec)_I - alpha rc_I)   (Ac symmetric)
+__global__ void loss_grad_k(int64_t nc, const float* __restrict__ aec,
+                            const float* __restrict__ rc, const float* __restrict__ scal,
+                            float inv_ea, float* __restrict__ dy) {
+  const int64_t I = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (I >= nc) return;
+  const float al = scal[2];
+  dy[I] = scal[0] * 2.f * inv_ea * al * (al * aec[I] - rc[I]);
 }
 
 // dz3 = bf16(dy * wout * (h3 > 0)); per-block partial of dwout = h3^T dy.
@@ -501,10 +537,12 @@ __global__ void restrict_k(int64_t nc, const int64_t* __restrict__ mptr,
   rc[I] = s;
 }
 
+// z_i += alpha ec_agg(i), alpha read from the device
 __global__ void prolong_add_k(int64_t nf, const int32_t* __restrict__ agg,
-                              const float* __restrict__ ec, float* __restrict__ z) {
+                              const float* __restrict__ ec, const float* __restrict__ alpha,
+                              float* __restrict__ z) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < nf) z[i] += ec[agg[i]];
+  if (i < nf) z[i] += *alpha * ec[agg[i]];
 }
 
 uint64_t fnv1a(const void* data, size_t n) {
@@ -541,40 +579,78 @@ void launch_gemm_wgrad(const uint16_t* xc, const uint16_t* dz, float* partial,
 void launch_restrict(const CoarseLevel& cl, const float* r, float* rc, cudaStream_t s) {
   restrict_k<<<gridn(cl.nc), kB, 0, s>>>(cl.nc, cl.mptr.p, cl.mrows.p, r, rc);
 }
-void launch_prolong_add(const CoarseLevel& cl, const float* ec, float* z, cudaStream_t s) {
-  prolong_add_k<<<gridn(cl.nf), kB, 0, s>>>(cl.nf, cl.agg.p, ec, z);
+void launch_prolong_add(const CoarseLevel& cl, const float* ec, const float* alpha, float* z,
+                        cudaStream_t s) {
+  prolong_add_k<<<gridn(cl.nf), kB, 0, s>>>(cl.nf, cl.agg.p, ec, alpha, z);
 }
 
 // ---------------------------------------------------------------------------
-// Plain aggregation: a node whose neighbours are all free starts an
-// aggregate with them; leftover nodes join the aggregate of their first
-// aggregated neighbour (column order). Deterministic.
-void CoarseLevel::setup(const HostGraph& g, cudaStream_t s) {
-  if (g.num_dof != 1) fail(NW_INVALID_ARG, "the learned preconditioner needs num_dof 1");
-  const int64_t R = g.node_rows;
-  nf = R;
-  agg_h.assign(R, -1);
+// Plain aggregation of a graph (rows 0..R-1, CSR ptr/col including the
+// diagonal): a row whose neighbours are all free starts an aggregate with
+// them; leftover rows join the aggregate of their first aggregated
+// neighbour (column order), or start their own. Deterministic.
+static int32_t plain_aggregate(int64_t R, const int64_t* ptr, const int32_t* col,
+                               std::vector<int32_t>& agg) {
+  agg.assign(R, -1);
   int32_t na = 0;
   for (int64_t r = 0; r < R; ++r) {
-    if (agg_h[r] >= 0) continue;
+    if (agg[r] >= 0) continue;
     bool free_nbrs = true;
-    for (int64_t p = g.nrow_ptr[r]; p < g.nrow_ptr[r + 1]; ++p)
-      if (agg_h[g.ncol[p]] >= 0) {
+    for (int64_t p = ptr[r]; p < ptr[r + 1]; ++p)
+      if (agg[col[p]] >= 0) {
         free_nbrs = false;
         break;
       }
     if (!free_nbrs) continue;
-    for (int64_t p = g.nrow_ptr[r]; p < g.nrow_ptr[r + 1]; ++p) agg_h[g.ncol[p]] = na;
-    agg_h[r] = na++;
+    for (int64_t p = ptr[r]; p < ptr[r + 1]; ++p) agg[col[p]] = na;
+    agg[r] = na++;
   }
   for (int64_t r = 0; r < R; ++r) {
-    if (agg_h[r] >= 0) continue;
-    for (int64_t p = g.nrow_ptr[r]; p < g.nrow_ptr[r + 1]; ++p)
-      if (agg_h[g.ncol[p]] >= 0) {
-        agg_h[r] = agg_h[g.ncol[p]];
+    if (agg[r] >= 0) continue;
+    for (int64_t p = ptr[r]; p < ptr[r + 1]; ++p)
+      if (agg[col[p]] >= 0) {
+        agg[r] = agg[col[p]];
         break;
       }
-    if (agg_h[r] < 0) agg_h[r] = na++;
+    if (agg[r] < 0) agg[r] = na++;
+  }
+  return na;
+}
+
+// Graph of the aggregates (sorted, unique columns) from a fine graph.
+static void aggregate_graph(int64_t R, const int64_t* ptr, const int32_t* col,
+                            const std::vector<int32_t>& agg, int64_t nagg,
+                            std::vector<int64_t>& cptr, std::vector<int32_t>& ccol) {
+  std::vector<std::vector<int32_t>> cols(nagg);
+  for (int64_t r = 0; r < R; ++r)
+    for (int64_t p = ptr[r]; p < ptr[r + 1]; ++p) cols[agg[r]].push_back(agg[col[p]]);
+  cptr.assign(nagg + 1, 0);
+  for (int64_t I = 0; I < nagg; ++I) {
+    auto& v = cols[I];
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    cptr[I + 1] = cptr[I] + int64_t(v.size());
+  }
+  ccol.resize(cptr[nagg]);
+  for (int64_t I = 0; I < nagg; ++I)
+    std::copy(cols[I].begin(), cols[I].end(), ccol.begin() + cptr[I]);
+}
+
+// Aggregation applied `passes` times (aggregates of aggregates), composed
+// into one fine-row -> aggregate map.
+void CoarseLevel::setup(const HostGraph& g, int npasses, cudaStream_t s) {
+  if (g.num_dof != 1) fail(NW_INVALID_ARG, "the learned preconditioner needs num_dof 1");
+  if (npasses < 1 || npasses > 4) fail(NW_INVALID_ARG, "aggregation passes must be 1..4");
+  passes = npasses;
+  const int64_t R = g.node_rows;
+  nf = R;
+  int32_t na = plain_aggregate(R, g.nrow_ptr.data(), g.ncol.data(), agg_h);
+  for (int pass = 1; pass < npasses; ++pass) {
+    std::vector<int64_t> p1;
+    std::vector<int32_t> c1, agg2;
+    aggregate_graph(R, g.nrow_ptr.data(), g.ncol.data(), agg_h, na, p1, c1);
+    na = plain_aggregate(na, p1.data(), c1.data(), agg2);
+    for (int64_t r = 0; r < R; ++r) agg_h[r] = agg2[agg_h[r]];
   }
   nc = na;
   // members
@@ -587,25 +663,12 @@ void CoarseLevel::setup(const HostGraph& g, cudaStream_t s) {
     for (int64_t r = 0; r < R; ++r) mr[pos[agg_h[r]]++] = int32_t(r);
   }
   // coarse graph and Galerkin contribution lists over the fine CSR
-  std::vector<std::vector<int32_t>> cols(nc);
-  for (int64_t r = 0; r < R; ++r)
-    for (int64_t p = g.nrow_ptr[r]; p < g.nrow_ptr[r + 1]; ++p)
-      cols[agg_h[r]].push_back(agg_h[g.ncol[p]]);
-  cptr_h.assign(nc + 1, 0);
-  for (int64_t I = 0; I < nc; ++I) {
-    auto& v = cols[I];
-    std::sort(v.begin(), v.end());
-    v.erase(std::unique(v.begin(), v.end()), v.end());
-    cptr_h[I + 1] = cptr_h[I] + int64_t(v.size());
-  }
+  aggregate_graph(R, g.nrow_ptr.data(), g.ncol.data(), agg_h, nc, cptr_h, ccol_h);
   nnzc = cptr_h[nc];
-  ccol_h.resize(nnzc);
   cdiag_h.assign(nc, -1);
   for (int64_t I = 0; I < nc; ++I)
-    for (size_t k = 0; k < cols[I].size(); ++k) {
-      ccol_h[cptr_h[I] + k] = cols[I][k];
-      if (cols[I][k] == I) cdiag_h[I] = int32_t(cptr_h[I] + k);
-    }
+    for (int64_t q = cptr_h[I]; q < cptr_h[I + 1]; ++q)
+      if (ccol_h[q] == I) cdiag_h[I] = int32_t(q);
   auto slot = [&](int64_t I, int32_t J) {
     auto b = ccol_h.begin() + cptr_h[I], e = ccol_h.begin() + cptr_h[I + 1];
     return int64_t(std::lower_bound(b, e, J) - ccol_h.begin());
@@ -657,7 +720,8 @@ void NetWork::resize(int64_t n) {
   y.resize(n);
   dy.resize(n);
   scal.resize(4);
-  partial.resize(gridn(n) + 1);
+  partial.resize(2 * gridn(n) + 2);
+  aec.resize(n);
   ec.resize(n);
   part2.resize(size_t(gridn(n * 64)) * 128);
   xc1.resize(n * 128);
@@ -681,12 +745,11 @@ void LearnedNet::init(uint64_t sd, cudaStream_t s) {
     st ^= st << 17;
     return float((st >> 11) * 0x1.0p-53) * 2.f - 1.f;
   };
-  const float a0 = std::sqrt(6.f / 2.f), a1 = std::sqrt(6.f / float(kIn2));
+  const float a0 = std::sqrt(6.f / 2.f), a1 = std::sqrt(6.f / float(kIn2)),
+              ao = std::sqrt(3.f / float(kHid));
   for (int i = 0; i < 2 * kHid; ++i) params_h[kOffW0 + i] = a0 * uni();
   for (int i = 0; i < 3 * kIn2 * kHid; ++i) params_h[kOffW1 + i] = a1 * uni();
-  // The output layer starts at zero: an untrained network adds no coarse
-  // correction, so the preconditioner starts as the plain SGS sweep and
-  // training moves it away from that only where the loss improves.
+  for (int i = 0; i < kHid; ++i) params_h[kOffWout + i] = ao * uni();
   upload(s);
   grads.resize(kNumParams);
   adam_m.resize(kNumParams);
@@ -747,6 +810,16 @@ void LearnedNet::forward(const CoarseLevel& cl, const float* wgt, const float* d
   NW_CUDA(cudaGetLastError());
 }
 
+void LearnedNet::coarse_correction(const CoarseLevel& cl, const float* rc, float* ec,
+                                   cudaStream_t s) {
+  forward(cl, cl.wgt.p, cl.dinv.p, rc, ec, s);
+  const int nb = int(gridn(cl.nc));
+  coarse_apply_k<<<nb, kB, 0, s>>>(cl.nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, cl.wgt.p, cl.dinv.p,
+                                   ec, rc, work.aec.p, work.partial.p);
+  alpha_k<<<1, 32, 0, s>>>(nb, work.partial.p, work.scal.p);
+  NW_CUDA(cudaGetLastError());
+}
+
 double LearnedNet::forward_backward(const CoarseLevel& cl, const float* wgt,
                                     const float* dinv, const float* rc, double ea,
                                     double ca, cudaStream_t s, bool with_grad) {
@@ -756,16 +829,15 @@ double LearnedNet::forward_backward(const CoarseLevel& cl, const float* wgt,
   forward(cl, wgt, dinv, rc, ec, s);
   const unsigned gw = gridn(nc * 32);
   const int nb = int(gridn(nc));
-  loss_k<<<nb, kB, 0, s>>>(nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, wgt, dinv, ec, rc, work.scal.p,
-                           float(1.0 / ea), work.dy.p, work.partial.p);
-  std::vector<float> lp(nb);
-  NW_CUDA(cudaMemcpyAsync(lp.data(), work.partial.p, nb * 4, cudaMemcpyDeviceToHost, s));
-  if (!with_grad) {
-    NW_CUDA(cudaStreamSynchronize(s));
-    double l = ca;
-    for (float v : lp) l += v;
-    return l / ea;
-  }
+  coarse_apply_k<<<nb, kB, 0, s>>>(nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, wgt, dinv, ec, rc,
+                                   work.aec.p, work.partial.p);
+  alpha_k<<<1, 32, 0, s>>>(nb, work.partial.p, work.scal.p);
+  float sc[4];
+  NW_CUDA(cudaMemcpyAsync(sc, work.scal.p, sizeof(sc), cudaMemcpyDeviceToHost, s));
+  NW_CUDA(cudaStreamSynchronize(s));
+  const double loss = (ca - double(sc[3])) / ea;
+  if (!with_grad) return loss;
+  loss_grad_k<<<nb, kB, 0, s>>>(nc, work.aec.p, rc, work.scal.p, float(1.0 / ea), work.dy.p);
   // output layer
   const int nb64 = int(gridn(nc * 64));
   float* part2 = work.part2.p;
@@ -786,9 +858,7 @@ double LearnedNet::forward_backward(const CoarseLevel& cl, const float* wgt,
   colsum_k<<<1, 128, 0, s>>>(nb64, 128, part2, grads.p + kOffW0, 1);
   NW_CUDA(cudaGetLastError());
   NW_CUDA(cudaStreamSynchronize(s));
-  double l = ca;
-  for (float v : lp) l += v;
-  return l / ea;
+  return loss;
 }
 
 void LearnedNet::adam(double lr, double scale, cudaStream_t s) {

@@ -1,9 +1,10 @@
 // Learned two-level preconditioner (learned.cu).
 //
-// M(v) = z1 + P Net(R (v - A z1)),  z1 = one multicolour symmetric
-// Gauss-Seidel sweep of A z = v (FP32),
-// R / P = restriction (sum) / prolongation (copy) over plain aggregates of
-// the matrix graph, and Net = a 4-layer edge message-passing network with
+// M(v) = z2 + S(v - A z2),  z2 = z1 + alpha P Net(R (v - A z1)),
+// z1 = S(v), S = one multicolour symmetric Gauss-Seidel sweep (FP32),
+// R / P = restriction (sum) / prolongation (copy) over aggregates of the
+// matrix graph (plain aggregation, applied twice by default: aggregates of
+// aggregates), and Net = a 4-layer edge message-passing network with
 // 64 channels acting as the coarse solver on the aggregate graph. The coarse
 // operator Ac = R A P (Galerkin, summed in a fixed order) supplies the edge
 // weights w_IJ = -Ac_IJ / Ac_II and the Jacobi scaling 1 / Ac_II.
@@ -13,17 +14,23 @@
 //   H0 = relu([x, W x] W0)                 W0: 2 x 64
 //   Hl = relu([H(l-1), W H(l-1)] Wl)       Wl: 128 x 64, l = 1..3
 //   e_c = s * (H3 wout)                    wout: 64
+// and the preconditioner adds alpha P e_c (alpha below).
 // where (W h)_I = sum_J w_IJ h_J. Trained on the GPU (forward, backward
 // and Adam kernels in learned.cu; the dense layers use mma.sync BF16 tensor
 // core instructions) over (residual, error) pairs harvested at the restarts
 // of plain Jacobi-GMRES, minimising the energy norm of the error left after
 // the smoothing and the coarse correction,
-//   L = ||z1 + P e_c - e||_A^2 / ||e||_A^2
-//     = (e_c' Ac e_c - 2 e_c' r_c + cA) / eA,
+// with the coarse correction scaled by its energy-optimal factor
+//   alpha = e_c' r_c / e_c' Ac e_c:
+//   L = min_alpha ||z1 + alpha P e_c - e||_A^2 / ||e||_A^2
+//     = (cA - (e_c' r_c)^2 / e_c' Ac e_c) / eA,
 // with r_c = R (r - A z1) = P' A (e - z1), cA = ||e - z1||_A^2 and
-// eA = ||e||_A^2 = e' r. The minimiser is the exact Galerkin coarse solve
-// e_c = Ac^-1 r_c, so the network learns to approximate it. The form
-// assumes a symmetric operator (the pressure Poisson system is).
+// eA = ||e||_A^2 = e' r. Its minimisers are the multiples of the exact
+// Galerkin coarse solve Ac^-1 r_c, so the network learns the direction
+// of that solve. The same alpha is applied at every use, so the coarse
+// correction never increases the A-norm error of the smoothed iterate
+// (whatever the network outputs). The form assumes a symmetric operator
+// (the pressure Poisson system is).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -48,6 +55,7 @@ constexpr int kNumParams = kOffWout + kHid;
 // Aggregation and Galerkin structures for one fine graph (1 dof).
 struct CoarseLevel {
   int64_t nf = 0, nc = 0, nnzc = 0;
+  int passes = 1;                          // aggregation passes
   std::vector<int32_t> agg_h;              // fine row -> aggregate
   std::vector<int64_t> cptr_h;             // coarse CSR
   std::vector<int32_t> ccol_h, cdiag_h, rev_h;
@@ -55,14 +63,14 @@ struct CoarseLevel {
   DeviceArray<int64_t> mptr, cptr, gptr;
   DeviceArray<double> ac;                  // Galerkin values
   DeviceArray<float> wgt, dinv;            // edge weights, 1 / Ac_II
-  void setup(const HostGraph& g, cudaStream_t s);
+  void setup(const HostGraph& g, int passes, cudaStream_t s);
   void refresh(const double* fine_values, cudaStream_t s);
 };
 
 // Activations of one forward pass on a coarse graph (sized to nc).
 struct NetWork {
   int64_t nc = 0;
-  DeviceArray<float> u, x, ax, y, dy, ec, scal, partial, part2;
+  DeviceArray<float> u, x, ax, y, dy, ec, aec, scal, partial, part2;
   DeviceArray<uint16_t> xc1, xc2, xc3, h3, dz;  // BF16
   DeviceArray<float> dxc, dh;
   void resize(int64_t n);
@@ -75,6 +83,8 @@ struct LearnedNet {
   DeviceArray<float> wpartial;           // weight-gradient partials
   int64_t adam_step = 0;
   uint64_t seed = 0;
+  int post_smooth = 1;  // SGS sweep after the coarse correction
+  int agg_passes = 2;   // aggregation passes of the coarse level
   // training data (coarse vectors of one aggregation)
   int64_t data_nc = 0, data_nnzc = 0;
   int npairs = 0, nsystems = 0;
@@ -91,6 +101,10 @@ struct LearnedNet {
   // forward: coarse residual -> coarse correction (FP32, device)
   void forward(const CoarseLevel& cl, const float* wgt, const float* dinv,
                const float* rc, float* ec, cudaStream_t s);
+  // network output ec plus its scaling alpha (device, alpha_dev()); ec
+  // must not alias the work buffers
+  void coarse_correction(const CoarseLevel& cl, const float* rc, float* ec, cudaStream_t s);
+  const float* alpha_dev() const { return work.scal.p + 2; }
   // loss and parameter gradients (accumulated into grads) for one pair;
   // returns the loss (host sync). with_grad = false: loss only.
   double forward_backward(const CoarseLevel& cl, const float* wgt,
@@ -113,6 +127,7 @@ void launch_gemm_wgrad(const uint16_t* xc, const uint16_t* dz, float* partial,
 
 // Two-level application helpers (FP32).
 void launch_restrict(const CoarseLevel& cl, const float* r, float* rc, cudaStream_t s);
-void launch_prolong_add(const CoarseLevel& cl, const float* ec, float* z, cudaStream_t s);
+void launch_prolong_add(const CoarseLevel& cl, const float* ec, const float* alpha, float* z,
+                        cudaStream_t s);
 
 }  // namespace nw

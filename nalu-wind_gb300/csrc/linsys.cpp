@@ -752,14 +752,25 @@ nw_status nw_learned_params(nw_learned* net, float* out, const float* in, int64_
   });
 }
 
+nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes) {
+  return guard([&] {
+    if (!net || (post_smooth != 0 && post_smooth != 1) || agg_passes < 1 || agg_passes > 4)
+      fail(NW_INVALID_ARG, "bad option");
+    if (agg_passes != net->net.agg_passes && net->net.npairs > 0)
+      fail(NW_INVALID_ARG, "harvested pairs use the current aggregation; clear them first");
+    net->net.post_smooth = post_smooth;
+    net->net.agg_passes = agg_passes;
+  });
+}
+
 nw_status nw_linsys_attach_learned(nw_linsys* ls, nw_learned* net) {
   return guard([&] {
     need_finalized(ls);
     if (!net) fail(NW_INVALID_ARG, "null network");
     if (ls->num_dof != 1) fail(NW_INVALID_ARG, "the learned preconditioner needs num_dof 1");
-    if (!ls->coarse) {
+    if (!ls->coarse || ls->coarse->passes != net->net.agg_passes) {
       auto cl = std::make_unique<CoarseLevel>();
-      cl->setup(ls->g, ls->stream);
+      cl->setup(ls->g, net->net.agg_passes, ls->stream);
       ls->coarse = std::move(cl);
     }
     ls->learned = net;

@@ -5,9 +5,11 @@ kernels (nalu-wind_gb300/csrc/learned.cu). Same architecture and loss:
   u = D^-1 rc, s = rms(u), x = u / s, (W h)_I = sum_J w_IJ h_J (no diagonal)
   H0 = relu([x, W x] W0); Hl = relu([H(l-1), W H(l-1)] Wl), l = 1..3
   ec = s * H3 wout
-  L = (ec' Ac ec - 2 ec' rc + cA) / eA, Ac = D (I - W), D = diag(1 / dinv)
-(the energy norm of the error left by smoothing and coarse correction,
-normalised by the energy norm of the error; the gradient takes Ac as
+  alpha = ec' rc / ec' Ac ec,  Ac = D (I - W), D = diag(1 / dinv)
+  L = (cA - (ec' rc)^2 / ec' Ac ec) / eA
+(the energy norm of the error left by smoothing and the alpha-scaled
+coarse correction, normalised by the energy norm of the error; alpha and
+the removed energy are 0 unless ec' Ac ec > 0; the gradient takes Ac as
 symmetric, as the GPU kernels do).
 Parameters are the library's flat layout: W0 (2 x 64) | W1 | W2 | W3
 (128 x 64 each, row-major) | wout (64). This network has no counterpart
@@ -91,8 +93,10 @@ def loss_and_grad(p, cg, rc, ea, ca, bf16_points=False):
     ec = s * y
     rc = np.asarray(rc, np.float64)
     aec = coarse_operator(cg) @ ec
-    L = (ec @ aec - 2 * ec @ rc + ca) / ea
-    dy = s * 2 * (aec - rc) / ea
+    num, den = ec @ rc, ec @ aec
+    alpha = num / den if den > 0 else 0.0
+    L = (ca - (num * num / den if den > 0 else 0.0)) / ea
+    dy = s * 2 * alpha * (alpha * aec - rc) / ea
     g_wout = Hs[-1].T @ dy
     dH = np.outer(dy, wout)
     g_ws = [None] * 3

@@ -58,13 +58,20 @@ def test_zero_network_loss_is_baseline():
 
 
 def test_exact_coarse_solve_minimises_loss():
-    """The loss is a quadratic in ec whose minimiser is Ac^-1 rc."""
+    """The scaled loss depends only on the direction of ec and is smallest
+    for the exact coarse solve Ac^-1 rc, where it is (cA - rc' Ac^-1 rc) / eA."""
     rng = np.random.default_rng(3)
     cg, A = _ring_graph(10, rng)
     rc = rng.normal(size=10)
-    ec = np.linalg.solve(A, rc)
-    f = lambda v: v @ A @ v - 2 * v @ rc
-    assert all(f(ec) < f(ec + 1e-3 * rng.normal(size=10)) for _ in range(20))
+    ex = np.linalg.solve(A, rc)
+
+    def loss(ec):
+        num, den = ec @ rc, ec @ A @ ec
+        return (5.0 - num * num / den) / 2.0
+
+    assert abs(loss(ex) - (5.0 - rc @ ex) / 2.0) <= 1e-12
+    assert abs(loss(-3.0 * ex) - loss(ex)) <= 1e-12
+    assert all(loss(ex) < loss(ex + 1e-2 * rng.normal(size=10)) for _ in range(20))
 
 
 def test_bf16_rounding_matches_torch():
