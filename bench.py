@@ -10,9 +10,11 @@ the C ABI. value = nnz assembled per second (Gnnz/s). Inputs are resident
 in HBM for `value`; `e2e` copies every input field from pinned host memory
 and reads both rhs vectors back inside the timed region.
 
---poisson adds the pressure-Poisson solve on the 256 x 256 x 128 box
-(8,520,321 rows): ms to 1e-8 FP64 relative residual for plain FP64
-GMRES(50) + Jacobi and for the mixed-precision method.
+The run also solves the pressure-Poisson system of the 256 x 256 x 128 box
+(8,520,321 rows; --no-poisson skips it): ms to 1e-8 FP64 relative residual
+for plain FP64 GMRES(50) + Jacobi, mixed-precision GMRES(50) + SGS, and the
+learned-preconditioned mixed-precision FGMRES(30) (network trained first,
+untimed, on other seeded systems).
 
 Multi-GPU (torchrun, N > 1): every rank runs an independent replica of the
 same workload (weak scaling); the timed region is bracketed by barriers and
@@ -220,11 +222,13 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("assembly_timed")
     t0.record(stream)
     for _ in range(args.steps):
         step()
     t1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     barrier(world)
     clocks = sampler.stop()
     ms_total = t0.elapsed_time(t1)
@@ -302,7 +306,7 @@ def run_ours(args, rank, world):
         "gpu_launches": 5 * args.steps,  # momentum: edge + row; continuity: node + edge + row
         "clocks": clocks,
     }
-    if args.poisson:
+    if not args.no_poisson:
         out["poisson"] = poisson_solves(nw, stream, args)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(case, args)
@@ -327,42 +331,68 @@ def _cudart():
 
 
 def poisson_solves(nw, stream, args) -> dict:
+    """Pressure Poisson to 1e-8 FP64 relative residual on the 256 x 256 x 128
+    stretched box: plain FP64 GMRES(50) + Jacobi against the mixed-precision
+    solvers, the headline being learned-preconditioned mixed FGMRES(30).
+    The network is trained first (untimed) on a family of 64 x 64 x 48
+    systems with other seeds. Every solve starts from x = 0; errors are
+    measured against the plain FP64 solution (zero-mean parts: the system is
+    singular, its null space the constants)."""
     import torch
-    case = nw.workload.poisson_case(*args.poisson_shape, seed=3)
-    mesh = case.mesh
-    nd = case.node
-    d = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in dict(
-        coords=mesh.coords, velocity=nd["velocity"], dpdx=nd["dpdx"], density=nd["density"],
-        pressure=nd["pressure"], udiag=nd["udiag"], area=mesh.area).items()}
-    ls = nw.LinearSystem(1, stream=stream.cuda_stream)
-    ls.build_edge_graph(mesh.num_nodes, mesh.edges)
-    ls.finalize()
-    ls.zero_system()
-    ls.assemble_continuity(nw.ContinuityFields(*(d[k].data_ptr() for k in (
-        "coords", "velocity", "dpdx", "density", "pressure", "udiag", "area"))), case.opts["continuity"])
-    ls.from_host(rhs=case.extra["rhs"])
+    ls = nw.workload.poisson_system(args.poisson_shape, seed=3, stretch=1.04, stream=stream.cuda_stream)
     nr, nnz = ls.sizes()
-    res = {"workload": f"poisson {args.poisson_shape}", "rows": nr, "nnz": nnz, "tol": 1e-8}
+    res = {"workload": f"pressure Poisson {'x'.join(map(str, args.poisson_shape))} box, stretch 1.04",
+           "rows": nr, "nnz": nnz, "tol": 1e-8}
+    net, info = nw.training.train_poisson_network(stream=stream.cuda_stream)
+    res["training"] = info
+    without = nw.Learned(seed=0)
+    p0 = without.params()
+    p0[-64:] = 0.0  # zero output layer: the same cycle with no coarse correction
+    without.set_params(p0)
+    maxit = args.poisson_maxit
     variants = [
-        ("plain_fp64_gmres50_jacobi", nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8)),
-        ("plain_fp64_gmres50_sgs", nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8,
-                                                 preconditioner=nw.PC_SGS)),
-        ("mixed_fp32_inner_jacobi", nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8,
-                                                  precision=nw.PREC_MIXED, inner_kspace=50,
-                                                  inner_tolerance=1e-4)),
-        ("mixed_fp32_inner_sgs", nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8,
-                                               precision=nw.PREC_MIXED, inner_kspace=50, inner_tolerance=1e-4,
-                                               preconditioner=nw.PC_SGS)),
+        ("plain_fp64_gmres50_jacobi", None,
+         nw.solver_cfg(kspace=50, max_iterations=maxit, tolerance=1e-8)),
+        ("mixed_gmres50_sgs", None,
+         nw.solver_cfg(kspace=50, max_iterations=maxit, tolerance=1e-8, precision=nw.PREC_MIXED,
+                       inner_kspace=50, inner_tolerance=1e-4, preconditioner=nw.PC_SGS)),
+        ("mixed_fgmres30_two_level_no_network", without,
+         nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=maxit, tolerance=1e-8,
+                       precision=nw.PREC_MIXED, inner_kspace=30, preconditioner=nw.PC_LEARNED)),
+        ("learned_mixed_fgmres30", net,
+         nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=maxit, tolerance=1e-8,
+                       precision=nw.PREC_MIXED, inner_kspace=30, preconditioner=nw.PC_LEARNED)),
     ]
-    for name, cfg in variants:
+    if args.poisson_variants:
+        keep = set(args.poisson_variants.split(","))
+        variants = [v for v in variants if v[0] in keep]
+    x_ref = None
+    for name, learned, cfg in variants:
+        if learned is not None:
+            ls.attach_learned(learned)
         ls.set_solver_cfg(cfg)
         x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push(name)  # NVTX range: profilers can select one solve
         t = time.perf_counter()
         rep = ls.solve(x)
         wall = (time.perf_counter() - t) * 1e3
-        res[name] = {"ms": round(rep.solve_ms, 2), "wall_ms": round(wall, 2), "iterations": rep.iterations,
-                     "outer": rep.outer_iterations, "rel_residual_fp64": rep.final_abs_residual / rep.rhs_norm,
-                     "converged": bool(rep.converged)}
+        torch.cuda.nvtx.range_pop()
+        r = {"ms": round(rep.solve_ms, 2), "wall_ms": round(wall, 2), "iterations": rep.iterations,
+             "outer": rep.outer_iterations, "rel_residual_fp64": rep.final_abs_residual / rep.rhs_norm,
+             "converged": bool(rep.converged), "fallback": bool(rep.fallback)}
+        xc = x - x.mean()
+        if x_ref is None:
+            x_ref = xc
+        else:
+            r["rel_error_vs_plain_fp64"] = float(torch.linalg.norm(xc - x_ref) / torch.linalg.norm(x_ref))
+        res[name] = r
+    if "plain_fp64_gmres50_jacobi" in res:
+        base = res["plain_fp64_gmres50_jacobi"]["ms"]
+        for name, key in (("learned_mixed_fgmres30", "speedup_learned_mixed_vs_plain_fp64"),
+                          ("mixed_gmres50_sgs", "speedup_mixed_sgs_vs_plain_fp64")):
+            if name in res:
+                res[key] = round(base / res[name]["ms"], 2)
     return res
 
 
@@ -426,10 +456,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shape", type=int, nargs=3, default=[128, 128, 64])
-    ap.add_argument("--poisson", action="store_true")
+    ap.add_argument("--no-poisson", action="store_true", help="skip the Poisson solves")
     ap.add_argument("--poisson-shape", type=int, nargs=3, default=[256, 256, 128])
     ap.add_argument("--poisson-maxit", type=int, default=20000)
-    ap.add_argument("--poisson-only", action="store_true")
+    ap.add_argument("--poisson-variants", default="", help="comma-separated subset of the solver variants")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.shape = tuple(args.shape)

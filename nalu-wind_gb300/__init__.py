@@ -474,3 +474,4 @@ class Mesh:
 
 
 from . import workload  # noqa: E402  (seeded synthetic inputs)
+from . import training  # noqa: E402  (learned preconditioner recipe)

@@ -169,3 +169,31 @@ def poisson_case(nx=256, ny=256, nz=128, seed=3, stretch=1.04, jitter=0.0) -> Ca
     return Case(mesh, node=dict(coords=mesh.coords, velocity=zeros3, dpdx=zeros3, density=np.ones(N),
                                 pressure=np.zeros(N), udiag=np.ones(N)),
                 edge=dict(area=mesh.area), opts=dict(continuity=co), extra=dict(rhs=b))
+
+
+def poisson_system(shape, seed=3, stretch=1.04, jitter=0.0, rhs_seed=None, stream=None):
+    """Assembled pressure-Poisson LinearSystem of a box (device inputs via
+    torch); the right-hand side is the case's seeded zero-mean Gaussian,
+    or a fresh one from rhs_seed."""
+    import torch
+
+    from . import ContinuityFields, LinearSystem
+    case = poisson_case(*shape, seed=seed, stretch=stretch, jitter=jitter)
+    mesh = case.mesh
+    nd = case.node
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in dict(
+        coords=mesh.coords, velocity=nd["velocity"], dpdx=nd["dpdx"], density=nd["density"],
+        pressure=nd["pressure"], udiag=nd["udiag"], area=mesh.area).items()}
+    ls = LinearSystem(1, stream=stream)
+    ls.build_edge_graph(mesh.num_nodes, mesh.edges)
+    ls.finalize()
+    ls.zero_system()
+    ls.assemble_continuity(ContinuityFields(*(d[k].data_ptr() for k in (
+        "coords", "velocity", "dpdx", "density", "pressure", "udiag", "area"))), case.opts["continuity"])
+    rhs = case.extra["rhs"]
+    if rhs_seed is not None:
+        rhs = np.random.default_rng(rhs_seed).normal(0.0, 1.0, rhs.shape)
+        rhs -= rhs.mean()
+    ls.from_host(rhs=rhs)
+    ls.sync()
+    return ls

@@ -53,24 +53,7 @@ def test_bf16_gemms_match_torch(nw, m):
 
 
 def _poisson(nw, shape, seed=3, stretch=1.04, jitter=0.0, rhs_seed=None):
-    case = nw.workload.poisson_case(*shape, seed=seed, stretch=stretch, jitter=jitter)
-    mesh = case.mesh
-    ls = nw.LinearSystem(1)
-    ls.build_edge_graph(mesh.num_nodes, mesh.edges)
-    ls.finalize()
-    nd = case.node
-    d = {k: dev(v) for k, v in dict(coords=mesh.coords, velocity=nd["velocity"], dpdx=nd["dpdx"],
-                                     density=nd["density"], pressure=nd["pressure"], udiag=nd["udiag"],
-                                     area=mesh.area).items()}
-    ls.zero_system()
-    ls.assemble_continuity(nw.ContinuityFields(*(d[k].data_ptr() for k in (
-        "coords", "velocity", "dpdx", "density", "pressure", "udiag", "area"))), case.opts["continuity"])
-    rhs = case.extra["rhs"]
-    if rhs_seed is not None:
-        rhs = np.random.default_rng(rhs_seed).normal(size=rhs.shape)
-        rhs -= rhs.mean()
-    ls.from_host(rhs=rhs)
-    return ls
+    return nw.workload.poisson_system(shape, seed=seed, stretch=stretch, jitter=jitter, rhs_seed=rhs_seed)
 
 
 def _rel(a, b):
