@@ -116,8 +116,16 @@ def peaks() -> dict:
 
 
 def traffic_table() -> dict:
-    p = ROOT / "profiles" / "traffic.json"
-    return json.loads(p.read_text()) if p.exists() else {}
+    """DRAM bytes per launch measured by ncu (profiles/traffic.txt: one
+    `key bytes` pair per line; the ncu command is in the matching summary)."""
+    p = ROOT / "profiles" / "traffic.txt"
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 2:
+                out[parts[0]] = {"bytes_per_launch": int(parts[1])}
+    return out
 
 
 def dist_setup(n_gpus: int):
