@@ -17,17 +17,23 @@
 //     coalesced stores (or read-add-writes when the system already holds
 //     values).
 //
-// GB300 issues FP64 at about 1/58 of its FP32 rate, and these kernels are
-// bound by FP64 issue, not by HBM. Divisions therefore use a MUFU
-// reciprocal seed refined by one cubic and one Newton step (5 FMAs, a few
-// ulp), constant divisors become multiplications, node-only factors are
-// computed once per node, and option branches are compile-time template
-// parameters.
+// GB300 issues FP64 at about 1/58 of its FP32 rate, so evaluated in FP64
+// these kernels are bound by FP64 issue, not by HBM. The momentum and
+// continuity kernels therefore evaluate the FP64 formulas in float-float
+// arithmetic (dd.h: about 48 significant bits, error within a few 2^-48 of
+// the operand magnitudes) on the FP32 pipes, split the FP64 inputs with
+// integer operations, keep their edge coefficients as float pairs (8 bytes,
+// the size of a double) and widen each finished CSR entry to FP64 once.
+// The scalar kernel stays in FP64 (MUFU-seeded reciprocals). Node-only
+// factors are computed once per node, and option branches are compile-time
+// template parameters.
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "assemble.h"
+#include "dd.h"
 #include "nw_internal.h"
 
 namespace nw {
@@ -172,7 +178,14 @@ __global__ void __launch_bounds__(kThreads)
 // w = |A|^2 / (A.dx), k = A - w dx, then tmdot /= tau. This is the
 // reference expression regrouped; the parity tests bound the difference by
 // eps times the running magnitude of each entry.
-constexpr int kNodeStride = 8;
+constexpr int kNodeStride = 8;  // dd slots (8 bytes each) per node
+
+__device__ __forceinline__ dd ldd(const double* p) { return dd_from_double(*p); }
+__device__ __forceinline__ void st4(dd* p, dd a, dd b, dd c, dd d) {
+  float4* q = reinterpret_cast<float4*>(p);
+  q[0] = make_float4(a.hi, a.lo, b.hi, b.lo);
+  q[1] = make_float4(c.hi, c.lo, d.hi, d.lo);
+}
 
 __global__ void __launch_bounds__(kThreads)
     continuity_node_k(int64_t N, const double* __restrict__ velocity,
@@ -180,57 +193,70 @@ __global__ void __launch_bounds__(kThreads)
                       const double* __restrict__ density,
                       const double* __restrict__ pressure,
                       const double* __restrict__ udiag,
-                      double* __restrict__ nodebuf) {
+                      dd* __restrict__ nodebuf) {
   const int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (n >= N) return;
-  const double iu = fast_rcp(udiag[n]);
-  const double rho = density[n];
-  double2* out = reinterpret_cast<double2*>(nodebuf + kNodeStride * n);
-  out[0] = make_double2(iu, rho * velocity[3 * n]);
-  out[1] = make_double2(rho * velocity[3 * n + 1], rho * velocity[3 * n + 2]);
-  out[2] = make_double2(Gpdx[3 * n] * iu, Gpdx[3 * n + 1] * iu);
-  out[3] = make_double2(Gpdx[3 * n + 2] * iu, pressure[n]);
+  const dd iu = dd_rcp(ldd(udiag + n));
+  const dd rho = ldd(density + n);
+  dd* out = nodebuf + kNodeStride * n;
+  st4(out, iu, rho * ldd(velocity + 3 * n), rho * ldd(velocity + 3 * n + 1),
+      rho * ldd(velocity + 3 * n + 2));
+  st4(out + 4, ldd(Gpdx + 3 * n) * iu, ldd(Gpdx + 3 * n + 1) * iu,
+      ldd(Gpdx + 3 * n + 2) * iu, ldd(pressure + n));
 }
 
 __global__ void __launch_bounds__(kThreads)
     continuity_edge_fast_k(int64_t E, const int2* __restrict__ edges,
                            const double* __restrict__ coords,
-                           const double* __restrict__ nodebuf,
-                           const double* __restrict__ area, double noc,
-                           double inv_tau, double* __restrict__ buf) {
+                           const dd* __restrict__ nodebuf,
+                           const double* __restrict__ area, dd noc,
+                           dd inv_tau, dd* __restrict__ buf) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= E) return;
   const int2 lr = edges[e];
   const int64_t L = lr.x, R = lr.y;
-  const double2* nl = reinterpret_cast<const double2*>(nodebuf + kNodeStride * L);
-  const double2* nr = reinterpret_cast<const double2*>(nodebuf + kNodeStride * R);
-  const double2 l0 = nl[0], l1 = nl[1], l2 = nl[2], l3 = nl[3];
-  const double2 r0 = nr[0], r1 = nr[1], r2 = nr[2], r3 = nr[3];
-  double av[3], dx[3];
-  for (int d = 0; d < 3; ++d) {
-    av[d] = area[3 * e + d];
-    dx[d] = coords[3 * R + d] - coords[3 * L + d];
+  dd nl[8], nr[8];
+  {
+    const float4* pl = reinterpret_cast<const float4*>(nodebuf + kNodeStride * L);
+    const float4* pr = reinterpret_cast<const float4*>(nodebuf + kNodeStride * R);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float4 a = pl[k], b = pr[k];
+      nl[2 * k] = {a.x, a.y};
+      nl[2 * k + 1] = {a.z, a.w};
+      nr[2 * k] = {b.x, b.y};
+      nr[2 * k + 1] = {b.z, b.w};
+    }
   }
-  const double asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
-  const double axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
-  const double w = asq * fast_rcp(axdx);
-  const double projTimeScale = 0.5 * (l0.x + r0.x);
-  const double m[3] = {l0.y + r0.y, l1.x + r1.x, l1.y + r1.y};
-  const double g[3] = {l2.x + r2.x, l2.y + r2.y, l3.x + r3.x};
-  double flux = 0.0, corr = 0.0;
+  dd av[3], dx[3];
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const double kxj = av[d] - w * dx[d];
-    flux = fma(m[d] + g[d], av[d], flux);
-    corr = fma(kxj, g[d], corr);
+    av[d] = ldd(area + 3 * e + d);
+    dx[d] = ldd(coords + 3 * R + d) - ldd(coords + 3 * L + d);
   }
-  double tmdot = -projTimeScale * (r3.y - l3.y) * w;
-  tmdot = fma(0.5, fma(-noc, corr, flux), tmdot);
-  tmdot *= inv_tau;
-  buf[e] = -w * projTimeScale * inv_tau;
-  buf[E + e] = tmdot;
+  const dd asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
+  const dd axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
+  const dd w = asq * dd_rcp(axdx);
+  const dd projTimeScale = scale2(nl[0] + nr[0], 0.5f);
+  dd flux = {0.f, 0.f}, corr = {0.f, 0.f};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const dd m = nl[1 + d] + nr[1 + d];
+    const dd g = nl[4 + d] + nr[4 + d];
+    flux = (m + g) * av[d] + flux;
+    corr = (av[d] - w * dx[d]) * g + corr;
+  }
+  dd tmdot = -(projTimeScale * (nr[7] - nl[7]) * w);
+  tmdot = (tmdot + scale2(flux - noc * corr, 0.5f)) * inv_tau;
+  const dd f = -(w * projTimeScale * inv_tau);
+  reinterpret_cast<float4*>(buf)[e] = make_float4(f.hi, f.lo, tmdot.hi, tmdot.lo);
 }
 
 // General options (interpolation blend, incompressible density scaling).
+struct ContinuityDD {
+  dd noc, inv_tau, interp, om_interp, incomp, om_incomp;
+};
+
 __global__ void __launch_bounds__(kThreads)
     continuity_edge_k(int64_t E, const int2* __restrict__ edges,
                       const double* __restrict__ coords,
@@ -239,44 +265,46 @@ __global__ void __launch_bounds__(kThreads)
                       const double* __restrict__ density,
                       const double* __restrict__ pressure,
                       const double* __restrict__ udiag,
-                      const double* __restrict__ area, ContinuityOpts o,
-                      double* __restrict__ buf) {
+                      const double* __restrict__ area, ContinuityDD c,
+                      dd* __restrict__ buf) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= E) return;
   const int2 lr = edges[e];
   const int64_t L = lr.x, R = lr.y;
-  double av[3];
-  for (int d = 0; d < 3; ++d) av[d] = area[3 * e + d];
-  const double iuL = fast_rcp(udiag[L]), iuR = fast_rcp(udiag[R]);
-  const double densityL = density[L], densityR = density[R];
-  const double projTimeScale = 0.5 * (iuL + iuR);
-  const double rhoIp = 0.5 * (densityL + densityR);
-  const double denScale =
-      fast_rcp(rhoIp) * o.solve_incompressible + (1.0 - o.solve_incompressible);
-  double dx[3];
-  double axdx = 0.0, asq = 0.0;
+  const dd iuL = dd_rcp(ldd(udiag + L)), iuR = dd_rcp(ldd(udiag + R));
+  const dd densityL = ldd(density + L), densityR = ldd(density + R);
+  const dd projTimeScale = scale2(iuL + iuR, 0.5f);
+  const dd rhoIp = scale2(densityL + densityR, 0.5f);
+  const dd denScale = dd_rcp(rhoIp) * c.incomp + c.om_incomp;
+  dd av[3], dx[3];
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    dx[d] = coords[3 * R + d] - coords[3 * L + d];
-    asq += av[d] * av[d];
-    axdx += av[d] * dx[d];
+    av[d] = ldd(area + 3 * e + d);
+    dx[d] = ldd(coords + 3 * R + d) - ldd(coords + 3 * L + d);
   }
-  const double inv_axdx = fast_rcp(axdx);
-  double tmdot = -projTimeScale * (pressure[R] - pressure[L]) * asq * inv_axdx;
-  const double interp = o.interp_together, om_interp = 1.0 - o.interp_together;
+  const dd asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
+  const dd axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
+  const dd w = asq * dd_rcp(axdx);
+  dd tmdot = -(projTimeScale * (ldd(pressure + R) - ldd(pressure + L)) * w);
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const double kxj = av[d] - asq * inv_axdx * dx[d];
-    const double uR = velocity[3 * R + d], uL = velocity[3 * L + d];
-    const double rhoUjIp = 0.5 * (densityR * uR + densityL * uL);
-    const double ujIp = 0.5 * (uR + uL);
-    const double GjIp = 0.5 * (Gpdx[3 * R + d] * iuR + Gpdx[3 * L + d] * iuL);
-    tmdot += (interp * rhoUjIp + om_interp * rhoIp * ujIp + GjIp) * av[d] -
-             kxj * GjIp * o.noc_fac;
+    const dd kxj = av[d] - w * dx[d];
+    const dd uR = ldd(velocity + 3 * R + d), uL = ldd(velocity + 3 * L + d);
+    const dd rhoUjIp = scale2(densityR * uR + densityL * uL, 0.5f);
+    const dd ujIp = scale2(uR + uL, 0.5f);
+    const dd GjIp = scale2(ldd(Gpdx + 3 * R + d) * iuR + ldd(Gpdx + 3 * L + d) * iuL, 0.5f);
+    tmdot = tmdot + ((c.interp * rhoUjIp + c.om_interp * rhoIp * ujIp + GjIp) * av[d] -
+                     kxj * GjIp * c.noc);
   }
-  const double inv_tau = 1.0 / o.tau_scale;
-  tmdot *= inv_tau;
-  tmdot *= denScale;
-  buf[e] = -asq * inv_axdx * projTimeScale * denScale * inv_tau;
-  buf[E + e] = tmdot;
+  tmdot = tmdot * c.inv_tau * denScale;
+  const dd f = -(w * projTimeScale * denScale * c.inv_tau);
+  reinterpret_cast<float4*>(buf)[e] = make_float4(f.hi, f.lo, tmdot.hi, tmdot.lo);
+}
+
+__device__ __forceinline__ dd van_leer_dd(dd dqm, dd dqp, dd eps) {
+  const dd p = dqm * dqp;
+  const dd s = dqm + dqp;
+  return scale2(p + dd_abs(p), 2.0f) * dd_rcp(s * s + eps);
 }
 
 // ---------------------------------------------------------------------------
@@ -286,10 +314,15 @@ __global__ void __launch_bounds__(kThreads)
 //   LL = cLL I - N/relax,  LR = cLR I + N,  RL = cRL I + N,
 //   RR = cRR I - N/relax,  N_ij = -viscIp A_i A_j / (A.dx)
 // because the advective and diffusive factors do not depend on the
-// component; the rhs is (-tf, +tf). Output per edge (13 SoA arrays):
-// cLL, cLR, cRL, cRR, N00, N01, N02, N11, N12, N22, tf0, tf1, tf2.
+// component; the rhs is (-tf, +tf). Output per edge (13 SoA arrays of
+// float pairs): cLL, cLR, cRL, cRR, N00, N01, N02, N11, N12, N22, tf0, tf1,
+// tf2.
+struct MomentumDD {
+  dd alpha, alpha_upw, om_alpha, om_alpha_upw, upw, divu_fac, irelax, eps;
+};
+
 template <bool LIMITER, bool DIVU>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
     momentum_edge_k(int64_t E, const int2* __restrict__ edges,
                     const double* __restrict__ coords,
                     const double* __restrict__ vel,
@@ -298,91 +331,92 @@ __global__ void __launch_bounds__(kThreads)
                     const double* __restrict__ mask,
                     const double* __restrict__ area,
                     const double* __restrict__ mdotA,
-                    const double* __restrict__ pecA, MomentumOpts o,
-                    double irelax, double* __restrict__ buf) {
+                    const double* __restrict__ pecA, MomentumDD c,
+                    dd* __restrict__ buf) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= E) return;
-  const double eps = 1.0e-16;
   const int2 lr = edges[e];
   const int64_t L = lr.x, R = lr.y;
-  double av[3], dx[3], uL[3], uR[3];
+  dd av[3], dx[3], uL[3], uR[3];
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    av[d] = area[3 * e + d];
-    dx[d] = coords[3 * R + d] - coords[3 * L + d];
-    uL[d] = vel[3 * L + d];
-    uR[d] = vel[3 * R + d];
+    av[d] = ldd(area + 3 * e + d);
+    dx[d] = ldd(coords + 3 * R + d) - ldd(coords + 3 * L + d);
+    uL[d] = ldd(vel + 3 * L + d);
+    uR[d] = ldd(vel + 3 * R + d);
   }
-  const double mdot = mdotA[e];
-  const double viscIp = 0.5 * (viscosity[L] + viscosity[R]);
-  const double asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
-  const double axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
-  const double inv_axdx = fast_rcp(axdx);
-  double gL[9], gR[9];
-  for (int k = 0; k < 9; ++k) {
-    gL[k] = dudx[9 * L + k];
-    gR[k] = dudx[9 * R + k];
-  }
-  const double hdx[3] = {0.5 * dx[0], 0.5 * dx[1], 0.5 * dx[2]};
-  double duL[3], duR[3];
+  const dd mdot = ldd(mdotA + e);
+  const dd viscIp = scale2(ldd(viscosity + L) + ldd(viscosity + R), 0.5f);
+  const dd asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
+  const dd axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
+  const dd inv_axdx = dd_rcp(axdx);
+  dd hdx[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) hdx[d] = scale2(dx[d], 0.5f);
+  // duidxj with the over-relaxed non-orthogonal correction (gj holds the
+  // sum, not the mean, of the two nodal gradients); duL / duR are the
+  // extrapolation increments 0.5 dx . grad u of each side
+  dd duidxj[3][3], duL[3], duR[3];
+#pragma unroll
   for (int i = 0; i < 3; ++i) {
-    duL[i] = hdx[0] * gL[3 * i] + hdx[1] * gL[3 * i + 1] + hdx[2] * gL[3 * i + 2];
-    duR[i] = hdx[0] * gR[3 * i] + hdx[1] * gR[3 * i + 1] + hdx[2] * gR[3 * i + 2];
+    dd gl[3], gr[3], gj[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      gl[j] = ldd(dudx + 9 * L + 3 * i + j);
+      gr[j] = ldd(dudx + 9 * R + 3 * i + j);
+      gj[j] = gr[j] + gl[j];
+    }
+    duL[i] = hdx[0] * gl[0] + hdx[1] * gl[1] + hdx[2] * gl[2];
+    duR[i] = hdx[0] * gr[0] + hdx[1] * gr[1] + hdx[2] * gr[2];
+    const dd gjuidx = hdx[0] * gj[0] + hdx[1] * gj[1] + hdx[2] * gj[2];
+    const dd corr = ((uR[i] - uL[i]) - gjuidx) * inv_axdx;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) duidxj[i][j] = corr * av[j] + scale2(gj[j], 0.5f);
   }
-  double limitL[3] = {1.0, 1.0, 1.0}, limitR[3] = {1.0, 1.0, 1.0};
+  dd limitL[3], limitR[3];
   if (LIMITER) {
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const double du = uR[d] - uL[d];
-      limitL[d] = van_leer(4.0 * duL[d] - du, du, eps);
-      limitR[d] = van_leer(4.0 * duR[d] - du, du, eps);
+      const dd du = uR[d] - uL[d];
+      limitL[d] = van_leer_dd(scale2(duL[d], 4.0f) - du, du, c.eps);
+      limitR[d] = van_leer_dd(scale2(duR[d], 4.0f) - du, du, c.eps);
     }
   }
-  const double pecfac = pecA[e];
-  const double om_pecfac = 1.0 - pecfac;
-  const double alpha = o.alpha, alphaUpw = o.alpha_upw;
-  const double om_alpha = 1.0 - alpha, om_alphaUpw = 1.0 - alphaUpw;
-  // duidxj with the over-relaxed non-orthogonal correction; gj holds the
-  // sum (not the mean) of the two nodal gradients
-  double duidxj[3][3];
-  for (int i = 0; i < 3; ++i) {
-    const double dui = uR[i] - uL[i];
-    double gj[3];
-    for (int j = 0; j < 3; ++j) gj[j] = gR[3 * i + j] + gL[3 * i + j];
-    const double gjuidx = hdx[0] * gj[0] + hdx[1] * gj[1] + hdx[2] * gj[2];
-    const double corr = (dui - gjuidx) * inv_axdx;
-    for (int j = 0; j < 3; ++j) duidxj[i][j] = fma(corr, av[j], 0.5 * gj[j]);
-  }
-  const double maskNode = fmin(mask[L], mask[R]);
-  double tf[3];
-  double divU = 0.0;
+  const dd pecfac = ldd(pecA + e);
+  const dd om_pecfac = dd{1.0f, 0.0f} - pecfac;
+  const dd maskNode = dd_min(ldd(mask + L), ldd(mask + R));
+  dd divU = {0.f, 0.f};
   if (DIVU) divU = duidxj[0][0] + duidxj[1][1] + duidxj[2][2];
-  const bool up = mdot > 0.0;
+  const bool up = dd_gt0(mdot);
+  dd tf[3];
+#pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const double uIpL = uL[i] + duL[i] * o.upw_factor * limitL[i];
-    const double uIpR = uR[i] - duR[i] * o.upw_factor * limitR[i];
-    const double uiIp = 0.5 * (uR[i] + uL[i]);
-    const double uiUpw = alphaUpw * (up ? uIpL : uIpR) + om_alphaUpw * uiIp;
-    const double uiCds = 0.5 * (alpha * (uIpL + uIpR)) + om_alpha * uiIp;
-    const double adv_flux = mdot * (pecfac * uiUpw + om_pecfac * uiCds);
-    double s = (duidxj[i][0] + duidxj[0][i]) * av[0] +
-               (duidxj[i][1] + duidxj[1][i]) * av[1] +
-               (duidxj[i][2] + duidxj[2][i]) * av[2];
-    double diff_flux = -viscIp * s;
-    if (DIVU) diff_flux = fma(divU, 2.0 / 3.0 * viscIp * av[i] * o.include_div_u, diff_flux);
-    tf[i] = fma(diff_flux, maskNode, adv_flux);
+    const dd uIpL = uL[i] + (LIMITER ? duL[i] * c.upw * limitL[i] : duL[i] * c.upw);
+    const dd uIpR = uR[i] - (LIMITER ? duR[i] * c.upw * limitR[i] : duR[i] * c.upw);
+    const dd uiIp = scale2(uR[i] + uL[i], 0.5f);
+    const dd uiUpw = c.alpha_upw * (up ? uIpL : uIpR) + c.om_alpha_upw * uiIp;
+    const dd uiCds = scale2(c.alpha * (uIpL + uIpR), 0.5f) + c.om_alpha * uiIp;
+    const dd adv_flux = mdot * (pecfac * uiUpw + om_pecfac * uiCds);
+    const dd sd = (duidxj[i][0] + duidxj[0][i]) * av[0] + (duidxj[i][1] + duidxj[1][i]) * av[1] +
+                  (duidxj[i][2] + duidxj[2][i]) * av[2];
+    dd diff_flux = -(viscIp * sd);
+    if (DIVU) diff_flux = divU * (c.divu_fac * viscIp * av[i]) + diff_flux;
+    tf[i] = diff_flux * maskNode + adv_flux;
   }
-  const double aUL = 0.5 * (mdot + fabs(mdot)) * pecfac * alphaUpw +
-                     0.5 * alpha * om_pecfac * mdot;
-  const double aUR = 0.5 * (mdot - fabs(mdot)) * pecfac * alphaUpw +
-                     0.5 * alpha * om_pecfac * mdot;
-  const double aC = 0.5 * mdot * (pecfac * om_alphaUpw + om_pecfac * om_alpha);
-  const double dlhsfac = -viscIp * asq * inv_axdx;
-  double* b = buf + e;
-  b[0] = ((aUL + aC) - dlhsfac) * irelax;
+  const dd hm = scale2(mdot, 0.5f);
+  const dd habs = scale2(dd_abs(mdot), 0.5f);
+  const dd cen = c.alpha * om_pecfac * hm;
+  const dd aUL = (hm + habs) * pecfac * c.alpha_upw + cen;
+  const dd aUR = (hm - habs) * pecfac * c.alpha_upw + cen;
+  const dd aC = hm * (pecfac * c.om_alpha_upw + om_pecfac * c.om_alpha);
+  const dd t = -(viscIp * inv_axdx);
+  const dd dlhsfac = t * asq;
+  const dd ta0 = t * av[0], ta1 = t * av[1], ta2 = t * av[2];
+  dd* b = buf + e;
+  b[0] = ((aUL + aC) - dlhsfac) * c.irelax;
   b[E] = (aUR + aC) + dlhsfac;
   b[2 * E] = (-aUL - aC) + dlhsfac;
-  b[3 * E] = ((-aUR - aC) - dlhsfac) * irelax;
-  const double t = -viscIp * inv_axdx;
-  const double ta0 = t * av[0], ta1 = t * av[1], ta2 = t * av[2];
+  b[3 * E] = ((-aUR - aC) - dlhsfac) * c.irelax;
   b[4 * E] = ta0 * av[0];
   b[5 * E] = ta0 * av[1];
   b[6 * E] = ta0 * av[2];
@@ -401,9 +435,12 @@ __global__ void __launch_bounds__(kThreads)
 // whole range with coalesced accesses. Blocks whose range exceeds the
 // staging capacity write straight to global memory.
 //
-// KIND 0: scalar (six coefficients per edge), KIND 1: continuity (f,
-// tmdot). Incident entries come in column order; bit 31 marks a repeat of
-// the previous column (periodic duplicates).
+// KIND 0: scalar (six FP64 coefficients per edge), KIND 1: continuity
+// (f, tmdot as float pairs). Incident entries come in column order; bit 31
+// marks a repeat of the previous column (periodic duplicates).
+__device__ __forceinline__ double to_f64(double v) { return v; }
+__device__ __forceinline__ double to_f64(dd v) { return dd_to_double(v); }
+
 template <int KIND>
 __global__ void __launch_bounds__(kRow1Threads)
     row1_k(int64_t R, const int32_t* __restrict__ inc_ptr,
@@ -411,6 +448,8 @@ __global__ void __launch_bounds__(kRow1Threads)
            const int64_t* __restrict__ row_ptr, const double* __restrict__ buf,
            int64_t E, double* __restrict__ values, double* __restrict__ rhs,
            int accumulate, int smem_bytes) {
+  using C = typename std::conditional<KIND == 0, double, dd>::type;
+  const C* cb = reinterpret_cast<const C*>(buf);
   extern __shared__ double stage[];
   const int64_t r0 = int64_t(blockIdx.x) * kRow1Threads;
   const int64_t r1 = (r0 + kRow1Threads < R) ? r0 + kRow1Threads : R;
@@ -425,20 +464,21 @@ __global__ void __launch_bounds__(kRow1Threads)
     const bool acc = accumulate && !staged;
     if (s != t) {
       const int dp = diag_pos[r];
-      double dg = 0.0, rr = 0.0, off = 0.0;
+      C dg{}, rr{}, off{};
       int slot = -1;
       for (int32_t qi = s; qi < t; ++qi) {
         const uint32_t w = inc[qi];
         const bool dup = (w >> 31) != 0;
         const int64_t e = (w & 0x7fffffffu) >> 1;
         const int side = w & 1u;
-        double co, cd, cr;
-        if (KIND == 0) {
-          co = buf[(side ? 2 : 1) * E + e];
-          cd = buf[(side ? 3 : 0) * E + e];
-          cr = buf[(side ? 5 : 4) * E + e];
+        C co, cd, cr;
+        if constexpr (KIND == 0) {
+          co = cb[(side ? 2 : 1) * E + e];
+          cd = cb[(side ? 3 : 0) * E + e];
+          cr = cb[(side ? 5 : 4) * E + e];
         } else {
-          const double f = buf[e], tm = buf[E + e];
+          const float4 q = reinterpret_cast<const float4*>(buf)[e];
+          const dd f{q.x, q.y}, tm{q.z, q.w};
           co = f;
           cd = -f;
           cr = side ? tm : -tm;
@@ -446,20 +486,22 @@ __global__ void __launch_bounds__(kRow1Threads)
         if (!dup) {
           if (slot >= 0) {
             double* p = out + (slot < dp ? slot : slot + 1);
-            *p = acc ? *p + off : off;
+            const double v = to_f64(off);
+            *p = acc ? *p + v : v;
           }
           ++slot;
           off = co;
         } else {
-          off += co;
+          off = off + co;
         }
-        dg += cd;
-        rr += cr;
+        dg = dg + cd;
+        rr = rr + cr;
       }
       double* p = out + (slot < dp ? slot : slot + 1);
-      *p = acc ? *p + off : off;
-      out[dp] = acc ? out[dp] + dg : dg;
-      rhs[r] = accumulate ? rhs[r] + rr : rr;
+      const double v = to_f64(off), vd = to_f64(dg), vr = to_f64(rr);
+      *p = acc ? *p + v : v;
+      out[dp] = acc ? out[dp] + vd : vd;
+      rhs[r] = accumulate ? rhs[r] + vr : vr;
     } else if (!acc) {
       // a row without edges: zero it (its entries are not otherwise written)
       for (int64_t k = 0; k < row_ptr[r + 1] - rb; ++k) out[k] = 0.0;
@@ -473,13 +515,14 @@ __global__ void __launch_bounds__(kRow1Threads)
 }
 
 // 3-dof momentum: one thread per node row builds the node's three CSR rows
-// (block column k at positions 3k..3k+2).
+// (block column k at positions 3k..3k+2) from the float-pair coefficients.
 __global__ void __launch_bounds__(kRow3Threads)
     row3_k(int64_t R, const int32_t* __restrict__ inc_ptr,
            const uint32_t* __restrict__ inc, const int32_t* __restrict__ diag_pos,
            const int64_t* __restrict__ row_ptr, const double* __restrict__ buf,
-           int64_t E, double irelax, double* __restrict__ values,
+           int64_t E, dd irelax, double* __restrict__ values,
            double* __restrict__ rhs, int accumulate, int smem_bytes) {
+  const dd* cb = reinterpret_cast<const dd*>(buf);
   extern __shared__ double stage[];
   const int64_t r0 = int64_t(blockIdx.x) * kRow3Threads;
   const int64_t r1 = (r0 + kRow3Threads < R) ? r0 + kRow3Threads : R;
@@ -497,63 +540,65 @@ __global__ void __launch_bounds__(kRow3Threads)
     const bool acc = accumulate && !staged;
     if (s != t) {
       const int dp = diag_pos[r];
-      double dgc = 0.0, dN[6] = {0, 0, 0, 0, 0, 0}, rr[3] = {0, 0, 0};
-      double ob[9];
+      dd dgc{}, dN[6] = {}, rr[3] = {};
+      dd ob[9];
       int slot = -1;
-      auto flush = [&](int sl) {
-        const int k = 3 * (sl < dp ? sl : sl + 1);
-        for (int c = 0; c < 3; ++c) {
-          v0[k + c] = acc ? v0[k + c] + ob[c] : ob[c];
-          v1[k + c] = acc ? v1[k + c] + ob[3 + c] : ob[3 + c];
-          v2[k + c] = acc ? v2[k + c] + ob[6 + c] : ob[6 + c];
+      // every 3x3 block is symmetric (c I + N, N symmetric): six widenings
+      auto put_block = [&](int k, const dd* bl) {
+        const double d00 = dd_to_double(bl[0]), d01 = dd_to_double(bl[1]),
+                     d02 = dd_to_double(bl[2]), d11 = dd_to_double(bl[4]),
+                     d12 = dd_to_double(bl[5]), d22 = dd_to_double(bl[8]);
+        const double o0[3] = {d00, d01, d02}, o1[3] = {d01, d11, d12}, o2[3] = {d02, d12, d22};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          v0[k + q] = acc ? v0[k + q] + o0[q] : o0[q];
+          v1[k + q] = acc ? v1[k + q] + o1[q] : o1[q];
+          v2[k + q] = acc ? v2[k + q] + o2[q] : o2[q];
         }
       };
+      auto flush = [&](int sl) { put_block(3 * (sl < dp ? sl : sl + 1), ob); };
       for (int32_t qi = s; qi < t; ++qi) {
         const uint32_t w = inc[qi];
         const bool dup = (w >> 31) != 0;
         const int64_t e = (w & 0x7fffffffu) >> 1;
         const int side = w & 1u;
-        const double co = buf[(side ? 2 : 1) * E + e];
-        const double cd = buf[(side ? 3 : 0) * E + e];
-        double n[6];
-        for (int k = 0; k < 6; ++k) n[k] = buf[(4 + k) * E + e];
-        const double f0 = buf[10 * E + e], f1 = buf[11 * E + e], f2 = buf[12 * E + e];
-        if (side) {
-          rr[0] += f0;
-          rr[1] += f1;
-          rr[2] += f2;
-        } else {
-          rr[0] -= f0;
-          rr[1] -= f1;
-          rr[2] -= f2;
+        const dd co = cb[(side ? 2 : 1) * E + e];
+        const dd cd = cb[(side ? 3 : 0) * E + e];
+        dd n[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) n[k] = cb[(4 + k) * E + e];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const dd f = cb[(10 + k) * E + e];
+          rr[k] = side ? rr[k] + f : rr[k] - f;
         }
-        const double blk[9] = {co + n[0], n[1], n[2], n[1], co + n[3], n[4],
-                               n[2], n[4], co + n[5]};
+        const dd blk[9] = {co + n[0], n[1], n[2], n[1], co + n[3], n[4], n[2], n[4], co + n[5]};
         if (!dup) {
           if (slot >= 0) flush(slot);
           ++slot;
+#pragma unroll
           for (int k = 0; k < 9; ++k) ob[k] = blk[k];
         } else {
-          for (int k = 0; k < 9; ++k) ob[k] += blk[k];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) ob[k] = ob[k] + blk[k];
         }
-        dgc += cd;
-        for (int k = 0; k < 6; ++k) dN[k] += n[k];
+        dgc = dgc + cd;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) dN[k] = dN[k] + n[k];
       }
       flush(slot);
       // diagonal block: sum(c) I - sum(N) / relax; cLL and cRR already
       // carry the 1/relax factor, N is scaled here
-      if (irelax != 1.0)
-        for (int q = 0; q < 6; ++q) dN[q] *= irelax;
-      const double db[9] = {dgc - dN[0], -dN[1], -dN[2], -dN[1], dgc - dN[3],
-                            -dN[4], -dN[2], -dN[4], dgc - dN[5]};
-      const int k = 3 * dp;
-      for (int c = 0; c < 3; ++c) {
-        v0[k + c] = acc ? v0[k + c] + db[c] : db[c];
-        v1[k + c] = acc ? v1[k + c] + db[3 + c] : db[3 + c];
-        v2[k + c] = acc ? v2[k + c] + db[6 + c] : db[6 + c];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) dN[q] = dN[q] * irelax;
+      const dd db[9] = {dgc - dN[0], -dN[1], -dN[2], -dN[1], dgc - dN[3],
+                        -dN[4], -dN[2], -dN[4], dgc - dN[5]};
+      put_block(3 * dp, db);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const double d = dd_to_double(rr[q]);
+        rhs[3 * r + q] = accumulate ? rhs[3 * r + q] + d : d;
       }
-      for (int q = 0; q < 3; ++q)
-        rhs[3 * r + q] = accumulate ? rhs[3 * r + q] + rr[q] : rr[q];
     } else if (!acc) {
       for (int64_t k = 0; k < row_ptr[3 * r + 3] - b0; ++k) v0[k] = 0.0;
       if (!accumulate)
@@ -647,20 +692,31 @@ bool continuity_fast_path(const ContinuityOpts& o) {
   return o.interp_together == 1.0 && o.solve_incompressible == 0.0;
 }
 
+dd dd_param(double x) { return dd_from_double(x); }
+
 void launch_continuity_edges(cudaStream_t s, int64_t E, int64_t N,
                              const int2* edges, const nw_continuity_fields& f,
                              const ContinuityOpts& o, double* buf,
                              double* nodebuf) {
   if (E == 0) return;
+  dd* b = reinterpret_cast<dd*>(buf);
   if (nodebuf && continuity_fast_path(o)) {
+    dd* nb = reinterpret_cast<dd*>(nodebuf);
     continuity_node_k<<<grid_for(N), kThreads, 0, s>>>(
-        N, f.velocity, f.dpdx, f.density, f.pressure, f.udiag, nodebuf);
+        N, f.velocity, f.dpdx, f.density, f.pressure, f.udiag, nb);
     continuity_edge_fast_k<<<grid_for(E), kThreads, 0, s>>>(
-        E, edges, f.coords, nodebuf, f.area, o.noc_fac, 1.0 / o.tau_scale, buf);
+        E, edges, f.coords, nb, f.area, dd_param(o.noc_fac), dd_param(1.0 / o.tau_scale), b);
   } else {
+    ContinuityDD c;
+    c.noc = dd_param(o.noc_fac);
+    c.inv_tau = dd_param(1.0 / o.tau_scale);
+    c.interp = dd_param(o.interp_together);
+    c.om_interp = dd_param(1.0 - o.interp_together);
+    c.incomp = dd_param(o.solve_incompressible);
+    c.om_incomp = dd_param(1.0 - o.solve_incompressible);
     continuity_edge_k<<<grid_for(E), kThreads, 0, s>>>(
         E, edges, f.coords, f.velocity, f.dpdx, f.density, f.pressure, f.udiag,
-        f.area, o, buf);
+        f.area, c, b);
   }
 }
 
@@ -674,12 +730,21 @@ void launch_momentum_edges(cudaStream_t s, int64_t E, const int2* edges,
                            const nw_momentum_fields& f, const MomentumOpts& o,
                            double* buf) {
   if (E == 0) return;
-  const double irelax = 1.0 / o.relax;
+  MomentumDD c;
+  c.alpha = dd_param(o.alpha);
+  c.alpha_upw = dd_param(o.alpha_upw);
+  c.om_alpha = dd_param(1.0 - o.alpha);
+  c.om_alpha_upw = dd_param(1.0 - o.alpha_upw);
+  c.upw = dd_param(o.upw_factor);
+  c.divu_fac = dd_param(2.0 / 3.0 * o.include_div_u);
+  c.irelax = dd_param(1.0 / o.relax);
+  c.eps = dd_param(1.0e-16);
+  dd* b = reinterpret_cast<dd*>(buf);
   const bool lim = o.use_limiter != 0, divu = o.include_div_u != 0.0;
 #define NW_MOM(LIM, DIV)                                                     \
   momentum_edge_k<LIM, DIV><<<grid_for(E), kThreads, 0, s>>>(                \
       E, edges, f.coords, f.velocity, f.dudx, f.viscosity, f.mask, f.area,   \
-      f.mdot, f.pecfac, o, irelax, buf)
+      f.mdot, f.pecfac, c, b)
   if (lim && divu) NW_MOM(true, true);
   else if (lim) NW_MOM(true, false);
   else if (divu) NW_MOM(false, true);
@@ -717,8 +782,8 @@ void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
         R, inc_ptr, inc, diag_pos, row_ptr, buf, E, values, rhs, accumulate, smem_bytes);
   else
     row3_k<<<grid_for(R, kRow3Threads), kRow3Threads, smem_bytes, s>>>(
-        R, inc_ptr, inc, diag_pos, row_ptr, buf, E, 1.0 / relax, values, rhs, accumulate,
-        smem_bytes);
+        R, inc_ptr, inc, diag_pos, row_ptr, buf, E, dd_param(1.0 / relax), values, rhs,
+        accumulate, smem_bytes);
 }
 
 void launch_reset_rows(cudaStream_t s, int64_t n, const int64_t* nodes,

@@ -12,7 +12,9 @@ using ScalarOpts = nw_scalar_opts;
 using ContinuityOpts = nw_continuity_opts;
 using MomentumOpts = nw_momentum_opts;
 
-// Coefficients written per edge by the edge phase (SoA arrays of E).
+// 8-byte coefficient slots per edge written by the edge phase: scalar, six
+// FP64 SoA arrays of E; continuity, one 16-byte record (f, tmdot as float
+// pairs) per edge; momentum, 13 SoA arrays of E float pairs.
 constexpr int kScalarCoefs = 6;
 constexpr int kContinuityCoefs = 2;
 constexpr int kMomentumCoefs = 13;
