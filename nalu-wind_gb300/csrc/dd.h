@@ -12,7 +12,7 @@
 //   mul:  |err| <= 4 u^2 |a b|
 //   rcp:  |err| <= 3 u^2 / |x|            (one Newton step from a float seed)
 // Conversions from double keep the top 48 significand bits (the split error
-// is <= 2^-48 relative); dd -> double adds the two widened halves once. The
+// is <= 2^-48 relative); dd -> double rounds hi + lo once. The
 // exponent range is the float range: |x| >= 2^128 becomes infinite, and
 // below 2^-126 the precision degrades gradually (subnormal lo, then hi).
 //
@@ -147,6 +147,11 @@ NW_HD double widen(float f) {
   return u2d(sign | bits);
 }
 
+// hi + lo rounded to the nearest double: both halves widen exactly, so the
+// one FP64 add rounds the exact sum once. (An integer-only rounding of the
+// pair was measured slower in the row kernels: its ~40-instruction
+// dependency chain is not hidden at their occupancy, while the add runs on
+// the otherwise idle FP64 pipe.)
 NW_HD double dd_to_double(dd a) { return widen(a.hi) + widen(a.lo); }
 
 // Split of a double into hi (top 24 significand bits) + lo (the next 24,

@@ -6,6 +6,7 @@ error bounds, on the CPU, in x87 extended precision (64-bit significand):
   a * b:              |err| <= 2^-45 |a b|
   1 / a:              |err| <= 2^-45 / |a|
   widen(float):       exact
+  dd -> double:       hi + lo correctly rounded (ties to even)
 
 The edge-assembly kernels evaluate their FP64 formulas in this arithmetic;
 the GPU parity tests then bound the assembled entries by 1e-12 times their
@@ -107,3 +108,23 @@ def test_add_mul_rcp_bounds(lib):
     q = _ld(_op(lib, 4, a, b))
     Bh = b[0].astype(np.longdouble)
     assert np.all(np.abs(q - A * Bh) <= 2.0 ** -45 * np.abs(A * Bh))
+
+
+def test_pair_to_double_is_correctly_rounded(lib):
+    from fractions import Fraction
+    rng = np.random.default_rng(3)
+    n = 4000
+    hi = (rng.choice([-1, 1], n) * 10.0 ** rng.uniform(-30, 30, n)).astype(np.float32)
+    # lo a few to many binades below hi, either sign, including exact ties
+    k = rng.integers(1, 80, n)
+    lo = (hi.astype(np.float64) * rng.choice([-1, 1], n) * 2.0 ** (-k.astype(np.float64))
+          * rng.uniform(0.5, 1.0, n)).astype(np.float32)
+    lo[:100] = (hi[:100].astype(np.float64) * 2.0 ** -53).astype(np.float32)   # half-ulp ties
+    lo[100:200] = (hi[100:200].astype(np.float64) * 3.0 * 2.0 ** -54).astype(np.float32)
+    lo[200:300] = -lo[200:300]
+    lo[300:310] = 0.0
+    out = np.zeros(n)
+    lib.dd_back(C.c_int64(n), _p(hi, C.c_float), _p(lo, C.c_float), _p(out, C.c_double))
+    for h, l, o in zip(hi.tolist(), lo.tolist(), out.tolist()):
+        exact = float(Fraction(h) + Fraction(l))
+        assert o == exact, (h, l, o, exact)
