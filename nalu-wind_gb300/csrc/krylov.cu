@@ -323,21 +323,28 @@ __global__ void scale_jacobi_k(int64_t n, const T* __restrict__ w,
   if (rd) z[i] = vi * rd[i];
 }
 
-// one colour of a Gauss-Seidel sweep: rows of this colour are mutually
-// independent, so they relax in parallel using the current y.
+// One colour class of the Gauss-Seidel sweep over the class-ordered sliced
+// copy (off-diagonal entries only, same column order as the CSR row):
+//   y_i = (x_i - sum_{j != i} a_ij y_j) / a_ii
+// `first`: every y_j is still zero, so y_i = x_i / a_ii without the sum.
 template <typename VT, typename T>
 __global__ void __launch_bounds__(kBlock)
-    gs_color_k(int64_t cnt, const int32_t* __restrict__ rows,
-               const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
-               const VT* __restrict__ v, const T* __restrict__ rd,
-               const T* __restrict__ x, T* __restrict__ y) {
+    gs_sell_k(int64_t cnt, const int32_t* __restrict__ rows,
+              const int64_t* __restrict__ off, const int32_t* __restrict__ len,
+              const int32_t* __restrict__ cols, const VT* __restrict__ v,
+              const T* __restrict__ rd, const T* __restrict__ x, T* __restrict__ y,
+              int first) {
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= cnt) return;
   const int32_t i = rows[k];
   T s = x[i];
-  for (int64_t p = rp[i]; p < rp[i + 1]; ++p) {
-    const int32_t j = ci[p];
-    if (j != i) s -= T(v[p]) * y[j];
+  if (!first) {
+    const int64_t base = off[k >> 5] + (k & 31);
+    const int n = len[k];
+    for (int q = 0; q < n; ++q) {
+      const int64_t p = base + 32 * int64_t(q);
+      s -= T(v[p]) * y[cols[p]];
+    }
   }
   y[i] = s * rd[i];
 }
@@ -487,6 +494,9 @@ void KrylovSolver::refresh(cudaStream_t s) {
   if (sell_slices_)
     sell_gather_k<<<grid1(int64_t(sell_vals_.n)), kBlock, 0, s>>>(
         int64_t(sell_vals_.n), sell_map_.p, A_.values, sell_vals_.p, nullptr);
+  if (gs_map_.n)
+    sell_gather_k<<<grid1(int64_t(gs_map_.n)), kBlock, 0, s>>>(
+        int64_t(gs_map_.n), gs_map_.p, A_.values, gs_vals_.p, nullptr);
   if (cl_) cl_->refresh(A_.values, s);
   NW_CUDA(cudaGetLastError());
   f32_valid_ = false;
@@ -507,6 +517,11 @@ void KrylovSolver::ensure_f32(cudaStream_t s) {
     sell_vals32_.resize(sell_vals_.n);
     sell_gather_k<<<grid1(int64_t(sell_vals_.n)), kBlock, 0, s>>>(
         int64_t(sell_vals_.n), sell_map_.p, A_.values, sell_vals_.p, sell_vals32_.p);
+  }
+  if (gs_map_.n) {
+    gs_vals32_.resize(gs_map_.n);
+    convert_k<double, float><<<grid1(int64_t(gs_map_.n)), kBlock, 0, s>>>(
+        int64_t(gs_map_.n), gs_vals_.p, gs_vals32_.p);
   }
   convert_k<double, float><<<grid1(n), kBlock, 0, s>>>(n, rdiag_.p, rdiag32_.p);
   NW_CUDA(cudaGetLastError());
@@ -562,19 +577,6 @@ void precond_apply_t(const Precond& pc, int64_t n, const int64_t* rp,
     NW_CUDA(cudaMemcpyAsync(y, x, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
   } else if (pc.kind == NW_PC_JACOBI) {
     jacobi_k<T><<<grid1(n), kBlock, 0, s>>>(n, rd, x, y);
-  } else if (pc.kind == NW_PC_SGS) {
-    fill_k<T><<<grid1(n), kBlock, 0, s>>>(n, y, T(0));
-    const int nc = int(pc.color_ptr.size()) - 1;
-    for (int c = 0; c < nc; ++c) {
-      const int64_t b = pc.color_ptr[c], cnt = pc.color_ptr[c + 1] - b;
-      if (cnt) gs_color_k<VT, T><<<grid1(cnt), kBlock, 0, s>>>(
-          cnt, pc.color_rows + b, rp, ci, v, rd, x, y);
-    }
-    for (int c = nc - 1; c >= 0; --c) {
-      const int64_t b = pc.color_ptr[c], cnt = pc.color_ptr[c + 1] - b;
-      if (cnt) gs_color_k<VT, T><<<grid1(cnt), kBlock, 0, s>>>(
-          cnt, pc.color_rows + b, rp, ci, v, rd, x, y);
-    }
   } else {
     fail(NW_INVALID_ARG, "preconditioner not available for this precision");
   }
@@ -593,6 +595,77 @@ bool stalled(int& stalls, double rnorm, double prev) {
 
 }  // namespace
 
+// Symmetric multicolour Gauss-Seidel, y = M^-1 x: forward over the colour
+// classes, then backward. The first class of the forward sweep reads only
+// zeros (y = x / diag); the last forward class is not repeated at the start
+// of the backward sweep (its rows would be recomputed from the same values,
+// giving the same bits). With at most two classes nothing reads a y value
+// before it is written, so y needs no zero fill.
+template <typename VT, typename T>
+void KrylovSolver::sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s) const {
+  const int nc = int(gs_cptr_.size()) - 1;
+  if (nc < 1) fail(NW_INTERNAL, "Gauss-Seidel colour classes not set up");
+  if (nc > 2) fill_k<T><<<grid1(A_.n), kBlock, 0, s>>>(A_.n, y, T(0));
+  auto pass = [&](int c, int first) {
+    const int64_t b = gs_cptr_[c], cnt = gs_cptr_[c + 1] - b;
+    if (cnt)
+      gs_sell_k<VT, T><<<grid1(cnt), kBlock, 0, s>>>(cnt, gs_rows_.p + b, gs_off_.p + gs_slice0_[c],
+                                                     gs_len_.p + b, gs_cols_.p, vals, rd, x, y,
+                                                     first);
+  };
+  for (int c = 0; c < nc; ++c) pass(c, c == 0);
+  for (int c = nc - 2; c >= 0; --c) pass(c, 0);
+  NW_CUDA(cudaGetLastError());
+}
+
+void KrylovSolver::setup_colors(const std::vector<int32_t>& rows,
+                                const std::vector<int64_t>& cptr, cudaStream_t s) {
+  const int64_t n = A_.n;
+  if (!A_.row_ptr_host || !A_.col_idx_host) fail(NW_INTERNAL, "host graph needed");
+  if (int64_t(rows.size()) != n || cptr.empty() || cptr.back() != n)
+    fail(NW_INTERNAL, "colour classes do not cover the rows");
+  const int nc = int(cptr.size()) - 1;
+  gs_cptr_ = cptr;
+  gs_slice0_.assign(nc + 1, 0);
+  for (int c = 0; c < nc; ++c) gs_slice0_[c + 1] = gs_slice0_[c] + (cptr[c + 1] - cptr[c] + 31) / 32;
+  const int64_t ns = gs_slice0_[nc];
+  std::vector<int32_t> len(n, 0);
+  std::vector<int64_t> off(ns + 1, 0);
+  for (int c = 0; c < nc; ++c)
+    for (int64_t k = cptr[c]; k < cptr[c + 1]; ++k) {
+      const int32_t i = rows[k];
+      int32_t cnt = 0;
+      for (int64_t p = A_.row_ptr_host[i]; p < A_.row_ptr_host[i + 1]; ++p)
+        cnt += A_.col_idx_host[p] != i;
+      len[k] = cnt;
+      const int64_t sl = gs_slice0_[c] + (k - cptr[c]) / 32;
+      off[sl + 1] = std::max<int64_t>(off[sl + 1], 32 * int64_t(cnt));
+    }
+  for (int64_t sl = 0; sl < ns; ++sl) off[sl + 1] += off[sl];
+  std::vector<int32_t> cols(off[ns], 0), map(off[ns], -1);
+  for (int c = 0; c < nc; ++c)
+    for (int64_t k = cptr[c]; k < cptr[c + 1]; ++k) {
+      const int32_t i = rows[k];
+      const int64_t kl = k - cptr[c];
+      const int64_t base = off[gs_slice0_[c] + kl / 32] + (kl & 31);
+      int64_t q = 0;
+      for (int64_t p = A_.row_ptr_host[i]; p < A_.row_ptr_host[i + 1]; ++p) {
+        if (A_.col_idx_host[p] == i) continue;
+        cols[base + 32 * q] = A_.col_idx_host[p];
+        map[base + 32 * q] = int32_t(p);
+        ++q;
+      }
+    }
+  gs_rows_.upload(rows, s);
+  gs_len_.upload(len, s);
+  gs_off_.upload(off, s);
+  gs_cols_.upload(cols, s);
+  gs_map_.upload(map, s);
+  gs_vals_.resize(std::max<int64_t>(off[ns], 1));
+  gs_vals32_.release();
+  f32_valid_ = false;
+}
+
 // FP32 preconditioner of the mixed method. Learned (two-level, symmetric
 // smoothing): z1 = SGS(x), r1 = x - A z1, ec = Net(R r1),
 // z2 = z1 + alpha P ec with the energy-optimal alpha, then the
@@ -600,16 +673,17 @@ bool stalled(int& stalls, double rnorm, double prev) {
 void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
                              cudaStream_t s) {
   const int64_t n = A_.n;
+  if (pc.kind == NW_PC_SGS) {
+    sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s);
+    return;
+  }
   if (pc.kind != NW_PC_LEARNED) {
     precond_apply_t<float, float>(pc, n, A_.row_ptr, A_.col_idx, vals32_.p,
                                   rdiag32_.p, x, y, s);
     return;
   }
   if (!has_learned()) fail(NW_INVALID_ARG, "no learned preconditioner attached");
-  Precond sgs = pc;
-  sgs.kind = NW_PC_SGS;
-  precond_apply_t<float, float>(sgs, n, A_.row_ptr, A_.col_idx, vals32_.p,
-                                rdiag32_.p, x, y, s);
+  sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s);
   tmp32_.resize(n);
   rc32_.resize(cl_->nc);
   ec32_.resize(cl_->nc);
@@ -622,8 +696,7 @@ void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
   post32_.resize(n);
   spmv32(y, tmp32_.p, s);
   rsub_f32_k<<<grid1(n), kBlock, 0, s>>>(n, x, tmp32_.p);
-  precond_apply_t<float, float>(sgs, n, A_.row_ptr, A_.col_idx, vals32_.p,
-                                rdiag32_.p, tmp32_.p, post32_.p, s);
+  sgs<float, float>(gs_vals32_.p, rdiag32_.p, tmp32_.p, post32_.p, s);
   add32_k<<<grid1(n), kBlock, 0, s>>>(n, post32_.p, y);
   NW_CUDA(cudaGetLastError());
 }
@@ -643,6 +716,10 @@ void KrylovSolver::apply_precond(const Precond& pc, const double* x, double* y,
     z32_.resize(n);
     precond32(pc, tmp32b_.p, z32_.p, s);
     convert_k<float, double><<<grid1(n), kBlock, 0, s>>>(n, z32_.p, y);
+    return;
+  }
+  if (pc.kind == NW_PC_SGS) {
+    sgs<double, double>(gs_vals_.p, rdiag_.p, x, y, s);
     return;
   }
   precond_apply_t<double, double>(pc, A_.n, A_.row_ptr, A_.col_idx, A_.values,

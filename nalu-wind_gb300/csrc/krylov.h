@@ -59,6 +59,11 @@ class KrylovSolver {
 
   // Bind to a matrix; allocates work space for restart length m.
   void setup(const DevCsr& A, int m, cudaStream_t s);
+  // Colour classes of the multicolour Gauss-Seidel sweep (rows of class 0,
+  // then class 1, ...; cptr on the host): builds the class-ordered sliced
+  // copy of the off-diagonal entries the sweep reads.
+  void setup_colors(const std::vector<int32_t>& rows, const std::vector<int64_t>& cptr,
+                    cudaStream_t s);
   // Recompute diagonal-dependent data after the values changed.
   void refresh(cudaStream_t s);
 
@@ -114,6 +119,16 @@ class KrylovSolver {
   DeviceArray<double> sell_vals_;
   DeviceArray<float> sell_vals32_;
   int64_t sell_slices_ = 0;
+  // Gauss-Seidel copy: per colour class, slices of 32 class rows holding
+  // their off-diagonal entries column-major; slice offsets, row lengths,
+  // columns, CSR positions (for the value gathers) and values.
+  std::vector<int64_t> gs_cptr_, gs_slice0_;  // host: class row / slice starts
+  DeviceArray<int32_t> gs_rows_, gs_len_, gs_cols_, gs_map_;
+  DeviceArray<int64_t> gs_off_;
+  DeviceArray<double> gs_vals_;
+  DeviceArray<float> gs_vals32_;
+  template <typename VT, typename T>
+  void sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s) const;
   // FP32 copies for the inner solve of the mixed method
   DeviceArray<float> vals32_, rdiag32_, V32_, w32_, z32_, r32_;
   bool f32_valid_ = false;

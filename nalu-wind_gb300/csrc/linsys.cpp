@@ -297,6 +297,7 @@ nw_status nw_linsys_finalize(nw_linsys* ls) {
     A.row_ptr_host = g.row_ptr.data();
     A.col_idx_host = g.col_idx.data();
     ls->solver.setup(A, std::max(ls->cfg.kspace, ls->cfg.inner_kspace), s);
+    ls->solver.setup_colors(ls->color_rows_host, ls->color_ptr, s);
     NW_CUDA(cudaStreamSynchronize(s));
     ls->finalized = true;
   });
