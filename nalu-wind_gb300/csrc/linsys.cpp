@@ -847,6 +847,12 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
     tight.max_iterations = 100000;
     pc.kind = NW_PC_SGS;
     SolveResult sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
+    if (!sr.converged) {
+      // FP32 inner solves cannot refine a system this ill-conditioned:
+      // the reference solution comes from FP64 SGS-GMRES instead
+      tight.precision = NW_PREC_FP64;
+      sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
+    }
     if (!sr.converged) fail(NW_NOT_CONVERGED, "harvest: reference solve did not converge");
     // system coarse weights
     const int sys = L.nsystems++;

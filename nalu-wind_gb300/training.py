@@ -18,8 +18,8 @@ from . import Learned
 from .workload import poisson_system
 
 
-def train_poisson_network(shape=(64, 64, 48), systems=4, restarts=30, kspace=30, epochs=40,
-                          batch=8, lr=2e-3, seed=0, agg_passes=2, stream=None):
+def train_poisson_network(shape=(64, 64, 48), systems=16, restarts=40, kspace=30, epochs=100,
+                          batch=8, lr=1e-3, seed=0, agg_passes=2, stream=None):
     """Returns (network, info). info: pairs, harvest / train seconds and
     the mean energy-norm loss over the pairs before and after training."""
     net = Learned(seed=seed)
