@@ -14,7 +14,9 @@ The run also solves the pressure-Poisson system of the 256 x 256 x 128 box
 (8,520,321 rows; --no-poisson skips it): ms to 1e-8 FP64 relative residual
 for plain FP64 GMRES(50) + Jacobi, mixed-precision GMRES(50) + SGS, and the
 learned-preconditioned mixed-precision FGMRES(30) (network trained first,
-untimed, on other seeded systems).
+untimed, on other seeded systems). It then times one implicit step on a
+perturbed 127^3-hex block split into tets (2,097,152 nodes), in random and
+in RCM node order (--no-step skips it).
 
 Multi-GPU (torchrun, N > 1): every rank runs an independent replica of the
 same workload (weak scaling); the timed region is bracketed by barriers and
@@ -316,6 +318,8 @@ def run_ours(args, rank, world):
     }
     if not args.no_poisson:
         out["poisson"] = poisson_solves(nw, stream, args)
+    if not args.no_step:
+        out["implicit_step_tets"] = implicit_step(nw, stream, args)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(case, args)
     return out
@@ -404,6 +408,82 @@ def poisson_solves(nw, stream, args) -> dict:
     return res
 
 
+def implicit_step(nw, stream, args) -> dict:
+    """One implicit step on an unstructured mesh: a perturbed block of n^3
+    hexes (n = 127: 2,097,152 nodes) split into 6 tets each, node ids
+    randomly permuted, then that order RCM-renumbered; both orderings timed.
+    The step is the momentum (3-dof) and continuity edge assembly, then the
+    continuity (pressure-Poisson) system solved to 1e-8 FP64 relative
+    residual by learned mixed FGMRES(30) and by plain FP64 GMRES(50) +
+    Jacobi. The network is trained first (untimed) on small tet systems."""
+    import torch
+    n = args.step_n
+    res = {"workload": f"{n}^3-hex block, 6 tets per hex, 5 % jitter; random and RCM node orders"}
+    net, info = nw.training.train_poisson_network(shape=(40, 40, 40), tets=True, systems=8, restarts=40,
+                                                  epochs=100, stream=stream.cuda_stream)
+    res["training"] = info
+    for name, ren in (("random", 1), ("rcm", 2)):
+        case = nw.workload.lowmach_case(n, n, n, seed=5, stretch=1.0, jitter=0.05, lz=1.0, tets=True,
+                                        renumber=ren, renumber_seed=7)
+        mesh = case.mesh
+        nd = case.node
+        d = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in dict(
+            coords=mesh.coords, velocity=nd["velocity"], dudx=nd["dudx"], viscosity=nd["viscosity"],
+            density=nd["density"], mask=nd["mask"], pressure=nd["pressure"], dpdx=nd["dpdx"],
+            udiag=nd["udiag"], area=mesh.area, mdot=case.edge["mdot"], pecfac=case.edge["pecfac"]).items()}
+        fm = nw.MomentumFields(*(d[k].data_ptr() for k in (
+            "coords", "velocity", "dudx", "viscosity", "density", "mask", "area", "mdot", "pecfac")))
+        fc = nw.ContinuityFields(*(d[k].data_ptr() for k in (
+            "coords", "velocity", "dpdx", "density", "pressure", "udiag", "area")))
+        lsm = nw.LinearSystem(3, stream=stream.cuda_stream)
+        lsm.build_edge_graph(mesh.num_nodes, mesh.edges)
+        lsm.finalize()
+        lsc = nw.LinearSystem(1, stream=stream.cuda_stream)
+        lsc.build_edge_graph(mesh.num_nodes, mesh.edges)
+        lsc.finalize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        mo, co = case.opts["momentum"], case.opts["continuity"]
+        mom, con = [], []
+        for it in range(5):
+            ev[0].record(stream)
+            lsm.zero_system()
+            lsm.assemble_momentum(fm, mo)
+            ev[1].record(stream)
+            lsc.zero_system()
+            lsc.assemble_continuity(fc, co)
+            ev[2].record(stream)
+            torch.cuda.synchronize()
+            if it >= 2:
+                mom.append(ev[0].elapsed_time(ev[1]))
+                con.append(ev[1].elapsed_time(ev[2]))
+        nnz_m, nnz_c = lsm.sizes()[1], lsc.sizes()[1]
+        r = {"nodes": mesh.num_nodes, "edges": mesh.num_edges, "nnz_momentum": nnz_m, "nnz_continuity": nnz_c,
+             "momentum_ms": round(float(np.mean(mom)), 4), "continuity_ms": round(float(np.mean(con)), 4)}
+        r["assembly_gnnz_s"] = round((nnz_m + nnz_c) / ((r["momentum_ms"] + r["continuity_ms"]) * 1e-3) / 1e9, 3)
+        nr = lsc.sizes()[0]
+        for vname, learned, cfg in (
+                ("plain_fp64_gmres50_jacobi", None,
+                 nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8)),
+                ("learned_mixed_fgmres30", net,
+                 nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=args.poisson_maxit, tolerance=1e-8,
+                               precision=nw.PREC_MIXED, inner_kspace=30, preconditioner=nw.PC_LEARNED))):
+            if learned is not None:
+                lsc.attach_learned(learned)
+            lsc.set_solver_cfg(cfg)
+            x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+            rep = lsc.solve(x)
+            r[vname] = {"ms": round(rep.solve_ms, 2), "iterations": rep.iterations,
+                        "rel_residual_fp64": rep.final_abs_residual / rep.rhs_norm,
+                        "converged": bool(rep.converged), "fallback": bool(rep.fallback)}
+        asm = r["momentum_ms"] + r["continuity_ms"]
+        r["step_ms_learned_mixed"] = round(asm + r["learned_mixed_fgmres30"]["ms"], 2)
+        r["step_ms_plain_fp64"] = round(asm + r["plain_fp64_gmres50_jacobi"]["ms"], 2)
+        res[name] = r
+        del lsm, lsc, d
+        torch.cuda.empty_cache()
+    return res
+
+
 def cpu_baseline(case, args, steps=1) -> dict:
     """Oracle (restated reference path) on the host cores: per-edge kernels
     plus the atomic sum_into, OpenMP on all cores, FP64."""
@@ -468,6 +548,8 @@ def main():
     ap.add_argument("--poisson-shape", type=int, nargs=3, default=[256, 256, 128])
     ap.add_argument("--poisson-maxit", type=int, default=20000)
     ap.add_argument("--poisson-variants", default="", help="comma-separated subset of the solver variants")
+    ap.add_argument("--no-step", action="store_true", help="skip the implicit step on the tet mesh")
+    ap.add_argument("--step-n", type=int, default=127, help="hexes per side of the tet-mesh block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.shape = tuple(args.shape)

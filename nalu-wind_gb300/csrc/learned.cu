@@ -586,14 +586,27 @@ void launch_prolong_add(const CoarseLevel& cl, const float* ec, const float* alp
 
 // ---------------------------------------------------------------------------
 // Plain aggregation of a graph (rows 0..R-1, CSR ptr/col including the
-// diagonal): a row whose neighbours are all free starts an aggregate with
-// them; leftover rows join the aggregate of their first aggregated
-// neighbour (column order), or start their own. Deterministic.
+// diagonal): visiting rows in a fixed pseudo-random order, a row whose
+// neighbours are all free starts an aggregate with them; leftover rows join
+// the aggregate of their first aggregated neighbour (column order), or start
+// their own. The seeded visiting order keeps the aggregates' shape
+// independent of the node numbering (in bandwidth-reducing orders such as
+// RCM, visiting rows in index order grows ragged aggregates: 240 instead of
+// 87 FGMRES iterations on a 2.1M-node tet mesh). Deterministic.
 static int32_t plain_aggregate(int64_t R, const int64_t* ptr, const int32_t* col,
                                std::vector<int32_t>& agg) {
   agg.assign(R, -1);
   int32_t na = 0;
-  for (int64_t r = 0; r < R; ++r) {
+  std::vector<int64_t> visit(R);
+  std::iota(visit.begin(), visit.end(), 0);
+  uint64_t st = 0x2545F4914F6CDD1Dull;  // xorshift64, fixed seed
+  for (int64_t i = R - 1; i > 0; --i) {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    std::swap(visit[i], visit[int64_t(st % uint64_t(i + 1))]);
+  }
+  for (const int64_t r : visit) {
     if (agg[r] >= 0) continue;
     bool free_nbrs = true;
     for (int64_t p = ptr[r]; p < ptr[r + 1]; ++p)

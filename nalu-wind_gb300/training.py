@@ -19,7 +19,7 @@ from .workload import poisson_system
 
 
 def train_poisson_network(shape=(64, 64, 48), systems=16, restarts=40, kspace=30, epochs=100,
-                          batch=8, lr=1e-3, seed=0, agg_passes=2, stream=None):
+                          batch=8, lr=1e-3, seed=0, agg_passes=2, stream=None, tets=False):
     """Returns (network, info). info: pairs, harvest / train seconds and
     the mean energy-norm loss over the pairs before and after training."""
     net = Learned(seed=seed)
@@ -30,7 +30,7 @@ def train_poisson_network(shape=(64, 64, 48), systems=16, restarts=40, kspace=30
     pairs = 0
     for k in range(systems):
         ls = poisson_system(shape, seed=100 + k, stretch=float(rng.uniform(1.0, 1.15)),
-                            jitter=float(rng.uniform(0.0, 0.1)), stream=stream)
+                            jitter=float(rng.uniform(0.0, 0.1)), stream=stream, tets=tets)
         ls.attach_learned(net)
         pairs = net.harvest(ls, restarts=restarts, kspace=kspace)
         if first is None:
@@ -41,7 +41,7 @@ def train_poisson_network(shape=(64, 64, 48), systems=16, restarts=40, kspace=30
     after = net.evaluate(first)
     t2 = time.perf_counter()
     net.clear_data()
-    info = {"systems": systems, "shape": list(shape), "pairs": pairs, "epochs": epochs,
+    info = {"systems": systems, "shape": list(shape), "tets": bool(tets), "pairs": pairs, "epochs": epochs,
             "harvest_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
             "loss_before": round(before, 5), "loss_after": round(after, 5)}
     return net, info

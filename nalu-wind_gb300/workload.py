@@ -131,9 +131,13 @@ def scalar_case(n: int = 32, seed: int = 1) -> Case:
                 extra=dict(dirichlet_nodes=np.concatenate([bottom, top]).astype(np.int64)))
 
 
-def lowmach_case(nx=128, ny=128, nz=64, seed=2, stretch=1.08, jitter=0.05, lz=0.5) -> Case:
-    """Momentum + continuity inputs on a stretched, jittered box."""
-    mesh = Mesh(nx, ny, nz, lx=1.0, ly=1.0, lz=lz, stretch_z=stretch, jitter=jitter, seed=seed)
+def lowmach_case(nx=128, ny=128, nz=64, seed=2, stretch=1.08, jitter=0.05, lz=0.5, tets=False,
+                 renumber=0, renumber_seed=0) -> Case:
+    """Momentum + continuity inputs on a stretched, jittered box (hex, or
+    each hex split into 6 tets; renumber 1 = random node order, 2 = random
+    then reverse Cuthill-McKee)."""
+    mesh = Mesh(nx, ny, nz, lx=1.0, ly=1.0, lz=lz, stretch_z=stretch, jitter=jitter, seed=seed, tets=tets,
+                renumber=renumber, renumber_seed=renumber_seed)
     rng = np.random.default_rng(seed)
     N = mesh.num_nodes
     z = mesh.coords[:, 2]
@@ -157,9 +161,9 @@ def lowmach_case(nx=128, ny=128, nz=64, seed=2, stretch=1.08, jitter=0.05, lz=0.
                 edge=dict(area=mesh.area, mdot=mdot, pecfac=pec), opts=dict(momentum=mo, continuity=co))
 
 
-def poisson_case(nx=256, ny=256, nz=128, seed=3, stretch=1.04, jitter=0.0) -> Case:
+def poisson_case(nx=256, ny=256, nz=128, seed=3, stretch=1.04, jitter=0.0, tets=False) -> Case:
     """Pressure-Poisson operator (continuity with zero velocity)."""
-    mesh = Mesh(nx, ny, nz, stretch_z=stretch, jitter=jitter, seed=seed)
+    mesh = Mesh(nx, ny, nz, stretch_z=stretch, jitter=jitter, seed=seed, tets=tets)
     rng = np.random.default_rng(seed)
     N = mesh.num_nodes
     zeros3 = np.zeros((N, 3))
@@ -171,14 +175,14 @@ def poisson_case(nx=256, ny=256, nz=128, seed=3, stretch=1.04, jitter=0.0) -> Ca
                 edge=dict(area=mesh.area), opts=dict(continuity=co), extra=dict(rhs=b))
 
 
-def poisson_system(shape, seed=3, stretch=1.04, jitter=0.0, rhs_seed=None, stream=None):
+def poisson_system(shape, seed=3, stretch=1.04, jitter=0.0, rhs_seed=None, stream=None, tets=False):
     """Assembled pressure-Poisson LinearSystem of a box (device inputs via
     torch); the right-hand side is the case's seeded zero-mean Gaussian,
     or a fresh one from rhs_seed."""
     import torch
 
     from . import ContinuityFields, LinearSystem
-    case = poisson_case(*shape, seed=seed, stretch=stretch, jitter=jitter)
+    case = poisson_case(*shape, seed=seed, stretch=stretch, jitter=jitter, tets=tets)
     mesh = case.mesh
     nd = case.node
     d = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in dict(
