@@ -340,6 +340,42 @@ nw_status nw_learned_forward(nw_learned* net, nw_linsys* ls, const float* rc,
 nw_status nw_gemm_bf16(int kind, int64_t m, const void* a, const void* b,
                        void* out);
 
+/* ---- input producers of the assembly (run before it every nonlinear
+ * iteration). Edge outputs are in the order given to
+ * nw_linsys_build_edge_graph; node inputs/outputs are indexed by the
+ * caller's nodes. All pointers are device pointers. ---- */
+
+/* MdotEdgeAlg::execute (src/ngp_algorithms/MdotEdgeAlg.C:117-190): mass
+ * flow rate per edge (E) from the continuity fields; no balanced-buoyancy
+ * forcing and no GCL term (as in nw_assemble_continuity_edges). */
+nw_status nw_compute_mdot_edges(nw_linsys* ls, const nw_continuity_fields* f,
+                                double noc_fac, double interp_together,
+                                double* mdot);
+/* NodalGradEdgeAlg::execute (src/ngp_algorithms/NodalGradEdgeAlg.C:85-109):
+ * edge-based Green-Gauss gradient of phi (N x dim1, dim1 = 1 or 3) into
+ * grad (N x dim1*3, component i, direction j at 3i + j). bnd_area (N x 3,
+ * or NULL) adds the lumped exposed-face closure bnd_area * phi (the role of
+ * NodalGradBndryElemAlg); periodic masters and slaves receive the summed
+ * value, divided by dualvol (already summed over periodic pairs). */
+nw_status nw_compute_nodal_gradient(nw_linsys* ls, int dim1, const double* phi,
+                                    const double* area, const double* dualvol,
+                                    const double* bnd_area, double* grad);
+/* Peclet blending function (EquationSystem::ngp_create_peclet_function,
+ * include/EquationSystem.h:399-413; src/PecletFunction.C:39-71). */
+typedef struct nw_peclet_opts {
+  int tanh_form;        /* 0 classic (hf Pe)^2 / (5 + (hf Pe)^2), 1 tanh */
+  double hybrid_factor; /* hf of the classic form */
+  double tanh_trans;    /* c1 of the tanh form */
+  double tanh_width;    /* c2 of the tanh form */
+  double eps;           /* 1e-16 in MomentumEdgePecletAlg */
+} nw_peclet_opts;
+/* MomentumEdgePecletAlg::execute (src/edge_kernels/MomentumEdgePecletAlg.C:
+ * 74-101): Peclet number (pecnum, optional) and factor per edge. */
+nw_status nw_compute_peclet_factor(nw_linsys* ls, const double* coords,
+                                   const double* density, const double* viscosity,
+                                   const double* velocity, const nw_peclet_opts* o,
+                                   double* pecnum, double* pecfac);
+
 /* ---- timing helpers (CUDA events on the handle's stream) ---- */
 nw_status nw_linsys_sync(nw_linsys* ls);
 /* Milliseconds of the last assembly call (edge + row phases). */

@@ -63,6 +63,11 @@ class ContinuityOpts(C.Structure):
                 ("interp_together", C.c_double), ("solve_incompressible", C.c_double)]
 
 
+class PecletOpts(C.Structure):
+    _fields_ = [("tanh_form", C.c_int), ("hybrid_factor", C.c_double), ("tanh_trans", C.c_double),
+                ("tanh_width", C.c_double), ("eps", C.c_double)]
+
+
 _P = C.c_void_p
 
 
@@ -149,6 +154,11 @@ SIGNATURES = {
                                        C.POINTER(C.c_double), C.POINTER(C.c_float)]),
     "nw_learned_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "nw_gemm_bf16": (C.c_int, [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "nw_compute_mdot_edges": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p]),
+    "nw_compute_nodal_gradient": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p]),
+    "nw_compute_peclet_factor": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.POINTER(PecletOpts), C.c_void_p, C.c_void_p]),
     "nw_mesh_box": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(BoxOpts), C.POINTER(C.c_void_p)]),
     "nw_mesh_destroy": (C.c_int, [C.c_void_p]),
     "nw_mesh_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P, _I64P, C.POINTER(C.c_int)]),
@@ -343,6 +353,21 @@ class LinearSystem:
 
     def sync(self) -> None:
         check(self.lib.nw_linsys_sync(self.h))
+
+    # -- input producers (device tensors in and out)
+    def compute_mdot(self, fields: "ContinuityFields", mdot_dev, noc_fac=1.0, interp_together=1.0) -> None:
+        check(self.lib.nw_compute_mdot_edges(self.h, C.byref(fields), noc_fac, interp_together, dptr(mdot_dev)))
+
+    def nodal_gradient(self, phi_dev, area_dev, dualvol_dev, grad_dev, bnd_area_dev=None, dim1=1) -> None:
+        check(self.lib.nw_compute_nodal_gradient(self.h, dim1, dptr(phi_dev), dptr(area_dev), dptr(dualvol_dev),
+                                                 dptr(bnd_area_dev), dptr(grad_dev)))
+
+    def peclet_factor(self, coords_dev, density_dev, viscosity_dev, velocity_dev, pecfac_dev,
+                      opts: "PecletOpts | None" = None, pecnum_dev=None) -> None:
+        o = opts if opts is not None else PecletOpts(0, 1.0, 2.0, 4.0, 1e-16)
+        check(self.lib.nw_compute_peclet_factor(self.h, dptr(coords_dev), dptr(density_dev), dptr(viscosity_dev),
+                                                dptr(velocity_dev), C.byref(o), dptr(pecnum_dev),
+                                                dptr(pecfac_dev)))
 
     # -- learned preconditioner
     def attach_learned(self, net: "Learned") -> None:

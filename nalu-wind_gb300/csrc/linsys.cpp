@@ -48,7 +48,8 @@ struct nw_linsys {
   bool finalized = false;
   bool pristine = false;  // zeroSystem issued, no values written since
   HostGraph g;
-  DeviceArray<int64_t> row_ptr, node_lid;
+  DeviceArray<int64_t> row_ptr, node_lid, row_nodes_ptr;
+  DeviceArray<int32_t> row_nodes;
   DeviceArray<int32_t> col_idx, inc_ptr, diag_pos, color_rows;
   DeviceArray<uint32_t> inc;
   DeviceArray<int2> edges;
@@ -245,6 +246,19 @@ nw_status nw_linsys_finalize(nw_linsys* ls) {
     ls->row_ptr.upload(g.row_ptr, s);
     ls->col_idx.upload(g.col_idx, s);
     ls->node_lid.upload(g.node_lid, s);
+    {
+      // node row -> nodes (periodic master first, then its slaves)
+      std::vector<int64_t> rp(g.node_rows + 1, 0);
+      for (int64_t k = 0; k < g.num_nodes; ++k) rp[g.node_lid[k] / g.num_dof + 1]++;
+      for (int64_t r = 0; r < g.node_rows; ++r) rp[r + 1] += rp[r];
+      std::vector<int32_t> rn(g.num_nodes);
+      std::vector<int64_t> pos(rp.begin(), rp.end() - 1);
+      for (int64_t r = 0; r < g.node_rows; ++r) rn[pos[r]++] = g.row_master[r];
+      for (int64_t k = 0; k < g.num_nodes; ++k)
+        if (g.row_master[g.node_lid[k] / g.num_dof] != k) rn[pos[g.node_lid[k] / g.num_dof]++] = int32_t(k);
+      ls->row_nodes_ptr.upload(rp, s);
+      ls->row_nodes.upload(rn, s);
+    }
     ls->inc_ptr.upload(g.inc_ptr, s);
     ls->inc.upload(g.inc, s);
     ls->diag_pos.upload(g.diag_pos, s);
@@ -682,6 +696,9 @@ PlanView plan_view(const nw_linsys* ls) {
   v.inc = ls->inc.p;
   v.diag_pos = ls->diag_pos.p;
   v.row_ptr = ls->row_ptr.p;
+  v.num_nodes = ls->g.num_nodes;
+  v.row_nodes_ptr = ls->row_nodes_ptr.p;
+  v.row_nodes = ls->row_nodes.p;
   return v;
 }
 }  // namespace nw

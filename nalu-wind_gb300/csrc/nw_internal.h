@@ -102,6 +102,9 @@ struct PlanView {
   const uint32_t* inc = nullptr;
   const int32_t* diag_pos = nullptr;
   const int64_t* row_ptr = nullptr;
+  int64_t num_nodes = 0;
+  const int64_t* row_nodes_ptr = nullptr;  // node row -> its nodes (master first)
+  const int32_t* row_nodes = nullptr;
 };
 // Throws Error unless the handle is finalized.
 PlanView plan_view(const nw_linsys* ls);
