@@ -376,6 +376,42 @@ nw_status nw_compute_peclet_factor(nw_linsys* ls, const double* coords,
                                    const double* velocity, const nw_peclet_opts* o,
                                    double* pecnum, double* pecfac);
 
+/* ---- node kernels: lumped-mass BDF time terms, added into the system
+ * (like sumInto) after the edge assembly. States Nm1, N, Np1; device
+ * pointers of the caller's nodes. ---- */
+typedef struct nw_mass_bdf_fields {
+  const double* density_nm1;     /* N */
+  const double* density_n;       /* N */
+  const double* density_np1;     /* N */
+  const double* dual_volume_nm1; /* N (dual_nodal_volume states) */
+  const double* dual_volume_n;   /* N */
+  const double* dual_volume_np1; /* N */
+  const double* q_nm1;           /* scalar: N; momentum: velocity N x 3 */
+  const double* q_n;
+  const double* q_np1;
+  const double* dpdx;            /* momentum: N x 3 */
+} nw_mass_bdf_fields;
+typedef struct nw_bdf_opts {
+  double dt;     /* Realm::get_time_step */
+  double gamma1; /* BDF coefficients (Realm::get_gamma1..3) */
+  double gamma2;
+  double gamma3;
+} nw_bdf_opts;
+/* ScalarMassBDFNodeKernel::execute (src/node_kernels/ScalarMassBDFNodeKernel.C:
+ * 75-97): diag += g1 rho dnv / dt; rhs -= (g1 rho q dnv |Np1 + g2 .. |N +
+ * g3 .. |Nm1) / dt. num_dof 1. */
+nw_status nw_assemble_scalar_mass_bdf(nw_linsys* ls, const nw_mass_bdf_fields* f,
+                                      const nw_bdf_opts* o);
+/* ContinuityMassBDFNodeKernel::execute (src/node_kernels/
+ * ContinuityMassBDFNodeKernel.C:60-82): rhs only. num_dof 1. */
+nw_status nw_assemble_continuity_mass_bdf(nw_linsys* ls, const nw_mass_bdf_fields* f,
+                                          const nw_bdf_opts* o);
+/* MomentumMassBDFNodeKernel::execute (src/node_kernels/
+ * MomentumMassBDFNodeKernel.C:78-107): per component, plus -dpdx dnv on the
+ * rhs. num_dof 3. */
+nw_status nw_assemble_momentum_mass_bdf(nw_linsys* ls, const nw_mass_bdf_fields* f,
+                                        const nw_bdf_opts* o);
+
 /* ---- timing helpers (CUDA events on the handle's stream) ---- */
 nw_status nw_linsys_sync(nw_linsys* ls);
 /* Milliseconds of the last assembly call (edge + row phases). */

@@ -63,6 +63,15 @@ class ContinuityOpts(C.Structure):
                 ("interp_together", C.c_double), ("solve_incompressible", C.c_double)]
 
 
+class MassBdfFields(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("density_nm1", "density_n", "density_np1", "dual_volume_nm1",
+                                           "dual_volume_n", "dual_volume_np1", "q_nm1", "q_n", "q_np1", "dpdx")]
+
+
+class BdfOpts(C.Structure):
+    _fields_ = [("dt", C.c_double), ("gamma1", C.c_double), ("gamma2", C.c_double), ("gamma3", C.c_double)]
+
+
 class PecletOpts(C.Structure):
     _fields_ = [("tanh_form", C.c_int), ("hybrid_factor", C.c_double), ("tanh_trans", C.c_double),
                 ("tanh_width", C.c_double), ("eps", C.c_double)]
@@ -159,6 +168,9 @@ SIGNATURES = {
                                             C.c_void_p, C.c_void_p]),
     "nw_compute_peclet_factor": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.POINTER(PecletOpts), C.c_void_p, C.c_void_p]),
+    "nw_assemble_scalar_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
+    "nw_assemble_continuity_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
+    "nw_assemble_momentum_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
     "nw_mesh_box": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(BoxOpts), C.POINTER(C.c_void_p)]),
     "nw_mesh_destroy": (C.c_int, [C.c_void_p]),
     "nw_mesh_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P, _I64P, C.POINTER(C.c_int)]),
@@ -353,6 +365,19 @@ class LinearSystem:
 
     def sync(self) -> None:
         check(self.lib.nw_linsys_sync(self.h))
+
+    # -- node kernels (lumped-mass BDF time terms)
+    def assemble_mass_bdf(self, kind: str, density, dual_volume, q=None, dpdx=None, dt=0.1,
+                          gamma=(1.0, -1.0, 0.0)) -> None:
+        """kind "scalar", "continuity" or "momentum"; density, dual_volume and
+        q are (Nm1, N, Np1) triples of device tensors."""
+        qq = q if q is not None else (None, None, None)
+        f = MassBdfFields(*(dptr(a) for a in (*density, *dual_volume, *qq, dpdx)))
+        o = BdfOpts(dt, *gamma)
+        fn = {"scalar": self.lib.nw_assemble_scalar_mass_bdf,
+              "continuity": self.lib.nw_assemble_continuity_mass_bdf,
+              "momentum": self.lib.nw_assemble_momentum_mass_bdf}[kind]
+        check(fn(self.h, C.byref(f), C.byref(o)))
 
     # -- input producers (device tensors in and out)
     def compute_mdot(self, fields: "ContinuityFields", mdot_dev, noc_fac=1.0, interp_together=1.0) -> None:

@@ -16,6 +16,7 @@
 #include "assemble.h"
 #include "krylov.h"
 #include "learned.h"
+#include "node_kernels.h"
 #include "nw_internal.h"
 
 namespace nw {
@@ -591,6 +592,37 @@ nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
     }
     if (r.status == NW_NAN_DETECTED) fail(NW_NAN_DETECTED, "non-finite value in the solve");
   });
+}
+
+static nw_status mass_bdf(nw_linsys* ls, int kind, const nw_mass_bdf_fields* f,
+                          const nw_bdf_opts* o) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+    if (ls->num_dof != (kind == 2 ? 3 : 1))
+      fail(NW_INVALID_ARG, kind == 2 ? "momentum mass terms need num_dof 3" : "mass terms need num_dof 1");
+    if (!f->density_nm1 || !f->density_n || !f->density_np1 || !f->dual_volume_nm1 ||
+        !f->dual_volume_n || !f->dual_volume_np1)
+      fail(NW_INVALID_ARG, "null density or dual volume");
+    if (kind != 1 && (!f->q_nm1 || !f->q_n || !f->q_np1)) fail(NW_INVALID_ARG, "null transported field");
+    if (kind == 2 && !f->dpdx) fail(NW_INVALID_ARG, "null dpdx");
+    if (!(o->dt != 0.0)) fail(NW_INVALID_ARG, "dt is zero");
+    materialize_zero(ls);
+    launch_mass_bdf(ls->stream, kind, plan_view(ls), *f, *o, ls->values.p, ls->rhs.p);
+  });
+}
+
+nw_status nw_assemble_scalar_mass_bdf(nw_linsys* ls, const nw_mass_bdf_fields* f,
+                                      const nw_bdf_opts* o) {
+  return mass_bdf(ls, 0, f, o);
+}
+nw_status nw_assemble_continuity_mass_bdf(nw_linsys* ls, const nw_mass_bdf_fields* f,
+                                          const nw_bdf_opts* o) {
+  return mass_bdf(ls, 1, f, o);
+}
+nw_status nw_assemble_momentum_mass_bdf(nw_linsys* ls, const nw_mass_bdf_fields* f,
+                                        const nw_bdf_opts* o) {
+  return mass_bdf(ls, 2, f, o);
 }
 
 nw_status nw_linsys_residual_history(const nw_linsys* ls, double* hist,

@@ -1,0 +1,85 @@
+// Node kernels of the momentum / continuity / scalar systems: the
+// lumped-mass BDF time terms, added to each node row's diagonal and rhs.
+// One thread per node row sums the row's nodes (a periodic master and its
+// slaves, master first) in FP64 and adds once: no atomics.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "node_kernels.h"
+#include "nw_internal.h"
+
+namespace nw {
+namespace {
+
+constexpr int kThreads = 256;
+
+// KIND 0: ScalarMassBDFNodeKernel::execute
+//         (src/node_kernels/ScalarMassBDFNodeKernel.C:75-97)
+// KIND 1: ContinuityMassBDFNodeKernel::execute
+//         (src/node_kernels/ContinuityMassBDFNodeKernel.C:60-82)
+// KIND 2: MomentumMassBDFNodeKernel::execute
+//         (src/node_kernels/MomentumMassBDFNodeKernel.C:78-107)
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+    mass_bdf_k(int64_t R, const int64_t* __restrict__ rn_ptr, const int32_t* __restrict__ rn,
+               const int32_t* __restrict__ diag_pos, const int64_t* __restrict__ row_ptr,
+               nw_mass_bdf_fields f, nw_bdf_opts o, double* __restrict__ values,
+               double* __restrict__ rhs) {
+  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  constexpr int ND = KIND == 2 ? 3 : 1;
+  const double dt = o.dt, g1 = o.gamma1, g2 = o.gamma2, g3 = o.gamma3;
+  double lhs = 0.0, b[ND];
+#pragma unroll
+  for (int d = 0; d < ND; ++d) b[d] = 0.0;
+  for (int64_t k = rn_ptr[r]; k < rn_ptr[r + 1]; ++k) {
+    const int64_t i = rn[k];
+    const double rNm1 = f.density_nm1[i], rN = f.density_n[i], rNp1 = f.density_np1[i];
+    const double vNm1 = f.dual_volume_nm1[i], vN = f.dual_volume_n[i], vNp1 = f.dual_volume_np1[i];
+    if (KIND == 0) {
+      lhs += g1 * rNp1 * vNp1 / dt;
+      b[0] += -(g1 * rNp1 * f.q_np1[i] * vNp1 + g2 * f.q_n[i] * rN * vN +
+                g3 * f.q_nm1[i] * rNm1 * vNm1) /
+              dt;
+    } else if (KIND == 1) {
+      b[0] += -(g1 * rNp1 * vNp1 + g2 * rN * vN + g3 * rNm1 * vNm1) / dt * (g1 / dt);
+    } else {
+      lhs += g1 * rNp1 * vNp1 / dt;
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        b[d] += -(g1 * rNp1 * f.q_np1[3 * i + d] * vNp1 + g2 * rN * f.q_n[3 * i + d] * vN +
+                  g3 * rNm1 * f.q_nm1[3 * i + d] * vNm1) /
+                    dt -
+                f.dpdx[3 * i + d] * vNp1;
+    }
+  }
+  const int dp = diag_pos[r];
+#pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    const int64_t row = ND * r + d;
+    if (KIND != 1) values[row_ptr[row] + int64_t(ND) * dp + d] += lhs;
+    rhs[row] += b[d];
+  }
+}
+
+inline unsigned grid_for(int64_t n) { return unsigned((n + kThreads - 1) / kThreads); }
+
+}  // namespace
+
+void launch_mass_bdf(cudaStream_t s, int kind, const PlanView& v, const nw_mass_bdf_fields& f,
+                     const nw_bdf_opts& o, double* values, double* rhs) {
+  if (v.node_rows == 0) return;
+  if (kind == 0)
+    mass_bdf_k<0><<<grid_for(v.node_rows), kThreads, 0, s>>>(
+        v.node_rows, v.row_nodes_ptr, v.row_nodes, v.diag_pos, v.row_ptr, f, o, values, rhs);
+  else if (kind == 1)
+    mass_bdf_k<1><<<grid_for(v.node_rows), kThreads, 0, s>>>(
+        v.node_rows, v.row_nodes_ptr, v.row_nodes, v.diag_pos, v.row_ptr, f, o, values, rhs);
+  else
+    mass_bdf_k<2><<<grid_for(v.node_rows), kThreads, 0, s>>>(
+        v.node_rows, v.row_nodes_ptr, v.row_nodes, v.diag_pos, v.row_ptr, f, o, values, rhs);
+  NW_CUDA(cudaGetLastError());
+}
+
+}  // namespace nw

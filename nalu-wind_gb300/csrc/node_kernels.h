@@ -1,0 +1,15 @@
+// Launchers of the node kernels (node_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "nw_capi.h"
+#include "nw_internal.h"
+
+namespace nw {
+
+// kind 0 scalar, 1 continuity, 2 momentum (3 dof): adds the lumped-mass BDF
+// terms to each node row's diagonal entry and rhs.
+void launch_mass_bdf(cudaStream_t s, int kind, const PlanView& v, const nw_mass_bdf_fields& f,
+                     const nw_bdf_opts& o, double* values, double* rhs);
+
+}  // namespace nw

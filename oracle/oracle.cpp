@@ -1224,6 +1224,45 @@ void or_mdot_edge(int64_t nedges, const int64_t* edges, const double* coords,
   }
 }
 
+// Lumped-mass BDF node kernels, per node: the diagonal LHS entry and the
+// rhs of each dof (added by the node algorithm into the node's own row):
+//   kind 0 ScalarMassBDFNodeKernel::execute
+//          (src/node_kernels/ScalarMassBDFNodeKernel.C:75-97)
+//   kind 1 ContinuityMassBDFNodeKernel::execute
+//          (src/node_kernels/ContinuityMassBDFNodeKernel.C:60-82)
+//   kind 2 MomentumMassBDFNodeKernel::execute
+//          (src/node_kernels/MomentumMassBDFNodeKernel.C:78-107)
+// q: scalar (N) or velocity (N x 3); dpdx: momentum only.
+void or_mass_bdf(int kind, int64_t n, const double* rhoNm1, const double* rhoN,
+                 const double* rhoNp1, const double* dnvNm1, const double* dnvN,
+                 const double* dnvNp1, const double* qNm1, const double* qN,
+                 const double* qNp1, const double* dpdx, double dt, double g1,
+                 double g2, double g3, double* lhs, double* rhs) {
+  for (int64_t i = 0; i < n; ++i) {
+    if (kind == 0) {
+      lhs[i] = g1 * rhoNp1[i] * dnvNp1[i] / dt;
+      rhs[i] = -(g1 * rhoNp1[i] * qNp1[i] * dnvNp1[i] + g2 * qN[i] * rhoN[i] * dnvN[i] +
+                 g3 * qNm1[i] * rhoNm1[i] * dnvNm1[i]) /
+               dt;
+    } else if (kind == 1) {
+      lhs[i] = 0.0;
+      rhs[i] = -(g1 * rhoNp1[i] * dnvNp1[i] + g2 * rhoN[i] * dnvN[i] +
+                 g3 * rhoNm1[i] * dnvNm1[i]) /
+               dt * (g1 / dt);
+    } else {
+      const double lhsfac = g1 * rhoNp1[i] * dnvNp1[i] / dt;
+      for (int d = 0; d < 3; ++d) {
+        lhs[3 * i + d] = lhsfac;
+        rhs[3 * i + d] = -(g1 * rhoNp1[i] * qNp1[3 * i + d] * dnvNp1[i] +
+                           g2 * rhoN[i] * qN[3 * i + d] * dnvN[i] +
+                           g3 * rhoNm1[i] * qNm1[3 * i + d] * dnvNm1[i]) /
+                             dt -
+                         dpdx[3 * i + d] * dnvNp1[i];
+      }
+    }
+  }
+}
+
 // NodalGradEdgeAlg::execute (src/ngp_algorithms/NodalGradEdgeAlg.C:58-111).
 void or_nodal_grad_edge(int64_t nedges, const int64_t* edges, int dim1,
                         const double* phi, const double* area,

@@ -273,3 +273,19 @@ def peclet_classic(pe, hf):
 
 def peclet_tanh(x, c1, c2):
     return lib().or_peclet_tanh(x, c1, c2)
+
+
+def mass_bdf(kind, rho, dnv, q=None, dpdx=None, dt=0.1, gamma=(1.0, -1.0, 0.0)):
+    """Lumped-mass BDF node kernels (kind 0 scalar, 1 continuity, 2 momentum):
+    rho, dnv, q are (Nm1, N, Np1) triples of node arrays; returns the per-node
+    diagonal LHS and rhs (N, or N x 3 for momentum)."""
+    n = rho[2].shape[0]
+    nd = 3 if kind == 2 else 1
+    zeros = np.zeros(n * nd)
+    qq = [(_f64(a) if a is not None else zeros) for a in (q if q is not None else (None, None, None))]
+    dp = _f64(dpdx) if dpdx is not None else np.zeros(3 * n)
+    lhs, rhs = np.zeros(n * nd), np.zeros(n * nd)
+    args = [_f64(a) for a in (*rho, *dnv)] + qq + [dp]
+    lib().or_mass_bdf(C.c_int(kind), C.c_int64(n), *[_p(a, C.c_double) for a in args], C.c_double(dt),
+                      *[C.c_double(g) for g in gamma], _p(lhs, C.c_double), _p(rhs, C.c_double))
+    return (lhs.reshape(n, 3), rhs.reshape(n, 3)) if nd == 3 else (lhs, rhs)

@@ -13,6 +13,8 @@ Sources (paths within the nalu-wind tree):
   unit_tests/UnitTestPecletFunction.C                   Peclet factors
   unit_tests/ngp_algorithms/UnitTestGeometryAlg.C       dual volume, |A|^2
   unit_tests/ngp_algorithms/UnitTestMdotAlg.C           mdot
+  unit_tests/node_kernels/UnitTest{Momentum,Continuity,Scalar}MassBDFNodeKernel.C
+      lumped-mass BDF node kernels: diagonal LHS and rhs
 """
 from __future__ import annotations
 
@@ -78,6 +80,20 @@ def main(ref: Path, out: Path) -> None:
     md = (ref / "unit_tests/ngp_algorithms/UnitTestMdotAlg.C").read_text()
     assert "EXPECT_NEAR(mdot[0], 2.5, tol)" in md and "field_fill(10.0, *velocity_)" in md
     g["mdot_hex8_unit_cube"] = {"density": 1.0, "velocity": 10.0, "mdot": 2.5}
+
+    nk = ref / "unit_tests/node_kernels"
+    mm = (nk / "UnitTestMomentumMassBDFNodeKernel.C").read_text()
+    assert "timeStepN_ = 0.1" in mm and "gamma2_ = -1.0" in mm and "lhsExact[i * 24 + i] = 1.25" in mm
+    g["momentum_mass_bdf_hex8"] = {"dt": 0.1, "gamma": [1.0, -1.0, 0.0], "lhs_diag": 1.25,
+                                   "rhs": _nums(_block(mm, "rhs[24]"))}
+    cm = (nk / "UnitTestContinuityMassBDFNodeKernel.C").read_text()
+    assert "expect_all_near(helperObjs.linsys->rhs_, -12.5)" in cm and "lhs_, 0.0)" in cm
+    g["continuity_mass_bdf_hex8"] = {"dt": 0.1, "gamma": [1.0, -1.0, 0.0], "lhs_diag": 0.0, "rhs": -12.5}
+    sm = (nk / "UnitTestScalarMassBDFNodeKernel.C").read_text()
+    lhs = _nums(_block(sm, "lhs[8][8]"))
+    assert len(lhs) == 64
+    g["scalar_mass_bdf_hex8"] = {"dt": 0.1, "gamma": [1.0, -1.0, 0.0],
+                                 "lhs_diag": [lhs[9 * i] for i in range(8)], "rhs": _nums(_block(sm, "rhs[8]"))}
 
     assert len(g["continuity_hex8"]["lhs"]) == 64 and len(g["momentum_hex8"]["lhs"]) == 576
     assert len(g["momentum_hex8"]["rhs"]) == 24

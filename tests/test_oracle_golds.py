@@ -169,3 +169,28 @@ def test_oracle_sgs_is_forward_then_backward(orc):
     # backward sweep solves (D + U) y = x - L y1
     np.testing.assert_allclose(y, y2, rtol=1e-12, atol=1e-12)
     del D
+
+
+def test_mass_bdf_node_kernels(orc, golds):
+    """UnitTest{Momentum,Continuity,Scalar}MassBDFNodeKernel.C: only the
+    current (Np1) states are filled by the fixtures; N and Nm1 stay zero."""
+    m = kat.hex1(orc)
+    V = m["dualvol"]
+    z = np.zeros(8)
+    dnv = (V, V, V)
+    g = golds["momentum_mass_bdf_hex8"]
+    cf = kat.continuity_fixture(orc)
+    lhs, rhs = orc.mass_bdf(2, (z, z, np.ones(8)), dnv, q=(np.zeros((8, 3)), np.zeros((8, 3)),
+                                                           kat.trig_velocity(m["coords"])),
+                            dpdx=cf["dpdx"], dt=g["dt"], gamma=g["gamma"])
+    np.testing.assert_allclose(rhs.ravel(), g["rhs"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(lhs, g["lhs_diag"], rtol=0, atol=1e-14)
+    g = golds["continuity_mass_bdf_hex8"]
+    lhs, rhs = orc.mass_bdf(1, (z, z, np.ones(8)), dnv, dt=g["dt"], gamma=g["gamma"])
+    np.testing.assert_allclose(rhs, g["rhs"], rtol=0, atol=1e-12)
+    assert np.all(lhs == 0.0)
+    g = golds["scalar_mass_bdf_hex8"]
+    sf = kat.scalar_fixture(orc)
+    lhs, rhs = orc.mass_bdf(0, (z, z, sf["density"]), dnv, q=(z, z, sf["q"]), dt=g["dt"], gamma=g["gamma"])
+    np.testing.assert_allclose(lhs, g["lhs_diag"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(rhs, g["rhs"], rtol=0, atol=1e-12)
