@@ -412,6 +412,20 @@ nw_status nw_assemble_continuity_mass_bdf(nw_linsys* ls, const nw_mass_bdf_field
 nw_status nw_assemble_momentum_mass_bdf(nw_linsys* ls, const nw_mass_bdf_fields* f,
                                         const nw_bdf_opts* o);
 
+/* ---- MatrixMarket export / import ---- */
+/* TpetraLinearSystem::writeToFile (src/TpetraLinearSystem.C:2017-2045):
+ * writes <base>-O-<count>.mm.1 (coordinate real general, 1-based global dof
+ * ids ndof (nalu id - 1) + d + 1) and <base>-O-<count>.rhs.1 (array real
+ * general); with x_host (nrows, row order) also <base>-O-<count>.sln.1.
+ * Values are written with 17 significant digits (round trip exact). */
+nw_status nw_linsys_write_matrix_market(nw_linsys* ls, const char* base, int count,
+                                        const double* x_host);
+/* Reads such files back into this handle's graph (values and, when
+ * rhs_path is not NULL, the rhs). No reference counterpart: it lets a
+ * system exported elsewhere be solved here. */
+nw_status nw_linsys_read_matrix_market(nw_linsys* ls, const char* matrix_path,
+                                       const char* rhs_path);
+
 /* ---- timing helpers (CUDA events on the handle's stream) ---- */
 nw_status nw_linsys_sync(nw_linsys* ls);
 /* Milliseconds of the last assembly call (edge + row phases). */

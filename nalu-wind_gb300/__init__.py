@@ -171,6 +171,8 @@ SIGNATURES = {
     "nw_assemble_scalar_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
     "nw_assemble_continuity_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
     "nw_assemble_momentum_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
+    "nw_linsys_write_matrix_market": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_void_p]),
+    "nw_linsys_read_matrix_market": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
     "nw_mesh_box": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(BoxOpts), C.POINTER(C.c_void_p)]),
     "nw_mesh_destroy": (C.c_int, [C.c_void_p]),
     "nw_mesh_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P, _I64P, C.POINTER(C.c_int)]),
@@ -365,6 +367,16 @@ class LinearSystem:
 
     def sync(self) -> None:
         check(self.lib.nw_linsys_sync(self.h))
+
+    # -- MatrixMarket
+    def write_matrix_market(self, base, count: int = 0, x=None) -> None:
+        xx = None if x is None else np.ascontiguousarray(x, np.float64)
+        check(self.lib.nw_linsys_write_matrix_market(self.h, str(base).encode(), count,
+                                                     None if xx is None else xx.ctypes.data))
+
+    def read_matrix_market(self, matrix_path, rhs_path=None) -> None:
+        check(self.lib.nw_linsys_read_matrix_market(self.h, str(matrix_path).encode(),
+                                                    None if rhs_path is None else str(rhs_path).encode()))
 
     # -- node kernels (lumped-mass BDF time terms)
     def assemble_mass_bdf(self, kind: str, density, dual_volume, q=None, dpdx=None, dt=0.1,

@@ -47,7 +47,11 @@ void build_graph(HostGraph& g, int num_dof, int64_t num_nodes,
   g.node_rows = R;
   g.nrows = R * num_dof;
   g.row_master.resize(R);
-  for (int64_t k = 0; k < R; ++k) g.row_master[k] = masters[k].second;
+  g.row_gid.resize(R);
+  for (int64_t k = 0; k < R; ++k) {
+    g.row_master[k] = masters[k].second;
+    g.row_gid[k] = masters[k].first;
+  }
   std::vector<int32_t> node_row(num_nodes);
   g.node_lid.resize(num_nodes);
   for (int64_t n = 0; n < num_nodes; ++n) {

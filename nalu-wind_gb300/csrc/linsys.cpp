@@ -594,6 +594,136 @@ nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
   });
 }
 
+// MatrixMarket files of the system in the layout of
+// TpetraLinearSystem::writeToFile (src/TpetraLinearSystem.C:2017-2045):
+// <base>-O-<count>.mm.1 (coordinate real general, 1-based global dof ids
+// GID = ndof (nalu id - 1) + d + 1, TpetraLinearSystemHelpers.h:33) and
+// <base>-O-<count>.rhs.1 (array real general); with x also .sln.1. Sizes
+// are the largest global dof id (global ids of periodic slaves are unused).
+nw_status nw_linsys_write_matrix_market(nw_linsys* ls, const char* base, int count,
+                                        const double* x_host) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!base) fail(NW_INVALID_ARG, "null file name");
+    materialize_zero(ls);
+    const HostGraph& g = ls->g;
+    const int nd = g.num_dof;
+    std::vector<double> v(g.nnz), b(g.nrows);
+    NW_CUDA(cudaMemcpyAsync(v.data(), ls->values.p, g.nnz * 8, cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaMemcpyAsync(b.data(), ls->rhs.p, g.nrows * 8, cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    auto gid = [&](int64_t row) { return nd * (g.row_gid[row / nd] - 1) + row % nd + 1; };
+    int64_t dim = 0;
+    for (int64_t r = 0; r < g.node_rows; ++r) dim = std::max<int64_t>(dim, nd * g.row_gid[r]);
+    const std::string stem = std::string(base) + "-O-" + std::to_string(count);
+    auto open = [&](const std::string& path) {
+      FILE* fp = std::fopen(path.c_str(), "w");
+      if (!fp) fail(NW_INVALID_ARG, "cannot open " + path + " for writing");
+      return fp;
+    };
+    FILE* fa = open(stem + ".mm.1");
+    std::fprintf(fa, "%%%%MatrixMarket matrix coordinate real general\n");
+    std::fprintf(fa, "%% nalu-wind linear system (%d dof per node), global dof ids\n", nd);
+    std::fprintf(fa, "%lld %lld %lld\n", (long long)dim, (long long)dim, (long long)g.nnz);
+    for (int64_t r = 0; r < g.nrows; ++r)
+      for (int64_t p = g.row_ptr[r]; p < g.row_ptr[r + 1]; ++p)
+        std::fprintf(fa, "%lld %lld %.17e\n", (long long)gid(r), (long long)gid(g.col_idx[p]), v[p]);
+    const bool ok_a = std::fclose(fa) == 0;
+    auto dense = [&](const std::string& path, const double* a) {
+      FILE* fb = open(path);
+      std::fprintf(fb, "%%%%MatrixMarket matrix array real general\n");
+      std::fprintf(fb, "%lld 1\n", (long long)dim);
+      // array format lists every global row; unused ids (periodic slaves) are 0
+      std::vector<double> full(dim, 0.0);
+      for (int64_t r = 0; r < g.nrows; ++r) full[gid(r) - 1] = a[r];
+      for (int64_t k = 0; k < dim; ++k) std::fprintf(fb, "%.17e\n", full[k]);
+      return std::fclose(fb) == 0;
+    };
+    const bool ok_b = dense(stem + ".rhs.1", b.data());
+    const bool ok_x = x_host ? dense(stem + ".sln.1", x_host) : true;
+    if (!ok_a || !ok_b || !ok_x) fail(NW_INVALID_ARG, "write failed: " + stem);
+  });
+}
+
+// Reads a coordinate MatrixMarket matrix (and optionally an array rhs)
+// written for this graph: every entry must be a column of the graph
+// (NW_INVALID_ARG otherwise); entries not in the file become zero.
+nw_status nw_linsys_read_matrix_market(nw_linsys* ls, const char* matrix_path,
+                                       const char* rhs_path) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!matrix_path) fail(NW_INVALID_ARG, "null file name");
+    const HostGraph& g = ls->g;
+    const int nd = g.num_dof;
+    // global dof id -> local row
+    std::vector<int64_t> row_of;
+    int64_t dim = 0;
+    for (int64_t r = 0; r < g.node_rows; ++r) dim = std::max<int64_t>(dim, nd * g.row_gid[r]);
+    row_of.assign(dim + 1, -1);
+    for (int64_t r = 0; r < g.nrows; ++r) row_of[nd * (g.row_gid[r / nd] - 1) + r % nd + 1] = r;
+    FILE* fa = std::fopen(matrix_path, "r");
+    if (!fa) fail(NW_INVALID_ARG, std::string("cannot open ") + matrix_path);
+    std::vector<double> v(g.nnz, 0.0), b(g.nrows, 0.0);
+    char line[512];
+    bool header = false, sized = false;
+    long long m = 0, n = 0, cnt = 0, seen = 0;
+    std::string err;
+    while (std::fgets(line, sizeof line, fa)) {
+      if (line[0] == '%') {
+        if (!header) header = std::strstr(line, "coordinate") && std::strstr(line, "real");
+        continue;
+      }
+      if (!sized) {
+        if (std::sscanf(line, "%lld %lld %lld", &m, &n, &cnt) != 3) { err = "bad size line"; break; }
+        if (m != dim || n != dim) { err = "matrix size does not match this system"; break; }
+        sized = true;
+        continue;
+      }
+      long long i, j;
+      double a;
+      if (std::sscanf(line, "%lld %lld %lf", &i, &j, &a) != 3) { err = "bad entry line"; break; }
+      const int64_t r = (i >= 1 && i <= dim) ? row_of[i] : -1, c = (j >= 1 && j <= dim) ? row_of[j] : -1;
+      if (r < 0 || c < 0) { err = "entry outside the system's rows"; break; }
+      const auto b0 = g.col_idx.begin() + g.row_ptr[r], b1 = g.col_idx.begin() + g.row_ptr[r + 1];
+      const auto it = std::lower_bound(b0, b1, int32_t(c));
+      if (it == b1 || *it != int32_t(c)) { err = "entry not in the graph"; break; }
+      v[it - g.col_idx.begin()] += a;
+      ++seen;
+    }
+    std::fclose(fa);
+    if (err.empty() && !header) err = "not a coordinate real MatrixMarket file";
+    if (err.empty() && seen != cnt) err = "entry count does not match the size line";
+    if (!err.empty()) fail(NW_INVALID_ARG, err + ": " + matrix_path);
+    if (rhs_path) {
+      FILE* fb = std::fopen(rhs_path, "r");
+      if (!fb) fail(NW_INVALID_ARG, std::string("cannot open ") + rhs_path);
+      bool sz = false;
+      int64_t k = 0;
+      while (std::fgets(line, sizeof line, fb)) {
+        if (line[0] == '%') continue;
+        if (!sz) {
+          long long mm = 0, nn = 0;
+          if (std::sscanf(line, "%lld %lld", &mm, &nn) != 2 || mm != dim || nn != 1) { err = "bad rhs size"; break; }
+          sz = true;
+          continue;
+        }
+        double a;
+        if (std::sscanf(line, "%lf", &a) != 1 || k >= dim) { err = "bad rhs entry"; break; }
+        if (row_of[k + 1] >= 0) b[row_of[k + 1]] = a;
+        ++k;
+      }
+      std::fclose(fb);
+      if (err.empty() && k != dim) err = "rhs length does not match";
+      if (!err.empty()) fail(NW_INVALID_ARG, err + ": " + rhs_path);
+    }
+    NW_CUDA(cudaMemcpyAsync(ls->values.p, v.data(), g.nnz * 8, cudaMemcpyHostToDevice, ls->stream));
+    if (rhs_path)
+      NW_CUDA(cudaMemcpyAsync(ls->rhs.p, b.data(), g.nrows * 8, cudaMemcpyHostToDevice, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    ls->pristine = false;
+  });
+}
+
 static nw_status mass_bdf(nw_linsys* ls, int kind, const nw_mass_bdf_fields* f,
                           const nw_bdf_opts* o) {
   return guard([&] {

@@ -73,6 +73,7 @@ struct HostGraph {
   std::vector<uint32_t> inc;         // packed (edge << 1 | side) | dup bit
   std::vector<int32_t> diag_pos;     // per node row: diagonal column slot
   std::vector<int32_t> row_master;   // per node row: caller node index
+  std::vector<int64_t> row_gid;      // per node row: the master's (nalu) global id
 };
 
 // Build the Tpetra-identical CSR graph and the assembly plan.
