@@ -21,6 +21,7 @@ def _scalar_system(nw):
     return ls, mesh
 
 
+@pytest.mark.filterwarnings("ignore::DeprecationWarning")
 def test_write_read_roundtrip(nw, tmp_path):
     scipy_io = pytest.importorskip("scipy.io")
     ls, mesh = _scalar_system(nw)
