@@ -349,6 +349,31 @@ __global__ void __launch_bounds__(kBlock)
   y[i] = s * rd[i];
 }
 
+// Residual r_i = x_i - a_ii y_i - sum_{j != i} a_ij y_j of the rows of one
+// colour class (float, over the class-ordered sliced copy).
+__global__ void __launch_bounds__(kBlock)
+    gs_resid_k(int64_t cnt, const int32_t* __restrict__ rows, const int64_t* __restrict__ off,
+               const int32_t* __restrict__ len, const int32_t* __restrict__ cols,
+               const float* __restrict__ v, const float* __restrict__ diag,
+               const float* __restrict__ x, const float* __restrict__ y, float* __restrict__ r) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= cnt) return;
+  const int32_t i = rows[k];
+  float s = fmaf(-diag[i], y[i], x[i]);
+  const int64_t base = off[k >> 5] + (k & 31);
+  const int n = len[k];
+  for (int q = 0; q < n; ++q) {
+    const int64_t p = base + 32 * int64_t(q);
+    s = fmaf(-v[p], y[cols[p]], s);
+  }
+  r[i] = s;
+}
+
+__global__ void zero_rows_k(int64_t cnt, const int32_t* __restrict__ rows, float* __restrict__ r) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < cnt) r[rows[k]] = 0.f;
+}
+
 template <typename T>
 __global__ void fill_k(int64_t n, T* y, T val) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -358,15 +383,14 @@ __global__ void fill_k(int64_t n, T* y, T val) {
 __global__ void rdiag_k(int64_t n, const int64_t* __restrict__ rp,
                         const int32_t* __restrict__ ci,
                         const double* __restrict__ v, double* __restrict__ rd,
-                        float* __restrict__ rd32) {
+                        float* __restrict__ d32) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double d = 0.0;
   for (int64_t p = rp[i]; p < rp[i + 1]; ++p)
     if (ci[p] == i) d = v[p];
-  const double r = 1.0 / d;
-  rd[i] = r;
-  if (rd32) rd32[i] = float(r);
+  rd[i] = 1.0 / d;
+  if (d32) d32[i] = float(d);
 }
 
 template <typename A, typename B>
@@ -376,16 +400,6 @@ __global__ void convert_k(int64_t n, const A* __restrict__ a, B* __restrict__ b)
 }
 
 // y = a - y (FP32)
-__global__ void rsub_f32_k(int64_t n, const float* __restrict__ a, float* __restrict__ y) {
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = a[i] - y[i];
-}
-// y += a (FP32)
-__global__ void add32_k(int64_t n, const float* __restrict__ a, float* __restrict__ y) {
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) y[i] += a[i];
-}
-
 // x += alpha * y (FP64)
 __global__ void axpy_k(int64_t n, double alpha, const double* __restrict__ y,
                        double* __restrict__ x) {
@@ -524,6 +538,13 @@ void KrylovSolver::ensure_f32(cudaStream_t s) {
         int64_t(gs_map_.n), gs_vals_.p, gs_vals32_.p);
   }
   convert_k<double, float><<<grid1(n), kBlock, 0, s>>>(n, rdiag_.p, rdiag32_.p);
+  diag32_.resize(n);
+  {
+    DeviceArray<double> tmp;
+    tmp.resize(n);
+    rdiag_k<<<grid1(n), kBlock, 0, s>>>(n, A_.row_ptr, A_.col_idx, A_.values, tmp.p, diag32_.p);
+    NW_CUDA(cudaStreamSynchronize(s));
+  }
   NW_CUDA(cudaGetLastError());
   f32_valid_ = true;
 }
@@ -602,10 +623,11 @@ bool stalled(int& stalls, double rnorm, double prev) {
 // giving the same bits). With at most two classes nothing reads a y value
 // before it is written, so y needs no zero fill.
 template <typename VT, typename T>
-void KrylovSolver::sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s) const {
+void KrylovSolver::sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s,
+                       bool from_guess) const {
   const int nc = int(gs_cptr_.size()) - 1;
   if (nc < 1) fail(NW_INTERNAL, "Gauss-Seidel colour classes not set up");
-  if (nc > 2) fill_k<T><<<grid1(A_.n), kBlock, 0, s>>>(A_.n, y, T(0));
+  if (nc > 2 && !from_guess) fill_k<T><<<grid1(A_.n), kBlock, 0, s>>>(A_.n, y, T(0));
   auto pass = [&](int c, int first) {
     const int64_t b = gs_cptr_[c], cnt = gs_cptr_[c + 1] - b;
     if (cnt)
@@ -613,8 +635,25 @@ void KrylovSolver::sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream
                                                      gs_len_.p + b, gs_cols_.p, vals, rd, x, y,
                                                      first);
   };
-  for (int c = 0; c < nc; ++c) pass(c, c == 0);
+  for (int c = 0; c < nc; ++c) pass(c, c == 0 && !from_guess);
   for (int c = nc - 2; c >= 0; --c) pass(c, 0);
+  NW_CUDA(cudaGetLastError());
+}
+
+// r = x - A y after a symmetric sweep that produced y: the rows of class 0,
+// relaxed last, have a zero residual (up to the reciprocal's rounding) and
+// get exactly 0; the other classes are evaluated over the sliced copy.
+void KrylovSolver::sgs_residual32(const float* x, const float* y, float* r, cudaStream_t s) const {
+  const int nc = int(gs_cptr_.size()) - 1;
+  const int64_t c0 = gs_cptr_[1];
+  if (c0) zero_rows_k<<<grid1(c0), kBlock, 0, s>>>(c0, gs_rows_.p, r);
+  for (int c = 1; c < nc; ++c) {
+    const int64_t b = gs_cptr_[c], cnt = gs_cptr_[c + 1] - b;
+    if (cnt)
+      gs_resid_k<<<grid1(cnt), kBlock, 0, s>>>(cnt, gs_rows_.p + b, gs_off_.p + gs_slice0_[c],
+                                               gs_len_.p + b, gs_cols_.p, gs_vals32_.p, diag32_.p,
+                                               x, y, r);
+  }
   NW_CUDA(cudaGetLastError());
 }
 
@@ -667,9 +706,10 @@ void KrylovSolver::setup_colors(const std::vector<int32_t>& rows,
 }
 
 // FP32 preconditioner of the mixed method. Learned (two-level, symmetric
-// smoothing): z1 = SGS(x), r1 = x - A z1, ec = Net(R r1),
-// z2 = z1 + alpha P ec with the energy-optimal alpha, then the
-// post-smoothing z = z2 + SGS(x - A z2).
+// smoothing): z1 = SGS(x), r1 = x - A z1 (evaluated on the classes the
+// sweep left a residual on), ec = Net(R r1), z2 = z1 + alpha P ec with the
+// energy-optimal alpha, then the post-smoothing z = z2 + SGS(x - A z2),
+// evaluated as one symmetric sweep starting from z2.
 void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
                              cudaStream_t s) {
   const int64_t n = A_.n;
@@ -687,17 +727,12 @@ void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
   tmp32_.resize(n);
   rc32_.resize(cl_->nc);
   ec32_.resize(cl_->nc);
-  spmv32(y, tmp32_.p, s);
-  rsub_f32_k<<<grid1(n), kBlock, 0, s>>>(n, x, tmp32_.p);
+  sgs_residual32(x, y, tmp32_.p, s);
   launch_restrict(*cl_, tmp32_.p, rc32_.p, s);
   net_->coarse_correction(*cl_, rc32_.p, ec32_.p, s);
   launch_prolong_add(*cl_, ec32_.p, net_->alpha_dev(), y, s);
-  if (!net_->post_smooth) return;
-  post32_.resize(n);
-  spmv32(y, tmp32_.p, s);
-  rsub_f32_k<<<grid1(n), kBlock, 0, s>>>(n, x, tmp32_.p);
-  sgs<float, float>(gs_vals32_.p, rdiag32_.p, tmp32_.p, post32_.p, s);
-  add32_k<<<grid1(n), kBlock, 0, s>>>(n, post32_.p, y);
+  // post-smoothing z2 + SGS(x - A z2) is one symmetric sweep from z2
+  if (net_->post_smooth) sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s, true);
   NW_CUDA(cudaGetLastError());
 }
 

@@ -100,7 +100,7 @@ class KrylovSolver {
                     const double* b, double* x, cudaStream_t s);
   LearnedNet* net_ = nullptr;
   CoarseLevel* cl_ = nullptr;
-  DeviceArray<float> Z32_, rc32_, ec32_, tmp32_, tmp32b_, post32_;
+  DeviceArray<float> Z32_, rc32_, ec32_, tmp32_, tmp32b_;
 
   DevCsr A_;
   int m_ = 0;
@@ -128,7 +128,10 @@ class KrylovSolver {
   DeviceArray<double> gs_vals_;
   DeviceArray<float> gs_vals32_;
   template <typename VT, typename T>
-  void sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s) const;
+  void sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s,
+           bool from_guess = false) const;
+  void sgs_residual32(const float* x, const float* y, float* r, cudaStream_t s) const;
+  DeviceArray<float> diag32_;   // FP32 diagonal
   // FP32 copies for the inner solve of the mixed method
   DeviceArray<float> vals32_, rdiag32_, V32_, w32_, z32_, r32_;
   bool f32_valid_ = false;

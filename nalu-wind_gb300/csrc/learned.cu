@@ -298,15 +298,33 @@ __global__ void input_k(int64_t nc, const float* __restrict__ rc,
   }
 }
 
-// scal[0] = s = sqrt(sum u^2 / nc), scal[1] = 1 / s (0 when s == 0)
-__global__ void rms_k(int nblocks, const float* __restrict__ partial, int64_t nc,
-                      float* __restrict__ scal) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// Fixed-order sum of partial[b * stride + which], b < nblocks, by one block
+// of kB threads (strided per-thread sums, then a tree).
+__device__ double block_sum(int nblocks, const float* __restrict__ partial, int stride, int which,
+                            double* red) {
   double t = 0.0;
-  for (int b = 0; b < nblocks; ++b) t += partial[b];
-  const double s = std::sqrt(t / double(nc > 0 ? nc : 1));
-  scal[0] = float(s);
-  scal[1] = s > 0 ? float(1.0 / s) : 0.f;
+  for (int b = threadIdx.x; b < nblocks; b += kB) t += partial[int64_t(b) * stride + which];
+  red[threadIdx.x] = t;
+  __syncthreads();
+  for (int h = kB / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  const double v = red[0];
+  __syncthreads();
+  return v;
+}
+
+// scal[0] = s = sqrt(sum u^2 / nc), scal[1] = 1 / s (0 when s == 0)
+__global__ void __launch_bounds__(kB)
+    rms_k(int nblocks, const float* __restrict__ partial, int64_t nc, float* __restrict__ scal) {
+  __shared__ double red[kB];
+  const double t = block_sum(nblocks, partial, 1, 0, red);
+  if (threadIdx.x == 0) {
+    const double s = std::sqrt(t / double(nc > 0 ? nc : 1));
+    scal[0] = float(s);
+    scal[1] = s > 0 ? float(1.0 / s) : 0.f;
+  }
 }
 
 // x = u / s; ax = sum_J w_IJ x_J; H0 = relu(x W0[0] + ax W0[1]) into
@@ -400,16 +418,16 @@ __global__ void coarse_apply_k(int64_t nc, const int64_t* __restrict__ cptr,
 // Energy-optimal scaling of the coarse correction, fixed-order sums:
 //   scal[2] = alpha = ec' rc / ec' Ac ec   (0 unless the denominator is > 0)
 //   scal[3] = (ec' rc)^2 / ec' Ac ec       (A-norm error energy removed)
-__global__ void alpha_k(int nblocks, const float* __restrict__ partial, float* __restrict__ scal) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double num = 0.0, den = 0.0;
-  for (int b = 0; b < nblocks; ++b) {
-    num += partial[2 * b];
-    den += partial[2 * b + 1];
+__global__ void __launch_bounds__(kB)
+    alpha_k(int nblocks, const float* __restrict__ partial, float* __restrict__ scal) {
+  __shared__ double red[kB];
+  const double num = block_sum(nblocks, partial, 2, 0, red);
+  const double den = block_sum(nblocks, partial, 2, 1, red);
+  if (threadIdx.x == 0) {
+    const bool ok = den > 0.0 && isfinite(num) && isfinite(den);
+    scal[2] = ok ? float(num / den) : 0.f;
+    scal[3] = ok ? float(num * num / den) : 0.f;
   }
-  const bool ok = den > 0.0 && isfinite(num) && isfinite(den);
-  scal[2] = ok ? float(num / den) : 0.f;
-  scal[3] = ok ? float(num * num / den) : 0.f;
 }
 
 // dL/dy for the scaled loss L = (cA - (ec' rc)^2 / ec' Ac ec) / eA:
@@ -527,14 +545,18 @@ __global__ void coarse_weights_k(int64_t nc, const int64_t* __restrict__ cptr,
     wgt[q] = q == cdiag[I] ? 0.f : float(-ac[q] * id);
 }
 
-__global__ void restrict_k(int64_t nc, const int64_t* __restrict__ mptr,
-                           const int32_t* __restrict__ mrows, const float* __restrict__ r,
-                           float* __restrict__ rc) {
-  const int64_t I = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+// rc_I = sum of r over aggregate I: warp per aggregate, lanes stride the
+// member list, fixed-order butterfly sum
+__global__ void __launch_bounds__(kB)
+    restrict_k(int64_t nc, const int64_t* __restrict__ mptr, const int32_t* __restrict__ mrows,
+               const float* __restrict__ r, float* __restrict__ rc) {
+  const int64_t I = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (I >= nc) return;
   float s = 0.f;
-  for (int64_t k = mptr[I]; k < mptr[I + 1]; ++k) s += r[mrows[k]];
-  rc[I] = s;
+  for (int64_t k = mptr[I] + lane; k < mptr[I + 1]; k += 32) s += r[mrows[k]];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if (lane == 0) rc[I] = s;
 }
 
 // z_i += alpha ec_agg(i), alpha read from the device
@@ -577,7 +599,7 @@ void launch_gemm_wgrad(const uint16_t* xc, const uint16_t* dz, float* partial,
 }
 
 void launch_restrict(const CoarseLevel& cl, const float* r, float* rc, cudaStream_t s) {
-  restrict_k<<<gridn(cl.nc), kB, 0, s>>>(cl.nc, cl.mptr.p, cl.mrows.p, r, rc);
+  restrict_k<<<gridn(cl.nc * 32), kB, 0, s>>>(cl.nc, cl.mptr.p, cl.mrows.p, r, rc);
 }
 void launch_prolong_add(const CoarseLevel& cl, const float* ec, const float* alpha, float* z,
                         cudaStream_t s) {
@@ -810,7 +832,7 @@ void LearnedNet::forward(const CoarseLevel& cl, const float* wgt, const float* d
   work.resize(nc);
   const unsigned gw = gridn(nc * 32);  // warp per row
   input_k<<<gridn(nc), kB, 0, s>>>(nc, rc, dinv, work.u.p, work.partial.p);
-  rms_k<<<1, 32, 0, s>>>(int(gridn(nc)), work.partial.p, nc, work.scal.p);
+  rms_k<<<1, kB, 0, s>>>(int(gridn(nc)), work.partial.p, nc, work.scal.p);
   layer0_k<<<gw, kB, 0, s>>>(nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, wgt, work.u.p, work.scal.p,
                              params.p + kOffW0, work.x.p, work.ax.p, work.xc1.p);
   uint16_t* xcs[4] = {work.xc1.p, work.xc2.p, work.xc3.p, nullptr};
@@ -829,7 +851,7 @@ void LearnedNet::coarse_correction(const CoarseLevel& cl, const float* rc, float
   const int nb = int(gridn(cl.nc));
   coarse_apply_k<<<nb, kB, 0, s>>>(cl.nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, cl.wgt.p, cl.dinv.p,
                                    ec, rc, work.aec.p, work.partial.p);
-  alpha_k<<<1, 32, 0, s>>>(nb, work.partial.p, work.scal.p);
+  alpha_k<<<1, kB, 0, s>>>(nb, work.partial.p, work.scal.p);
   NW_CUDA(cudaGetLastError());
 }
 
@@ -844,7 +866,7 @@ double LearnedNet::forward_backward(const CoarseLevel& cl, const float* wgt,
   const int nb = int(gridn(nc));
   coarse_apply_k<<<nb, kB, 0, s>>>(nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, wgt, dinv, ec, rc,
                                    work.aec.p, work.partial.p);
-  alpha_k<<<1, 32, 0, s>>>(nb, work.partial.p, work.scal.p);
+  alpha_k<<<1, kB, 0, s>>>(nb, work.partial.p, work.scal.p);
   float sc[4];
   NW_CUDA(cudaMemcpyAsync(sc, work.scal.p, sizeof(sc), cudaMemcpyDeviceToHost, s));
   NW_CUDA(cudaStreamSynchronize(s));
