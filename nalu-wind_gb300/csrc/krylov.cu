@@ -220,6 +220,122 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// FP32 basis with a padded leading dimension (ld a multiple of 32 floats):
+// the multi-dot and multi-axpy below move four consecutive elements per
+// thread with 16-byte loads. Elements in [n, ld) are padding and never
+// enter a result.
+__global__ void __launch_bounds__(kBlock)
+    mdot4_k(int64_t n, int nv, const float* __restrict__ V, int64_t ld,
+            const float* __restrict__ w, double* __restrict__ partial) {
+  __shared__ double red[kTile][kBlock / 32];
+  const int G = gridDim.x;
+  const int64_t ng = (n + 3) >> 2, full = n >> 2;  // groups of 4; full groups
+  const int64_t stride = int64_t(G) * blockDim.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float4* w4 = reinterpret_cast<const float4*>(w);
+  for (int k0 = 0; k0 < nv; k0 += kTile) {
+    const int kt = min(kTile, nv - k0);
+    float s[kTile], c[kTile];
+#pragma unroll
+    for (int k = 0; k < kTile; ++k) s[k] = c[k] = 0.f;
+    for (int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < ng; g += stride) {
+      float4 wv = w4[g];
+      if (g >= full) {  // the last, partial group
+        const int64_t i0 = 4 * g;
+        if (i0 + 1 >= n) wv.y = 0.f;
+        if (i0 + 2 >= n) wv.z = 0.f;
+        if (i0 + 3 >= n) wv.w = 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < kTile; ++k)
+        if (k < kt) {
+          float4 a = reinterpret_cast<const float4*>(V + int64_t(k0 + k) * ld)[g];
+          if (g >= full) {
+            const int64_t i0 = 4 * g;
+            if (i0 + 1 >= n) a.y = 0.f;
+            if (i0 + 2 >= n) a.z = 0.f;
+            if (i0 + 3 >= n) a.w = 0.f;
+          }
+          acc_prod(a.x, wv.x, s[k], c[k]);
+          acc_prod(a.y, wv.y, s[k], c[k]);
+          acc_prod(a.z, wv.z, s[k], c[k]);
+          acc_prod(a.w, wv.w, s[k], c[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kTile; ++k) {
+      if (k < kt) {
+        const double v = warp_sum(s[k], c[k]);
+        if (lane == 0) red[k][warp] = v;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < kt) {
+      double v = 0.0;
+      for (int q = 0; q < kBlock / 32; ++q) v += red[threadIdx.x][q];
+      partial[int64_t(k0 + threadIdx.x) * G + blockIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// w -= V h for groups of four elements; optional per-block partial sums of
+// the updated |w|^2 (elements below n only).
+__global__ void __launch_bounds__(kBlock)
+    maxpy4_k(int64_t n, int nv, const float* __restrict__ V, int64_t ld,
+             const double* __restrict__ h, float* __restrict__ w,
+             double* __restrict__ nrm_partial) {
+  __shared__ float hs[1024];
+  __shared__ double red[kBlock / 32];
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) hs[k] = float(h[k]);
+  __syncthreads();
+  const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t ng = (n + 3) >> 2;
+  float ss = 0.f, cc = 0.f;
+  if (g < ng) {
+    float4 acc = reinterpret_cast<float4*>(w)[g];
+    int k = 0;
+    for (; k + 4 <= nv; k += 4) {
+      float4 a[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) a[q] = reinterpret_cast<const float4*>(V + int64_t(k + q) * ld)[g];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float hk = hs[k + q];
+        acc.x = fmaf(-hk, a[q].x, acc.x);
+        acc.y = fmaf(-hk, a[q].y, acc.y);
+        acc.z = fmaf(-hk, a[q].z, acc.z);
+        acc.w = fmaf(-hk, a[q].w, acc.w);
+      }
+    }
+    for (; k < nv; ++k) {
+      const float4 a = reinterpret_cast<const float4*>(V + int64_t(k) * ld)[g];
+      const float hk = hs[k];
+      acc.x = fmaf(-hk, a.x, acc.x);
+      acc.y = fmaf(-hk, a.y, acc.y);
+      acc.z = fmaf(-hk, a.z, acc.z);
+      acc.w = fmaf(-hk, a.w, acc.w);
+    }
+    reinterpret_cast<float4*>(w)[g] = acc;
+    if (nrm_partial) {
+      const int64_t i0 = 4 * g;
+      acc_prod(acc.x, acc.x, ss, cc);
+      if (i0 + 1 < n) acc_prod(acc.y, acc.y, ss, cc);
+      if (i0 + 2 < n) acc_prod(acc.z, acc.z, ss, cc);
+      if (i0 + 3 < n) acc_prod(acc.w, acc.w, ss, cc);
+    }
+  }
+  if (!nrm_partial) return;
+  const double v = warp_sum(ss, cc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < kBlock / 32; ++q) t += red[q];
+    nrm_partial[blockIdx.x] = t;
+  }
+}
+
 // out[k] = sum of partial[k][0..G) (one block per k, fixed tree).
 __global__ void reduce_partials_k(int G, const double* __restrict__ partial,
                                   double* __restrict__ out, int mode,
@@ -521,8 +637,9 @@ void KrylovSolver::ensure_f32(cudaStream_t s) {
   const int64_t n = A_.n;
   vals32_.resize(A_.nnz);
   rdiag32_.resize(n);
-  V32_.resize(size_t(m_ + 1) * n);
-  w32_.resize(n);
+  ld32_ = (n + 31) / 32 * 32;
+  V32_.resize(size_t(m_ + 1) * ld32_);
+  w32_.resize(ld32_);
   z32_.resize(n);
   r32_.resize(n);
   convert_k<double, float><<<grid1(A_.nnz), kBlock, 0, s>>>(A_.nnz, A_.values,
@@ -1015,8 +1132,10 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
   std::vector<double> H(size_t(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
   const bool fuse_jacobi = pc.kind == NW_PC_JACOBI;
   const bool flexible = pc.kind == NW_PC_LEARNED;
-  if (flexible && Z32_.n < size_t(m) * n) Z32_.resize(size_t(m) * n);
+  const int64_t ld = ld32_;
+  if (flexible && Z32_.n < size_t(m) * ld) Z32_.resize(size_t(m) * ld);
   float* V = V32_.p;
+  const unsigned g4 = grid1((n + 3) / 4);
   double* hs = scal_.p;
   double* h2 = scal_.p + (m_ + 2);
   double rel = 1.0;
@@ -1033,19 +1152,19 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
     g[0] = 1.0;  // inner system solved for r / ||r||
     int j = 0;
     for (; j < m && its < cfg.max_iterations; ++j) {
-      float* vj = V + size_t(j) * n;
-      float* zj = flexible ? Z32_.p + size_t(j) * n : z32_.p;
+      float* vj = V + size_t(j) * ld;
+      float* zj = flexible ? Z32_.p + size_t(j) * ld : z32_.p;
       if (!fuse_jacobi) precond32(pc, vj, zj, s);
       spmv32(zj, w32_.p, s);
-      mdot_k<float><<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, n, w32_.p, partial_.p);
+      mdot4_k<<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, ld, w32_.p, partial_.p);
       reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, hs, 0, nullptr);
-      maxpy_k<float><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, hs, w32_.p, nullptr);
-      mdot_k<float><<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, n, w32_.p, partial_.p);
+      maxpy4_k<<<g4, kBlock, 0, s>>>(n, j + 1, V, ld, hs, w32_.p, nullptr);
+      mdot4_k<<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, ld, w32_.p, partial_.p);
       reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, h2 + 1, 1, hs);
-      maxpy_k<float><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, h2 + 1, w32_.p, partial_.p);
-      reduce_partials_k<<<1, kBlock, 0, s>>>(int(grid1(n)), partial_.p, h2, 0, nullptr);
+      maxpy4_k<<<g4, kBlock, 0, s>>>(n, j + 1, V, ld, h2 + 1, w32_.p, partial_.p);
+      reduce_partials_k<<<1, kBlock, 0, s>>>(int(g4), partial_.p, h2, 0, nullptr);
       sqrt_scalar_k<<<1, 1, 0, s>>>(h2);
-      scale_jacobi_k<float><<<grid1(n), kBlock, 0, s>>>(n, w32_.p, V + size_t(j + 1) * n, h2,
+      scale_jacobi_k<float><<<grid1(n), kBlock, 0, s>>>(n, w32_.p, V + size_t(j + 1) * ld, h2,
                                                         fuse_jacobi ? rdiag32_.p : nullptr, z32_.p);
       NW_CUDA(cudaGetLastError());
       NW_CUDA(cudaMemcpyAsync(h_pinned_, hs, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
@@ -1089,9 +1208,9 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
       for (int i = 0; i < kk; ++i) y[i] *= rnorm;
       NW_CUDA(cudaMemcpyAsync(h2, y.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
       if (flexible) {
-        combine_k<float><<<grid1(n), kBlock, 0, s>>>(n, kk, Z32_.p, n, h2, z32_.p);
+        combine_k<float><<<grid1(n), kBlock, 0, s>>>(n, kk, Z32_.p, ld, h2, z32_.p);
       } else {
-        combine_k<float><<<grid1(n), kBlock, 0, s>>>(n, kk, V, n, h2, w32_.p);
+        combine_k<float><<<grid1(n), kBlock, 0, s>>>(n, kk, V, ld, h2, w32_.p);
         precond32(pc, w32_.p, z32_.p, s);
       }
       add_f32_k<<<grid1(n), kBlock, 0, s>>>(n, z32_.p, x);

@@ -134,6 +134,7 @@ class KrylovSolver {
   DeviceArray<float> diag32_;   // FP32 diagonal
   // FP32 copies for the inner solve of the mixed method
   DeviceArray<float> vals32_, rdiag32_, V32_, w32_, z32_, r32_;
+  int64_t ld32_ = 0;  // leading dimension of the FP32 basis (n rounded up to 32)
   bool f32_valid_ = false;
   int red_blocks_ = 0;
 };
