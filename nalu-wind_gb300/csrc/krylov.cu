@@ -1107,8 +1107,9 @@ SolveResult KrylovSolver::cg(const nw_solver_cfg& cfg, double tol,
 // Mixed precision: FP64 iterative refinement around an FP32 inner GMRES.
 // Outer: r = b - A x in FP64, stop when ||r||/||b|| <= tol. Inner: GMRES
 // restarted once per outer step on A d = r in FP32 storage (FP32 SpMV with
-// FP32 accumulation, FP32 Jacobi/SGS), FP64-accurate Gram-Schmidt dots,
-// FP64 Hessenberg least squares on the host; x += d in FP64.
+// FP32 accumulation, FP32 Jacobi/SGS), one classical Gram-Schmidt pass
+// with FP64-accurate dots, FP64 Hessenberg least squares on the host;
+// x += d in FP64.
 SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
                                 const Precond& pc, const double* b, double* x,
                                 cudaStream_t s) {
@@ -1156,12 +1157,14 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
       float* zj = flexible ? Z32_.p + size_t(j) * ld : z32_.p;
       if (!fuse_jacobi) precond32(pc, vj, zj, s);
       spmv32(zj, w32_.p, s);
+      // one classical Gram-Schmidt pass (dots accumulated exactly in FP32
+      // pairs): the inner solve only reduces the residual by inner_tol per
+      // cycle and the FP64 outer loop recomputes the true residual, so the
+      // second pass of the FP64 method is not needed here (same iteration
+      // counts on the Poisson systems measured)
       mdot4_k<<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, ld, w32_.p, partial_.p);
       reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, hs, 0, nullptr);
-      maxpy4_k<<<g4, kBlock, 0, s>>>(n, j + 1, V, ld, hs, w32_.p, nullptr);
-      mdot4_k<<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, ld, w32_.p, partial_.p);
-      reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, h2 + 1, 1, hs);
-      maxpy4_k<<<g4, kBlock, 0, s>>>(n, j + 1, V, ld, h2 + 1, w32_.p, partial_.p);
+      maxpy4_k<<<g4, kBlock, 0, s>>>(n, j + 1, V, ld, hs, w32_.p, partial_.p);
       reduce_partials_k<<<1, kBlock, 0, s>>>(int(g4), partial_.p, h2, 0, nullptr);
       sqrt_scalar_k<<<1, 1, 0, s>>>(h2);
       scale_jacobi_k<float><<<grid1(n), kBlock, 0, s>>>(n, w32_.p, V + size_t(j + 1) * ld, h2,
