@@ -296,8 +296,10 @@ nw_status nw_learned_params(nw_learned* net, float* out, const float* in,
  * v - A z (symmetric two-level cycle); 0: no post-smoothing.
  * agg_passes (1..4, default 2): plain aggregation applied that many times
  * (aggregates of aggregates) to build the coarse level; takes effect at
- * the next nw_linsys_attach_learned. */
-nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes);
+ * the next nw_linsys_attach_learned. smoother 0 (default): symmetric GS
+ * sweeps before and after the coarse step; 1: a forward sweep before and
+ * a backward sweep after (half the smoothing work, still symmetric). */
+nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes, int smoother);
 /* Build the aggregation / coarse level of this system's graph (num_dof 1)
  * and use `net` for NW_PC_LEARNED solves of this handle. */
 nw_status nw_linsys_attach_learned(nw_linsys* ls, nw_learned* net);

@@ -149,7 +149,7 @@ SIGNATURES = {
     "nw_learned_load": (C.c_int, [C.c_void_p, C.c_char_p]),
     "nw_learned_num_params": (C.c_int64, []),
     "nw_learned_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64]),
-    "nw_learned_configure": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "nw_learned_configure": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "nw_linsys_attach_learned": (C.c_int, [C.c_void_p, C.c_void_p]),
     "nw_linsys_coarse_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P]),
     "nw_linsys_coarse_graph": (C.c_int, [C.c_void_p, _I32P, _I64P, _I32P, C.POINTER(C.c_float),
@@ -461,8 +461,8 @@ class Learned:
         p = np.ascontiguousarray(p, np.float32)
         check(self.lib.nw_learned_params(self.h, None, _ptr(p, C.c_float), self.num_params))
 
-    def configure(self, post_smooth: bool = True, agg_passes: int = 2) -> None:
-        check(self.lib.nw_learned_configure(self.h, int(post_smooth), int(agg_passes)))
+    def configure(self, post_smooth: bool = True, agg_passes: int = 2, smoother: int = 0) -> None:
+        check(self.lib.nw_learned_configure(self.h, int(post_smooth), int(agg_passes), int(smoother)))
 
     def save(self, path) -> None:
         check(self.lib.nw_learned_save(self.h, str(path).encode()))

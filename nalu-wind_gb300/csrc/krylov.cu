@@ -741,9 +741,10 @@ bool stalled(int& stalls, double rnorm, double prev) {
 // before it is written, so y needs no zero fill.
 template <typename VT, typename T>
 void KrylovSolver::sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s,
-                       bool from_guess) const {
+                       bool from_guess, int sweep) const {
   const int nc = int(gs_cptr_.size()) - 1;
   if (nc < 1) fail(NW_INTERNAL, "Gauss-Seidel colour classes not set up");
+  // sweep 0: symmetric (forward then backward); 1: forward only; 2: backward only
   if (nc > 2 && !from_guess) fill_k<T><<<grid1(A_.n), kBlock, 0, s>>>(A_.n, y, T(0));
   auto pass = [&](int c, int first) {
     const int64_t b = gs_cptr_[c], cnt = gs_cptr_[c + 1] - b;
@@ -752,19 +753,28 @@ void KrylovSolver::sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream
                                                      gs_len_.p + b, gs_cols_.p, vals, rd, x, y,
                                                      first);
   };
-  for (int c = 0; c < nc; ++c) pass(c, c == 0 && !from_guess);
-  for (int c = nc - 2; c >= 0; --c) pass(c, 0);
+  if (sweep == 2) {
+    for (int c = nc - 1; c >= 0; --c) pass(c, c == nc - 1 && !from_guess);
+  } else {
+    for (int c = 0; c < nc; ++c) pass(c, c == 0 && !from_guess);
+    if (sweep == 0)
+      for (int c = nc - 2; c >= 0; --c) pass(c, 0);
+  }
   NW_CUDA(cudaGetLastError());
 }
 
-// r = x - A y after a symmetric sweep that produced y: the rows of class 0,
-// relaxed last, have a zero residual (up to the reciprocal's rounding) and
+// r = x - A y after a sweep that produced y: the rows of the class relaxed
+// last (`last`) have a zero residual (up to the reciprocal's rounding) and
 // get exactly 0; the other classes are evaluated over the sliced copy.
-void KrylovSolver::sgs_residual32(const float* x, const float* y, float* r, cudaStream_t s) const {
+void KrylovSolver::sgs_residual32(const float* x, const float* y, float* r, cudaStream_t s,
+                                  int last) const {
   const int nc = int(gs_cptr_.size()) - 1;
-  const int64_t c0 = gs_cptr_[1];
-  if (c0) zero_rows_k<<<grid1(c0), kBlock, 0, s>>>(c0, gs_rows_.p, r);
-  for (int c = 1; c < nc; ++c) {
+  {
+    const int64_t b = gs_cptr_[last], cnt = gs_cptr_[last + 1] - b;
+    if (cnt) zero_rows_k<<<grid1(cnt), kBlock, 0, s>>>(cnt, gs_rows_.p + b, r);
+  }
+  for (int c = 0; c < nc; ++c) {
+    if (c == last) continue;
     const int64_t b = gs_cptr_[c], cnt = gs_cptr_[c + 1] - b;
     if (cnt)
       gs_resid_k<<<grid1(cnt), kBlock, 0, s>>>(cnt, gs_rows_.p + b, gs_off_.p + gs_slice0_[c],
@@ -822,6 +832,14 @@ void KrylovSolver::setup_colors(const std::vector<int32_t>& rows,
   f32_valid_ = false;
 }
 
+// Pre-smoothing of the learned cycle (also used when harvesting pairs):
+// a symmetric sweep, or a forward sweep with smoother 1.
+void KrylovSolver::learned_presmooth32(const float* x, float* y, cudaStream_t s) {
+  if (!has_learned()) fail(NW_INVALID_ARG, "no learned preconditioner attached");
+  ensure_f32(s);
+  sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s, false, net_->smoother == 1 ? 1 : 0);
+}
+
 // FP32 preconditioner of the mixed method. Learned (two-level, symmetric
 // smoothing): z1 = SGS(x), r1 = x - A z1 (evaluated on the classes the
 // sweep left a residual on), ec = Net(R r1), z2 = z1 + alpha P ec with the
@@ -840,16 +858,21 @@ void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
     return;
   }
   if (!has_learned()) fail(NW_INVALID_ARG, "no learned preconditioner attached");
-  sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s);
+  // smoother 0: symmetric sweeps before and after; 1: forward sweep before,
+  // backward sweep after (the cycle stays symmetric)
+  const bool half = net_->smoother == 1;
+  const int nc = int(gs_cptr_.size()) - 1;
+  learned_presmooth32(x, y, s);
   tmp32_.resize(n);
   rc32_.resize(cl_->nc);
   ec32_.resize(cl_->nc);
-  sgs_residual32(x, y, tmp32_.p, s);
+  sgs_residual32(x, y, tmp32_.p, s, half ? nc - 1 : 0);
   launch_restrict(*cl_, tmp32_.p, rc32_.p, s);
   net_->coarse_correction(*cl_, rc32_.p, ec32_.p, s);
   launch_prolong_add(*cl_, ec32_.p, net_->alpha_dev(), y, s);
-  // post-smoothing z2 + SGS(x - A z2) is one symmetric sweep from z2
-  if (net_->post_smooth) sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s, true);
+  // post-smoothing z2 + S(x - A z2) is one sweep starting from z2
+  if (net_->post_smooth)
+    sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s, true, half ? 2 : 0);
   NW_CUDA(cudaGetLastError());
 }
 

@@ -88,6 +88,8 @@ class KrylovSolver {
   // FP32 preconditioner application (Jacobi, SGS or learned) of the mixed
   // method; y and x must not alias.
   void precond32(const Precond& pc, const float* x, float* y, cudaStream_t s);
+  // the learned cycle's pre-smoothing sweep alone (pair harvesting)
+  void learned_presmooth32(const float* x, float* y, cudaStream_t s);
   const float* vals32() const { return vals32_.p; }
 
  private:
@@ -129,8 +131,8 @@ class KrylovSolver {
   DeviceArray<float> gs_vals32_;
   template <typename VT, typename T>
   void sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s,
-           bool from_guess = false) const;
-  void sgs_residual32(const float* x, const float* y, float* r, cudaStream_t s) const;
+           bool from_guess = false, int sweep = 0) const;
+  void sgs_residual32(const float* x, const float* y, float* r, cudaStream_t s, int last) const;
   DeviceArray<float> diag32_;   // FP32 diagonal
   // FP32 copies for the inner solve of the mixed method
   DeviceArray<float> vals32_, rdiag32_, V32_, w32_, z32_, r32_;

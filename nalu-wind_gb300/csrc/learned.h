@@ -85,6 +85,7 @@ struct LearnedNet {
   uint64_t seed = 0;
   int post_smooth = 1;  // SGS sweep after the coarse correction
   int agg_passes = 2;   // aggregation passes of the coarse level
+  int smoother = 0;     // 0: symmetric GS sweeps around the coarse step; 1: forward / backward
   // training data (coarse vectors of one aggregation)
   int64_t data_nc = 0, data_nnzc = 0;
   int npairs = 0, nsystems = 0;

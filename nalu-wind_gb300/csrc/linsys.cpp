@@ -932,10 +932,12 @@ nw_status nw_learned_params(nw_learned* net, float* out, const float* in, int64_
   });
 }
 
-nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes) {
+nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes, int smoother) {
   return guard([&] {
-    if (!net || (post_smooth != 0 && post_smooth != 1) || agg_passes < 1 || agg_passes > 4)
+    if (!net || (post_smooth != 0 && post_smooth != 1) || agg_passes < 1 || agg_passes > 4 ||
+        (smoother != 0 && smoother != 1))
       fail(NW_INVALID_ARG, "bad option");
+    net->net.smoother = smoother;
     if (agg_passes != net->net.agg_passes && net->net.npairs > 0)
       fail(NW_INVALID_ARG, "harvested pairs use the current aggregation; clear them first");
     net->net.post_smooth = post_smooth;
@@ -1073,10 +1075,8 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
       }
       if (!(rn > 0.0)) break;
       NW_CUDA(cudaMemcpyAsync(r32.p, h32.data(), n * 4, cudaMemcpyHostToDevice, s));
-      // z1 = SGS(r), r1 = r - A z1, rc = R r1
-      Precond sg = ls->pc;
-      sg.kind = NW_PC_SGS;
-      ks.precond32(sg, r32.p, z1.p, s);
+      // z1 = pre-smoothing sweep of r, r1 = r - A z1, rc = R r1
+      ks.learned_presmooth32(r32.p, z1.p, s);
       auto* rc = new DeviceArray<float>();
       rc->resize(cl.nc);
       DeviceArray<float> az;

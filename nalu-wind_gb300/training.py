@@ -19,11 +19,11 @@ from .workload import poisson_system
 
 
 def train_poisson_network(shape=(64, 64, 48), systems=16, restarts=40, kspace=30, epochs=100,
-                          batch=8, lr=1e-3, seed=0, agg_passes=2, stream=None, tets=False):
+                          batch=8, lr=1e-3, seed=0, agg_passes=2, stream=None, tets=False, smoother=0):
     """Returns (network, info). info: pairs, harvest / train seconds and
     the mean energy-norm loss over the pairs before and after training."""
     net = Learned(seed=seed)
-    net.configure(post_smooth=True, agg_passes=agg_passes)
+    net.configure(post_smooth=True, agg_passes=agg_passes, smoother=smoother)
     rng = np.random.default_rng(seed)
     t0 = time.perf_counter()
     first = None
