@@ -41,7 +41,6 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kRow1Threads = 128;  // node rows per block, 1-dof row phase
-constexpr int kRow3Threads = 64;   // node rows per block, 3-dof row phase
 constexpr int kMaxRowSmem = 96 * 1024;  // staging capacity limit per block
 
 // 1/x from the MUFU approximation (rcp.approx.ftz.f64) refined by a cubic
@@ -514,49 +513,49 @@ __global__ void __launch_bounds__(kRow1Threads)
     values[base + k] = accumulate ? values[base + k] + stage[k] : stage[k];
 }
 
-// 3-dof momentum: one thread per node row builds the node's three CSR rows
-// (block column k at positions 3k..3k+2) from the float-pair coefficients.
-__global__ void __launch_bounds__(kRow3Threads)
-    row3_k(int64_t R, const int32_t* __restrict__ inc_ptr,
-           const uint32_t* __restrict__ inc, const int32_t* __restrict__ diag_pos,
-           const int64_t* __restrict__ row_ptr, const double* __restrict__ buf,
-           int64_t E, dd irelax, double* __restrict__ values,
-           double* __restrict__ rhs, int accumulate, int smem_bytes) {
+// 3-dof momentum, one thread per CSR row (three per node row, dof q =
+// thread % 3): each thread accumulates its row of every 3x3 block from the
+// float-pair coefficients and widens it to FP64; a block of kRow3Nodes node
+// rows stages their CSR range in shared memory and writes it coalesced.
+// (One thread per node row, with the symmetric blocks widened once, needs
+// a third fewer FP64 adds but ran at a third of the occupancy: the shared
+// staging per node is the same, so measured 0.357 against 0.328 ms.)
+constexpr int kRow3Nodes = 64;
+__global__ void __launch_bounds__(3 * kRow3Nodes)
+    row3t_k(int64_t R, const int32_t* __restrict__ inc_ptr,
+            const uint32_t* __restrict__ inc, const int32_t* __restrict__ diag_pos,
+            const int64_t* __restrict__ row_ptr, const double* __restrict__ buf,
+            int64_t E, dd irelax, double* __restrict__ values,
+            double* __restrict__ rhs, int accumulate, int smem_bytes) {
   const dd* cb = reinterpret_cast<const dd*>(buf);
   extern __shared__ double stage[];
-  const int64_t r0 = int64_t(blockIdx.x) * kRow3Threads;
-  const int64_t r1 = (r0 + kRow3Threads < R) ? r0 + kRow3Threads : R;
+  const int64_t r0 = int64_t(blockIdx.x) * kRow3Nodes;
+  const int64_t r1 = (r0 + kRow3Nodes < R) ? r0 + kRow3Nodes : R;
   const int64_t base = row_ptr[3 * r0];
   const int64_t cnt = row_ptr[3 * r1] - base;
   const bool staged = cnt * int64_t(sizeof(double)) <= smem_bytes;
-  const int64_t r = r0 + threadIdx.x;
+  const int local = threadIdx.x / 3, q = threadIdx.x - 3 * (threadIdx.x / 3);
+  const int64_t r = r0 + local;
+  // N slots of row q of the symmetric 3x3 N (N00 N01 N02 N11 N12 N22 at 4..9)
+  const int n0 = q == 0 ? 4 : (q == 1 ? 5 : 6);
+  const int n1 = q == 0 ? 5 : (q == 1 ? 7 : 8);
+  const int n2 = q == 0 ? 6 : (q == 1 ? 8 : 9);
   if (r < r1) {
     const int32_t s = inc_ptr[r], t = inc_ptr[r + 1];
-    const int64_t b0 = row_ptr[3 * r], b1 = row_ptr[3 * r + 1],
-                  b2 = row_ptr[3 * r + 2];
-    double* v0 = staged ? stage + (b0 - base) : values + b0;
-    double* v1 = staged ? stage + (b1 - base) : values + b1;
-    double* v2 = staged ? stage + (b2 - base) : values + b2;
+    const int64_t bq = row_ptr[3 * r + q];
+    double* v = staged ? stage + (bq - base) : values + bq;
     const bool acc = accumulate && !staged;
     if (s != t) {
       const int dp = diag_pos[r];
-      dd dgc{}, dN[6] = {}, rr[3] = {};
-      dd ob[9];
+      dd dgc{}, dN[3] = {}, rr{}, ob[3];
       int slot = -1;
-      // every 3x3 block is symmetric (c I + N, N symmetric): six widenings
-      auto put_block = [&](int k, const dd* bl) {
-        const double d00 = dd_to_double(bl[0]), d01 = dd_to_double(bl[1]),
-                     d02 = dd_to_double(bl[2]), d11 = dd_to_double(bl[4]),
-                     d12 = dd_to_double(bl[5]), d22 = dd_to_double(bl[8]);
-        const double o0[3] = {d00, d01, d02}, o1[3] = {d01, d11, d12}, o2[3] = {d02, d12, d22};
+      auto put3 = [&](int k, const dd* x) {
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          v0[k + q] = acc ? v0[k + q] + o0[q] : o0[q];
-          v1[k + q] = acc ? v1[k + q] + o1[q] : o1[q];
-          v2[k + q] = acc ? v2[k + q] + o2[q] : o2[q];
+        for (int c = 0; c < 3; ++c) {
+          const double d = dd_to_double(x[c]);
+          v[k + c] = acc ? v[k + c] + d : d;
         }
       };
-      auto flush = [&](int sl) { put_block(3 * (sl < dp ? sl : sl + 1), ob); };
       for (int32_t qi = s; qi < t; ++qi) {
         const uint32_t w = inc[qi];
         const bool dup = (w >> 31) != 0;
@@ -564,50 +563,39 @@ __global__ void __launch_bounds__(kRow3Threads)
         const int side = w & 1u;
         const dd co = cb[(side ? 2 : 1) * E + e];
         const dd cd = cb[(side ? 3 : 0) * E + e];
-        dd n[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) n[k] = cb[(4 + k) * E + e];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const dd f = cb[(10 + k) * E + e];
-          rr[k] = side ? rr[k] + f : rr[k] - f;
-        }
-        const dd blk[9] = {co + n[0], n[1], n[2], n[1], co + n[3], n[4], n[2], n[4], co + n[5]};
+        const dd na = cb[n0 * E + e], nb = cb[n1 * E + e], nc = cb[n2 * E + e];
+        const dd f = cb[(10 + q) * E + e];
+        rr = side ? rr + f : rr - f;
+        const dd blk[3] = {q == 0 ? na + co : na, q == 1 ? nb + co : nb, q == 2 ? nc + co : nc};
         if (!dup) {
-          if (slot >= 0) flush(slot);
+          if (slot >= 0) put3(3 * (slot < dp ? slot : slot + 1), ob);
           ++slot;
 #pragma unroll
-          for (int k = 0; k < 9; ++k) ob[k] = blk[k];
+          for (int c = 0; c < 3; ++c) ob[c] = blk[c];
         } else {
 #pragma unroll
-          for (int k = 0; k < 9; ++k) ob[k] = ob[k] + blk[k];
+          for (int c = 0; c < 3; ++c) ob[c] = ob[c] + blk[c];
         }
         dgc = dgc + cd;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) dN[k] = dN[k] + n[k];
+        dN[0] = dN[0] + na;
+        dN[1] = dN[1] + nb;
+        dN[2] = dN[2] + nc;
       }
-      flush(slot);
-      // diagonal block: sum(c) I - sum(N) / relax; cLL and cRR already
-      // carry the 1/relax factor, N is scaled here
-#pragma unroll
-      for (int q = 0; q < 6; ++q) dN[q] = dN[q] * irelax;
-      const dd db[9] = {dgc - dN[0], -dN[1], -dN[2], -dN[1], dgc - dN[3],
-                        -dN[4], -dN[2], -dN[4], dgc - dN[5]};
-      put_block(3 * dp, db);
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        const double d = dd_to_double(rr[q]);
-        rhs[3 * r + q] = accumulate ? rhs[3 * r + q] + d : d;
-      }
+      put3(3 * (slot < dp ? slot : slot + 1), ob);
+      // diagonal block row q: sum(c) e_q - sum(N)_q / relax
+      const dd m0 = -(dN[0] * irelax), m1 = -(dN[1] * irelax), m2 = -(dN[2] * irelax);
+      const dd db[3] = {q == 0 ? m0 + dgc : m0, q == 1 ? m1 + dgc : m1, q == 2 ? m2 + dgc : m2};
+      put3(3 * dp, db);
+      const double d = dd_to_double(rr);
+      rhs[3 * r + q] = accumulate ? rhs[3 * r + q] + d : d;
     } else if (!acc) {
-      for (int64_t k = 0; k < row_ptr[3 * r + 3] - b0; ++k) v0[k] = 0.0;
-      if (!accumulate)
-        for (int q = 0; q < 3; ++q) rhs[3 * r + q] = 0.0;
+      for (int64_t k = 0; k < row_ptr[3 * r + q + 1] - bq; ++k) v[k] = 0.0;
+      if (!accumulate) rhs[3 * r + q] = 0.0;
     }
   }
   if (!staged) return;
   __syncthreads();
-  for (int64_t k = threadIdx.x; k < cnt; k += kRow3Threads)
+  for (int64_t k = threadIdx.x; k < cnt; k += 3 * kRow3Nodes)
     values[base + k] = accumulate ? values[base + k] + stage[k] : stage[k];
 }
 
@@ -673,7 +661,7 @@ void set_smem_attrs() {
   if (g_smem_set_device == dev) return;
   NW_CUDA(cudaFuncSetAttribute(row1_k<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
   NW_CUDA(cudaFuncSetAttribute(row1_k<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
-  NW_CUDA(cudaFuncSetAttribute(row3_k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
+  NW_CUDA(cudaFuncSetAttribute(row3t_k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
   g_smem_set_device = dev;
 }
 
@@ -752,7 +740,7 @@ void launch_momentum_edges(cudaStream_t s, int64_t E, const int2* edges,
 #undef NW_MOM
 }
 
-int row_block_nodes(int kind) { return kind == 2 ? kRow3Threads : kRow1Threads; }
+int row_block_nodes(int kind) { return kind == 2 ? kRow3Nodes : kRow1Threads; }
 
 int row_stage_bytes(int kind, const int64_t* row_ptr_host, int64_t R) {
   const int nb = row_block_nodes(kind);
@@ -781,7 +769,7 @@ void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
     row1_k<1><<<grid_for(R, kRow1Threads), kRow1Threads, smem_bytes, s>>>(
         R, inc_ptr, inc, diag_pos, row_ptr, buf, E, values, rhs, accumulate, smem_bytes);
   else
-    row3_k<<<grid_for(R, kRow3Threads), kRow3Threads, smem_bytes, s>>>(
+    row3t_k<<<grid_for(R, kRow3Nodes), 3 * kRow3Nodes, smem_bytes, s>>>(
         R, inc_ptr, inc, diag_pos, row_ptr, buf, E, dd_param(1.0 / relax), values, rhs,
         accumulate, smem_bytes);
 }
