@@ -380,7 +380,9 @@ nw_status nw_compute_peclet_factor(nw_linsys* ls, const double* coords,
 
 /* ---- node kernels: lumped-mass BDF time terms, added into the system
  * (like sumInto) after the edge assembly. States Nm1, N, Np1; device
- * pointers of the caller's nodes. ---- */
+ * pointers of the caller's nodes. The edge graph has no entry at all in
+ * the row of a node that is in no edge; the scalar and momentum kernels
+ * then return NW_INVALID_ARG (their diagonal term has nowhere to go). ---- */
 typedef struct nw_mass_bdf_fields {
   const double* density_nm1;     /* N */
   const double* density_n;       /* N */

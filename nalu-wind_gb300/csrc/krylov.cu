@@ -787,7 +787,7 @@ void KrylovSolver::sgs_residual32(const float* x, const float* y, float* r, cuda
 void KrylovSolver::setup_colors(const std::vector<int32_t>& rows,
                                 const std::vector<int64_t>& cptr, cudaStream_t s) {
   const int64_t n = A_.n;
-  if (!A_.row_ptr_host || !A_.col_idx_host) fail(NW_INTERNAL, "host graph needed");
+  if (!A_.row_ptr_host || (!A_.col_idx_host && A_.nnz > 0)) fail(NW_INTERNAL, "host graph needed");
   if (int64_t(rows.size()) != n || cptr.empty() || cptr.back() != n)
     fail(NW_INTERNAL, "colour classes do not cover the rows");
   const int nc = int(cptr.size()) - 1;

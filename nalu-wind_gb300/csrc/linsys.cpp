@@ -737,6 +737,12 @@ static nw_status mass_bdf(nw_linsys* ls, int kind, const nw_mass_bdf_fields* f,
     if (kind != 1 && (!f->q_nm1 || !f->q_n || !f->q_np1)) fail(NW_INVALID_ARG, "null transported field");
     if (kind == 2 && !f->dpdx) fail(NW_INVALID_ARG, "null dpdx");
     if (!(o->dt != 0.0)) fail(NW_INVALID_ARG, "dt is zero");
+    if (kind != 1)
+      for (int32_t dp : ls->g.diag_pos)
+        if (dp < 0)
+          fail(NW_INVALID_ARG,
+               "a node in no edge has no diagonal entry in the edge graph; its mass term "
+               "cannot be added");
     materialize_zero(ls);
     launch_mass_bdf(ls->stream, kind, plan_view(ls), *f, *o, ls->values.p, ls->rhs.p);
   });

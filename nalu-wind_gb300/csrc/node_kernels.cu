@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
   for (int d = 0; d < ND; ++d) {
     const int64_t row = ND * r + d;
-    if (KIND != 1) values[row_ptr[row] + int64_t(ND) * dp + d] += lhs;
+    if (KIND != 1 && dp >= 0) values[row_ptr[row] + int64_t(ND) * dp + d] += lhs;
     rhs[row] += b[d];
   }
 }

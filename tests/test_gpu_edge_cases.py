@@ -1,0 +1,118 @@
+"""Edge cases through the C ABI: no edges (empty rows, zero rhs, trivial
+solve), nodes in no edge, a system too small for aggregation to coarsen,
+and the smallest 3-dof system (one edge)."""
+import numpy as np
+import pytest
+
+from gpu_util import check_close, dev, oracle_continuity, oracle_momentum
+
+pytestmark = pytest.mark.gpu
+
+
+def _continuity_fields(nw, coords, area, N, rng):
+    d = dict(coords=coords, velocity=rng.normal(size=(N, 3)), dpdx=rng.normal(size=(N, 3)),
+             density=np.ones(N), pressure=rng.normal(size=N), udiag=np.ones(N), area=area)
+    t = {k: dev(np.ascontiguousarray(v)) for k, v in d.items()}
+    f = nw.ContinuityFields(*(t[k].data_ptr() for k in ("coords", "velocity", "dpdx", "density", "pressure",
+                                                        "udiag", "area")))
+    return f, t
+
+
+def test_no_edges_gives_zero_rows_and_a_trivial_solve(nw, orc):
+    import torch
+    N = 17
+    rng = np.random.default_rng(0)
+    edges = np.zeros((0, 2), np.int64)
+    ls = nw.LinearSystem(1)
+    ls.build_edge_graph(N, edges)
+    ls.finalize()
+    rp, ci = ls.graph()
+    orp, oci, _ = orc.build_graph(np.arange(1, N + 1), edges, 1)
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    # as in the reference's edge graph, a node in no edge has an empty row
+    assert len(ci) == 0 and np.all(rp == 0)
+    f, keep = _continuity_fields(nw, rng.normal(size=(N, 3)), np.zeros((1, 3)), N, rng)
+    ls.from_host(rhs=np.full(N, 3.0))
+    ls.zero_system()
+    ls.assemble_continuity(f, nw.ContinuityOpts(1.0, 1.0, 1.0, 0.0))
+    vals, rhs = ls.to_host()
+    assert len(vals) == 0 and np.all(rhs == 0.0)
+    # a node kernel needs the diagonal entry, which these rows do not have
+    z = dev(np.zeros(N))
+    with pytest.raises(nw.NwError, match="no diagonal"):
+        ls.assemble_mass_bdf("scalar", [z, z, z], [z, z, z], q=[z, z, z])
+    x = torch.zeros(N, dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    assert rep.converged == 1 and rep.iterations == 0 and rep.rhs_norm == 0.0
+    assert torch.count_nonzero(x).item() == 0
+
+
+def test_isolated_nodes_match_oracle(nw, orc):
+    mesh = nw.Mesh(4, 3, 3, jitter=0.05, seed=2)
+    N0 = mesh.num_nodes
+    extra = 5  # nodes in no edge, appended after the mesh nodes
+    N = N0 + extra
+    rng = np.random.default_rng(1)
+    coords = np.vstack([mesh.coords, rng.normal(size=(extra, 3))])
+    f, keep = _continuity_fields(nw, coords, mesh.area, N, rng)
+    ls = nw.LinearSystem(1)
+    ls.build_edge_graph(N, mesh.edges)
+    ls.finalize()
+    ls.zero_system()
+    co = nw.ContinuityOpts(1.0, 1.0, 1.0, 0.0)
+    ls.assemble_continuity(f, co)
+    vals, rhs = ls.to_host()
+    rp, ci = ls.graph()
+    h = {k: v.cpu().numpy() for k, v in keep.items()}
+    o = oracle_continuity(orc, mesh.edges, np.arange(1, N + 1), h,
+                          {k: getattr(co, k) for k, _ in co._fields_})
+    assert np.array_equal(rp, o["rp"]) and np.array_equal(ci, o["ci"])
+    check_close(vals, o["vals"], o["vabs"], "values")
+    check_close(rhs, o["rhs"], o["rabs"], "rhs")
+    # the isolated nodes' rows are empty and their rhs zero
+    lid = ls.node_lid(N)
+    for node in range(N0, N):
+        r = lid[node]
+        assert rp[r + 1] == rp[r] and rhs[r] == 0.0
+
+
+def test_learned_preconditioner_on_a_tiny_graph(nw):
+    import torch
+    ls = nw.workload.poisson_system((3, 3, 2), seed=3)
+    net = nw.Learned(seed=0)
+    ls.attach_learned(net)
+    cg = ls.coarse_graph()
+    assert cg["nc"] >= 1
+    ls.set_solver_cfg(nw.solver_cfg(method=nw.FGMRES, preconditioner=nw.PC_LEARNED, precision=nw.PREC_MIXED,
+                                    kspace=30, inner_kspace=30, max_iterations=500, tolerance=1e-8))
+    x = torch.zeros(ls.sizes()[0], dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    assert rep.converged == 1 and rep.final_abs_residual <= 1.01e-8 * rep.rhs_norm
+
+
+def test_single_edge_momentum(nw, orc):
+    """Two nodes, one edge: the smallest 3-dof system (6 x 6, fully dense)."""
+    N = 2
+    edges = np.array([[0, 1]], np.int64)
+    coords = np.array([[0.0, 0.0, 0.0], [0.3, 0.1, -0.05]])
+    area = np.array([[0.2, 0.05, 0.01]])
+    rng = np.random.default_rng(4)
+    host = dict(coords=coords, velocity=rng.normal(size=(N, 3)), dudx=rng.normal(size=(N, 9)),
+                viscosity=np.array([1e-3, 2e-3]), density=np.ones(N), mask=np.ones(N), area=area,
+                mdot=np.array([0.7]), pecfac=np.array([0.3]))
+    t = {k: dev(np.ascontiguousarray(v)) for k, v in host.items()}
+    fm = nw.MomentumFields(*(t[k].data_ptr() for k in ("coords", "velocity", "dudx", "viscosity", "density",
+                                                        "mask", "area", "mdot", "pecfac")))
+    ls = nw.LinearSystem(3)
+    ls.build_edge_graph(N, edges)
+    ls.finalize()
+    ls.zero_system()
+    mo = nw.MomentumOpts(alpha=0.3, alpha_upw=0.8, upw_factor=1.0, relax=0.7, include_div_u=1.0, use_limiter=1)
+    ls.assemble_momentum(fm, mo)
+    vals, rhs = ls.to_host()
+    rp, ci = ls.graph()
+    assert vals.shape[0] == 36
+    o = oracle_momentum(orc, edges, np.arange(1, N + 1), host, {k: getattr(mo, k) for k, _ in mo._fields_})
+    assert np.array_equal(rp, o["rp"]) and np.array_equal(ci, o["ci"])
+    check_close(vals, o["vals"], o["vabs"], "values")
+    check_close(rhs, o["rhs"], o["rabs"], "rhs")
