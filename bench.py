@@ -359,7 +359,9 @@ def poisson_solves(nw, stream, args) -> dict:
     ls = nw.workload.poisson_system(args.poisson_shape, seed=3, stretch=1.04, stream=stream.cuda_stream)
     nr, nnz = ls.sizes()
     res = {"workload": f"pressure Poisson {'x'.join(map(str, args.poisson_shape))} box, stretch 1.04",
-           "rows": nr, "nnz": nnz, "tol": 1e-8}
+           "rows": nr, "nnz": nnz, "tol": 1e-8,
+           "mixed_precision": "FP64 outer residual / refinement; FP32 inner Krylov, SpMV and network "
+                              "coarse step; BF16 Gauss-Seidel matrix values with FP32 accumulation"}
     net, info = nw.training.train_poisson_network(stream=stream.cuda_stream)
     res["training"] = info
     res["_net"] = net
@@ -372,18 +374,19 @@ def poisson_solves(nw, stream, args) -> dict:
         ("plain_fp64_gmres50_jacobi", None,
          nw.solver_cfg(kspace=50, max_iterations=maxit, tolerance=1e-8)),
         ("mixed_gmres50_sgs", None,
-         nw.solver_cfg(kspace=50, max_iterations=maxit, tolerance=1e-8, precision=nw.PREC_MIXED,
+         nw.solver_cfg(kspace=50, max_iterations=maxit, tolerance=1e-8, precision=nw.PREC_MIXED_BF16,
                        inner_kspace=50, inner_tolerance=1e-4, preconditioner=nw.PC_SGS)),
         ("mixed_fgmres30_two_level_no_network", without,
          nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=maxit, tolerance=1e-8,
-                       precision=nw.PREC_MIXED, inner_kspace=30, preconditioner=nw.PC_LEARNED)),
+                       precision=nw.PREC_MIXED_BF16, inner_kspace=30, preconditioner=nw.PC_LEARNED)),
         ("learned_mixed_fgmres30", net,
          nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=maxit, tolerance=1e-8,
-                       precision=nw.PREC_MIXED, inner_kspace=30, preconditioner=nw.PC_LEARNED)),
+                       precision=nw.PREC_MIXED_BF16, inner_kspace=30, preconditioner=nw.PC_LEARNED)),
     ]
     variants.append(("mixed_gmres50_sgs_to_1e-10", None,
-                     nw.solver_cfg(kspace=50, max_iterations=maxit, tolerance=1e-10, precision=nw.PREC_MIXED,
-                                   inner_kspace=50, inner_tolerance=1e-4, preconditioner=nw.PC_SGS)))
+                     nw.solver_cfg(kspace=50, max_iterations=maxit, tolerance=1e-10,
+                                   precision=nw.PREC_MIXED_BF16, inner_kspace=50, inner_tolerance=1e-4,
+                                   preconditioner=nw.PC_SGS)))
     if args.poisson_variants:
         keep = set(args.poisson_variants.split(","))
         variants = [v for v in variants if v[0] in keep]
@@ -445,7 +448,7 @@ def heldout_poisson(nw, stream, args, net) -> dict:
                                                             tolerance=1e-8)),
                 ("learned_mixed_fgmres30", nw.solver_cfg(method=nw.FGMRES, kspace=30, inner_kspace=30,
                                                          max_iterations=args.poisson_maxit, tolerance=1e-8,
-                                                         precision=nw.PREC_MIXED,
+                                                         precision=nw.PREC_MIXED_BF16,
                                                          preconditioner=nw.PC_LEARNED))):
             ls.set_solver_cfg(cfg)
             x = torch.zeros(nr, dtype=torch.float64, device="cuda")
@@ -536,7 +539,7 @@ def implicit_step(nw, stream, args) -> dict:
                  nw.solver_cfg(kspace=50, max_iterations=args.poisson_maxit, tolerance=1e-8)),
                 ("learned_mixed_fgmres30", net,
                  nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=args.poisson_maxit, tolerance=1e-8,
-                               precision=nw.PREC_MIXED, inner_kspace=30, preconditioner=nw.PC_LEARNED))):
+                               precision=nw.PREC_MIXED_BF16, inner_kspace=30, preconditioner=nw.PC_LEARNED))):
             if learned is not None:
                 lsc.attach_learned(learned)
             lsc.set_solver_cfg(cfg)

@@ -52,8 +52,10 @@ enum {
 };
 /* Arithmetic of the solve. */
 enum {
-  NW_PREC_FP64 = 0,  /* FP64 Krylov, FP64 SpMV and preconditioner */
-  NW_PREC_MIXED = 1  /* FP32 inner Krylov inside FP64 iterative refinement */
+  NW_PREC_FP64 = 0,       /* FP64 Krylov, FP64 SpMV and preconditioner */
+  NW_PREC_MIXED = 1,      /* FP32 inner Krylov inside FP64 iterative refinement */
+  NW_PREC_MIXED_BF16 = 2  /* as NW_PREC_MIXED, with the Gauss-Seidel sweeps
+                             reading BF16 matrix values (FP32 accumulation) */
 };
 
 /* TpetraLinearSolverConfig::load keys (src/LinearSolverConfig.C:37-140). */

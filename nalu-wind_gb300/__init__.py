@@ -24,7 +24,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "CUDA_ERROR", 3: "NOT_FINALIZED", 
                 5: "NOT_CONVERGED", 6: "BREAKDOWN", 7: "TIMEOUT", 8: "NO_DEVICE", 9: "INTERNAL"}
 GMRES, CG, FGMRES = 0, 1, 2
 PC_NONE, PC_JACOBI, PC_SGS, PC_LEARNED = 0, 1, 2, 3
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_BF16 = 0, 1, 2
 
 
 class NwError(RuntimeError):

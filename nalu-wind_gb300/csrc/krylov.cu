@@ -23,6 +23,7 @@
 // compensated two-float sum (Dekker/Knuth error-free transformations) on
 // the FP32 pipes, then combine threads in FP64: FP64-accurate dots without
 // spending GB300's scarce FP64 throughput.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -485,6 +486,11 @@ __global__ void __launch_bounds__(kBlock)
   r[i] = s;
 }
 
+__global__ void to_bf16_vals_k(int64_t n, const float* __restrict__ a, __nv_bfloat16* __restrict__ b) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = __float2bfloat16_rn(a[i]);
+}
+
 __global__ void zero_rows_k(int64_t cnt, const int32_t* __restrict__ rows, float* __restrict__ r) {
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k < cnt) r[rows[k]] = 0.f;
@@ -630,6 +636,7 @@ void KrylovSolver::refresh(cudaStream_t s) {
   if (cl_) cl_->refresh(A_.values, s);
   NW_CUDA(cudaGetLastError());
   f32_valid_ = false;
+  gs_vals16_.release();
 }
 
 void KrylovSolver::ensure_f32(cudaStream_t s) {
@@ -837,7 +844,11 @@ void KrylovSolver::setup_colors(const std::vector<int32_t>& rows,
 void KrylovSolver::learned_presmooth32(const float* x, float* y, cudaStream_t s) {
   if (!has_learned()) fail(NW_INVALID_ARG, "no learned preconditioner attached");
   ensure_f32(s);
-  sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s, false, net_->smoother == 1 ? 1 : 0);
+  const int sweep = net_->smoother == 1 ? 1 : 0;
+  if (gs_bf16_)
+    sgs<__nv_bfloat16, float>(gs_vals16_.p, rdiag32_.p, x, y, s, false, sweep);
+  else
+    sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s, false, sweep);
 }
 
 // FP32 preconditioner of the mixed method. Learned (two-level, symmetric
@@ -849,7 +860,10 @@ void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
                              cudaStream_t s) {
   const int64_t n = A_.n;
   if (pc.kind == NW_PC_SGS) {
-    sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s);
+    if (gs_bf16_)
+      sgs<__nv_bfloat16, float>(gs_vals16_.p, rdiag32_.p, x, y, s);
+    else
+      sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s);
     return;
   }
   if (pc.kind != NW_PC_LEARNED) {
@@ -871,8 +885,12 @@ void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
   net_->coarse_correction(*cl_, rc32_.p, ec32_.p, s);
   launch_prolong_add(*cl_, ec32_.p, net_->alpha_dev(), y, s);
   // post-smoothing z2 + S(x - A z2) is one sweep starting from z2
-  if (net_->post_smooth)
-    sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s, true, half ? 2 : 0);
+  if (net_->post_smooth) {
+    if (gs_bf16_)
+      sgs<__nv_bfloat16, float>(gs_vals16_.p, rdiag32_.p, x, y, s, true, half ? 2 : 0);
+    else
+      sgs<float, float>(gs_vals32_.p, rdiag32_.p, x, y, s, true, half ? 2 : 0);
+  }
   NW_CUDA(cudaGetLastError());
 }
 
@@ -905,7 +923,7 @@ SolveResult KrylovSolver::solve(const nw_solver_cfg& cfg, double tol,
                                 const Precond& pc, const double* b, double* x,
                                 cudaStream_t s) {
   SolveResult r;
-  if (cfg.precision == NW_PREC_MIXED)
+  if (cfg.precision == NW_PREC_MIXED || cfg.precision == NW_PREC_MIXED_BF16)
     r = mixed(cfg, tol, pc, b, x, s);
   else if (cfg.method == NW_CG && pc.kind != NW_PC_LEARNED)
     r = cg(cfg, tol, pc, b, x, s);
@@ -918,7 +936,8 @@ SolveResult KrylovSolver::solve(const nw_solver_cfg& cfg, double tol,
     Precond sgs = pc;
     sgs.kind = NW_PC_SGS;
     const SolveResult first = r;
-    r = cfg.precision == NW_PREC_MIXED ? mixed(cfg, tol, sgs, b, x, s)
+    r = (cfg.precision == NW_PREC_MIXED || cfg.precision == NW_PREC_MIXED_BF16)
+            ? mixed(cfg, tol, sgs, b, x, s)
                                        : gmres(cfg, tol, sgs, b, x, false, s);
     r.fallback = 1;
     r.iterations += first.iterations;
@@ -1138,6 +1157,13 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
                                 cudaStream_t s) {
   const int64_t n = A_.n;
   ensure_f32(s);
+  gs_bf16_ = cfg.precision == NW_PREC_MIXED_BF16;
+  if (gs_bf16_ && gs_vals16_.n != gs_vals32_.n) {
+    gs_vals16_.resize(gs_vals32_.n);
+    if (gs_vals32_.n)
+      to_bf16_vals_k<<<grid1(int64_t(gs_vals32_.n)), kBlock, 0, s>>>(int64_t(gs_vals32_.n), gs_vals32_.p,
+                                                                    gs_vals16_.p);
+  }
   const int m = std::min(m_, std::max(1, cfg.inner_kspace > 0 ? cfg.inner_kspace : cfg.kspace));
   const double itol = cfg.inner_tolerance > 0 ? cfg.inner_tolerance : 1e-4;
   SolveResult res;

@@ -2,6 +2,7 @@
 // multicolour Gauss-Seidel relaxation, GMRES / FGMRES / CG, and the
 // mixed-precision iterative-refinement driver (krylov.cu).
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -129,6 +130,8 @@ class KrylovSolver {
   DeviceArray<int64_t> gs_off_;
   DeviceArray<double> gs_vals_;
   DeviceArray<float> gs_vals32_;
+  DeviceArray<__nv_bfloat16> gs_vals16_;  // BF16 copy (NW_PREC_MIXED_BF16)
+  bool gs_bf16_ = false;
   template <typename VT, typename T>
   void sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s,
            bool from_guess = false, int sweep = 0) const;

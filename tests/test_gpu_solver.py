@@ -48,7 +48,7 @@ def _poisson_system(nw, shape=(24, 24, 16)):
     return ls, case
 
 
-@pytest.mark.parametrize("pc", [1, 2])
+@pytest.mark.parametrize("pc,prec", [(1, 1), (2, 1), (2, 2)])
 def test_gmres_matches_oracle_history(nw, orc, pc):
     import torch
     ls, case, d = _scalar_system(nw)
@@ -90,12 +90,13 @@ def test_cg_and_gmres_on_poisson(nw, orc):
         np.testing.assert_allclose(ls.residual_history()[:k], ho[:k], rtol=1e-9, atol=0)
 
 
-@pytest.mark.parametrize("pc", [1, 2])
-def test_mixed_precision_reaches_fp64_tolerance(nw, orc, pc):
+@pytest.mark.parametrize("pc,prec", [(1, 1), (2, 1), (2, 2)])
+def test_mixed_precision_reaches_fp64_tolerance(nw, orc, pc, prec):
+    """prec 1: FP32 inner solve; 2: the same with BF16 Gauss-Seidel values."""
     import torch
     ls, case = _poisson_system(nw)
     nr, _ = ls.sizes()
-    ls.set_solver_cfg(nw.solver_cfg(method=nw.GMRES, preconditioner=pc, precision=nw.PREC_MIXED, kspace=30,
+    ls.set_solver_cfg(nw.solver_cfg(method=nw.GMRES, preconditioner=pc, precision=prec, kspace=30,
                                     max_iterations=5000, tolerance=1e-10, inner_kspace=30,
                                     inner_tolerance=1e-4))
     x = torch.zeros(nr, dtype=torch.float64, device="cuda")
