@@ -61,6 +61,17 @@ nw_status nw_mesh_get(const nw_mesh* m, double* coords, int64_t* global_id,
                       int64_t* nalu_id, int64_t* edges, int64_t* conn,
                       double* area, double* dualvol, double* bnd_area);
 
+/* Exposed-face integration points on the box sides selected by side_mask
+ * (bit s: s = 0..5 for x-, x+, y-, y+, z-, z+; the sidesets surface_1 ..
+ * surface_6 of a "generated:...|sideset:xXyYzZ" mesh; periodic sides have
+ * none). One IP per face node, in side order, then element order, then
+ * face-node order; faces are oriented outward. Outputs (any may be NULL):
+ * ip_nodes count x 2 (face node, opposing element node), area count x 3
+ * (exposed area vector of the IP's sub-face), side count. Call with NULL
+ * outputs to get count. */
+nw_status nw_mesh_face_ips(const nw_mesh* m, int side_mask, int64_t* count,
+                           int64_t* ip_nodes, double* area, int32_t* side);
+
 #ifdef __cplusplus
 }
 #endif

@@ -177,6 +177,7 @@ SIGNATURES = {
     "nw_mesh_destroy": (C.c_int, [C.c_void_p]),
     "nw_mesh_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P, _I64P, C.POINTER(C.c_int)]),
     "nw_mesh_get": (C.c_int, [C.c_void_p, _DP, _I64P, _I64P, _I64P, _I64P, _DP, _DP, _DP]),
+    "nw_mesh_face_ips": (C.c_int, [C.c_void_p, C.c_int, _I64P, _I64P, _DP, C.POINTER(C.c_int32)]),
 }
 
 _lib = None
@@ -529,10 +530,25 @@ class Mesh:
                                   _ptr(self.nalu_id, C.c_int64), _ptr(self.edges, C.c_int64),
                                   _ptr(self.conn, C.c_int64), _ptr(self.area, C.c_double),
                                   _ptr(self.dualvol, C.c_double), _ptr(self.bnd_area, C.c_double)))
+            cnt = C.c_int64()
+            check(lib.nw_mesh_face_ips(h, 63, C.byref(cnt), None, None, None))
+            self._fip_nodes = np.zeros((cnt.value, 2), np.int64)
+            self._fip_area = np.zeros((cnt.value, 3))
+            self._fip_side = np.zeros(cnt.value, np.int32)
+            check(lib.nw_mesh_face_ips(h, 63, C.byref(cnt), _ptr(self._fip_nodes, C.c_int64),
+                                       _ptr(self._fip_area, C.c_double), _ptr(self._fip_side, C.c_int32)))
         finally:
             lib.nw_mesh_destroy(h)
         self.shape = (nx, ny, nz)
         self.periodic = (bool(periodic_x), bool(periodic_y))
+
+    SIDES = {"x-": 0, "x+": 1, "y-": 2, "y+": 3, "z-": 4, "z+": 5}
+
+    def face_ips(self, sides=("x-", "x+", "y-", "y+", "z-", "z+")):
+        """Exposed-face integration points of the given box sides:
+        (ip_nodes (n, 2) = face node, opposing element node; area (n, 3))."""
+        want = np.isin(self._fip_side, [self.SIDES[s] for s in sides])
+        return self._fip_nodes[want].copy(), self._fip_area[want].copy()
 
 
 from . import workload  # noqa: E402  (seeded synthetic inputs)

@@ -22,6 +22,10 @@ struct nw_mesh {
   int64_t N = 0, E = 0, M = 0;
   std::vector<double> coords, area, dualvol, bnd;
   std::vector<int64_t> gid, nid, edges, conn;
+  // exposed-face integration points on the non-periodic box sides
+  std::vector<int32_t> fip_side;   // 0..5 = x-, x+, y-, y+, z-, z+
+  std::vector<int64_t> fip_nodes;  // (face node, opposing node) per IP
+  std::vector<double> fip_area;    // exposed area vector per IP
 };
 
 namespace {
@@ -229,6 +233,75 @@ std::vector<int64_t> rcm_order(int64_t N, const std::vector<int64_t>& ap,
   return order;  // order[k] = old node placed at new position k
 }
 
+// Exposed faces of the block, as face integration points. A face of nn
+// nodes (quad or triangle, ordered counter-clockwise seen from outside) has
+// one IP per node; its area vector is that of the sub-face bounded by the
+// node, the midpoints of its two face edges and the face centroid
+// (Quad3DSCS::determinant_scs, src/master_element/Quad43DCVFEM.C:84-124;
+// Tri3DSCS::determinant_scs, src/master_element/Tri33DCVFEM.C:56-129; the
+// vector area of a quadrilateral does not depend on its triangulation). The
+// opposing node of a face node is the element node joined to it by the one
+// element edge that leaves the face (HexSCS::opposingNodes, src/
+// master_element/Hex8CVFEM.C:727; TetSCS: the node off the face).
+struct FaceIps {
+  std::vector<int32_t> side;
+  std::vector<int64_t> nodes;
+  std::vector<double> area;
+  void add(int sd, int nn, const int64_t* fn, const int64_t* opp,
+           const std::vector<double>& coords) {
+    double p[4][3], c[3] = {0, 0, 0};
+    for (int k = 0; k < nn; ++k)
+      for (int d = 0; d < 3; ++d) {
+        p[k][d] = coords[3 * fn[k] + d];
+        c[d] += p[k][d] / nn;
+      }
+    for (int k = 0; k < nn; ++k) {
+      const int kn = (k + 1) % nn, kp = (k + nn - 1) % nn;
+      double q[4][3];
+      for (int d = 0; d < 3; ++d) {
+        q[0][d] = p[k][d];
+        q[1][d] = 0.5 * (p[k][d] + p[kn][d]);
+        q[2][d] = c[d];
+        q[3][d] = 0.5 * (p[kp][d] + p[k][d]);
+      }
+      double a[3];
+      quad_area(q, a);
+      side.push_back(sd);
+      nodes.push_back(fn[k]);
+      nodes.push_back(opp[k]);
+      for (int d = 0; d < 3; ++d) area.push_back(a[d]);
+    }
+  }
+};
+
+// Orders a face's nodes so that its normal points away from `inner` (a
+// point inside the element).
+void orient_outward(int nn, int64_t* fn, int64_t* opp, const double* inner,
+                    const std::vector<double>& coords) {
+  double c[3] = {0, 0, 0}, nrm[3] = {0, 0, 0};
+  for (int k = 0; k < nn; ++k)
+    for (int d = 0; d < 3; ++d) c[d] += coords[3 * fn[k] + d] / nn;
+  for (int k = 0; k < nn; ++k) {
+    const double* a = &coords[3 * fn[k]];
+    const double* b = &coords[3 * fn[(k + 1) % nn]];
+    nrm[0] += (a[1] - c[1]) * (b[2] - c[2]) - (a[2] - c[2]) * (b[1] - c[1]);
+    nrm[1] += (a[2] - c[2]) * (b[0] - c[0]) - (a[0] - c[0]) * (b[2] - c[2]);
+    nrm[2] += (a[0] - c[0]) * (b[1] - c[1]) - (a[1] - c[1]) * (b[0] - c[0]);
+  }
+  double dot = 0;
+  for (int d = 0; d < 3; ++d) dot += nrm[d] * (c[d] - inner[d]);
+  if (dot < 0) {
+    std::reverse(fn + 1, fn + nn);
+    std::reverse(opp + 1, opp + nn);
+  }
+}
+
+// Hex sides in element-local ordinals (the Exodus side numbering of
+// HexSCS::sideNodeOrdinals_, include/master_element/Hex8CVFEM.h:395-401),
+// indexed by box side x-, x+, y-, y+, z-, z+.
+const int kHexBoxSide[6][4] = {{0, 4, 7, 3}, {1, 2, 6, 5}, {0, 1, 5, 4},
+                               {2, 3, 7, 6}, {0, 3, 2, 1}, {4, 5, 6, 7}};
+
 void build(nw_mesh& m, int nx, int ny, int nz, const nw_box_opts& o) {
   if (nx < 1 || ny < 1 || nz < 1) fail(NW_INVALID_ARG, "box dimensions < 1");
   if (!(o.lx > 0 && o.ly > 0 && o.lz > 0)) fail(NW_INVALID_ARG, "box lengths <= 0");
@@ -300,6 +373,69 @@ void build(nw_mesh& m, int nx, int ny, int nz, const nw_box_opts& o) {
           }
         }
   }
+  // exposed faces (lattice numbering; mapped through any renumbering below)
+  FaceIps fips;
+  {
+    auto lat = [&](int64_t n, int d) {
+      return d == 0 ? n % NX : (d == 1 ? (n / NX) % NY : n / (NX * NY));
+    };
+    const int64_t hi_l[3] = {nx, ny, nz};
+    for (int sd = 0; sd < 6; ++sd) {
+      const int dir = sd / 2, up = sd % 2;
+      if ((dir == 0 && o.periodic_x) || (dir == 1 && o.periodic_y)) continue;
+      const int64_t plane = up ? hi_l[dir] : 0;
+      const int64_t layer = up ? hi_l[dir] - 1 : 0;
+      const int64_t n1 = dir == 0 ? ny : nx, n2 = dir == 2 ? ny : nz;
+      for (int64_t b = 0; b < n2; ++b)
+        for (int64_t a = 0; a < n1; ++a) {
+          int64_t ijk[3];
+          ijk[dir] = layer;
+          ijk[dir == 0 ? 1 : 0] = a;
+          ijk[dir == 2 ? 1 : 2] = b;
+          const int64_t h = ijk[0] + int64_t(nx) * (ijk[1] + int64_t(ny) * ijk[2]);
+          if (!o.tets) {
+            const int64_t* ce = &conn[8 * h];
+            double inner[3] = {0, 0, 0};
+            for (int q = 0; q < 8; ++q)
+              for (int d = 0; d < 3; ++d) inner[d] += coords[3 * ce[q] + d] / 8;
+            int64_t fn[4], opp[4];
+            for (int k = 0; k < 4; ++k) {
+              const int ln = kHexBoxSide[sd][k];
+              fn[k] = ce[ln];
+              for (int q = 0; q < 12; ++q) {
+                const int other = kHexEdge[q][0] == ln ? kHexEdge[q][1]
+                                  : kHexEdge[q][1] == ln ? kHexEdge[q][0] : -1;
+                if (other < 0) continue;
+                bool on_face = false;
+                for (int t = 0; t < 4; ++t) on_face |= kHexBoxSide[sd][t] == other;
+                if (!on_face) opp[k] = ce[other];
+              }
+            }
+            orient_outward(4, fn, opp, inner, coords);
+            fips.add(sd, 4, fn, opp, coords);
+          } else {
+            for (int t = 0; t < 6; ++t) {
+              const int64_t* ce = &conn[4 * (6 * h + t)];
+              for (int off = 0; off < 4; ++off) {
+                int64_t fn[3], opp[3];
+                int k = 0;
+                bool on = true;
+                for (int q = 0; q < 4; ++q)
+                  if (q != off) {
+                    fn[k] = ce[q];
+                    opp[k++] = ce[off];
+                    on = on && lat(ce[q], dir) == plane;
+                  }
+                if (!on) continue;
+                const double* inner = &coords[3 * ce[off]];
+                orient_outward(3, fn, opp, inner, coords);
+                fips.add(sd, 3, fn, opp, coords);
+              }
+            }
+          }
+        }
+    }
+  }
   // renumbering (relabels ids and reorders node storage by new id)
   if (o.renumber) {
     std::vector<int64_t> perm(N);  // perm[new] = old
@@ -312,6 +448,7 @@ void build(nw_mesh& m, int nx, int ny, int nz, const nw_box_opts& o) {
     std::vector<int64_t> inv(N);
     for (int64_t k = 0; k < N; ++k) inv[perm[k]] = k;
     for (auto& c : conn) c = inv[c];
+    for (auto& c : fips.nodes) c = inv[c];
     {
       std::vector<double> nc(3 * N);
       for (int64_t k = 0; k < N; ++k)
@@ -345,6 +482,7 @@ void build(nw_mesh& m, int nx, int ny, int nz, const nw_box_opts& o) {
       std::vector<int64_t> inv2(N);
       for (int64_t k = 0; k < N; ++k) inv2[ord[k]] = k;
       for (auto& c : conn) c = inv2[c];
+      for (auto& c : fips.nodes) c = inv2[c];
       std::vector<double> nc(3 * N);
       for (int64_t k = 0; k < N; ++k)
         for (int d = 0; d < 3; ++d) nc[3 * k + d] = coords[3 * ord[k] + d];
@@ -483,6 +621,9 @@ void build(nw_mesh& m, int nx, int ny, int nz, const nw_box_opts& o) {
   m.area.swap(area);
   m.dualvol.swap(dualvol);
   m.bnd.swap(bnd);
+  m.fip_side.swap(fips.side);
+  m.fip_nodes.swap(fips.nodes);
+  m.fip_area.swap(fips.area);
   m.conn.swap(conn);
   m.edges.swap(edges);
   m.gid.resize(N);
@@ -559,3 +700,25 @@ nw_status nw_mesh_get(const nw_mesh* m, double* coords, int64_t* global_id,
 }
 
 }  // extern "C"
+
+extern "C" nw_status nw_mesh_face_ips(const nw_mesh* m, int side_mask,
+                                      int64_t* count, int64_t* ip_nodes,
+                                      double* area, int32_t* side) {
+  return guard([&] {
+    if (!m || !count) fail(NW_INVALID_ARG, "null argument");
+    int64_t n = 0;
+    const int64_t total = int64_t(m->fip_side.size());
+    for (int64_t i = 0; i < total; ++i) {
+      if (!((side_mask >> m->fip_side[i]) & 1)) continue;
+      if (ip_nodes) {
+        ip_nodes[2 * n] = m->fip_nodes[2 * i];
+        ip_nodes[2 * n + 1] = m->fip_nodes[2 * i + 1];
+      }
+      if (area)
+        for (int d = 0; d < 3; ++d) area[3 * n + d] = m->fip_area[3 * i + d];
+      if (side) side[n] = m->fip_side[i];
+      ++n;
+    }
+    *count = n;
+  });
+}

@@ -16,6 +16,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <random>
 #include <stdexcept>
 #include <unordered_map>
 #include <vector>
@@ -1281,6 +1282,324 @@ void or_nodal_grad_edge(int64_t nedges, const int64_t* edges, int dim1,
         counter++;
       }
     }
+  }
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Boundary face-IP kernels. Each face integration point contributes to the
+// rows of its face node R, with columns R and L (L the element node opposite
+// R across the element edge that leaves the face). The local systems use the
+// edge layout with node order (R, L): lhs 2x2 (1 dof) or 6x6 (3 dofs), rhs
+// 2 or 6, and the L rows left zero, so or_sum_into_edges assembles them.
+namespace {
+
+inline double tsqrt(double x) { return std::sqrt(x); }
+inline Mag tsqrt(Mag x) { return {std::sqrt(x.v), std::sqrt(x.m)}; }
+
+// ContinuityOpenEdgeKernel::execute (src/edge_kernels/
+// ContinuityOpenEdgeKernel.C:92-160), one face IP.
+template <typename T>
+void continuity_open_ip(int64_t ip, const int64_t* ipn, const double* coords,
+                        const double* velocity, const double* Gpdx,
+                        const double* density, const double* pressure,
+                        const double* pbcF, const double* udiag,
+                        const double* areav, const double* dynp,
+                        const or_continuity_open_opts* o, T* A, T* b) {
+  const int64_t R = ipn[2 * ip], L = ipn[2 * ip + 1];
+  const double tauScale = o->tau_scale, pstabFac = o->pstab_fac,
+               nocFac = o->noc_fac, mdotCorr = o->mdot_corr,
+               solveInc = o->solve_incompressible;
+  T av[3];
+  for (int d = 0; d < 3; ++d) av[d] = T(areav[3 * ip + d]);
+  const T projTimeScale = T(1.0) / T(udiag[R]);
+  const T pressureIp = 0.5 * (T(pressure[R]) + T(pressure[L]));
+  T asq = T(0.0), axdx = T(0.0);
+  for (int d = 0; d < 3; ++d) {
+    const T coordIp = 0.5 * (T(coords[3 * R + d]) + T(coords[3 * L + d]));
+    const T dxj = T(coords[3 * R + d]) - coordIp;
+    asq += av[d] * av[d];
+    axdx += av[d] * dxj;
+  }
+  const T inv_axdx = T(1.0) / axdx;
+  const T pbc = T(pbcF[R]) - T(dynp ? dynp[ip] : 0.0);
+  T tmdot = -projTimeScale * (pbc - pressureIp) * asq * inv_axdx * T(pstabFac) -
+            T(mdotCorr);
+  for (int d = 0; d < 3; ++d) {
+    const T coordIp = 0.5 * (T(coords[3 * R + d]) + T(coords[3 * L + d]));
+    const T dxj = T(coords[3 * R + d]) - coordIp;
+    const T kxj = av[d] - asq * inv_axdx * dxj;
+    const T Gjp = T(Gpdx[3 * R + d]);
+    tmdot += ((T(solveInc) + T(density[R]) * T(1.0 - solveInc)) *
+                  T(velocity[3 * R + d]) +
+              projTimeScale * Gjp * T(pstabFac)) *
+                 av[d] -
+             projTimeScale * kxj * Gjp * T(nocFac) * T(pstabFac);
+  }
+  const T lhsfac = 0.5 * asq * inv_axdx * T(pstabFac) * projTimeScale / T(tauScale);
+  for (int k = 0; k < 4; ++k) A[k] = T(0.0);
+  b[0] = -tmdot / T(tauScale);
+  b[1] = T(0.0);
+  A[0] = lhsfac;  // (R, R)
+  A[1] = lhsfac;  // (R, L)
+}
+
+// duidxj with the over-relaxed non-orthogonal correction and the viscous
+// face flux shared by the open and symmetry momentum kernels
+// (MomentumOpenEdgeKernel.C:137-177, MomentumSymmetryEdgeKernel.C:112-152).
+template <typename T>
+void face_visc_flux(int64_t ip, int64_t R, int64_t L, const double* coords,
+                    const double* vel, const double* dudx, const T av[3],
+                    T inv_axdx, T visc, const T nx[3], double includeDivU,
+                    T fx[3], T& fxnx) {
+  T duidxj[3][3];
+  for (int i = 0; i < 3; ++i) {
+    const T dui = T(vel[3 * R + i]) - T(vel[3 * L + i]);
+    T gjuidx = T(0.0);
+    for (int j = 0; j < 3; ++j) {
+      const T dxj = T(coords[3 * R + j]) - T(coords[3 * L + j]);
+      gjuidx += T(dudx[9 * R + 3 * i + j]) * dxj;
+    }
+    for (int j = 0; j < 3; ++j)
+      duidxj[i][j] = T(dudx[9 * R + 3 * i + j]) + (dui - gjuidx) * av[j] * inv_axdx;
+  }
+  (void)ip;
+  T divU = T(0.0);
+  for (int d = 0; d < 3; ++d) divU += duidxj[d][d];
+  fxnx = T(0.0);
+  for (int i = 0; i < 3; ++i) {
+    fx[i] = 2.0 / 3.0 * visc * divU * av[i] * T(includeDivU);
+    for (int j = 0; j < 3; ++j) fx[i] += -visc * (duidxj[i][j] + duidxj[j][i]) * av[j];
+    fxnx += nx[i] * fx[i];
+  }
+}
+
+// MomentumOpenEdgeKernel::execute (src/edge_kernels/
+// MomentumOpenEdgeKernel.C:80-270), one face IP; entrainment 0 = COMPUTED,
+// 1 = SPECIFIED.
+template <typename T>
+void momentum_open_ip(int64_t ip, const int64_t* ipn, const double* coords,
+                      const double* vel, const double* dudx,
+                      const double* viscosity, const double* ubc,
+                      const double* areav, const double* mdot,
+                      const or_momentum_open_opts* o, T* A, T* b) {
+  const int64_t R = ipn[2 * ip], L = ipn[2 * ip + 1];
+  const double nfEntrain = o->nf_entrain, om_nfEntrain = 1.0 - nfEntrain;
+  auto lhs = [&](int r, int c) -> T& { return A[6 * r + c]; };
+  for (int k = 0; k < 36; ++k) A[k] = T(0.0);
+  for (int k = 0; k < 6; ++k) b[k] = T(0.0);
+  T av[3], nx[3], fx[3];
+  for (int d = 0; d < 3; ++d) av[d] = T(areav[3 * ip + d]);
+  const T visc = T(viscosity[R]);
+  T axdx = T(0.0), asq = T(0.0);
+  for (int d = 0; d < 3; ++d) {
+    const T dxj = T(coords[3 * R + d]) - T(coords[3 * L + d]);
+    asq += av[d] * av[d];
+    axdx += av[d] * dxj;
+  }
+  const T inv_axdx = T(1.0) / axdx;
+  const T amag = tsqrt(asq);
+  T uxnx = T(0.0), uxnxip = T(0.0), uspecxnx = T(0.0);
+  for (int d = 0; d < 3; ++d) {
+    nx[d] = av[d] / amag;
+    uxnx += nx[d] * T(vel[3 * R + d]);
+    uxnxip += 0.5 * nx[d] * (T(vel[3 * L + d]) + T(vel[3 * R + d]));
+    uspecxnx += nx[d] * T(ubc[3 * R + d]);
+  }
+  T fxnx;
+  face_visc_flux(ip, R, L, coords, vel, dudx, av, inv_axdx, visc, nx, o->include_div_u, fx, fxnx);
+  // local dofs: R = 0..2, L = 3..5
+  for (int i = 0; i < 3; ++i) {
+    const int rowR = i, rowL = 3 + i;
+    const T axi = av[i];
+    b[rowR] -= (fx[i] - nx[i] * fxnx);
+    const T om_nxinxi = T(1.0) - nx[i] * nx[i];
+    T lhsFac = -visc * asq * inv_axdx * om_nxinxi;
+    lhs(rowR, rowL) -= lhsFac;
+    lhs(rowR, rowR) += lhsFac;
+    for (int j = 0; j < 3; ++j) {
+      const int colL = 3 + j, colR = j;
+      const T axj = av[j];
+      lhsFac = -visc * axi * axj * inv_axdx * om_nxinxi;
+      lhs(rowR, colL) -= lhsFac;
+      lhs(rowR, colR) += lhsFac;
+      if (i == j) continue;
+      const T nxinxj = nx[i] * nx[j];
+      lhsFac = visc * asq * inv_axdx * nxinxj;
+      lhs(rowR, colL) -= lhsFac;
+      lhs(rowR, colR) += lhsFac;
+      lhsFac = visc * axj * axj * inv_axdx * nxinxj;
+      lhs(rowR, colL) -= lhsFac;
+      lhs(rowR, colR) += lhsFac;
+      lhsFac = visc * axj * axi * inv_axdx * nxinxj;
+      lhs(rowR, rowL) -= lhsFac;
+      lhs(rowR, rowR) += lhsFac;
+    }
+  }
+  const T tmdot = T(mdot[ip]);
+  if (o->entrainment == 1) {  // SPECIFIED
+    for (int i = 0; i < 3; ++i) {
+      const int rowR = i;
+      const T sigma = visc * asq * inv_axdx;
+      const T lambda = 0.5 * (tmdot - tsqrt(tmdot * tmdot + 8.0 * sigma * sigma));
+      const T uR = T(vel[3 * R + i]);
+      if (tmdot > 0.0) {
+        b[rowR] -= tmdot * uR;
+        lhs(rowR, rowR) += tmdot;
+      } else {
+        b[rowR] -= tmdot * uR - lambda * (uR - T(ubc[3 * R + i]));
+        lhs(rowR, rowR) += tmdot - lambda;
+      }
+    }
+  } else {  // COMPUTED
+    for (int i = 0; i < 3; ++i) {
+      const int rowR = i;
+      if (tmdot > 0.0) {
+        b[rowR] -= tmdot * T(vel[3 * R + i]);
+        lhs(rowR, rowR) += tmdot;
+      } else {
+        b[rowR] -= tmdot * ((T(nfEntrain) * uxnx + T(om_nfEntrain) * uxnxip) * nx[i] +
+                            (T(ubc[3 * R + i]) - uspecxnx * nx[i]));
+        for (int j = 0; j < 3; ++j) {
+          lhs(rowR, 3 + j) += tmdot * T(om_nfEntrain) * 0.5 * nx[i] * nx[j];
+          lhs(rowR, j) += tmdot * T(nfEntrain + om_nfEntrain * 0.5) * nx[i] * nx[j];
+        }
+      }
+    }
+  }
+}
+
+// MomentumSymmetryEdgeKernel::execute (src/edge_kernels/
+// MomentumSymmetryEdgeKernel.C:64-206), one face IP.
+template <typename T>
+void momentum_symmetry_ip(int64_t ip, const int64_t* ipn, const double* coords,
+                          const double* vel, const double* dudx,
+                          const double* viscosity, const double* areav,
+                          const or_momentum_symmetry_opts* o, T* A, T* b) {
+  const int64_t R = ipn[2 * ip], L = ipn[2 * ip + 1];
+  auto lhs = [&](int r, int c) -> T& { return A[6 * r + c]; };
+  for (int k = 0; k < 36; ++k) A[k] = T(0.0);
+  for (int k = 0; k < 6; ++k) b[k] = T(0.0);
+  T av[3], nx[3], fx[3];
+  for (int d = 0; d < 3; ++d) av[d] = T(areav[3 * ip + d]);
+  const T visc = T(viscosity[R]);
+  T axdx = T(0.0), asq = T(0.0);
+  for (int d = 0; d < 3; ++d) {
+    const T dxj = T(coords[3 * R + d]) - T(coords[3 * L + d]);
+    asq += av[d] * av[d];
+    axdx += av[d] * dxj;
+  }
+  const T inv_axdx = T(1.0) / axdx;
+  const T amag = tsqrt(asq);
+  for (int d = 0; d < 3; ++d) nx[d] = av[d] / amag;
+  T fxnx;
+  face_visc_flux(ip, R, L, coords, vel, dudx, av, inv_axdx, visc, nx, o->include_div_u, fx, fxnx);
+  const T diffusionMassRate = -visc * asq * inv_axdx;
+  const T penaltyFac = T(o->penalty_factor) * diffusionMassRate;
+  T uN = T(0.0);
+  for (int i = 0; i < 3; ++i) uN += T(vel[3 * R + i]) * nx[i];
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) lhs(i, j) -= penaltyFac * nx[i] * nx[j];
+    b[i] += penaltyFac * uN * nx[i];
+  }
+  for (int i = 0; i < 3; ++i) {
+    const int rowL = 3 + i, rowR = i;
+    b[rowR] -= fxnx * nx[i];
+    T lhsfac = diffusionMassRate * nx[i] * nx[i];
+    lhs(rowR, rowL) -= lhsfac;
+    lhs(rowR, rowR) += lhsfac;
+    const T axi = av[i];
+    const T nxnx = nx[i] * nx[i];
+    for (int j = 0; j < 3; ++j) {
+      const int colL = 3 + j, colR = j;
+      const T axj = av[j];
+      lhsfac = -visc * axi * axj * inv_axdx * nxnx;
+      lhs(rowR, colL) -= lhsfac;
+      lhs(rowR, colR) += lhsfac;
+      if (i == j) continue;
+      lhsfac = -visc * asq * inv_axdx * nx[i] * nx[j];
+      lhs(rowR, colL) -= lhsfac;
+      lhs(rowR, colR) += lhsfac;
+      // these two terms carry no 1/axdx in the reference
+      lhsfac = -visc * axj * axj * nx[i] * nx[j];
+      lhs(rowR, colL) -= lhsfac;
+      lhs(rowR, colR) += lhsfac;
+      lhsfac = -visc * axj * axi * nx[i] * nx[j];
+      lhs(rowR, rowL) -= lhsfac;
+      lhs(rowR, rowR) += lhsfac;
+    }
+  }
+}
+
+// ScalarOpenEdgeKernel::execute (src/edge_kernels/ScalarOpenEdgeKernel.C:
+// 49-72) and ScalarEdgeOpenSolverAlg::execute (src/edge_kernels/
+// ScalarEdgeOpenSolverAlg.C:64-104): the same upwind outflow / entrainment
+// flux, one face IP.
+template <typename T>
+void scalar_open_ip(int64_t ip, const int64_t* ipn, const double* q,
+                    const double* qbc, const double* mdot, double relax, T* A,
+                    T* b) {
+  const int64_t R = ipn[2 * ip];
+  for (int k = 0; k < 4; ++k) A[k] = T(0.0);
+  b[0] = b[1] = T(0.0);
+  const T md = T(mdot[ip]);
+  const T uUpw = md > 0.0 ? T(q[R]) : T(qbc[R]);
+  b[0] -= md * uUpw;
+  if (md > 0.0) A[0] += md / T(relax);
+}
+
+}  // namespace
+
+extern "C" {
+
+#define NW_OR_BOTH(name, nl, call)                                          \
+  void name(OR_ARGS) { run_local<double>(nip, nl, lhs, rhs, 0, [&](int64_t ip, double* A, double* b) { call; }); } \
+  void name##_mag(OR_ARGS) { run_local<Mag>(nip, nl, lhs, rhs, 1, [&](int64_t ip, Mag* A, Mag* b) { call; }); }
+
+#define OR_ARGS                                                                          \
+  int64_t nip, const int64_t *ipn, const double *coords, const double *velocity,          \
+      const double *Gpdx, const double *density, const double *pressure,                \
+      const double *pbc, const double *udiag, const double *areav, const double *dynp,  \
+      const or_continuity_open_opts *o, double *lhs, double *rhs
+NW_OR_BOTH(or_continuity_open_local, 2,
+           continuity_open_ip(ip, ipn, coords, velocity, Gpdx, density, pressure, pbc, udiag,
+                              areav, dynp, o, A, b))
+#undef OR_ARGS
+
+#define OR_ARGS                                                                          \
+  int64_t nip, const int64_t *ipn, const double *coords, const double *vel,               \
+      const double *dudx, const double *viscosity, const double *ubc,                    \
+      const double *areav, const double *mdot, const or_momentum_open_opts *o,           \
+      double *lhs, double *rhs
+NW_OR_BOTH(or_momentum_open_local, 6,
+           momentum_open_ip(ip, ipn, coords, vel, dudx, viscosity, ubc, areav, mdot, o, A, b))
+#undef OR_ARGS
+
+#define OR_ARGS                                                                          \
+  int64_t nip, const int64_t *ipn, const double *coords, const double *vel,               \
+      const double *dudx, const double *viscosity, const double *areav,                  \
+      const or_momentum_symmetry_opts *o, double *lhs, double *rhs
+NW_OR_BOTH(or_momentum_symmetry_local, 6,
+           momentum_symmetry_ip(ip, ipn, coords, vel, dudx, viscosity, areav, o, A, b))
+#undef OR_ARGS
+
+#define OR_ARGS                                                                          \
+  int64_t nip, const int64_t *ipn, const double *q, const double *qbc,                    \
+      const double *mdot, double relax, double *lhs, double *rhs
+NW_OR_BOTH(or_scalar_open_local, 2, scalar_open_ip(ip, ipn, q, qbc, mdot, relax, A, b))
+#undef OR_ARGS
+#undef NW_OR_BOTH
+
+// The uniform(lo, hi) draws of one default-seeded std::mt19937 with
+// std::uniform_real_distribution<double>, in order (the random inputs of
+// unit_tests/edge_kernels/UnitTestScalarOpenEdge.C:216-222).
+void or_mt19937_uniform(int n, const double* lo, const double* hi, double* out) {
+  std::mt19937 rng;
+  rng.seed(std::mt19937::default_seed);
+  for (int i = 0; i < n; ++i) {
+    std::uniform_real_distribution<double> u(lo[i], hi[i]);
+    out[i] = u(rng);
   }
 }
 

@@ -82,6 +82,47 @@ typedef struct or_continuity_opts {
   double noc_fac, tau_scale, interp_together, solve_incompressible;
 } or_continuity_opts;
 
+/* ---- boundary face-IP kernels ----
+ * ipn: nip x 2 (face node R, opposing element node L). Local systems in the
+ * edge layout with node order (R, L), L rows zero: lhs nip x 4 / rhs nip x 2
+ * (1 dof) or lhs nip x 36 / rhs nip x 6 (3 dofs). areav: exposed area
+ * vector per face IP (nip x 3); dynp, mdot: per face IP. The *_mag variants
+ * return running magnitudes instead of values. */
+typedef struct or_continuity_open_opts {
+  double tau_scale, noc_fac, pstab_fac, mdot_corr, solve_incompressible;
+} or_continuity_open_opts;
+typedef struct or_momentum_open_opts {
+  double include_div_u, nf_entrain;
+  int entrainment; /* 0 = COMPUTED, 1 = SPECIFIED */
+} or_momentum_open_opts;
+typedef struct or_momentum_symmetry_opts {
+  double include_div_u, penalty_factor;
+} or_momentum_symmetry_opts;
+/* ContinuityOpenEdgeKernel.C:92-160 (dynp may be NULL: zero) */
+void or_continuity_open_local(int64_t nip, const int64_t* ipn, const double* coords,
+                              const double* velocity, const double* dpdx,
+                              const double* density, const double* pressure,
+                              const double* pressure_bc, const double* udiag,
+                              const double* areav, const double* dynp,
+                              const or_continuity_open_opts* o, double* lhs, double* rhs);
+/* MomentumOpenEdgeKernel.C:80-270 */
+void or_momentum_open_local(int64_t nip, const int64_t* ipn, const double* coords,
+                            const double* velocity, const double* dudx,
+                            const double* viscosity, const double* velocity_bc,
+                            const double* areav, const double* mdot,
+                            const or_momentum_open_opts* o, double* lhs, double* rhs);
+/* MomentumSymmetryEdgeKernel.C:64-206 */
+void or_momentum_symmetry_local(int64_t nip, const int64_t* ipn, const double* coords,
+                                const double* velocity, const double* dudx,
+                                const double* viscosity, const double* areav,
+                                const or_momentum_symmetry_opts* o, double* lhs, double* rhs);
+/* ScalarOpenEdgeKernel.C:49-72 / ScalarEdgeOpenSolverAlg.C:64-104 */
+void or_scalar_open_local(int64_t nip, const int64_t* ipn, const double* q,
+                          const double* q_bc, const double* mdot, double relax,
+                          double* lhs, double* rhs);
+/* default-seeded std::mt19937 uniform(lo[i], hi[i]) draws, in order */
+void or_mt19937_uniform(int n, const double* lo, const double* hi, double* out);
+
 /* Per-edge local systems: lhs (E x 4) row-major 2x2 and rhs (E x 2). */
 void or_scalar_edge_local(int64_t nedges, const int64_t* edges,
                           const double* coords, const double* vrtm,

@@ -36,6 +36,19 @@ class ContinuityOpts(C.Structure):
                 ("interp_together", C.c_double), ("solve_incompressible", C.c_double)]
 
 
+class ContinuityOpenOpts(C.Structure):
+    _fields_ = [("tau_scale", C.c_double), ("noc_fac", C.c_double), ("pstab_fac", C.c_double),
+                ("mdot_corr", C.c_double), ("solve_incompressible", C.c_double)]
+
+
+class MomentumOpenOpts(C.Structure):
+    _fields_ = [("include_div_u", C.c_double), ("nf_entrain", C.c_double), ("entrainment", C.c_int)]
+
+
+class MomentumSymmetryOpts(C.Structure):
+    _fields_ = [("include_div_u", C.c_double), ("penalty_factor", C.c_double)]
+
+
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("final_rel_implicit", C.c_double),
                 ("final_abs_explicit", C.c_double), ("rhs_norm", C.c_double)]
@@ -289,3 +302,49 @@ def mass_bdf(kind, rho, dnv, q=None, dpdx=None, dt=0.1, gamma=(1.0, -1.0, 0.0)):
     lib().or_mass_bdf(C.c_int(kind), C.c_int64(n), *[_p(a, C.c_double) for a in args], C.c_double(dt),
                       *[C.c_double(g) for g in gamma], _p(lhs, C.c_double), _p(rhs, C.c_double))
     return (lhs.reshape(n, 3), rhs.reshape(n, 3)) if nd == 3 else (lhs, rhs)
+
+
+def _face_local(fn, nl, ipn, arrays, tail):
+    ipn = _i64(ipn)
+    n = ipn.shape[0]
+    lhs = np.zeros((n, nl * nl))
+    rhs = np.zeros((n, nl))
+    keep = [None if a is None else _f64(a) for a in arrays]
+    ptrs = [None if a is None else _p(a, C.c_double) for a in keep]
+    fn(C.c_int64(n), _p(ipn, C.c_int64), *ptrs, *tail, _p(lhs, C.c_double), _p(rhs, C.c_double))
+    return lhs, rhs
+
+
+def continuity_open_local(ipn, coords, vel, dpdx, density, pressure, pressure_bc, udiag, areav, dynp,
+                          opts: ContinuityOpenOpts, mag=False):
+    """Face-IP local systems (node order R, L) of ContinuityOpenEdgeKernel."""
+    fn = lib().or_continuity_open_local_mag if mag else lib().or_continuity_open_local
+    return _face_local(fn, 2, ipn, (coords, vel, dpdx, density, pressure, pressure_bc, udiag, areav, dynp),
+                       [C.byref(opts)])
+
+
+def momentum_open_local(ipn, coords, vel, dudx, visc, velocity_bc, areav, mdot, opts: MomentumOpenOpts,
+                        mag=False):
+    fn = lib().or_momentum_open_local_mag if mag else lib().or_momentum_open_local
+    return _face_local(fn, 6, ipn, (coords, vel, dudx, visc, velocity_bc, areav, mdot), [C.byref(opts)])
+
+
+def momentum_symmetry_local(ipn, coords, vel, dudx, visc, areav, opts: MomentumSymmetryOpts, mag=False):
+    fn = lib().or_momentum_symmetry_local_mag if mag else lib().or_momentum_symmetry_local
+    return _face_local(fn, 6, ipn, (coords, vel, dudx, visc, areav), [C.byref(opts)])
+
+
+def scalar_open_local(ipn, q, q_bc, mdot, relax=1.0, mag=False):
+    fn = lib().or_scalar_open_local_mag if mag else lib().or_scalar_open_local
+    return _face_local(fn, 2, ipn, (q, q_bc, mdot), [C.c_double(relax)])
+
+
+def mt19937_uniform(bounds):
+    """Draws of a default-seeded std::mt19937 through
+    std::uniform_real_distribution<double>(lo, hi), one per (lo, hi)."""
+    lo = np.array([b[0] for b in bounds], np.float64)
+    hi = np.array([b[1] for b in bounds], np.float64)
+    out = np.zeros(len(bounds))
+    lib().or_mt19937_uniform(C.c_int(len(bounds)), _p(lo, C.c_double), _p(hi, C.c_double),
+                             _p(out, C.c_double))
+    return out

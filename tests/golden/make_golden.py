@@ -15,6 +15,14 @@ Sources (paths within the nalu-wind tree):
   unit_tests/ngp_algorithms/UnitTestMdotAlg.C           mdot
   unit_tests/node_kernels/UnitTest{Momentum,Continuity,Scalar}MassBDFNodeKernel.C
       lumped-mass BDF node kernels: diagonal LHS and rhs
+  unit_tests/edge_kernels/UnitTestContinuityOpenEdge.C  open boundary (x+ side),
+      dense 8x8 in node-id order
+  unit_tests/edge_kernels/UnitTestMomentumOpenEdge.C    open boundary, COMPUTED
+      entrainment, dense 24x24 in node-id order
+  unit_tests/edge_kernels/UnitTestMomentumSymmetryEdge.C symmetry boundary, plain
+      and penalty factor 2, dense 24x24 in element-node order
+  unit_tests/edge_kernels/UnitTestScalarOpenEdge.C      scalar open flux with
+      relaxation 0.5 and mt19937-drawn inputs (closed-form expectation)
 """
 from __future__ import annotations
 
@@ -94,6 +102,29 @@ def main(ref: Path, out: Path) -> None:
     assert len(lhs) == 64
     g["scalar_mass_bdf_hex8"] = {"dt": 0.1, "gamma": [1.0, -1.0, 0.0],
                                  "lhs_diag": [lhs[9 * i] for i in range(8)], "rhs": _nums(_block(sm, "rhs[8]"))}
+
+    ek = ref / "unit_tests/edge_kernels"
+    co = (ek / "UnitTestContinuityOpenEdge.C").read_text()
+    assert 'get_part("surface_2")' in co and "gamma1_ = 1.0" in co and "timeStepN_ = 1.0" in co
+    g["continuity_open_hex8_xplus"] = {"rhs": _nums(_block(co, "rhs[8]")), "lhs": _nums(_block(co, "lhs[8][8]"))}
+    mo = (ek / "UnitTestMomentumOpenEdge.C").read_text()
+    assert 'get_part("surface_2")' in mo and "EntrainmentMethod::COMPUTED" in mo
+    g["momentum_open_hex8_xplus"] = {"rhs": _nums(_block(mo, "rhs[24]")), "lhs": _nums(_block(mo, "lhs[24][24]"))}
+    sy = (ek / "UnitTestMomentumSymmetryEdge.C").read_text()
+    assert 'get_part("surface_2")' in sy and "symmetryBcPenaltyFactor_ = 2.0" in sy
+    assert "check_against_gold_values" in sy  # element-node ordering
+    pen = sy.index("namespace hex8_golds_penalty")
+    g["momentum_symmetry_hex8_xplus"] = {
+        "element_node_order": True, "penalty_factor": [0.0, 2.0],
+        "rhs": [_nums(_block(sy, "rhs[24]")), _nums(_block(sy[pen:], "rhs[24]"))],
+        "lhs": [_nums(_block(sy, "lhs[24][24]")), _nums(_block(sy[pen:], "lhs[24][24]"))]}
+    so = (ek / "UnitTestScalarOpenEdge.C").read_text()
+    for frag in ("rand_num(1.0, 2.0)", "rand_mdot(-1.0, 1.0)", "const double tkeVal = rand_num(rng);",
+                 "const double bcTkeVal = rand_num(rng);", "const double mdotVal = rand_mdot(rng);",
+                 'relaxFactorMap_["turbulent_ke"] = 0.5', "(-mdotVal * tkeVal) : (-mdotVal * bcTkeVal)",
+                 "(mdotVal * 2.0) : 0.0"):
+        assert frag in so, frag
+    g["scalar_open_quad4"] = {"draws": [[1.0, 2.0], [1.0, 2.0], [-1.0, 1.0]], "relax": 0.5, "nodes": 4}
 
     assert len(g["continuity_hex8"]["lhs"]) == 64 and len(g["momentum_hex8"]["lhs"]) == 576
     assert len(g["momentum_hex8"]["rhs"]) == 24

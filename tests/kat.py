@@ -114,3 +114,54 @@ def dense_accumulate(edges, lhs, rhs, num_dof, n_nodes, same_dof_only=False):
                         for c in range(nd):
                             Ld[ns[a] * nd + d, ns[b] * nd + c] += lhs[e, (a * nd + d) * nl + b * nd + c]
     return Ld, B
+
+
+# The x+ side ("surface_2") of the unit cube: Exodus side 1 of the hex,
+# element nodes (1, 2, 6, 5) = node ids (1, 3, 7, 5) (0-based), opposed
+# across the element by (0, 3, 7, 4) = ids (0, 2, 6, 4). Each face IP's
+# sub-face is a quarter of the unit square, normal +x.
+XPLUS_IPN = np.array([[1, 0], [3, 2], [7, 6], [5, 4]], np.int64)
+XPLUS_AREA = np.tile([0.25, 0.0, 0.0], (4, 1))
+
+
+def quad_scv_weights():
+    """Bilinear shape functions of a quad at its four sub-control-volume
+    centroids (AlgTraitsQuad4 SCV quadrature, unshifted): 9/16 for the IP's
+    own node, 3/16 for its two face neighbours, 1/16 for the opposite node."""
+    w = np.zeros((4, 4))
+    for ip in range(4):
+        w[ip, ip] = 9 / 16
+        w[ip, (ip + 1) % 4] = 3 / 16
+        w[ip, (ip + 3) % 4] = 3 / 16
+        w[ip, (ip + 2) % 4] = 1 / 16
+    return w
+
+
+def open_mdot(ipn, area, vel, rho):
+    """calc_open_mass_flow_rate (unit_tests/kernels/UnitTestKernelUtils.C:
+    856-940) on one quad face: rho u interpolated to each IP, dotted with its
+    exposed area vector."""
+    fn = ipn[:, 0]
+    rhoU = quad_scv_weights() @ (rho[fn, None] * vel[fn])
+    return np.einsum("id,id->i", rhoU, area)
+
+
+def continuity_open_fixture(orc):
+    """ContinuityKernelHex8Mesh (UnitTestKernelUtils.h:442-468) as used by
+    UnitTestContinuityOpenEdge.C:104-147: pressure_bc = dynamic_pressure = 0,
+    tauScale = dt / gamma1 = 1, open mdot correction off (pstabFac = 1)."""
+    m = continuity_fixture(orc)
+    m.update(ipn=XPLUS_IPN, areav=XPLUS_AREA, pressure_bc=np.zeros(8), dynp=np.zeros(4),
+             open_opts=dict(tau_scale=1.0, noc_fac=1.0, pstab_fac=1.0, mdot_corr=0.0,
+                            solve_incompressible=0.0))
+    return m
+
+
+def momentum_face_fixture(orc):
+    """MomentumKernelHex8Mesh (UnitTestKernelUtils.h:484-545) on the x+
+    side: open_velocity_bc left zero, open mass flow from the face
+    interpolation of rho u, includeDivU = nearestFaceEntrain = 0."""
+    m = momentum_fixture(orc)
+    m.update(ipn=XPLUS_IPN, areav=XPLUS_AREA, velocity_bc=np.zeros((8, 3)),
+             open_mdot=open_mdot(XPLUS_IPN, XPLUS_AREA, m["velocity"], m["density"]))
+    return m

@@ -152,3 +152,39 @@ def test_bad_inputs_rejected(nw):
         ls.build_edge_graph(2, np.array([[0, 1]]), nalu_id=np.array([1, 1]))
     with pytest.raises(nw.NwError):
         nw.Mesh(0, 2, 2)
+
+
+def test_face_ips_of_the_unit_cube_match_the_reference_side(nw):
+    import kat
+    ipn, area = nw.Mesh(1, 1, 1).face_ips(("x+",))
+    assert np.array_equal(ipn, kat.XPLUS_IPN)
+    np.testing.assert_allclose(area, kat.XPLUS_AREA, rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("tets,renumber", [(False, 0), (True, 0), (False, 1), (True, 2)])
+def test_face_ips_close_the_surface(nw, tets, renumber):
+    """Sub-face area vectors of each side sum to the side's area vector; the
+    whole surface is closed; each opposing node is a graph neighbour of its
+    face node, off the face's plane."""
+    m = nw.Mesh(5, 4, 3, lx=1.0, ly=2.0, lz=0.5, stretch_z=1.3, jitter=0.2, seed=3, tets=tets,
+                renumber=renumber, renumber_seed=7)
+    ipn, area = m.face_ips()
+    np.testing.assert_allclose(area.sum(0), 0.0, atol=1e-13)
+    want = {"x-": [-1.0, 0, 0], "x+": [1.0, 0, 0], "y-": [0, -0.5, 0], "y+": [0, 0.5, 0],
+            "z-": [0, 0, -2.0], "z+": [0, 0, 2.0]}
+    for side, w in want.items():
+        i, a = m.face_ips((side,))
+        np.testing.assert_allclose(a.sum(0), w, atol=1e-13)
+        # each IP's sub-face points outward
+        assert np.all(a @ np.array(w) > 0)
+    pairs = set(map(tuple, np.sort(m.edges, 1).tolist()))
+    assert all(tuple(sorted(p)) in pairs for p in ipn.tolist())
+    d = m.coords[ipn[:, 0]] - m.coords[ipn[:, 1]]
+    assert np.all(np.einsum("id,id->i", d, area) > 0)
+
+
+def test_periodic_sides_have_no_face_ips(nw):
+    m = nw.Mesh(4, 4, 2, periodic_x=True, periodic_y=True)
+    for side in ("x-", "x+", "y-", "y+"):
+        assert len(m.face_ips((side,))[0]) == 0
+    assert len(m.face_ips(("z-", "z+"))[0]) == 2 * 4 * 16

@@ -194,3 +194,53 @@ def test_mass_bdf_node_kernels(orc, golds):
     lhs, rhs = orc.mass_bdf(0, (z, z, sf["density"]), dnv, q=(z, z, sf["q"]), dt=g["dt"], gamma=g["gamma"])
     np.testing.assert_allclose(lhs, g["lhs_diag"], rtol=0, atol=1e-12)
     np.testing.assert_allclose(rhs, g["rhs"], rtol=0, atol=1e-12)
+
+
+def test_continuity_open_boundary(orc, golds):
+    m = kat.continuity_open_fixture(orc)
+    o = orc.ContinuityOpenOpts(**m["open_opts"])
+    lhs, rhs = orc.continuity_open_local(m["ipn"], m["coords"], m["velocity"], m["dpdx"], m["density"],
+                                         m["pressure"], m["pressure_bc"], m["udiag"], m["areav"], m["dynp"], o)
+    L, B = kat.dense_accumulate(m["ipn"], lhs, rhs, 1, 8)
+    g = golds["continuity_open_hex8_xplus"]
+    np.testing.assert_allclose(L.ravel(), g["lhs"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(B, g["rhs"], rtol=0, atol=1e-12)
+
+
+def test_momentum_open_boundary_computed_entrainment(orc, golds):
+    m = kat.momentum_face_fixture(orc)
+    o = orc.MomentumOpenOpts(include_div_u=0.0, nf_entrain=0.0, entrainment=0)
+    lhs, rhs = orc.momentum_open_local(m["ipn"], m["coords"], m["velocity"], m["dudx"], m["viscosity"],
+                                       m["velocity_bc"], m["areav"], m["open_mdot"], o)
+    L, B = kat.dense_accumulate(m["ipn"], lhs, rhs, 3, 8)
+    g = golds["momentum_open_hex8_xplus"]
+    np.testing.assert_allclose(L.ravel(), g["lhs"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(B, g["rhs"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", [0, 1])
+def test_momentum_symmetry_boundary(orc, golds, case):
+    m = kat.momentum_face_fixture(orc)
+    g = golds["momentum_symmetry_hex8_xplus"]
+    o = orc.MomentumSymmetryOpts(include_div_u=0.0, penalty_factor=g["penalty_factor"][case])
+    lhs, rhs = orc.momentum_symmetry_local(m["ipn"], m["coords"], m["velocity"], m["dudx"], m["viscosity"],
+                                           m["areav"], o)
+    L, B = kat.dense_accumulate(m["ipn"], lhs, rhs, 3, 8)
+    # the gold is ordered by element node (check_against_gold_values)
+    dof = (3 * m["conn"][0][:, None] + np.arange(3)).ravel()
+    np.testing.assert_allclose(L[np.ix_(dof, dof)].ravel(), g["lhs"][case], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(B[dof], g["rhs"][case], rtol=0, atol=1e-12)
+
+
+def test_scalar_open_boundary(orc, golds):
+    g = golds["scalar_open_quad4"]
+    tke, bc, mdot = orc.mt19937_uniform(g["draws"])
+    n = g["nodes"]
+    ipn = np.stack([np.arange(n), np.zeros(n, np.int64)], 1)
+    for md in (mdot, -mdot):  # both branches of the upwind choice
+        lhs, rhs = orc.scalar_open_local(ipn, np.full(n, tke), np.full(n, bc), np.full(n, md), relax=g["relax"])
+        exp_rhs = -md * tke if md > 0 else -md * bc
+        exp_lhs = md * 2.0 if md > 0 else 0.0
+        np.testing.assert_allclose(rhs[:, 0], exp_rhs, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(lhs[:, 0], exp_lhs, rtol=0, atol=1e-12)
+        assert np.all(lhs[:, 1:] == 0) and np.all(rhs[:, 1] == 0)
