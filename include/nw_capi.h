@@ -418,6 +418,105 @@ nw_status nw_assemble_continuity_mass_bdf(nw_linsys* ls, const nw_mass_bdf_field
 nw_status nw_assemble_momentum_mass_bdf(nw_linsys* ls, const nw_mass_bdf_fields* f,
                                         const nw_bdf_opts* o);
 
+/* ---- boundary face kernels (edge-based open / symmetry conditions) ----
+ * The reference assembles these through AssembleFaceElemSolverAlgorithm
+ * (src/AssembleFaceElemSolverAlgorithm.C) with the face-element kernels of
+ * src/edge_kernels/ (ContinuityOpenEdgeKernel, MomentumOpenEdgeKernel,
+ * MomentumSymmetryEdgeKernel, ScalarOpenEdgeKernel), each adding through
+ * sumInto. Here a side set is registered once as its face integration
+ * points: per IP the face node R (ipNodeMap[ip] / side_node_ordinals) and
+ * the element node L opposite it (MasterElement::opposingNodes). Every IP
+ * adds to the rows of R only, at columns R and L. The kernels run one thread
+ * per boundary node row over that row's IPs in IP order (no atomics) and
+ * ADD to the values and rhs already in the handle: call them after the
+ * interior edge assembly. Face-IP fields (exposed_area_vector, open mass
+ * flow rate, dynamic pressure) are indexed by IP in registration order;
+ * node fields by the caller's node index. */
+typedef struct nw_sideset nw_sideset;
+/* ip_nodes: host, num_ips x 2 (face node, opposing node). The handle must be
+ * finalized and outlive the side set. NW_INVALID_ARG when a node index is
+ * out of range or a pair is not joined by a graph edge. */
+nw_status nw_sideset_create(nw_linsys* ls, int64_t num_ips, const int64_t* ip_nodes,
+                            nw_sideset** out);
+nw_status nw_sideset_destroy(nw_sideset* s);
+/* number of IPs and of distinct boundary node rows */
+nw_status nw_sideset_sizes(const nw_sideset* s, int64_t* num_ips, int64_t* num_rows);
+
+typedef struct nw_continuity_open_fields {
+  const double* coords;           /* N x 3 */
+  const double* velocity;         /* N x 3 (velocity_rtm on moving meshes) */
+  const double* dpdx;             /* N x 3 */
+  const double* density;          /* N */
+  const double* pressure;         /* N */
+  const double* pressure_bc;      /* N; the pressure itself with the open mdot correction */
+  const double* udiag;            /* N (momentum_diag) */
+  const double* exposed_area;     /* num_ips x 3 */
+  const double* dynamic_pressure; /* num_ips, or NULL for zero */
+} nw_continuity_open_fields;
+typedef struct nw_continuity_open_opts {
+  double tau_scale;            /* dt / gamma1 */
+  double noc_fac;              /* get_noc_usage("pressure") */
+  double pstab_fac;            /* 1; 0 with activateOpenMdotCorrection_ */
+  double mdot_corr;            /* mdotAlgOpenCorrection_ with the correction, else 0 */
+  double solve_incompressible; /* solveIncompressibleContinuity_ ? 1 : 0 */
+} nw_continuity_open_opts;
+/* ContinuityOpenEdgeKernel::execute (src/edge_kernels/
+ * ContinuityOpenEdgeKernel.C:92-160). num_dof 1. */
+nw_status nw_assemble_continuity_open(nw_linsys* ls, const nw_sideset* s,
+                                      const nw_continuity_open_fields* f,
+                                      const nw_continuity_open_opts* o);
+
+#define NW_ENTRAIN_COMPUTED 0
+#define NW_ENTRAIN_SPECIFIED 1
+typedef struct nw_momentum_open_fields {
+  const double* coords;              /* N x 3 */
+  const double* velocity;            /* N x 3 (state np1) */
+  const double* dudx;                /* N x 9 */
+  const double* viscosity;           /* N */
+  const double* velocity_bc;         /* N x 3 (open_velocity_bc) */
+  const double* exposed_area;        /* num_ips x 3 */
+  const double* open_mass_flow_rate; /* num_ips */
+} nw_momentum_open_fields;
+typedef struct nw_momentum_open_opts {
+  double include_div_u; /* includeDivU_ */
+  double nf_entrain;    /* nearestFaceEntrain_ */
+  int entrainment;      /* NW_ENTRAIN_COMPUTED or NW_ENTRAIN_SPECIFIED */
+} nw_momentum_open_opts;
+/* MomentumOpenEdgeKernel::execute (src/edge_kernels/
+ * MomentumOpenEdgeKernel.C:80-270). num_dof 3. */
+nw_status nw_assemble_momentum_open(nw_linsys* ls, const nw_sideset* s,
+                                    const nw_momentum_open_fields* f,
+                                    const nw_momentum_open_opts* o);
+
+typedef struct nw_momentum_symmetry_fields {
+  const double* coords;       /* N x 3 */
+  const double* velocity;     /* N x 3 (state np1) */
+  const double* dudx;         /* N x 9 */
+  const double* viscosity;    /* N */
+  const double* exposed_area; /* num_ips x 3 */
+} nw_momentum_symmetry_fields;
+typedef struct nw_momentum_symmetry_opts {
+  double include_div_u;  /* includeDivU_ */
+  double penalty_factor; /* symmetryBcPenaltyFactor_ */
+} nw_momentum_symmetry_opts;
+/* MomentumSymmetryEdgeKernel::execute (src/edge_kernels/
+ * MomentumSymmetryEdgeKernel.C:64-206). num_dof 3. */
+nw_status nw_assemble_momentum_symmetry(nw_linsys* ls, const nw_sideset* s,
+                                        const nw_momentum_symmetry_fields* f,
+                                        const nw_momentum_symmetry_opts* o);
+
+typedef struct nw_scalar_open_fields {
+  const double* q;                   /* N (state np1) */
+  const double* q_bc;                /* N (entrained value) */
+  const double* open_mass_flow_rate; /* num_ips */
+} nw_scalar_open_fields;
+/* ScalarOpenEdgeKernel::execute (src/edge_kernels/ScalarOpenEdgeKernel.C:
+ * 49-72) = ScalarEdgeOpenSolverAlg::execute (ScalarEdgeOpenSolverAlg.C:
+ * 64-104): upwind outflow, entrainment at q_bc; relax = the equation's
+ * relaxation factor. num_dof 1. */
+nw_status nw_assemble_scalar_open(nw_linsys* ls, const nw_sideset* s,
+                                  const nw_scalar_open_fields* f, double relax);
+
 /* ---- MatrixMarket export / import ---- */
 /* TpetraLinearSystem::writeToFile (src/TpetraLinearSystem.C:2017-2045):
  * writes <base>-O-<count>.mm.1 (coordinate real general, 1-based global dof

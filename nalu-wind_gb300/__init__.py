@@ -77,6 +77,40 @@ class PecletOpts(C.Structure):
                 ("tanh_width", C.c_double), ("eps", C.c_double)]
 
 
+class ContinuityOpenFields(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("coords", "velocity", "dpdx", "density", "pressure", "pressure_bc",
+                                           "udiag", "exposed_area", "dynamic_pressure")]
+
+
+class ContinuityOpenOpts(C.Structure):
+    _fields_ = [("tau_scale", C.c_double), ("noc_fac", C.c_double), ("pstab_fac", C.c_double),
+                ("mdot_corr", C.c_double), ("solve_incompressible", C.c_double)]
+
+
+class MomentumOpenFields(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("coords", "velocity", "dudx", "viscosity", "velocity_bc",
+                                           "exposed_area", "open_mass_flow_rate")]
+
+
+ENTRAIN_COMPUTED, ENTRAIN_SPECIFIED = 0, 1
+
+
+class MomentumOpenOpts(C.Structure):
+    _fields_ = [("include_div_u", C.c_double), ("nf_entrain", C.c_double), ("entrainment", C.c_int)]
+
+
+class MomentumSymmetryFields(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("coords", "velocity", "dudx", "viscosity", "exposed_area")]
+
+
+class MomentumSymmetryOpts(C.Structure):
+    _fields_ = [("include_div_u", C.c_double), ("penalty_factor", C.c_double)]
+
+
+class ScalarOpenFields(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("q", "q_bc", "open_mass_flow_rate")]
+
+
 _P = C.c_void_p
 
 
@@ -169,6 +203,16 @@ SIGNATURES = {
     "nw_compute_peclet_factor": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.POINTER(PecletOpts), C.c_void_p, C.c_void_p]),
     "nw_assemble_scalar_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
+    "nw_sideset_create": (C.c_int, [C.c_void_p, C.c_int64, _I64P, C.POINTER(C.c_void_p)]),
+    "nw_sideset_destroy": (C.c_int, [C.c_void_p]),
+    "nw_sideset_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P]),
+    "nw_assemble_continuity_open": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ContinuityOpenFields),
+                                              C.POINTER(ContinuityOpenOpts)]),
+    "nw_assemble_momentum_open": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(MomentumOpenFields),
+                                            C.POINTER(MomentumOpenOpts)]),
+    "nw_assemble_momentum_symmetry": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(MomentumSymmetryFields),
+                                                C.POINTER(MomentumSymmetryOpts)]),
+    "nw_assemble_scalar_open": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ScalarOpenFields), C.c_double]),
     "nw_assemble_continuity_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
     "nw_assemble_momentum_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
     "nw_linsys_write_matrix_market": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_void_p]),
@@ -392,6 +436,24 @@ class LinearSystem:
               "momentum": self.lib.nw_assemble_momentum_mass_bdf}[kind]
         check(fn(self.h, C.byref(f), C.byref(o)))
 
+    # -- boundary face kernels (add to the assembled system)
+    def sideset(self, ip_nodes) -> "SideSet":
+        return SideSet(self, ip_nodes)
+
+    def assemble_continuity_open(self, ss: "SideSet", fields: ContinuityOpenFields,
+                                 opts: ContinuityOpenOpts) -> None:
+        check(self.lib.nw_assemble_continuity_open(self.h, ss.h, C.byref(fields), C.byref(opts)))
+
+    def assemble_momentum_open(self, ss: "SideSet", fields: MomentumOpenFields, opts: MomentumOpenOpts) -> None:
+        check(self.lib.nw_assemble_momentum_open(self.h, ss.h, C.byref(fields), C.byref(opts)))
+
+    def assemble_momentum_symmetry(self, ss: "SideSet", fields: MomentumSymmetryFields,
+                                   opts: MomentumSymmetryOpts) -> None:
+        check(self.lib.nw_assemble_momentum_symmetry(self.h, ss.h, C.byref(fields), C.byref(opts)))
+
+    def assemble_scalar_open(self, ss: "SideSet", fields: ScalarOpenFields, relax=1.0) -> None:
+        check(self.lib.nw_assemble_scalar_open(self.h, ss.h, C.byref(fields), relax))
+
     # -- input producers (device tensors in and out)
     def compute_mdot(self, fields: "ContinuityFields", mdot_dev, noc_fac=1.0, interp_together=1.0) -> None:
         check(self.lib.nw_compute_mdot_edges(self.h, C.byref(fields), noc_fac, interp_together, dptr(mdot_dev)))
@@ -502,6 +564,29 @@ class Learned:
 
 def gemm_bf16(kind: int, m: int, a_dev, b_dev, out_dev) -> None:
     check(load().nw_gemm_bf16(kind, m, dptr(a_dev), dptr(b_dev), dptr(out_dev)))
+
+
+class SideSet:
+    """Face integration points of one boundary registered on a finalized
+    LinearSystem: ip_nodes (n, 2) = (face node, opposing element node)."""
+
+    def __init__(self, ls: "LinearSystem", ip_nodes):
+        self.lib = ls.lib
+        self._ls = ls  # the handle must outlive the side set
+        ipn = np.ascontiguousarray(np.asarray(ip_nodes, np.int64).reshape(-1, 2))
+        h = C.c_void_p()
+        check(self.lib.nw_sideset_create(ls.h, ipn.shape[0], _ptr(ipn, C.c_int64), C.byref(h)))
+        self.h = h
+
+    def sizes(self):
+        n, r = C.c_int64(), C.c_int64()
+        check(self.lib.nw_sideset_sizes(self.h, C.byref(n), C.byref(r)))
+        return n.value, r.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.nw_sideset_destroy(self.h)
+            self.h = None
 
 
 class Mesh:

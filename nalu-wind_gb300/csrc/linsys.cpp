@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "assemble.h"
+#include "boundary.h"
 #include "krylov.h"
 #include "learned.h"
 #include "node_kernels.h"
@@ -745,6 +746,180 @@ static nw_status mass_bdf(nw_linsys* ls, int kind, const nw_mass_bdf_fields* f,
                "cannot be added");
     materialize_zero(ls);
     launch_mass_bdf(ls->stream, kind, plan_view(ls), *f, *o, ls->values.p, ls->rhs.p);
+  });
+}
+
+}  // extern "C"
+
+// A side set: face IPs grouped by the node row of their face node.
+struct nw_sideset {
+  const nw_linsys* ls = nullptr;
+  int64_t num_ips = 0;
+  int64_t nb = 0;
+  DeviceArray<int32_t> brow, bptr;
+  DeviceArray<int4> ips;
+};
+
+namespace {
+
+SideView side_view(const nw_linsys* ls, const nw_sideset* s) {
+  need_finalized(ls);
+  if (!s) fail(NW_INVALID_ARG, "null side set");
+  if (s->ls != ls) fail(NW_INVALID_ARG, "side set was registered on another linear system");
+  SideView v;
+  v.nb = s->nb;
+  v.brow = s->brow.p;
+  v.bptr = s->bptr.p;
+  v.ips = s->ips.p;
+  v.row_ptr = ls->row_ptr.p;
+  v.diag_pos = ls->diag_pos.p;
+  return v;
+}
+
+void need_dof(const nw_linsys* ls, int nd, const char* what) {
+  if (ls->num_dof != nd)
+    fail(NW_INVALID_ARG, std::string(what) + (nd == 3 ? " needs num_dof 3" : " needs num_dof 1"));
+}
+
+}  // namespace
+
+extern "C" {
+
+nw_status nw_sideset_create(nw_linsys* ls, int64_t num_ips, const int64_t* ip_nodes,
+                            nw_sideset** out) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!out) fail(NW_INVALID_ARG, "null output");
+    *out = nullptr;
+    if (num_ips < 0 || num_ips >= (int64_t(1) << 31)) fail(NW_INVALID_ARG, "bad IP count");
+    if (num_ips > 0 && !ip_nodes) fail(NW_INVALID_ARG, "null ip_nodes");
+    const HostGraph& g = ls->g;
+    const int nd = ls->num_dof;
+    struct Ip {
+      int32_t row, ip, R, L, kL;
+    };
+    std::vector<Ip> v(static_cast<size_t>(num_ips));
+    for (int64_t i = 0; i < num_ips; ++i) {
+      const int64_t R = ip_nodes[2 * i], L = ip_nodes[2 * i + 1];
+      if (R < 0 || R >= g.num_nodes || L < 0 || L >= g.num_nodes)
+        fail(NW_INVALID_ARG, "face IP node index out of range");
+      const int64_t rowR = g.node_lid[R] / nd, rowL = g.node_lid[L] / nd;
+      const int32_t* b = g.ncol.data() + g.nrow_ptr[rowR];
+      const int32_t* e = g.ncol.data() + g.nrow_ptr[rowR + 1];
+      const int32_t* it = std::lower_bound(b, e, int32_t(rowL));
+      if (it == e || *it != rowL || g.diag_pos[rowR] < 0)
+        fail(NW_INVALID_ARG, "face node " + std::to_string(R) + " and opposing node " +
+                                 std::to_string(L) + " are not joined by a graph edge");
+      v[size_t(i)] = {int32_t(rowR), int32_t(i), int32_t(R), int32_t(L), int32_t(it - b)};
+    }
+    std::stable_sort(v.begin(), v.end(), [](const Ip& a, const Ip& b) { return a.row < b.row; });
+    std::vector<int32_t> brow, bptr{0};
+    std::vector<int4> ips(v.size());
+    for (size_t k = 0; k < v.size(); ++k) {
+      if (k == 0 || v[k].row != v[k - 1].row) {
+        if (k) bptr.push_back(int32_t(k));
+        brow.push_back(v[k].row);
+      }
+      ips[k] = make_int4(v[k].ip, v[k].R, v[k].L, v[k].kL);
+    }
+    if (!v.empty()) bptr.push_back(int32_t(v.size()));
+    auto s = std::make_unique<nw_sideset>();
+    s->ls = ls;
+    s->num_ips = num_ips;
+    s->nb = int64_t(brow.size());
+    NW_CUDA(cudaSetDevice(ls->device));
+    s->brow.upload(brow, ls->stream);
+    s->bptr.upload(bptr, ls->stream);
+    s->ips.upload(ips, ls->stream);
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    *out = s.release();
+  });
+}
+
+nw_status nw_sideset_destroy(nw_sideset* s) {
+  delete s;
+  return NW_OK;
+}
+
+nw_status nw_sideset_sizes(const nw_sideset* s, int64_t* num_ips, int64_t* num_rows) {
+  return guard([&] {
+    if (!s) fail(NW_INVALID_ARG, "null side set");
+    if (num_ips) *num_ips = s->num_ips;
+    if (num_rows) *num_rows = s->nb;
+  });
+}
+
+nw_status nw_assemble_continuity_open(nw_linsys* ls, const nw_sideset* s,
+                                      const nw_continuity_open_fields* f,
+                                      const nw_continuity_open_opts* o) {
+  return guard([&] {
+    const SideView v = side_view(ls, s);
+    need_dof(ls, 1, "continuity open boundary");
+    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+    check_ptr(f->coords, "coords");
+    check_ptr(f->velocity, "velocity");
+    check_ptr(f->dpdx, "dpdx");
+    check_ptr(f->density, "density");
+    check_ptr(f->pressure, "pressure");
+    check_ptr(f->pressure_bc, "pressure_bc");
+    check_ptr(f->udiag, "udiag");
+    check_ptr(f->exposed_area, "exposed_area");
+    if (!(o->tau_scale != 0.0)) fail(NW_INVALID_ARG, "tau_scale is zero");
+    materialize_zero(ls);
+    launch_continuity_open(ls->stream, v, *f, *o, ls->values.p, ls->rhs.p);
+  });
+}
+
+nw_status nw_assemble_momentum_open(nw_linsys* ls, const nw_sideset* s,
+                                    const nw_momentum_open_fields* f,
+                                    const nw_momentum_open_opts* o) {
+  return guard([&] {
+    const SideView v = side_view(ls, s);
+    need_dof(ls, 3, "momentum open boundary");
+    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+    check_ptr(f->coords, "coords");
+    check_ptr(f->velocity, "velocity");
+    check_ptr(f->dudx, "dudx");
+    check_ptr(f->viscosity, "viscosity");
+    check_ptr(f->velocity_bc, "velocity_bc");
+    check_ptr(f->exposed_area, "exposed_area");
+    check_ptr(f->open_mass_flow_rate, "open_mass_flow_rate");
+    if (o->entrainment != NW_ENTRAIN_COMPUTED && o->entrainment != NW_ENTRAIN_SPECIFIED)
+      fail(NW_INVALID_ARG, "invalid entrainment method");
+    materialize_zero(ls);
+    launch_momentum_open(ls->stream, v, *f, *o, ls->values.p, ls->rhs.p);
+  });
+}
+
+nw_status nw_assemble_momentum_symmetry(nw_linsys* ls, const nw_sideset* s,
+                                        const nw_momentum_symmetry_fields* f,
+                                        const nw_momentum_symmetry_opts* o) {
+  return guard([&] {
+    const SideView v = side_view(ls, s);
+    need_dof(ls, 3, "momentum symmetry boundary");
+    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+    check_ptr(f->coords, "coords");
+    check_ptr(f->velocity, "velocity");
+    check_ptr(f->dudx, "dudx");
+    check_ptr(f->viscosity, "viscosity");
+    check_ptr(f->exposed_area, "exposed_area");
+    materialize_zero(ls);
+    launch_momentum_symmetry(ls->stream, v, *f, *o, ls->values.p, ls->rhs.p);
+  });
+}
+
+nw_status nw_assemble_scalar_open(nw_linsys* ls, const nw_sideset* s,
+                                  const nw_scalar_open_fields* f, double relax) {
+  return guard([&] {
+    const SideView v = side_view(ls, s);
+    need_dof(ls, 1, "scalar open boundary");
+    if (!f) fail(NW_INVALID_ARG, "null argument");
+    check_ptr(f->q, "q");
+    check_ptr(f->q_bc, "q_bc");
+    check_ptr(f->open_mass_flow_rate, "open_mass_flow_rate");
+    if (!(relax != 0.0)) fail(NW_INVALID_ARG, "relaxation factor is zero");
+    materialize_zero(ls);
+    launch_scalar_open(ls->stream, v, *f, relax, ls->values.p, ls->rhs.p);
   });
 }
 

@@ -1,0 +1,249 @@
+"""Boundary face-IP kernels (continuity open, momentum open and symmetry,
+scalar open) through the C ABI against the oracle, and the reference's
+unit-cube golds on the GPU.
+
+Tolerance: the running-magnitude bound of gpu_util (|gpu - oracle| <=
+1e-12 S per entry, S from the oracle's *_local_mag kernels summed like the
+values).
+"""
+import numpy as np
+import pytest
+
+import kat
+from gpu_util import check_close, dev
+
+pytestmark = pytest.mark.gpu
+
+SIDES = ("x-", "x+", "y-", "y+", "z-", "z+")
+
+
+def _mesh(nw, kind):
+    if kind == "hex":
+        return nw.Mesh(10, 8, 6, lx=1.0, ly=0.8, lz=0.5, stretch_z=1.15, jitter=0.15, seed=5)
+    if kind == "tets":
+        return nw.Mesh(6, 5, 4, jitter=0.1, seed=6, tets=True)
+    if kind == "periodic":  # z sides only; their seam nodes are periodic slaves
+        return nw.Mesh(8, 6, 5, periodic_x=True, periodic_y=True, jitter=0.1, seed=7)
+    return nw.Mesh(7, 6, 5, jitter=0.1, seed=8, renumber=1, renumber_seed=3)
+
+
+def _system(nw, mesh, nd):
+    ls = nw.LinearSystem(nd)
+    ls.build_edge_graph(mesh.num_nodes, mesh.edges, mesh.global_id, mesh.nalu_id)
+    ls.finalize()
+    ls.zero_system()
+    return ls
+
+
+def _oracle_sum(orc, mesh, nd, ipn, lhs, rhs, ml, mr):
+    rp, ci, lid = orc.build_graph(mesh.nalu_id, mesh.edges, nd)
+    vals, b, _, _ = orc.sum_into(ipn, nd, lhs, rhs, lid, rp, ci, with_abs=False)
+    va, ba, _, _ = orc.sum_into(ipn, nd, ml, mr, lid, rp, ci, with_abs=False)
+    return vals, b, va, ba
+
+
+def _node_fields(mesh, rng):
+    N = mesh.num_nodes
+    master = mesh.nalu_id - 1
+    f = dict(coords=mesh.coords, velocity=rng.normal(0, 1, (N, 3)), dpdx=rng.normal(0, 1, (N, 3)),
+             density=rng.uniform(0.8, 1.2, N), pressure=rng.normal(0, 1, N), pressure_bc=rng.normal(0, 1, N),
+             udiag=rng.uniform(0.5, 2.0, N), dudx=rng.normal(0, 1, (N, 9)), viscosity=rng.uniform(0.01, 0.2, N),
+             velocity_bc=rng.normal(0, 1, (N, 3)), q=rng.normal(0, 1, N), q_bc=rng.normal(0, 1, N))
+    for k, v in f.items():  # slaves carry their master's values
+        if k != "coords":
+            f[k] = np.ascontiguousarray(v[master])
+    return f
+
+
+@pytest.mark.parametrize("kind", ["hex", "tets", "periodic", "renumbered"])
+def test_continuity_open_matches_oracle(nw, orc, kind):
+    mesh = _mesh(nw, kind)
+    rng = np.random.default_rng(11)
+    f = _node_fields(mesh, rng)
+    ipn, area = mesh.face_ips(("x+", "y-", "z+") if kind != "periodic" else ("z-", "z+"))
+    dynp = rng.normal(0, 0.1, len(ipn))
+    ls = _system(nw, mesh, 1)
+    ss = ls.sideset(ipn)
+    d = {k: dev(v) for k, v in dict(f, area=area, dynp=dynp).items()}
+    fld = nw.ContinuityOpenFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dpdx", "density", "pressure",
+                                                               "pressure_bc", "udiag", "area", "dynp")))
+    oo = dict(tau_scale=0.7, noc_fac=1.0, pstab_fac=1.0, mdot_corr=0.01, solve_incompressible=0.0)
+    ls.assemble_continuity_open(ss, fld, nw.ContinuityOpenOpts(**oo))
+    vals, rhs = ls.to_host()
+    o = orc.ContinuityOpenOpts(**oo)
+    args = (ipn, f["coords"], f["velocity"], f["dpdx"], f["density"], f["pressure"], f["pressure_bc"],
+            f["udiag"], area, dynp, o)
+    ref = _oracle_sum(orc, mesh, 1, ipn, *orc.continuity_open_local(*args),
+                      *orc.continuity_open_local(*args, mag=True))
+    check_close(vals, ref[0], ref[2], "values")
+    check_close(rhs, ref[1], ref[3], "rhs")
+    n, rows = ss.sizes()
+    assert n == len(ipn) and 0 < rows <= len(ipn)
+
+
+@pytest.mark.parametrize("entrain", [0, 1])
+@pytest.mark.parametrize("kind", ["hex", "tets", "periodic"])
+def test_momentum_open_matches_oracle(nw, orc, kind, entrain):
+    mesh = _mesh(nw, kind)
+    rng = np.random.default_rng(12)
+    f = _node_fields(mesh, rng)
+    ipn, area = mesh.face_ips(SIDES)
+    mdot = rng.normal(0, 0.05, len(ipn))  # both signs: outflow and entrainment
+    ls = _system(nw, mesh, 3)
+    ss = ls.sideset(ipn)
+    d = {k: dev(v) for k, v in dict(f, area=area, mdot=mdot).items()}
+    fld = nw.MomentumOpenFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dudx", "viscosity",
+                                                             "velocity_bc", "area", "mdot")))
+    oo = dict(include_div_u=1.0, nf_entrain=0.3, entrainment=entrain)
+    ls.assemble_momentum_open(ss, fld, nw.MomentumOpenOpts(**oo))
+    vals, rhs = ls.to_host()
+    o = orc.MomentumOpenOpts(**oo)
+    args = (ipn, f["coords"], f["velocity"], f["dudx"], f["viscosity"], f["velocity_bc"], area, mdot, o)
+    ref = _oracle_sum(orc, mesh, 3, ipn, *orc.momentum_open_local(*args), *orc.momentum_open_local(*args, mag=True))
+    check_close(vals, ref[0], ref[2], "values")
+    check_close(rhs, ref[1], ref[3], "rhs")
+
+
+@pytest.mark.parametrize("penalty", [0.0, 2.0])
+@pytest.mark.parametrize("kind", ["hex", "tets", "renumbered"])
+def test_momentum_symmetry_matches_oracle(nw, orc, kind, penalty):
+    mesh = _mesh(nw, kind)
+    rng = np.random.default_rng(13)
+    f = _node_fields(mesh, rng)
+    ipn, area = mesh.face_ips(("y-", "y+", "z-"))
+    ls = _system(nw, mesh, 3)
+    ss = ls.sideset(ipn)
+    d = {k: dev(v) for k, v in dict(f, area=area).items()}
+    fld = nw.MomentumSymmetryFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dudx", "viscosity", "area")))
+    oo = dict(include_div_u=1.0, penalty_factor=penalty)
+    ls.assemble_momentum_symmetry(ss, fld, nw.MomentumSymmetryOpts(**oo))
+    vals, rhs = ls.to_host()
+    o = orc.MomentumSymmetryOpts(**oo)
+    args = (ipn, f["coords"], f["velocity"], f["dudx"], f["viscosity"], area, o)
+    ref = _oracle_sum(orc, mesh, 3, ipn, *orc.momentum_symmetry_local(*args),
+                      *orc.momentum_symmetry_local(*args, mag=True))
+    check_close(vals, ref[0], ref[2], "values")
+    check_close(rhs, ref[1], ref[3], "rhs")
+
+
+@pytest.mark.parametrize("kind", ["hex", "tets"])
+def test_scalar_open_matches_oracle(nw, orc, kind):
+    mesh = _mesh(nw, kind)
+    rng = np.random.default_rng(14)
+    f = _node_fields(mesh, rng)
+    ipn, area = mesh.face_ips(("x-", "x+"))
+    mdot = rng.normal(0, 0.05, len(ipn))
+    ls = _system(nw, mesh, 1)
+    ss = ls.sideset(ipn)
+    d = {k: dev(v) for k, v in dict(q=f["q"], q_bc=f["q_bc"], mdot=mdot).items()}
+    ls.assemble_scalar_open(ss, nw.ScalarOpenFields(d["q"].data_ptr(), d["q_bc"].data_ptr(), d["mdot"].data_ptr()),
+                            relax=0.7)
+    vals, rhs = ls.to_host()
+    args = (ipn, f["q"], f["q_bc"], mdot)
+    ref = _oracle_sum(orc, mesh, 1, ipn, *orc.scalar_open_local(*args, relax=0.7),
+                      *orc.scalar_open_local(*args, relax=0.7, mag=True))
+    check_close(vals, ref[0], ref[2], "values")
+    check_close(rhs, ref[1], ref[3], "rhs")
+
+
+def _dense(nw, ls, nd, n_nodes):
+    vals, rhs = ls.to_host()
+    rp, ci = ls.graph()
+    A = np.zeros((n_nodes * nd, n_nodes * nd))
+    for r in range(len(rp) - 1):
+        A[r, ci[rp[r]:rp[r + 1]]] = vals[rp[r]:rp[r + 1]]
+    return A, rhs
+
+
+def test_unit_cube_golds_on_the_gpu(nw, orc, golds):
+    """The reference's open / symmetry known answers through the C ABI."""
+    mesh = nw.Mesh(1, 1, 1)
+    ipn, area = mesh.face_ips(("x+",))
+    c = kat.continuity_open_fixture(orc)
+    ls = _system(nw, mesh, 1)
+    ss = ls.sideset(ipn)
+    d = {k: dev(v) for k, v in dict(coords=c["coords"], velocity=c["velocity"], dpdx=c["dpdx"], density=c["density"],
+                                     pressure=c["pressure"], pbc=c["pressure_bc"], udiag=c["udiag"], area=area,
+                                     dynp=c["dynp"]).items()}
+    ls.assemble_continuity_open(ss, nw.ContinuityOpenFields(*(d[k].data_ptr() for k in (
+        "coords", "velocity", "dpdx", "density", "pressure", "pbc", "udiag", "area", "dynp"))),
+        nw.ContinuityOpenOpts(**c["open_opts"]))
+    A, b = _dense(nw, ls, 1, 8)
+    g = golds["continuity_open_hex8_xplus"]
+    np.testing.assert_allclose(A.ravel(), g["lhs"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(b, g["rhs"], rtol=0, atol=1e-12)
+
+    m = kat.momentum_face_fixture(orc)
+    d = {k: dev(v) for k, v in dict(coords=m["coords"], velocity=m["velocity"], dudx=m["dudx"],
+                                     viscosity=m["viscosity"], ubc=m["velocity_bc"], area=area,
+                                     mdot=m["open_mdot"]).items()}
+    ls = _system(nw, mesh, 3)
+    ss = ls.sideset(ipn)
+    ls.assemble_momentum_open(ss, nw.MomentumOpenFields(*(d[k].data_ptr() for k in (
+        "coords", "velocity", "dudx", "viscosity", "ubc", "area", "mdot"))),
+        nw.MomentumOpenOpts(0.0, 0.0, nw.ENTRAIN_COMPUTED))
+    A, b = _dense(nw, ls, 3, 8)
+    g = golds["momentum_open_hex8_xplus"]
+    np.testing.assert_allclose(A.ravel(), g["lhs"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(b, g["rhs"], rtol=0, atol=1e-12)
+
+    g = golds["momentum_symmetry_hex8_xplus"]
+    dof = (3 * m["conn"][0][:, None] + np.arange(3)).ravel()
+    for case, pen in enumerate(g["penalty_factor"]):
+        ls = _system(nw, mesh, 3)
+        ss = ls.sideset(ipn)
+        ls.assemble_momentum_symmetry(ss, nw.MomentumSymmetryFields(*(d[k].data_ptr() for k in (
+            "coords", "velocity", "dudx", "viscosity", "area"))), nw.MomentumSymmetryOpts(0.0, pen))
+        A, b = _dense(nw, ls, 3, 8)
+        np.testing.assert_allclose(A[np.ix_(dof, dof)].ravel(), g["lhs"][case], rtol=0, atol=1e-12)
+        np.testing.assert_allclose(b[dof], g["rhs"][case], rtol=0, atol=1e-12)
+
+
+def test_boundary_adds_to_the_interior_assembly(nw, orc):
+    """Interior continuity edges, then the open boundary: the sum matches the
+    oracle's interior + boundary contributions."""
+    from gpu_util import continuity_fields, oracle_continuity
+    mesh = _mesh(nw, "hex")
+    rng = np.random.default_rng(15)
+    f = _node_fields(mesh, rng)
+    ipn, area = mesh.face_ips(SIDES)
+    ls = _system(nw, mesh, 1)
+    ss = ls.sideset(ipn)
+    d = {k: dev(v) for k, v in dict(f, area=mesh.area, farea=area).items()}
+    co = nw.ContinuityOpts(1.0, 0.7, 1.0, 0.0)
+    ls.assemble_continuity(continuity_fields(nw, d), co)
+    oo = dict(tau_scale=0.7, noc_fac=1.0, pstab_fac=1.0, mdot_corr=0.0, solve_incompressible=0.0)
+    ls.assemble_continuity_open(ss, nw.ContinuityOpenFields(*(d[k].data_ptr() for k in (
+        "coords", "velocity", "dpdx", "density", "pressure", "pressure_bc", "udiag", "farea")), None),
+        nw.ContinuityOpenOpts(**oo))
+    vals, rhs = ls.to_host()
+    hi = oracle_continuity(orc, mesh.edges, mesh.nalu_id, dict(f, area=mesh.area),
+                           {k: getattr(co, k) for k, _ in co._fields_})
+    args = (ipn, f["coords"], f["velocity"], f["dpdx"], f["density"], f["pressure"], f["pressure_bc"],
+            f["udiag"], area, None, orc.ContinuityOpenOpts(**oo))
+    bo = _oracle_sum(orc, mesh, 1, ipn, *orc.continuity_open_local(*args),
+                     *orc.continuity_open_local(*args, mag=True))
+    check_close(vals, hi["vals"] + bo[0], hi["vabs"] + bo[2], "values")
+    check_close(rhs, hi["rhs"] + bo[1], hi["rabs"] + bo[3], "rhs")
+
+
+def test_side_set_errors(nw):
+    mesh = _mesh(nw, "hex")
+    ls = _system(nw, mesh, 1)
+    with pytest.raises(nw.NwError, match="not joined"):
+        ls.sideset(np.array([[0, mesh.num_nodes - 1]]))
+    with pytest.raises(nw.NwError, match="out of range"):
+        ls.sideset(np.array([[0, mesh.num_nodes]]))
+    ipn, area = mesh.face_ips(("x+",))
+    ss = ls.sideset(ipn)
+    z = dev(np.zeros(mesh.num_nodes * 9))
+    with pytest.raises(nw.NwError, match="num_dof 3"):
+        ls.assemble_momentum_symmetry(ss, nw.MomentumSymmetryFields(*(z.data_ptr(),) * 5),
+                                      nw.MomentumSymmetryOpts(0.0, 0.0))
+    ls3 = _system(nw, mesh, 3)
+    with pytest.raises(nw.NwError, match="another linear system"):
+        ls3.assemble_momentum_symmetry(ss, nw.MomentumSymmetryFields(*(z.data_ptr(),) * 5),
+                                       nw.MomentumSymmetryOpts(0.0, 0.0))
+    empty = ls.sideset(np.zeros((0, 2), np.int64))
+    assert empty.sizes() == (0, 0)
+    ls.assemble_scalar_open(empty, nw.ScalarOpenFields(z.data_ptr(), z.data_ptr(), z.data_ptr()), relax=1.0)
