@@ -42,8 +42,9 @@ typedef enum nw_status {
 
 /* Krylov methods (the `method` strings passed to the Belos factory,
  * src/LinearSolver.C:114) and preconditioners (src/LinearSolverConfig.C:
- * 89-121). */
-enum { NW_GMRES = 0, NW_CG = 1, NW_FGMRES = 2 };
+ * 89-121). CG, BiCGStab and TFQMR run in FP64; with a NW_PREC_MIXED*
+ * precision or NW_PC_LEARNED the solve is (F)GMRES whatever the method. */
+enum { NW_GMRES = 0, NW_CG = 1, NW_FGMRES = 2, NW_BICGSTAB = 3, NW_TFQMR = 4 };
 enum {
   NW_PC_NONE = 0,
   NW_PC_JACOBI = 1, /* "jacobi" / "default": Ifpack2 Jacobi, 1 sweep */
@@ -60,7 +61,7 @@ enum {
 
 /* TpetraLinearSolverConfig::load keys (src/LinearSolverConfig.C:37-140). */
 typedef struct nw_solver_cfg {
-  int method;             /* NW_GMRES, NW_CG, NW_FGMRES */
+  int method;             /* NW_GMRES, NW_CG, NW_FGMRES, NW_BICGSTAB, NW_TFQMR */
   int preconditioner;     /* NW_PC_* */
   int precision;          /* NW_PREC_* */
   int kspace;             /* "kspace", default 50 */
@@ -516,6 +517,24 @@ typedef struct nw_scalar_open_fields {
  * relaxation factor. num_dof 1. */
 nw_status nw_assemble_scalar_open(nw_linsys* ls, const nw_sideset* s,
                                   const nw_scalar_open_fields* f, double relax);
+
+/* MdotOpenEdgeAlg::execute (src/ngp_algorithms/MdotOpenEdgeAlg.C:55-150):
+ * the open_mass_flow_rate of every face IP into mdot (device, num_ips, IP
+ * order) from the same fields as the continuity open kernel
+ * (dynamic_pressure may be NULL), with noc_fac = get_noc_usage("pressure")
+ * and pstab_fac = 0 with activateOpenMdotCorrection_ else 1; *total (host,
+ * may be NULL) gets the sum over the IPs in a fixed order (the value
+ * MdotAlgDriver::add_open_mdot receives). */
+nw_status nw_compute_open_mdot(nw_linsys* ls, const nw_sideset* s,
+                               const nw_continuity_open_fields* f, double noc_fac,
+                               double pstab_fac, double* mdot, double* total);
+/* MdotOpenCorrectorAlg::execute (src/ngp_algorithms/MdotOpenCorrectorAlg.C:
+ * 37-60): mdot -= correction on every IP of the side set; *total gets the
+ * corrected sum (MdotAlgDriver's mdot_open_post). The correction itself is
+ * (density accumulation + inflow + open) / (open IP count)
+ * (src/ngp_algorithms/MdotAlgDriver.C:145-146), computed by the caller. */
+nw_status nw_correct_open_mdot(nw_linsys* ls, const nw_sideset* s, double correction,
+                               double* mdot, double* total);
 
 /* ---- MatrixMarket export / import ---- */
 /* TpetraLinearSystem::writeToFile (src/TpetraLinearSystem.C:2017-2045):

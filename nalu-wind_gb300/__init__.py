@@ -22,7 +22,7 @@ LIB_PATH = PKG_DIR / "libnw_gb300.so"
 NW_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "CUDA_ERROR", 3: "NOT_FINALIZED", 4: "NAN_DETECTED",
                 5: "NOT_CONVERGED", 6: "BREAKDOWN", 7: "TIMEOUT", 8: "NO_DEVICE", 9: "INTERNAL"}
-GMRES, CG, FGMRES = 0, 1, 2
+GMRES, CG, FGMRES, BICGSTAB, TFQMR = 0, 1, 2, 3, 4
 PC_NONE, PC_JACOBI, PC_SGS, PC_LEARNED = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED, PREC_MIXED_BF16 = 0, 1, 2
 
@@ -213,6 +213,10 @@ SIGNATURES = {
     "nw_assemble_momentum_symmetry": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(MomentumSymmetryFields),
                                                 C.POINTER(MomentumSymmetryOpts)]),
     "nw_assemble_scalar_open": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ScalarOpenFields), C.c_double]),
+    "nw_compute_open_mdot": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ContinuityOpenFields), C.c_double,
+                                       C.c_double, C.c_void_p, C.POINTER(C.c_double)]),
+    "nw_correct_open_mdot": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
+                                       C.POINTER(C.c_double)]),
     "nw_assemble_continuity_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
     "nw_assemble_momentum_mass_bdf": (C.c_int, [C.c_void_p, C.POINTER(MassBdfFields), C.POINTER(BdfOpts)]),
     "nw_linsys_write_matrix_market": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_void_p]),
@@ -453,6 +457,18 @@ class LinearSystem:
 
     def assemble_scalar_open(self, ss: "SideSet", fields: ScalarOpenFields, relax=1.0) -> None:
         check(self.lib.nw_assemble_scalar_open(self.h, ss.h, C.byref(fields), relax))
+
+    def open_mdot(self, ss: "SideSet", fields: ContinuityOpenFields, mdot_dev, noc_fac=1.0, pstab_fac=1.0) -> float:
+        """Open mass flow rate per face IP into mdot_dev; returns the sum."""
+        t = C.c_double()
+        check(self.lib.nw_compute_open_mdot(self.h, ss.h, C.byref(fields), noc_fac, pstab_fac, dptr(mdot_dev),
+                                            C.byref(t)))
+        return t.value
+
+    def correct_open_mdot(self, ss: "SideSet", correction: float, mdot_dev) -> float:
+        t = C.c_double()
+        check(self.lib.nw_correct_open_mdot(self.h, ss.h, correction, dptr(mdot_dev), C.byref(t)))
+        return t.value
 
     # -- input producers (device tensors in and out)
     def compute_mdot(self, fields: "ContinuityFields", mdot_dev, noc_fac=1.0, interp_together=1.0) -> None:

@@ -304,9 +304,75 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// MdotOpenEdgeAlg::execute (src/ngp_algorithms/MdotOpenEdgeAlg.C:55-150):
+// one thread per face IP (in row-sorted position; writes at its IP index).
+__global__ void __launch_bounds__(kThreads)
+    open_mdot_k(SideView v, nw_continuity_open_fields f, double noc_fac, double pstab_fac,
+                double* __restrict__ mdot) {
+  const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= v.nip) return;
+  const int4 q = v.ips[p];
+  const int ip = q.x, R = q.y, L = q.z;
+  const double pts = pstab_fac / f.udiag[R];
+  double asq = 0.0, axdx = 0.0, av[3], dxj[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    av[d] = f.exposed_area[3 * ip + d];
+    dxj[d] = f.coords[3 * R + d] - 0.5 * (f.coords[3 * R + d] + f.coords[3 * L + d]);
+    asq += av[d] * av[d];
+    axdx += av[d] * dxj[d];
+  }
+  const double inv_axdx = 1.0 / axdx;
+  const double pbc = f.pressure_bc[R] - (f.dynamic_pressure ? f.dynamic_pressure[ip] : 0.0);
+  const double pIp = 0.5 * (f.pressure[L] + f.pressure[R]);
+  double tmdot = -pts * (pbc - pIp) * asq * inv_axdx;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double kxj = av[d] - asq * inv_axdx * dxj[d];
+    const double G = f.dpdx[3 * R + d];
+    tmdot += (f.density[R] * f.velocity[3 * R + d] + pts * G) * av[d] - pts * kxj * G * noc_fac;
+  }
+  mdot[ip] = tmdot;
+}
+
+// MdotOpenCorrectorAlg::execute (src/ngp_algorithms/MdotOpenCorrectorAlg.C:
+// 37-60): the same correction off every open IP.
+__global__ void correct_k(int64_t n, double corr, double* __restrict__ mdot) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) mdot[i] -= corr;
+}
+
+// Sum of mdot[0..n) by one block in a fixed order (deterministic).
+__global__ void __launch_bounds__(256) sum_k(int64_t n, const double* __restrict__ a,
+                                             double* __restrict__ out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += 256) s += a[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
 unsigned blocks(int64_t n) { return unsigned((n + kThreads - 1) / kThreads); }
 
 }  // namespace
+
+void launch_open_mdot(cudaStream_t s, const SideView& v, const nw_continuity_open_fields& f,
+                      double noc_fac, double pstab_fac, double* mdot, double* total_dev) {
+  if (v.nip > 0) open_mdot_k<<<blocks(v.nip), kThreads, 0, s>>>(v, f, noc_fac, pstab_fac, mdot);
+  sum_k<<<1, 256, 0, s>>>(v.nip, mdot, total_dev);
+  NW_CUDA(cudaGetLastError());
+}
+void launch_correct_open_mdot(cudaStream_t s, const SideView& v, double correction, double* mdot,
+                              double* total_dev) {
+  if (v.nip > 0) correct_k<<<blocks(v.nip), kThreads, 0, s>>>(v.nip, correction, mdot);
+  sum_k<<<1, 256, 0, s>>>(v.nip, mdot, total_dev);
+  NW_CUDA(cudaGetLastError());
+}
 
 void launch_continuity_open(cudaStream_t s, const SideView& v, const nw_continuity_open_fields& f,
                             const nw_continuity_open_opts& o, double* values, double* rhs) {

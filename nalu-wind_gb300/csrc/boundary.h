@@ -12,6 +12,7 @@ namespace nw {
 // range of face IPs sorted by IP index. ips[p] = (ip index, face node R,
 // opposing node L, column slot of L's row in the node row's column list).
 struct SideView {
+  int64_t nip = 0;  // face IPs
   int64_t nb = 0;
   const int32_t* brow = nullptr;  // nb node rows
   const int32_t* bptr = nullptr;  // nb + 1
@@ -28,5 +29,13 @@ void launch_momentum_symmetry(cudaStream_t s, const SideView& v, const nw_moment
                               const nw_momentum_symmetry_opts& o, double* values, double* rhs);
 void launch_scalar_open(cudaStream_t s, const SideView& v, const nw_scalar_open_fields& f, double relax,
                         double* values, double* rhs);
+
+// MdotOpenEdgeAlg: per-IP open mass flow rate into mdot (num_ips), and
+// its sum (fixed order) into *total_dev.
+void launch_open_mdot(cudaStream_t s, const SideView& v, const nw_continuity_open_fields& f,
+                      double noc_fac, double pstab_fac, double* mdot, double* total_dev);
+// MdotOpenCorrectorAlg: mdot -= correction on every IP, then the sum.
+void launch_correct_open_mdot(cudaStream_t s, const SideView& v, double correction, double* mdot,
+                              double* total_dev);
 
 }  // namespace nw

@@ -534,6 +534,44 @@ __global__ void add_f32_k(int64_t n, const float* __restrict__ y,
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) x[i] += double(y[i]);
 }
+// out = a x + b y (out may alias x or y)
+__global__ void lincomb_k(int64_t n, double a, const double* x, double b, const double* y, double* out) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a * x[i] + b * y[i];
+}
+// BiCGStab direction: p = r + beta (p - omega v)
+__global__ void bicg_dir_k(int64_t n, const double* __restrict__ r, double beta, double omega,
+                           const double* __restrict__ v, double* __restrict__ p) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+}
+// BiCGStab update: x += alpha ph + omega sh; r = s - omega t
+__global__ void bicg_upd_k(int64_t n, double alpha, const double* __restrict__ ph, double omega,
+                           const double* __restrict__ sh, const double* __restrict__ sv,
+                           const double* __restrict__ t, double* __restrict__ x,
+                           double* __restrict__ r) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) {
+    x[i] += alpha * ph[i] + omega * sh[i];
+    r[i] = sv[i] - omega * t[i];
+  }
+}
+// TFQMR half step: w -= alpha Au; dh = uh + coef dh
+__global__ void tfqmr_wd_k(int64_t n, double alpha, const double* __restrict__ Au, double coef,
+                           const double* __restrict__ uh, double* __restrict__ w,
+                           double* __restrict__ dh) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) {
+    w[i] -= alpha * Au[i];
+    dh[i] = uh[i] + coef * dh[i];
+  }
+}
+// TFQMR: v = Aun + beta (Au + beta v)
+__global__ void tfqmr_v_k(int64_t n, const double* __restrict__ Aun, double beta,
+                          const double* __restrict__ Au, double* __restrict__ v) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = Aun[i] + beta * (Au[i] + beta * v[i]);
+}
 // p = z + beta p
 __global__ void xpby_k(int64_t n, const double* __restrict__ z, double beta,
                        double* __restrict__ p) {
@@ -927,6 +965,10 @@ SolveResult KrylovSolver::solve(const nw_solver_cfg& cfg, double tol,
     r = mixed(cfg, tol, pc, b, x, s);
   else if (cfg.method == NW_CG && pc.kind != NW_PC_LEARNED)
     r = cg(cfg, tol, pc, b, x, s);
+  else if (cfg.method == NW_BICGSTAB && pc.kind != NW_PC_LEARNED)
+    r = bicgstab(cfg, tol, pc, b, x, s);
+  else if (cfg.method == NW_TFQMR && pc.kind != NW_PC_LEARNED)
+    r = tfqmr(cfg, tol, pc, b, x, s);
   else
     r = gmres(cfg, tol, pc, b, x, cfg.method == NW_FGMRES || pc.kind == NW_PC_LEARNED, s);
   // The learned preconditioner is judged by the FP64 residual: if the
@@ -1139,6 +1181,160 @@ SolveResult KrylovSolver::cg(const nw_solver_cfg& cfg, double tol,
   }
   spmv64(x, b, r, s);
   res.final_abs = std::sqrt(dot(r, r, s));
+  res.final_rel = rel;
+  res.iterations = its;
+  res.converged = rel <= tol ? 1 : 0;
+  if (res.status == NW_OK && !res.converged) res.status = NW_NOT_CONVERGED;
+  return res;
+}
+
+// BiCGStab (van der Vorst 1992), right preconditioned, FP64: Belos
+// "bicgstab" as src/LinearSolver.C:114 selects it. Converged when the
+// recursively updated residual satisfies ||r|| / ||b|| <= tol.
+SolveResult KrylovSolver::bicgstab(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                                   const double* b, double* x, cudaStream_t s) {
+  const int64_t n = A_.n;
+  SolveResult res;
+  fill_k<double><<<grid1(n), kBlock, 0, s>>>(n, x, 0.0);
+  const double bnorm = std::sqrt(dot(b, b, s));
+  res.bnorm = bnorm;
+  res.history.push_back(1.0);
+  if (!std::isfinite(bnorm)) {
+    res.status = NW_NAN_DETECTED;
+    return res;
+  }
+  if (bnorm == 0.0) {
+    res.converged = 1;
+    return res;
+  }
+  aux_.resize(size_t(7) * n);
+  double *rh = aux_.p, *p = rh + n, *v = p + n, *ph = v + n, *sv = ph + n, *sh = sv + n,
+         *t = sh + n;
+  double* r = r_.p;
+  NW_CUDA(cudaMemcpyAsync(r, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  NW_CUDA(cudaMemcpyAsync(rh, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  fill_k<double><<<grid1(n), kBlock, 0, s>>>(n, p, 0.0);
+  fill_k<double><<<grid1(n), kBlock, 0, s>>>(n, v, 0.0);
+  double rho = 1.0, alpha = 1.0, omega = 1.0, rel = 1.0;
+  int its = 0;
+  while (its < cfg.max_iterations) {
+    const double rho_n = dot(rh, r, s);
+    if (rho_n == 0.0 || omega == 0.0 || !std::isfinite(rho_n)) {
+      res.status = NW_BREAKDOWN;
+      break;
+    }
+    const double beta = (rho_n / rho) * (alpha / omega);
+    rho = rho_n;
+    bicg_dir_k<<<grid1(n), kBlock, 0, s>>>(n, r, beta, omega, v, p);
+    apply_precond(pc, p, ph, s);
+    spmv(ph, v, s);
+    const double rv = dot(rh, v, s);
+    if (rv == 0.0 || !std::isfinite(rv)) {
+      res.status = NW_BREAKDOWN;
+      break;
+    }
+    alpha = rho / rv;
+    lincomb_k<<<grid1(n), kBlock, 0, s>>>(n, 1.0, r, -alpha, v, sv);
+    apply_precond(pc, sv, sh, s);
+    spmv(sh, t, s);
+    const double tt = dot(t, t, s);
+    omega = tt > 0.0 ? dot(t, sv, s) / tt : 0.0;
+    bicg_upd_k<<<grid1(n), kBlock, 0, s>>>(n, alpha, ph, omega, sh, sv, t, x, r);
+    ++its;
+    rel = std::sqrt(dot(r, r, s)) / bnorm;
+    res.history.push_back(rel);
+    if (rel <= tol) break;
+  }
+  spmv64(x, b, r, s);
+  res.final_abs = std::sqrt(dot(r, r, s));
+  res.final_rel = rel;
+  res.iterations = its;
+  res.converged = rel <= tol ? 1 : 0;
+  if (res.status == NW_OK && !res.converged) res.status = NW_NOT_CONVERGED;
+  return res;
+}
+
+// TFQMR (Freund 1993; Saad, Iterative Methods for Sparse Linear Systems,
+// 2003, Algorithm 7.8) on A M^-1, FP64, with the direction vectors kept as
+// dh = M^-1 d so x is updated directly: Belos "tfqmr". One iteration is an
+// even and an odd half step (two products with A M^-1); after each the
+// residual bound sqrt(k + 1) tau_k (k half steps) is tested against
+// tol ||b||.
+SolveResult KrylovSolver::tfqmr(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                                const double* b, double* x, cudaStream_t s) {
+  const int64_t n = A_.n;
+  SolveResult res;
+  fill_k<double><<<grid1(n), kBlock, 0, s>>>(n, x, 0.0);
+  const double bnorm = std::sqrt(dot(b, b, s));
+  res.bnorm = bnorm;
+  res.history.push_back(1.0);
+  if (!std::isfinite(bnorm)) {
+    res.status = NW_NAN_DETECTED;
+    return res;
+  }
+  if (bnorm == 0.0) {
+    res.converged = 1;
+    return res;
+  }
+  aux_.resize(size_t(7) * n);
+  double *w = aux_.p, *u = w + n, *uh = u + n, *Au = uh + n, *Aun = Au + n, *v = Aun + n,
+         *dh = v + n;
+  const double* rt = b;  // shadow residual r0* = r0 = b
+  NW_CUDA(cudaMemcpyAsync(w, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  NW_CUDA(cudaMemcpyAsync(u, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  fill_k<double><<<grid1(n), kBlock, 0, s>>>(n, dh, 0.0);
+  apply_precond(pc, u, uh, s);
+  spmv(uh, Au, s);
+  NW_CUDA(cudaMemcpyAsync(v, Au, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  double tau = bnorm, theta = 0.0, eta = 0.0, alpha = 0.0, rel = 1.0;
+  double rho = dot(rt, b, s);
+  int its = 0;
+  for (int64_t mm = 0; its < cfg.max_iterations; ++mm) {
+    if (mm % 2 == 0) {
+      const double vr = dot(v, rt, s);
+      if (vr == 0.0 || !std::isfinite(vr)) {
+        res.status = NW_BREAKDOWN;
+        break;
+      }
+      alpha = rho / vr;
+    }
+    const double coef = alpha != 0.0 ? theta * theta / alpha * eta : 0.0;
+    tfqmr_wd_k<<<grid1(n), kBlock, 0, s>>>(n, alpha, Au, coef, uh, w, dh);
+    theta = std::sqrt(dot(w, w, s)) / tau;
+    const double c = 1.0 / std::sqrt(1.0 + theta * theta);
+    tau = tau * theta * c;
+    eta = c * c * alpha;
+    axpy_k<<<grid1(n), kBlock, 0, s>>>(n, eta, dh, x);
+    if (mm % 2 == 0) {
+      axpy_k<<<grid1(n), kBlock, 0, s>>>(n, -alpha, v, u);
+      apply_precond(pc, u, uh, s);
+      spmv(uh, Aun, s);
+      std::swap(Au, Aun);
+    } else {
+      ++its;
+      rel = std::sqrt(double(mm + 2)) * tau / bnorm;
+      res.history.push_back(rel);
+      if (!std::isfinite(rel)) {
+        res.status = NW_BREAKDOWN;
+        break;
+      }
+      if (rel <= tol) break;
+      if (rho == 0.0) {
+        res.status = NW_BREAKDOWN;
+        break;
+      }
+      const double rho_n = dot(w, rt, s);
+      const double beta = rho_n / rho;
+      rho = rho_n;
+      xpby_k<<<grid1(n), kBlock, 0, s>>>(n, w, beta, u);
+      apply_precond(pc, u, uh, s);
+      spmv(uh, Aun, s);
+      tfqmr_v_k<<<grid1(n), kBlock, 0, s>>>(n, Aun, beta, Au, v);
+      std::swap(Au, Aun);
+    }
+  }
+  spmv64(x, b, r_.p, s);
+  res.final_abs = std::sqrt(dot(r_.p, r_.p, s));
   res.final_rel = rel;
   res.iterations = its;
   res.converged = rel <= tol ? 1 : 0;

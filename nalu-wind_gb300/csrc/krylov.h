@@ -101,6 +101,11 @@ class KrylovSolver {
                  const double* b, double* x, cudaStream_t s);
   SolveResult mixed(const nw_solver_cfg& cfg, double tol, const Precond& pc,
                     const double* b, double* x, cudaStream_t s);
+  SolveResult bicgstab(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                       const double* b, double* x, cudaStream_t s);
+  SolveResult tfqmr(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                    const double* b, double* x, cudaStream_t s);
+  DeviceArray<double> aux_;     // work vectors of BiCGStab / TFQMR
   LearnedNet* net_ = nullptr;
   CoarseLevel* cl_ = nullptr;
   DeviceArray<float> Z32_, rc32_, ec32_, tmp32_, tmp32b_;

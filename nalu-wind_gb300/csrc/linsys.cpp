@@ -114,7 +114,7 @@ void check_cfg(const nw_solver_cfg& c) {
   if (c.kspace < 1 || c.kspace > 1000) fail(NW_INVALID_ARG, "kspace out of range");
   if (c.max_iterations < 0) fail(NW_INVALID_ARG, "max_iterations < 0");
   if (!(c.tolerance >= 0.0)) fail(NW_INVALID_ARG, "tolerance < 0");
-  if (c.method < NW_GMRES || c.method > NW_FGMRES) fail(NW_INVALID_ARG, "bad method");
+  if (c.method < NW_GMRES || c.method > NW_TFQMR) fail(NW_INVALID_ARG, "bad method");
   if (c.preconditioner < NW_PC_NONE || c.preconditioner > NW_PC_LEARNED)
     fail(NW_INVALID_ARG, "bad preconditioner");
 }
@@ -758,6 +758,7 @@ struct nw_sideset {
   int64_t nb = 0;
   DeviceArray<int32_t> brow, bptr;
   DeviceArray<int4> ips;
+  DeviceArray<double> total;  // device sum of the open mass flow rates
 };
 
 namespace {
@@ -767,6 +768,7 @@ SideView side_view(const nw_linsys* ls, const nw_sideset* s) {
   if (!s) fail(NW_INVALID_ARG, "null side set");
   if (s->ls != ls) fail(NW_INVALID_ARG, "side set was registered on another linear system");
   SideView v;
+  v.nip = s->num_ips;
   v.nb = s->nb;
   v.brow = s->brow.p;
   v.bptr = s->bptr.p;
@@ -831,6 +833,7 @@ nw_status nw_sideset_create(nw_linsys* ls, int64_t num_ips, const int64_t* ip_no
     s->brow.upload(brow, ls->stream);
     s->bptr.upload(bptr, ls->stream);
     s->ips.upload(ips, ls->stream);
+    s->total.resize(1);
     NW_CUDA(cudaStreamSynchronize(ls->stream));
     *out = s.release();
   });
@@ -905,6 +908,42 @@ nw_status nw_assemble_momentum_symmetry(nw_linsys* ls, const nw_sideset* s,
     check_ptr(f->exposed_area, "exposed_area");
     materialize_zero(ls);
     launch_momentum_symmetry(ls->stream, v, *f, *o, ls->values.p, ls->rhs.p);
+  });
+}
+
+nw_status nw_compute_open_mdot(nw_linsys* ls, const nw_sideset* s,
+                               const nw_continuity_open_fields* f, double noc_fac,
+                               double pstab_fac, double* mdot, double* total) {
+  return guard([&] {
+    const SideView v = side_view(ls, s);
+    if (!f) fail(NW_INVALID_ARG, "null argument");
+    check_ptr(f->coords, "coords");
+    check_ptr(f->velocity, "velocity");
+    check_ptr(f->dpdx, "dpdx");
+    check_ptr(f->density, "density");
+    check_ptr(f->pressure, "pressure");
+    check_ptr(f->pressure_bc, "pressure_bc");
+    check_ptr(f->udiag, "udiag");
+    check_ptr(f->exposed_area, "exposed_area");
+    if (v.nip > 0) check_ptr(mdot, "mdot");
+    launch_open_mdot(ls->stream, v, *f, noc_fac, pstab_fac, mdot, s->total.p);
+    double t = 0.0;
+    NW_CUDA(cudaMemcpyAsync(&t, s->total.p, sizeof(double), cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    if (total) *total = t;
+  });
+}
+
+nw_status nw_correct_open_mdot(nw_linsys* ls, const nw_sideset* s, double correction,
+                               double* mdot, double* total) {
+  return guard([&] {
+    const SideView v = side_view(ls, s);
+    if (v.nip > 0) check_ptr(mdot, "mdot");
+    launch_correct_open_mdot(ls->stream, v, correction, mdot, s->total.p);
+    double t = 0.0;
+    NW_CUDA(cudaMemcpyAsync(&t, s->total.p, sizeof(double), cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    if (total) *total = t;
   });
 }
 

@@ -1089,6 +1089,89 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
       rz = rzn;
       for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
     }
+  } else if (method == 3) {  // BiCGStab
+    // van der Vorst (1992), right preconditioned: the iterate x and the
+    // recursively updated residual r of A M^-1 y = b, x = M^-1 y.
+    std::vector<double> rh(res), p(n, 0.0), vv(n, 0.0), ph(n), sv(n), sh(n), t(n);
+    double rho = 1.0, alpha = 1.0, omega = 1.0;
+    bool broke = false;
+    while (its < maxit) {
+      const double rho_n = dot(c, rh.data(), res.data());
+      if (rho_n == 0.0 || omega == 0.0) { broke = true; break; }
+      const double beta = (rho_n / rho) * (alpha / omega);
+      rho = rho_n;
+      for (int64_t i = 0; i < n; ++i) p[i] = res[i] + beta * (p[i] - omega * vv[i]);
+      precond(c, pc, p.data(), ph.data());
+      or_spmv(n, rp, ci, v, ph.data(), vv.data(), c.nthreads);
+      const double rv = dot(c, rh.data(), vv.data());
+      if (rv == 0.0) { broke = true; break; }
+      alpha = rho / rv;
+      for (int64_t i = 0; i < n; ++i) sv[i] = res[i] - alpha * vv[i];
+      precond(c, pc, sv.data(), sh.data());
+      or_spmv(n, rp, ci, v, sh.data(), t.data(), c.nthreads);
+      const double tt = dot(c, t.data(), t.data());
+      omega = tt > 0.0 ? dot(c, t.data(), sv.data()) / tt : 0.0;
+      for (int64_t i = 0; i < n; ++i) {
+        x[i] += alpha * ph[i] + omega * sh[i];
+        res[i] = sv[i] - omega * t[i];
+      }
+      ++its;
+      rel = std::sqrt(dot(c, res.data(), res.data())) / bnorm;
+      if (history) history[its] = rel;
+      if (rel <= tol) break;
+    }
+    (void)broke;  // a breakdown ends the iteration unconverged
+  } else if (method == 4) {  // TFQMR
+    // Freund (1993), as in Saad, Iterative Methods for Sparse Linear
+    // Systems (2003), Algorithm 7.8, on A M^-1 with the direction vectors
+    // kept in the unpreconditioned space (dh = M^-1 d), so x is updated
+    // directly. One iteration = the even and the odd half step (two
+    // products with A M^-1); convergence is tested after each iteration on
+    // the bound ||r_k|| <= sqrt(k + 1) tau_k (k = half steps).
+    std::vector<double> wv(res), u(res), uh(n), Au(n), Au_n(n), vv(n), dh(n, 0.0), rt(res);
+    precond(c, pc, u.data(), uh.data());
+    or_spmv(n, rp, ci, v, uh.data(), Au.data(), c.nthreads);
+    vv = Au;
+    double tau = bnorm, theta = 0.0, eta = 0.0, alpha = 0.0;
+    double rho = dot(c, rt.data(), res.data());
+    for (int64_t mm = 0; its < maxit; ++mm) {
+      if (mm % 2 == 0) {
+        const double vr = dot(c, vv.data(), rt.data());
+        if (vr == 0.0) break;
+        alpha = rho / vr;
+      }
+      const double coef = alpha != 0.0 ? theta * theta / alpha * eta : 0.0;
+      for (int64_t i = 0; i < n; ++i) {
+        wv[i] -= alpha * Au[i];
+        dh[i] = uh[i] + coef * dh[i];
+      }
+      theta = std::sqrt(dot(c, wv.data(), wv.data())) / tau;
+      const double cc = 1.0 / std::sqrt(1.0 + theta * theta);
+      tau = tau * theta * cc;
+      eta = cc * cc * alpha;
+      for (int64_t i = 0; i < n; ++i) x[i] += eta * dh[i];
+      if (mm % 2 == 0) {
+        for (int64_t i = 0; i < n; ++i) u[i] -= alpha * vv[i];
+        precond(c, pc, u.data(), uh.data());
+        or_spmv(n, rp, ci, v, uh.data(), Au_n.data(), c.nthreads);
+        std::swap(Au, Au_n);  // Au = A M^-1 u_{m+1}
+      } else {
+        ++its;
+        rel = std::sqrt(double(mm + 2)) * tau / bnorm;
+        if (history) history[its] = rel;
+        if (rel <= tol) break;
+        const double rho_n = dot(c, wv.data(), rt.data());
+        if (rho == 0.0) break;
+        const double beta = rho_n / rho;
+        rho = rho_n;
+        for (int64_t i = 0; i < n; ++i) u[i] = wv[i] + beta * u[i];
+        precond(c, pc, u.data(), uh.data());
+        // Au holds A M^-1 u_m; Au_n gets A M^-1 u_{m+1}
+        or_spmv(n, rp, ci, v, uh.data(), Au_n.data(), c.nthreads);
+        for (int64_t i = 0; i < n; ++i) vv[i] = Au_n[i] + beta * (Au[i] + beta * vv[i]);
+        std::swap(Au, Au_n);
+      }
+    }
   } else {  // GMRES(m)
     std::vector<double> V(size_t(n) * (m + 1));
     std::vector<double> H(size_t(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
@@ -1590,6 +1673,40 @@ NW_OR_BOTH(or_momentum_symmetry_local, 6,
 NW_OR_BOTH(or_scalar_open_local, 2, scalar_open_ip(ip, ipn, q, qbc, mdot, relax, A, b))
 #undef OR_ARGS
 #undef NW_OR_BOTH
+
+// MdotOpenEdgeAlg::execute (src/ngp_algorithms/MdotOpenEdgeAlg.C:55-150):
+// the open mass flow rate of each face IP (ipn as for the face kernels).
+void or_mdot_open(int64_t nip, const int64_t* ipn, const double* coords,
+                  const double* velocity, const double* Gpdx, const double* density,
+                  const double* pressure, const double* pbcF, const double* udiag,
+                  const double* areav, const double* dynp, double nocFac,
+                  double pstabFac, double* mdot) {
+  for (int64_t ip = 0; ip < nip; ++ip) {
+    const int64_t R = ipn[2 * ip], L = ipn[2 * ip + 1];
+    const double projTimeScale = pstabFac / udiag[R];
+    double asq = 0.0, axdx = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      const double coordIp = 0.5 * (coords[3 * R + d] + coords[3 * L + d]);
+      const double dxj = coords[3 * R + d] - coordIp;
+      asq += areav[3 * ip + d] * areav[3 * ip + d];
+      axdx += areav[3 * ip + d] * dxj;
+    }
+    const double inv_axdx = 1.0 / axdx;
+    const double pbc = pbcF[R] - (dynp ? dynp[ip] : 0.0);
+    const double pressureIp = 0.5 * (pressure[L] + pressure[R]);
+    double tmdot = -projTimeScale * (pbc - pressureIp) * asq * inv_axdx;
+    for (int d = 0; d < 3; ++d) {
+      const double coordIp = 0.5 * (coords[3 * R + d] + coords[3 * L + d]);
+      const double axj = areav[3 * ip + d];
+      const double dxj = coords[3 * R + d] - coordIp;
+      const double kxj = axj - asq * inv_axdx * dxj;
+      const double Gjp = Gpdx[3 * R + d];
+      tmdot += (density[R] * velocity[3 * R + d] + projTimeScale * Gjp) * axj -
+               projTimeScale * kxj * Gjp * nocFac;
+    }
+    mdot[ip] = tmdot;
+  }
+}
 
 // The uniform(lo, hi) draws of one default-seeded std::mt19937 with
 // std::uniform_real_distribution<double>, in order (the random inputs of

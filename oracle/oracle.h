@@ -120,6 +120,12 @@ void or_momentum_symmetry_local(int64_t nip, const int64_t* ipn, const double* c
 void or_scalar_open_local(int64_t nip, const int64_t* ipn, const double* q,
                           const double* q_bc, const double* mdot, double relax,
                           double* lhs, double* rhs);
+/* MdotOpenEdgeAlg.C:55-150: open mass flow rate per face IP */
+void or_mdot_open(int64_t nip, const int64_t* ipn, const double* coords,
+                  const double* velocity, const double* dpdx, const double* density,
+                  const double* pressure, const double* pressure_bc, const double* udiag,
+                  const double* areav, const double* dynp, double noc_fac,
+                  double pstab_fac, double* mdot);
 /* default-seeded std::mt19937 uniform(lo[i], hi[i]) draws, in order */
 void or_mt19937_uniform(int n, const double* lo, const double* hi, double* out);
 
@@ -209,8 +215,11 @@ typedef struct or_solve_report {
 } or_solve_report;
 
 /* precond: 0 none, 1 Jacobi, 2 symmetric Gauss-Seidel in the row order
- * given by `order` (NULL = natural order). method: 0 GMRES(kspace), 1 CG.
- * history (optional, capacity max_iters+1) gets ||r_k||/||r_0||. */
+ * given by `order` (NULL = natural order). method: 0 GMRES(kspace), 1 CG,
+ * 3 BiCGStab, 4 TFQMR (Belos "bicgstab" / "tfqmr", the strings
+ * src/LinearSolver.C:114 passes to the Belos factory; right preconditioned).
+ * history (optional, capacity max_iters+1) gets ||r_k||/||r_0|| (TFQMR:
+ * its residual bound sqrt(k+1) tau_k / ||r_0||). */
 int or_solve(int64_t nrows, const int64_t* row_ptr, const int32_t* col_idx,
              const double* vals, const double* b, double* x, int method,
              int precond, const int64_t* order, int kspace, int max_iters,

@@ -348,3 +348,15 @@ def mt19937_uniform(bounds):
     lib().or_mt19937_uniform(C.c_int(len(bounds)), _p(lo, C.c_double), _p(hi, C.c_double),
                              _p(out, C.c_double))
     return out
+
+
+def mdot_open(ipn, coords, vel, dpdx, density, pressure, pressure_bc, udiag, areav, dynp=None, noc_fac=1.0,
+              pstab_fac=1.0):
+    """Open mass flow rate per face IP (MdotOpenEdgeAlg)."""
+    ipn = _i64(ipn)
+    out = np.zeros(ipn.shape[0])
+    keep = [None if a is None else _f64(a) for a in (coords, vel, dpdx, density, pressure, pressure_bc, udiag,
+                                                     areav, dynp)]
+    lib().or_mdot_open(C.c_int64(ipn.shape[0]), _p(ipn, C.c_int64), *[_p(a, C.c_double) for a in keep],
+                       C.c_double(noc_fac), C.c_double(pstab_fac), _p(out, C.c_double))
+    return out

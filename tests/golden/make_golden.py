@@ -23,6 +23,8 @@ Sources (paths within the nalu-wind tree):
       and penalty factor 2, dense 24x24 in element-node order
   unit_tests/edge_kernels/UnitTestScalarOpenEdge.C      scalar open flux with
       relaxation 0.5 and mt19937-drawn inputs (closed-form expectation)
+  unit_tests/ngp_algorithms/UnitTestMdotAlg.C           open mass flow rate on the
+      z+ side and the open mass-flow correction
 """
 from __future__ import annotations
 
@@ -124,6 +126,20 @@ def main(ref: Path, out: Path) -> None:
                  'relaxFactorMap_["turbulent_ke"] = 0.5', "(-mdotVal * tkeVal) : (-mdotVal * bcTkeVal)",
                  "(mdotVal * 2.0) : 0.0"):
         assert frag in so, frag
+    md = (ref / "unit_tests/ngp_algorithms/UnitTestMdotAlg.C").read_text()
+    i0 = md.index("NGP_mdot_open_edge")
+    blk = md[i0:]
+    for frag in ('field_fill(1.0, *density_)', 'field_fill(1.0, *velocity_)', 'field_fill(0.0, *pressure_)',
+                 'field_fill(0.0, *dpdx_)', 'get_part("surface_6")', "activateOpenMdotCorrection_ = true",
+                 "EXPECT_NEAR(mdotDriver.mdot_open(), 1.0, 1.0e-15)"):
+        assert frag in blk, frag
+    g["mdot_open_hex8_zplus"] = {"density": 1.0, "velocity": 1.0, "pstab_fac": 0.0, "mdot_open": 1.0}
+    blk = md[md.index("NGP_mdot_open_correction"):]
+    for frag in ("mdotInflow = -124.0", "mdotOpen = 100.0", "(mdotInflow + mdotOpen) / 24.0",
+                 "-mdotCorrection * 4.0", 'get_part("surface_5")', "field_fill(0.0, *openMassFlowRate_)"):
+        assert frag in blk, frag
+    g["mdot_open_correction_hex8"] = {"inflow": -124.0, "open": 100.0, "ip_count": 24, "side_ips": 4,
+                                      "correction": -1.0, "post": 4.0}
     g["scalar_open_quad4"] = {"draws": [[1.0, 2.0], [1.0, 2.0], [-1.0, 1.0]], "relax": 0.5, "nodes": 4}
 
     assert len(g["continuity_hex8"]["lhs"]) == 64 and len(g["momentum_hex8"]["lhs"]) == 576

@@ -247,3 +247,67 @@ def test_side_set_errors(nw):
     empty = ls.sideset(np.zeros((0, 2), np.int64))
     assert empty.sizes() == (0, 0)
     ls.assemble_scalar_open(empty, nw.ScalarOpenFields(z.data_ptr(), z.data_ptr(), z.data_ptr()), relax=1.0)
+
+
+@pytest.mark.parametrize("kind", ["hex", "tets", "periodic"])
+def test_open_mdot_matches_oracle(nw, orc, kind):
+    import torch
+    mesh = _mesh(nw, kind)
+    rng = np.random.default_rng(16)
+    f = _node_fields(mesh, rng)
+    ipn, area = mesh.face_ips(("z-", "z+") if kind == "periodic" else SIDES)
+    dynp = rng.normal(0, 0.1, len(ipn))
+    ls = _system(nw, mesh, 1)
+    ss = ls.sideset(ipn)
+    d = {k: dev(v) for k, v in dict(f, area=area, dynp=dynp).items()}
+    fld = nw.ContinuityOpenFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dpdx", "density", "pressure",
+                                                               "pressure_bc", "udiag", "area", "dynp")))
+    for pstab in (1.0, 0.0):
+        md = torch.zeros(len(ipn), dtype=torch.float64, device="cuda")
+        total = ls.open_mdot(ss, fld, md, noc_fac=1.0, pstab_fac=pstab)
+        ref = orc.mdot_open(ipn, f["coords"], f["velocity"], f["dpdx"], f["density"], f["pressure"],
+                            f["pressure_bc"], f["udiag"], area, dynp, noc_fac=1.0, pstab_fac=pstab)
+        got = md.cpu().numpy()
+        # running magnitude of each IP's formula
+        R, L = ipn[:, 0], ipn[:, 1]
+        A = np.abs(area)
+        pts = pstab / np.abs(f["udiag"][R])
+        dx = 0.5 * np.abs(f["coords"][R] - f["coords"][L])
+        asq = (A * A).sum(1)
+        axdx = np.abs(np.einsum("id,id->i", area, 0.5 * (f["coords"][R] - f["coords"][L])))
+        G = np.abs(f["dpdx"][R])
+        S = pts * (np.abs(f["pressure_bc"][R]) + np.abs(dynp) + np.abs(f["pressure"][R]) + np.abs(f["pressure"][L])) \
+            * asq / axdx + ((np.abs(f["density"][R, None] * f["velocity"][R]) + pts[:, None] * G) * A).sum(1) \
+            + (pts[:, None] * (A + asq[:, None] / axdx[:, None] * dx) * G).sum(1)
+        check_close(got, ref, S, "open mdot")
+        assert abs(total - got.sum()) <= 1e-12 * S.sum()
+        # deterministic: a second call gives the same bits
+        md2 = torch.zeros_like(md)
+        assert ls.open_mdot(ss, fld, md2, noc_fac=1.0, pstab_fac=pstab) == total
+        assert torch.equal(md, md2)
+
+
+def test_open_mdot_golds_on_the_gpu(nw, golds):
+    import torch
+    mesh = nw.Mesh(1, 1, 1)
+    g = golds["mdot_open_hex8_zplus"]
+    ipn, area = mesh.face_ips(("z+",))
+    ls = _system(nw, mesh, 1)
+    ss = ls.sideset(ipn)
+    N = 8
+    d = {k: dev(v) for k, v in dict(coords=mesh.coords, velocity=np.full((N, 3), g["velocity"]),
+                                     dpdx=np.zeros((N, 3)), density=np.full(N, g["density"]), p=np.zeros(N),
+                                     pbc=np.zeros(N), udiag=np.ones(N), area=area).items()}
+    fld = nw.ContinuityOpenFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dpdx", "density", "p", "pbc",
+                                                               "udiag", "area")), None)
+    md = torch.zeros(len(ipn), dtype=torch.float64, device="cuda")
+    assert abs(ls.open_mdot(ss, fld, md, pstab_fac=g["pstab_fac"]) - g["mdot_open"]) <= 1e-15
+    # MdotAlgDriver's open correction on the z- side ("surface_5", 4 IPs),
+    # the open field zero: correction (inflow + open) / 24 IPs
+    c = golds["mdot_open_correction_hex8"]
+    corr = (c["inflow"] + c["open"]) / c["ip_count"]
+    assert corr == c["correction"]
+    ipn5, _ = mesh.face_ips(("z-",))
+    ss5 = ls.sideset(ipn5)
+    md5 = torch.zeros(len(ipn5), dtype=torch.float64, device="cuda")
+    assert abs(ls.correct_open_mdot(ss5, corr, md5) - c["post"]) <= 1e-15

@@ -157,3 +157,61 @@ def test_not_converged_status(nw):
     x = torch.zeros(nr, dtype=torch.float64, device="cuda")
     rep = ls.solve(x)
     assert rep.converged == 0 and rep.status == 5 and rep.iterations == 5
+
+
+@pytest.mark.parametrize("method", ["bicgstab", "tfqmr"])
+@pytest.mark.parametrize("pc", [0, 1, 2])
+def test_bicgstab_and_tfqmr_match_oracle(nw, orc, method, pc):
+    """Belos "bicgstab" / "tfqmr" on the 24x24x16 pressure Poisson system
+    (37-166 iterations). TFQMR: iteration counts within one, the first 30
+    history entries to 1e-8 relative, solution to 1e-7 relative. BiCGStab
+    amplifies a change of summation order by about 2.5x per iteration (the
+    oracle run on 1 and on 7 threads differs by 3e-8 at iteration 25 and by
+    up to 5 iterations in the count), so for it: the first 15 entries to
+    1e-8, the count within 5% + 2, the solution to 1e-5 relative."""
+    import torch
+    m = {"bicgstab": nw.BICGSTAB, "tfqmr": nw.TFQMR}[method]
+    ls, case = _poisson_system(nw)
+    ls.set_solver_cfg(nw.solver_cfg(method=m, preconditioner=pc, kspace=50, max_iterations=3000, tolerance=1e-9))
+    nr, _ = ls.sizes()
+    x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    assert rep.converged == 1 and rep.status == 0
+    rp, ci = ls.graph()
+    vals, rhs = ls.to_host()
+    order = ls.sgs_order()[0] if pc == 2 else None
+    xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=m, precond=pc, order=order, kspace=50,
+                             max_iters=3000, tol=1e-9)
+    strict = method == "tfqmr"
+    assert orep.converged == 1
+    assert abs(rep.iterations - orep.iterations) <= (1 if strict else 2 + 0.05 * orep.iterations)
+    k = min(len(ho), len(ls.residual_history()), 30 if strict else 15)
+    np.testing.assert_allclose(ls.residual_history()[:k], ho[:k], rtol=1e-8, atol=0)
+    xg = x.cpu().numpy()
+    assert np.linalg.norm(xg - xo) <= (1e-7 if strict else 1e-5) * np.linalg.norm(xo)
+    assert rep.final_abs_residual <= 1e-8 * rep.rhs_norm
+
+
+@pytest.mark.parametrize("method", ["bicgstab", "tfqmr"])
+@pytest.mark.parametrize("pc", [1, 2])
+def test_bicgstab_and_tfqmr_on_advection_diffusion(nw, orc, method, pc):
+    """The nonsymmetric 32^3 advection-diffusion system takes these methods
+    hundreds of erratic iterations, over which the GPU and CPU paths drift
+    apart in the last bits: both converge, with iteration counts within 10%,
+    and the GPU's true residual meets the tolerance's neighbourhood."""
+    import torch
+    m = {"bicgstab": nw.BICGSTAB, "tfqmr": nw.TFQMR}[method]
+    ls, case, d = _scalar_system(nw)
+    ls.set_solver_cfg(nw.solver_cfg(method=m, preconditioner=pc, kspace=50, max_iterations=3000, tolerance=1e-9))
+    nr, _ = ls.sizes()
+    x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    assert rep.converged == 1 and rep.status == 0
+    rp, ci = ls.graph()
+    vals, rhs = ls.to_host()
+    order = ls.sgs_order()[0] if pc == 2 else None
+    xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=m, precond=pc, order=order, kspace=50,
+                             max_iters=3000, tol=1e-9)
+    assert orep.converged == 1
+    assert abs(rep.iterations - orep.iterations) <= max(2, 0.1 * orep.iterations)
+    assert rep.final_abs_residual <= 1e-8 * rep.rhs_norm
