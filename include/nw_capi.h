@@ -221,6 +221,18 @@ nw_status nw_assemble_continuity_edges_noalloc(const nw_linsys* ls,
 nw_status nw_assemble_momentum_edges(nw_linsys* ls,
                                      const nw_momentum_fields* f,
                                      const nw_momentum_opts* o);
+/* The same assembly in two parts, for callers that stream the edge inputs
+ * in while earlier edges assemble (the reference walks its edge buckets one
+ * by one, AssembleEdgeSolverAlgorithm::execute): the edge phase over edges
+ * [edge_begin, edge_end) of the graph's edge list (it reads area, mdot and
+ * pecfac of those edges only, and every node field), then, once every edge
+ * has been covered exactly once, the row phase, which adds the result into
+ * the CSR values and rhs. Both are ordered on the handle's stream; the sum
+ * equals nw_assemble_momentum_edges bit for bit. */
+nw_status nw_assemble_momentum_edge_range(nw_linsys* ls, const nw_momentum_fields* f,
+                                          const nw_momentum_opts* o, int64_t edge_begin,
+                                          int64_t edge_end);
+nw_status nw_assemble_momentum_rows(nw_linsys* ls, const nw_momentum_opts* o);
 
 /* LinearSystem::sumInto, host-vector overload (include/LinearSystem.h:
  * 167-173): one entity block. nodes (host, n_ent) are node indices; rhs

@@ -157,6 +157,9 @@ SIGNATURES = {
     "nw_assemble_continuity_edges": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
                                                C.POINTER(ContinuityOpts)]),
     "nw_assemble_momentum_edges": (C.c_int, [C.c_void_p, C.POINTER(MomentumFields), C.POINTER(MomentumOpts)]),
+    "nw_assemble_momentum_edge_range": (C.c_int, [C.c_void_p, C.POINTER(MomentumFields), C.POINTER(MomentumOpts),
+                                                  C.c_int64, C.c_int64]),
+    "nw_assemble_momentum_rows": (C.c_int, [C.c_void_p, C.POINTER(MomentumOpts)]),
     "nw_assemble_continuity_edges_noalloc": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
                                                        C.POINTER(ContinuityOpts), C.c_void_p, C.c_void_p]),
     "nw_linsys_sum_into": (C.c_int, [C.c_void_p, C.c_int, _I64P, _DP, _DP]),
@@ -352,6 +355,15 @@ class LinearSystem:
 
     def assemble_momentum(self, f: MomentumFields, o: MomentumOpts) -> None:
         check(self.lib.nw_assemble_momentum_edges(self.h, C.byref(f), C.byref(o)))
+
+    def assemble_momentum_range(self, fields: "MomentumFields", opts: "MomentumOpts", edge_begin: int,
+                                edge_end: int) -> None:
+        """Edge phase over edges [edge_begin, edge_end); finish with assemble_momentum_rows."""
+        check(self.lib.nw_assemble_momentum_edge_range(self.h, C.byref(fields), C.byref(opts), edge_begin,
+                                                       edge_end))
+
+    def assemble_momentum_rows(self, opts: "MomentumOpts") -> None:
+        check(self.lib.nw_assemble_momentum_rows(self.h, C.byref(opts)))
 
     def sum_into(self, nodes, rhs, lhs) -> None:
         nodes = np.ascontiguousarray(nodes, np.int64)

@@ -322,7 +322,7 @@ struct MomentumDD {
 
 template <bool LIMITER, bool DIVU>
 __global__ void __launch_bounds__(kThreads, 4)
-    momentum_edge_k(int64_t E, const int2* __restrict__ edges,
+    momentum_edge_k(int64_t E, int64_t e0, int64_t e1, const int2* __restrict__ edges,
                     const double* __restrict__ coords,
                     const double* __restrict__ vel,
                     const double* __restrict__ dudx,
@@ -332,8 +332,8 @@ __global__ void __launch_bounds__(kThreads, 4)
                     const double* __restrict__ mdotA,
                     const double* __restrict__ pecA, MomentumDD c,
                     dd* __restrict__ buf) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= E) return;
+  const int64_t e = e0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= e1) return;
   const int2 lr = edges[e];
   const int64_t L = lr.x, R = lr.y;
   dd av[3], dx[3], uL[3], uR[3];
@@ -714,10 +714,10 @@ void launch_continuity_edges(cudaStream_t s, int64_t E, const int2* edges,
   launch_continuity_edges(s, E, 0, edges, f, o, buf, nullptr);
 }
 
-void launch_momentum_edges(cudaStream_t s, int64_t E, const int2* edges,
+void launch_momentum_edges(cudaStream_t s, int64_t E, int64_t e0, int64_t e1, const int2* edges,
                            const nw_momentum_fields& f, const MomentumOpts& o,
                            double* buf) {
-  if (E == 0) return;
+  if (e1 <= e0) return;
   MomentumDD c;
   c.alpha = dd_param(o.alpha);
   c.alpha_upw = dd_param(o.alpha_upw);
@@ -730,8 +730,8 @@ void launch_momentum_edges(cudaStream_t s, int64_t E, const int2* edges,
   dd* b = reinterpret_cast<dd*>(buf);
   const bool lim = o.use_limiter != 0, divu = o.include_div_u != 0.0;
 #define NW_MOM(LIM, DIV)                                                     \
-  momentum_edge_k<LIM, DIV><<<grid_for(E), kThreads, 0, s>>>(                \
-      E, edges, f.coords, f.velocity, f.dudx, f.viscosity, f.mask, f.area,   \
+  momentum_edge_k<LIM, DIV><<<grid_for(e1 - e0), kThreads, 0, s>>>(        \
+      E, e0, e1, edges, f.coords, f.velocity, f.dudx, f.viscosity, f.mask, f.area,   \
       f.mdot, f.pecfac, c, b)
   if (lim && divu) NW_MOM(true, true);
   else if (lim) NW_MOM(true, false);

@@ -32,7 +32,9 @@ void launch_continuity_edges(cudaStream_t s, int64_t E, int64_t N,
                              const ContinuityOpts& o, double* buf,
                              double* nodebuf);
 constexpr int kContinuityNodeStride = 8;
-void launch_momentum_edges(cudaStream_t s, int64_t E, const int2* edges,
+// Edge phase of the momentum assembly over edges [e0, e1) of E (the
+// coefficient buffer is laid out with stride E).
+void launch_momentum_edges(cudaStream_t s, int64_t E, int64_t e0, int64_t e1, const int2* edges,
                            const nw_momentum_fields& f, const MomentumOpts& o,
                            double* buf);
 // kind 0 scalar, 1 continuity, 2 momentum (3 dof). smem_bytes: staging

@@ -410,31 +410,63 @@ nw_status nw_assemble_continuity_edges(nw_linsys* ls,
   });
 }
 
+static void check_momentum_args(const nw_linsys* ls, const nw_momentum_fields* f,
+                                const nw_momentum_opts* o) {
+  need_finalized(ls);
+  if (ls->num_dof != 3) fail(NW_INVALID_ARG, "momentum assembly needs num_dof 3");
+  if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+  check_ptr(f->coords, "coords");
+  check_ptr(f->velocity, "velocity");
+  check_ptr(f->dudx, "dudx");
+  check_ptr(f->viscosity, "viscosity");
+  check_ptr(f->density, "density");
+  check_ptr(f->mask, "mask");
+  check_ptr(f->area, "area");
+  check_ptr(f->mdot, "mdot");
+  check_ptr(f->pecfac, "pecfac");
+  if (!(o->relax != 0.0)) fail(NW_INVALID_ARG, "relaxation factor is zero");
+}
+
+static void momentum_rows(nw_linsys* ls, double relax) {
+  launch_rows(ls->stream, 2, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
+              ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, ls->g.num_edges, relax,
+              ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[2]);
+  NW_CUDA(cudaGetLastError());
+  ls->pristine = false;
+}
+
 nw_status nw_assemble_momentum_edges(nw_linsys* ls, const nw_momentum_fields* f,
                                      const nw_momentum_opts* o) {
   return guard([&] {
-    need_finalized(ls);
-    if (ls->num_dof != 3) fail(NW_INVALID_ARG, "momentum assembly needs num_dof 3");
-    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
-    check_ptr(f->coords, "coords");
-    check_ptr(f->velocity, "velocity");
-    check_ptr(f->dudx, "dudx");
-    check_ptr(f->viscosity, "viscosity");
-    check_ptr(f->density, "density");
-    check_ptr(f->mask, "mask");
-    check_ptr(f->area, "area");
-    check_ptr(f->mdot, "mdot");
-    check_ptr(f->pecfac, "pecfac");
-    if (!(o->relax != 0.0)) fail(NW_INVALID_ARG, "relaxation factor is zero");
+    check_momentum_args(ls, f, o);
     begin_timing(ls);
     const int64_t E = ls->g.num_edges;
-    launch_momentum_edges(ls->stream, E, ls->edges.p, *f, *o, ls->buf.p);
-    launch_rows(ls->stream, 2, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
-                ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, o->relax,
-                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[2]);
-    NW_CUDA(cudaGetLastError());
+    launch_momentum_edges(ls->stream, E, 0, E, ls->edges.p, *f, *o, ls->buf.p);
+    momentum_rows(ls, o->relax);
     end_timing(ls);
-    ls->pristine = false;
+  });
+}
+
+nw_status nw_assemble_momentum_edge_range(nw_linsys* ls, const nw_momentum_fields* f,
+                                          const nw_momentum_opts* o, int64_t edge_begin,
+                                          int64_t edge_end) {
+  return guard([&] {
+    check_momentum_args(ls, f, o);
+    const int64_t E = ls->g.num_edges;
+    if (edge_begin < 0 || edge_end > E || edge_begin > edge_end)
+      fail(NW_INVALID_ARG, "edge range out of bounds");
+    launch_momentum_edges(ls->stream, E, edge_begin, edge_end, ls->edges.p, *f, *o, ls->buf.p);
+    NW_CUDA(cudaGetLastError());
+  });
+}
+
+nw_status nw_assemble_momentum_rows(nw_linsys* ls, const nw_momentum_opts* o) {
+  return guard([&] {
+    need_finalized(ls);
+    if (ls->num_dof != 3) fail(NW_INVALID_ARG, "momentum assembly needs num_dof 3");
+    if (!o) fail(NW_INVALID_ARG, "null argument");
+    if (!(o->relax != 0.0)) fail(NW_INVALID_ARG, "relaxation factor is zero");
+    momentum_rows(ls, o->relax);
   });
 }
 

@@ -116,3 +116,36 @@ def test_single_edge_momentum(nw, orc):
     assert np.array_equal(rp, o["rp"]) and np.array_equal(ci, o["ci"])
     check_close(vals, o["vals"], o["vabs"], "values")
     check_close(rhs, o["rhs"], o["rabs"], "rhs")
+
+
+def test_momentum_in_edge_ranges_equals_one_call(nw):
+    """Edge phase over uneven edge ranges, then the row phase: the same
+    values and rhs, bit for bit, as one nw_assemble_momentum_edges call; the
+    range bounds are checked."""
+    import torch
+    case = nw.workload.lowmach_case(20, 16, 12, seed=2)
+    mesh = case.mesh
+    nd = case.node
+    host = dict(coords=mesh.coords, velocity=nd["velocity"], dudx=nd["dudx"], viscosity=nd["viscosity"],
+                density=nd["density"], mask=nd["mask"], area=mesh.area, mdot=case.edge["mdot"],
+                pecfac=case.edge["pecfac"])
+    d = {k: dev(v) for k, v in host.items()}
+    fm = nw.MomentumFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dudx", "viscosity", "density", "mask",
+                                                        "area", "mdot", "pecfac")))
+    mo = case.opts["momentum"]
+    out = []
+    for split in (None, [0, 1, 777, 5000, mesh.num_edges]):
+        ls = nw.LinearSystem(3)
+        ls.build_edge_graph(mesh.num_nodes, mesh.edges)
+        ls.finalize()
+        ls.zero_system()
+        if split is None:
+            ls.assemble_momentum(fm, mo)
+        else:
+            for a, b in zip(split[:-1], split[1:]):
+                ls.assemble_momentum_range(fm, mo, a, b)
+            ls.assemble_momentum_rows(mo)
+            with pytest.raises(nw.NwError, match="edge range"):
+                ls.assemble_momentum_range(fm, mo, 5, mesh.num_edges + 1)
+        out.append(ls.to_host())
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
