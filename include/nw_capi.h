@@ -353,7 +353,8 @@ nw_status nw_learned_forward(nw_learned* net, nw_linsys* ls, const float* rc,
  * kind 0: out_bf16[m x 64] = relu(a_bf16[m x 128] b), b given transposed
  *         (64 x 128); kind 1: out_f32[m x 128] = a_bf16[m x 64] b^T, b
  *         row-major 128 x 64; kind 2: out_f32[128 x 64] = a_bf16[m x 128]^T
- *         b_bf16[m x 64]. */
+ *         b_bf16[m x 64]; kind 3: kind 0 on the tcgen05 tensor cores (TMEM
+ *         accumulator), NW_TIMEOUT if one of its bounded waits gave up. */
 nw_status nw_gemm_bf16(int kind, int64_t m, const void* a, const void* b,
                        void* out);
 

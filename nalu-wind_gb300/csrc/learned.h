@@ -119,6 +119,11 @@ void save_params(const std::string& path, const std::vector<float>& p, uint64_t 
 void load_params(const std::string& path, std::vector<float>& p);
 
 // Kernel launchers used by the tests through the C ABI.
+// The same forward GEMM on the tcgen05 tensor cores (tc_gemm.cu); tc_status
+// reads and clears its timeout flag (non-zero: a wait gave up).
+void launch_gemm_fwd_tc(const uint16_t* a, const uint16_t* wt, uint16_t* out, int64_t m,
+                        int ldo, cudaStream_t s);
+int tc_status(cudaStream_t s);
 void launch_gemm_fwd(const uint16_t* a, const uint16_t* wt, uint16_t* out,
                      int64_t m, int ldo, cudaStream_t s);
 void launch_gemm_dx(const uint16_t* dz, const uint16_t* w, float* dx, int64_t m,

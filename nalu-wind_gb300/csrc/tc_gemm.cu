@@ -1,0 +1,227 @@
+// Forward layer GEMM of the learned preconditioner on the 5th-generation
+// tensor cores: out[r, 0:64] = relu(A[r, 0:128] . W), BF16 inputs, FP32
+// accumulation in tensor memory, BF16 output.
+//
+// One CTA of 4 warps per 128-row tile. The A tile (128 x 128) and W
+// (64 x 128, given transposed, so both operands are K-major) are staged in
+// shared memory in the no-swizzle canonical layout: 8-row x 16-byte core
+// matrices, K-adjacent cores 128 bytes apart (leading byte offset) and
+// 8-row groups 2048 bytes apart (stride byte offset). One elected thread
+// issues eight tcgen05.mma (M 128, N 64, K 16) into a 64-column TMEM
+// accumulator and commits them to an mbarrier; after the wait each warp
+// reads its 32 TMEM lanes (= rows) with tcgen05.ld, applies the ReLU and
+// stores BF16 rows. Every wait is bounded: on a timeout the kernel records
+// an error, waits once more (bounded) for its MMAs, frees its TMEM and
+// returns without writing.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "nw_internal.h"
+
+namespace nw {
+namespace {
+
+constexpr int kTileM = 128;
+constexpr int kN = 64;
+constexpr int kK = 128;
+constexpr int kABytes = kTileM * kK * 2;  // 32 KiB
+constexpr int kBBytes = kN * kK * 2;      // 16 KiB
+constexpr int kLbo = 128;                 // K-adjacent core matrices
+constexpr int kSbo = (kK / 8) * 128;      // 8-row groups (2048 B)
+constexpr int kSmem = kABytes + kBBytes + 1024 + 64;
+constexpr uint32_t kTmemCols = 64;
+constexpr int kWaitLimit = 1 << 20;
+
+__device__ int g_tc_status;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// tcgen05 shared-memory matrix descriptor: start address, leading and
+// stride byte offsets (all >> 4), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = uint64_t((addr >> 4) & 0x3FFFu);
+  d |= uint64_t((lbo >> 4) & 0x3FFFu) << 16;
+  d |= uint64_t((sbo >> 4) & 0x3FFFu) << 32;
+  d |= uint64_t(1) << 46;
+  return d;
+}
+
+// kind::f16 instruction descriptor: D FP32, A and B BF16, both K-major,
+// N = 64, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kN >> 3) << 17) |
+                            (uint32_t(kTileM >> 4) << 24);
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < kWaitLimit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16_relu(float a, float b) {
+  const __nv_bfloat16 x = __float2bfloat16_rn(fmaxf(a, 0.f));
+  const __nv_bfloat16 y = __float2bfloat16_rn(fmaxf(b, 0.f));
+  return uint32_t(__bfloat16_as_ushort(x)) | (uint32_t(__bfloat16_as_ushort(y)) << 16);
+}
+
+__global__ void __launch_bounds__(128)
+    gemm_fwd_tc_k(const uint16_t* __restrict__ a, const uint16_t* __restrict__ wt,
+                  uint16_t* __restrict__ out, int64_t m, int ldo) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint8_t* sA = base;
+  uint8_t* sB = base + kABytes;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sB + kBBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t r0 = int64_t(blockIdx.x) * kTileM;
+
+  // stage A (rows past m are zero) and W in the canonical layout
+  const uint4* a4 = reinterpret_cast<const uint4*>(a);
+  for (int q = tid; q < kTileM * (kK / 8); q += 128) {
+    const int row = q >> 4, kg = q & 15;
+    const int64_t gr = r0 + row;
+    const uint4 v = gr < m ? a4[gr * (kK / 8) + kg] : make_uint4(0, 0, 0, 0);
+    *reinterpret_cast<uint4*>(sA + (row >> 3) * kSbo + kg * kLbo + (row & 7) * 16) = v;
+  }
+  const uint4* w4 = reinterpret_cast<const uint4*>(wt);
+  for (int q = tid; q < kN * (kK / 8); q += 128) {
+    const int row = q >> 4, kg = q & 15;
+    *reinterpret_cast<uint4*>(sB + (row >> 3) * kSbo + kg * kLbo + (row & 7) * 16) = w4[q];
+  }
+  // generic-proxy shared stores become visible to the tensor cores
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t bar = smem_u32(mbar);
+
+  if (tid == 0) {
+    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+#pragma unroll
+    for (int k = 0; k < kK / 16; ++k) {
+      // K step of 16 = two core matrices along K
+      const uint64_t da = smem_desc(a0 + k * 2 * kLbo, kLbo, kSbo);
+      const uint64_t db = smem_desc(b0 + k * 2 * kLbo, kLbo, kSbo);
+      const uint32_t acc = k > 0 ? 1u : 0u;
+      asm volatile(
+          "{\n\t.reg .pred p;\n\t"
+          "setp.ne.b32 p, %4, 0;\n\t"
+          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+          "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+          : "memory");
+    }
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+        : "memory");
+  }
+  bool ok = mbar_wait(bar, 0);
+  if (!ok) {
+    atomicExch(&g_tc_status, 1);
+    ok = mbar_wait(bar, 0);  // let the MMAs drain before the TMEM is freed
+  }
+  ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld is warp-collective
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    uint32_t v[64];
+    const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16);
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+          "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+          "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+          "=r"(v[31])
+        : "r"(taddr));
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]),
+          "=r"(v[38]), "=r"(v[39]), "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]),
+          "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]), "=r"(v[48]), "=r"(v[49]),
+          "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]),
+          "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]),
+          "=r"(v[62]), "=r"(v[63])
+        : "r"(taddr + 32u));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    const int64_t r = r0 + warp * 32 + lane;
+    if (r < m) {
+      uint4* dst = reinterpret_cast<uint4*>(out + r * ldo);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        uint4 o;
+        o.x = pack_bf16_relu(__uint_as_float(v[8 * c + 0]), __uint_as_float(v[8 * c + 1]));
+        o.y = pack_bf16_relu(__uint_as_float(v[8 * c + 2]), __uint_as_float(v[8 * c + 3]));
+        o.z = pack_bf16_relu(__uint_as_float(v[8 * c + 4]), __uint_as_float(v[8 * c + 5]));
+        o.w = pack_bf16_relu(__uint_as_float(v[8 * c + 6]), __uint_as_float(v[8 * c + 7]));
+        dst[c] = o;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+}  // namespace
+
+void launch_gemm_fwd_tc(const uint16_t* a, const uint16_t* wt, uint16_t* out, int64_t m,
+                        int ldo, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    NW_CUDA(cudaFuncSetAttribute(gemm_fwd_tc_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kSmem));
+    attr = true;
+  }
+  if (m <= 0) return;
+  const unsigned grid = unsigned((m + kTileM - 1) / kTileM);
+  gemm_fwd_tc_k<<<grid, 128, kSmem, s>>>(a, wt, out, m, ldo);
+  NW_CUDA(cudaGetLastError());
+}
+
+// Reads and clears the timeout flag of the tensor-core kernels (stream
+// ordered; synchronises the stream).
+int tc_status(cudaStream_t s) {
+  int v = 0;
+  NW_CUDA(cudaMemcpyFromSymbolAsync(&v, g_tc_status, sizeof(int), 0, cudaMemcpyDeviceToHost, s));
+  const int zero = 0;
+  NW_CUDA(cudaMemcpyToSymbolAsync(g_tc_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s));
+  NW_CUDA(cudaStreamSynchronize(s));
+  return v;
+}
+
+}  // namespace nw

@@ -52,6 +52,28 @@ def test_bf16_gemms_match_torch(nw, m):
     assert bool(((dw - ref).abs() <= 1e-5 * (a.float().abs().T @ dz.float().abs()) + 1e-30).all())
 
 
+@pytest.mark.parametrize("m", [1, 127, 128, 129, 5003, 65553])
+def test_tcgen05_forward_gemm_matches_torch_and_mma_sync(nw, m):
+    """The tensor-core (tcgen05, TMEM accumulator) forward layer GEMM: within
+    BF16 rounding of torch's FP32 product, on full and ragged 128-row tiles;
+    and against the mma.sync kernel, which differs at most by the BF16
+    rounding of FP32 sums taken in another order."""
+    import torch
+    rng = np.random.default_rng(100 + m)
+    a = _bf16_tensor(rng.normal(size=(m, 128)))
+    wt = _bf16_tensor(rng.normal(size=(64, 128)) * 0.1)
+    out = torch.full((m, 64), 7.0, dtype=torch.bfloat16, device="cuda")
+    nw.gemm_bf16(3, m, a, wt, out)
+    ref = a.float() @ wt.float().T
+    scale = a.float().abs() @ wt.float().abs().T
+    err = (out.float() - torch.relu(ref)).abs()
+    assert bool((err <= 2.0 ** -7 * ref.abs() + 1e-5 * scale).all())
+    out0 = torch.empty_like(out)
+    nw.gemm_bf16(0, m, a, wt, out0)
+    d = (out.float() - out0.float()).abs()
+    assert bool((d <= 2.0 ** -7 * out0.float().abs() + 1e-5 * scale).all())
+
+
 def _poisson(nw, shape, seed=3, stretch=1.04, jitter=0.0, rhs_seed=None):
     return nw.workload.poisson_system(shape, seed=seed, stretch=stretch, jitter=jitter, rhs_seed=rhs_seed)
 
