@@ -972,9 +972,11 @@ SolveResult KrylovSolver::solve(const nw_solver_cfg& cfg, double tol,
   else
     r = gmres(cfg, tol, pc, b, x, cfg.method == NW_FGMRES || pc.kind == NW_PC_LEARNED, s);
   // The learned preconditioner is judged by the FP64 residual: if the
-  // flexible solve fails (no convergence, breakdown, non-finite values)
-  // the same solve is repeated with plain symmetric Gauss-Seidel.
-  if (pc.kind == NW_PC_LEARNED && !r.converged && std::isfinite(r.bnorm)) {
+  // flexible solve fails (no convergence, breakdown, non-finite values, or
+  // a tensor-core wait of the network that gave up) the same solve is
+  // repeated with plain symmetric Gauss-Seidel.
+  const bool tc_timeout = pc.kind == NW_PC_LEARNED && tc_status(s) != 0;
+  if (pc.kind == NW_PC_LEARNED && (!r.converged || tc_timeout) && std::isfinite(r.bnorm)) {
     Precond sgs = pc;
     sgs.kind = NW_PC_SGS;
     const SolveResult first = r;

@@ -1412,6 +1412,7 @@ nw_status nw_learned_train(nw_learned* net, nw_linsys* ls, int epochs, int batch
       last = sum / L.npairs;
     }
     NW_CUDA(cudaStreamSynchronize(s));
+    if (tc_status(s)) fail(NW_TIMEOUT, "tensor-core GEMM wait timed out during training");
     if (loss) *loss = last;
   });
 }
@@ -1431,6 +1432,7 @@ nw_status nw_learned_evaluate(nw_learned* net, nw_linsys* ls, double* loss) {
       sum += L.forward_backward(cl, L.sys_wgt[sys]->p, L.sys_dinv[sys]->p, L.pair_rc[p]->p,
                                 L.pair_ea[p], L.pair_ca[p], ls->stream, false);
     }
+    if (tc_status(ls->stream)) fail(NW_TIMEOUT, "tensor-core GEMM wait timed out");
     *loss = sum / L.npairs;
   });
 }
@@ -1452,6 +1454,7 @@ nw_status nw_learned_loss_grad(nw_learned* net, nw_linsys* ls, const float* rc, 
       NW_CUDA(cudaStreamSynchronize(ls->stream));
     }
     NW_CUDA(cudaMemsetAsync(L.grads.p, 0, kNumParams * 4, ls->stream));
+    if (tc_status(ls->stream)) fail(NW_TIMEOUT, "tensor-core GEMM wait timed out");
   });
 }
 
@@ -1463,7 +1466,7 @@ nw_status nw_learned_forward(nw_learned* net, nw_linsys* ls, const float* rc, fl
     CoarseLevel& cl = *ls->coarse;
     cl.refresh(ls->values.p, ls->stream);
     net->net.forward(cl, cl.wgt.p, cl.dinv.p, rc, ec, ls->stream);
-    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    if (tc_status(ls->stream)) fail(NW_TIMEOUT, "tensor-core GEMM wait timed out");
   });
 }
 
