@@ -2,17 +2,18 @@
 // tensor cores: out[r, 0:64] = relu(A[r, 0:128] . W), BF16 inputs, FP32
 // accumulation in tensor memory, BF16 output.
 //
-// One CTA of 4 warps per 128-row tile. The A tile (128 x 128) and W
-// (64 x 128, given transposed, so both operands are K-major) are staged in
-// shared memory in the no-swizzle canonical layout: 8-row x 16-byte core
-// matrices, K-adjacent cores 128 bytes apart (leading byte offset) and
-// 8-row groups 2048 bytes apart (stride byte offset). One elected thread
-// issues eight tcgen05.mma (M 128, N 64, K 16) into a 64-column TMEM
-// accumulator and commits them to an mbarrier; after the wait each warp
-// reads its 32 TMEM lanes (= rows) with tcgen05.ld, applies the ReLU and
-// stores BF16 rows. Every wait is bounded: on a timeout the kernel records
-// an error, waits once more (bounded) for its MMAs, frees its TMEM and
-// returns without writing.
+// Persistent CTAs of 4 warps (two per SM) walk the 128-row tiles. A tile of
+// A (128 x 128) and W (64 x 128, given transposed, so both operands are
+// K-major) sit in shared memory in the no-swizzle canonical layout: 8-row x
+// 16-byte core matrices, K-adjacent cores 128 bytes apart (leading byte
+// offset) and 8-row groups 2048 bytes apart (stride byte offset), written
+// by 16-byte cp.async copies; the next tile is copied into a second buffer
+// while the current one computes. One thread issues eight tcgen05.mma
+// (M 128, N 64, K 16) into a 64-column TMEM accumulator and commits them to
+// an mbarrier; after the wait each warp reads its 32 TMEM lanes (= rows)
+// with tcgen05.ld, applies the ReLU and stores BF16 rows. Every wait is
+// bounded: on a timeout the kernel records an error, waits once more
+// (bounded) for its MMAs, stops, frees its TMEM and returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -30,7 +31,7 @@ constexpr int kABytes = kTileM * kK * 2;  // 32 KiB
 constexpr int kBBytes = kN * kK * 2;      // 16 KiB
 constexpr int kLbo = 128;                 // K-adjacent core matrices
 constexpr int kSbo = (kK / 8) * 128;      // 8-row groups (2048 B)
-constexpr int kSmem = kABytes + kBBytes + 1024 + 64;
+constexpr int kSmem = 2 * kABytes + kBBytes + 128 + 64;
 constexpr uint32_t kTmemCols = 64;
 constexpr int kWaitLimit = 1 << 20;
 
@@ -76,34 +77,54 @@ __device__ __forceinline__ uint32_t pack_bf16_relu(float a, float b) {
   return uint32_t(__bfloat16_as_ushort(x)) | (uint32_t(__bfloat16_as_ushort(y)) << 16);
 }
 
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+
+// One 128-row tile of A into a shared buffer in the canonical layout; rows
+// past m are zero-filled (source size 0, nothing is read).
+__device__ __forceinline__ void load_tile(uint32_t dst, const uint16_t* __restrict__ a, int64_t r0,
+                                          int64_t m, int tid) {
+#pragma unroll
+  for (int i = 0; i < kTileM * (kK / 8) / 128; ++i) {
+    const int q = tid + 128 * i;
+    const int row = q >> 4, kg = q & 15;
+    const int64_t gr = r0 + row;
+    const bool in = gr < m;
+    cp_async16(dst + (row >> 3) * kSbo + kg * kLbo + (row & 7) * 16,
+               in ? static_cast<const void*>(a + gr * kK + kg * 8) : static_cast<const void*>(a),
+               in ? 16u : 0u);
+  }
+}
+
+// Persistent CTAs over 128-row tiles: W is staged once per CTA, the next
+// tile's A is copied (cp.async) into the other shared buffer while the
+// current tile's MMAs and epilogue run.
 __global__ void __launch_bounds__(128)
     gemm_fwd_tc_k(const uint16_t* __restrict__ a, const uint16_t* __restrict__ wt,
                   uint16_t* __restrict__ out, int64_t m, int ldo) {
   extern __shared__ uint8_t smem_raw[];
-  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                             ~uintptr_t(1023));
-  uint8_t* sA = base;
-  uint8_t* sB = base + kABytes;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(sB + kBBytes);
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
+                                             ~uintptr_t(127));
+  uint8_t* sB = base;
+  uint8_t* sA0 = base + kBBytes;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sA0 + 2 * kABytes);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t r0 = int64_t(blockIdx.x) * kTileM;
+  const int64_t ntiles = (m + kTileM - 1) / kTileM;
+  const uint32_t b0 = smem_u32(sB), a0 = smem_u32(sA0);
 
-  // stage A (rows past m are zero) and W in the canonical layout
-  const uint4* a4 = reinterpret_cast<const uint4*>(a);
-  for (int q = tid; q < kTileM * (kK / 8); q += 128) {
+  // W (64 x 128) and the first A tile form the first copy group
+#pragma unroll
+  for (int i = 0; i < kN * (kK / 8) / 128; ++i) {
+    const int q = tid + 128 * i;
     const int row = q >> 4, kg = q & 15;
-    const int64_t gr = r0 + row;
-    const uint4 v = gr < m ? a4[gr * (kK / 8) + kg] : make_uint4(0, 0, 0, 0);
-    *reinterpret_cast<uint4*>(sA + (row >> 3) * kSbo + kg * kLbo + (row & 7) * 16) = v;
+    cp_async16(b0 + (row >> 3) * kSbo + kg * kLbo + (row & 7) * 16, wt + q * 8, 16u);
   }
-  const uint4* w4 = reinterpret_cast<const uint4*>(wt);
-  for (int q = tid; q < kN * (kK / 8); q += 128) {
-    const int row = q >> 4, kg = q & 15;
-    *reinterpret_cast<uint4*>(sB + (row >> 3) * kSbo + kg * kLbo + (row & 7) * 16) = w4[q];
-  }
-  // generic-proxy shared stores become visible to the tensor cores
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (blockIdx.x < ntiles) load_tile(a0, a, int64_t(blockIdx.x) * kTileM, m, tid);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -121,33 +142,43 @@ __global__ void __launch_bounds__(128)
   const uint32_t tmem = *tmem_slot;
   const uint32_t bar = smem_u32(mbar);
 
-  if (tid == 0) {
-    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+  int it = 0;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+    const uint32_t abuf = a0 + uint32_t(it & 1) * kABytes;
+    const int64_t tn = t + gridDim.x;
+    if (tn < ntiles) load_tile(a0 + uint32_t((it + 1) & 1) * kABytes, a, tn * kTileM, m, tid);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 1;" ::: "memory");  // this tile (and W) landed
+    // the copies become visible to the tensor cores (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
 #pragma unroll
-    for (int k = 0; k < kK / 16; ++k) {
-      // K step of 16 = two core matrices along K
-      const uint64_t da = smem_desc(a0 + k * 2 * kLbo, kLbo, kSbo);
-      const uint64_t db = smem_desc(b0 + k * 2 * kLbo, kLbo, kSbo);
-      const uint32_t acc = k > 0 ? 1u : 0u;
+      for (int k = 0; k < kK / 16; ++k) {
+        // K step of 16 = two core matrices along K
+        const uint64_t da = smem_desc(abuf + k * 2 * kLbo, kLbo, kSbo);
+        const uint64_t db = smem_desc(b0 + k * 2 * kLbo, kLbo, kSbo);
+        const uint32_t acc = k > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+            : "memory");
+      }
       asm volatile(
-          "{\n\t.reg .pred p;\n\t"
-          "setp.ne.b32 p, %4, 0;\n\t"
-          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-          "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              bar)
           : "memory");
     }
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-        : "memory");
-  }
-  bool ok = mbar_wait(bar, 0);
-  if (!ok) {
-    atomicExch(&g_tc_status, 1);
-    ok = mbar_wait(bar, 0);  // let the MMAs drain before the TMEM is freed
-  }
-  ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld is warp-collective
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ok) {
+    const uint32_t parity = uint32_t(it & 1);
+    bool ok = mbar_wait(bar, parity);
+    if (!ok) {
+      atomicExch(&g_tc_status, 1);
+      ok = mbar_wait(bar, parity);  // let the MMAs drain before the TMEM is freed
+    }
+    if (!__syncthreads_and(ok)) break;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     uint32_t v[64];
     const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16);
     asm volatile(
@@ -173,7 +204,7 @@ __global__ void __launch_bounds__(128)
           "=r"(v[62]), "=r"(v[63])
         : "r"(taddr + 32u));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    const int64_t r = r0 + warp * 32 + lane;
+    const int64_t r = t * kTileM + warp * 32 + lane;
     if (r < m) {
       uint4* dst = reinterpret_cast<uint4*>(out + r * ldo);
 #pragma unroll
@@ -186,7 +217,12 @@ __global__ void __launch_bounds__(128)
         dst[c] = o;
       }
     }
+    // every warp has read the accumulator before the next tile's MMAs
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
@@ -207,8 +243,16 @@ void launch_gemm_fwd_tc(const uint16_t* a, const uint16_t* wt, uint16_t* out, in
                                  kSmem));
     attr = true;
   }
+  static int ctas = 0;
+  if (!ctas) {
+    int dev = 0, sms = 0;
+    NW_CUDA(cudaGetDevice(&dev));
+    NW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    ctas = 2 * sms;  // two 80 KiB CTAs per SM
+  }
   if (m <= 0) return;
-  const unsigned grid = unsigned((m + kTileM - 1) / kTileM);
+  const int64_t tiles = (m + kTileM - 1) / kTileM;
+  const unsigned grid = unsigned(tiles < ctas ? tiles : ctas);
   gemm_fwd_tc_k<<<grid, 128, kSmem, s>>>(a, wt, out, m, ldo);
   NW_CUDA(cudaGetLastError());
 }
