@@ -407,7 +407,8 @@ def poisson_solves(nw, stream, args) -> dict:
            "rows": nr, "nnz": nnz, "tol": 1e-8,
            "mixed_precision": "FP64 outer residual / refinement; FP32 inner Krylov, SpMV and network "
                               "coarse step; BF16 Gauss-Seidel matrix values with FP32 accumulation"}
-    net, info = nw.training.train_poisson_network(stream=stream.cuda_stream)
+    net, info = nw.training.train_poisson_network(epochs=args.train_epochs, lr=args.train_lr,
+                                                  stream=stream.cuda_stream)
     res["training"] = info
     res["_net"] = net
     without = nw.Learned(seed=0)
@@ -510,16 +511,19 @@ def implicit_step(nw, stream, args) -> dict:
     """One implicit step on an unstructured mesh: a perturbed block of n^3
     hexes (n = 127: 2,097,152 nodes) split into 6 tets each, node ids
     randomly permuted, then that order RCM-renumbered; both orderings timed.
-    The step is the input producers (mass flow rate, nodal gradients of u
-    and p, Peclet factor), the momentum (3-dof) and continuity edge assembly,
-    then the continuity (pressure-Poisson) system solved to 1e-8 FP64 relative
-    residual by learned mixed FGMRES(30) and by plain FP64 GMRES(50) +
-    Jacobi. The network is trained first (untimed) on small tet systems."""
+    The step is the input producers (mass flow rate, open-boundary mass
+    flow rate, nodal gradients of u and p, Peclet factor), the momentum
+    (3-dof) and continuity edge assembly, the boundary face kernels (an open
+    boundary on the x+ side for both systems, symmetry on the y and z sides
+    for momentum), then the continuity (pressure-Poisson) system solved to
+    1e-8 FP64 relative residual by learned mixed FGMRES(30) and by plain FP64
+    GMRES(50) + Jacobi. The network is trained first (untimed) on small tet
+    systems."""
     import torch
     n = args.step_n
     res = {"workload": f"{n}^3-hex block, 6 tets per hex, 5 % jitter; random and RCM node orders",
-           "step": "producers (mdot, grad u, grad p, Peclet factor) + momentum and continuity assembly + "
-                   "continuity solve to 1e-8"}
+           "step": "producers (mdot, open mdot, grad u, grad p, Peclet factor) + momentum and continuity "
+                   "assembly + open (x+) and symmetry (y, z sides) boundary kernels + continuity solve to 1e-8"}
 
     def dev_t(a):
         return torch.from_numpy(np.ascontiguousarray(a)).cuda()
@@ -545,19 +549,37 @@ def implicit_step(nw, stream, args) -> dict:
         lsc = nw.LinearSystem(1, stream=stream.cuda_stream)
         lsc.build_edge_graph(mesh.num_nodes, mesh.edges)
         lsc.finalize()
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
         mo, co = case.opts["momentum"], case.opts["continuity"]
+        # boundaries: open on x+, symmetry on the y and z sides
+        ipn_o, area_o = mesh.face_ips(("x+",))
+        ipn_s, area_s = mesh.face_ips(("y-", "y+", "z-", "z+"))
+        ss_oc, ss_om, ss_s = lsc.sideset(ipn_o), lsm.sideset(ipn_o), lsm.sideset(ipn_s)
+        bd = {"area_o": dev_t(area_o), "area_s": dev_t(area_s), "pbc": dev_t(np.zeros(mesh.num_nodes)),
+              "omdot": torch.zeros(len(ipn_o), dtype=torch.float64, device="cuda")}
+        fco = nw.ContinuityOpenFields(*(d[k].data_ptr() for k in (
+            "coords", "velocity", "dpdx", "density", "pressure")), bd["pbc"].data_ptr(), d["udiag"].data_ptr(),
+            bd["area_o"].data_ptr(), None)
+        fmo = nw.MomentumOpenFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dudx", "viscosity")),
+                                    d["velocity"].data_ptr(), bd["area_o"].data_ptr(), bd["omdot"].data_ptr())
+        fms = nw.MomentumSymmetryFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dudx", "viscosity")),
+                                        bd["area_s"].data_ptr())
+        oco = nw.ContinuityOpenOpts(tau_scale=co.tau_scale, noc_fac=co.noc_fac, pstab_fac=1.0, mdot_corr=0.0,
+                                    solve_incompressible=co.solve_incompressible)
+        omo = nw.MomentumOpenOpts(include_div_u=mo.include_div_u, nf_entrain=0.0, entrainment=nw.ENTRAIN_COMPUTED)
+        osy = nw.MomentumSymmetryOpts(include_div_u=mo.include_div_u, penalty_factor=0.0)
         # input producers: mdot, nodal gradients of u and p, Peclet factor
         dv, ba = dev_t(mesh.dualvol), dev_t(mesh.bnd_area)
         pec_o = nw.PecletOpts(0, 1.0, 2.0, 4.0, 1e-16)
 
         def producers():
             lsc.compute_mdot(fc, d["mdot"], noc_fac=co.noc_fac, interp_together=co.interp_together)
+            lsc.open_mdot(ss_oc, fco, bd["omdot"], noc_fac=co.noc_fac, pstab_fac=1.0)
             lsc.nodal_gradient(d["velocity"], d["area"], dv, d["dudx"], bnd_area_dev=ba, dim1=3)
             lsc.nodal_gradient(d["pressure"], d["area"], dv, d["dpdx"], bnd_area_dev=ba, dim1=1)
             lsc.peclet_factor(d["coords"], d["density"], d["viscosity"], d["velocity"], d["pecfac"], opts=pec_o)
 
-        prod, mom, con = [], [], []
+        prod, mom, con, bnd = [], [], [], []
         for it in range(5):
             ev[0].record(stream)
             producers()
@@ -568,15 +590,22 @@ def implicit_step(nw, stream, args) -> dict:
             lsc.zero_system()
             lsc.assemble_continuity(fc, co)
             ev[3].record(stream)
+            lsm.assemble_momentum_open(ss_om, fmo, omo)
+            lsm.assemble_momentum_symmetry(ss_s, fms, osy)
+            lsc.assemble_continuity_open(ss_oc, fco, oco)
+            ev[4].record(stream)
             torch.cuda.synchronize()
             if it >= 2:
                 prod.append(ev[0].elapsed_time(ev[1]))
                 mom.append(ev[1].elapsed_time(ev[2]))
                 con.append(ev[2].elapsed_time(ev[3]))
+                bnd.append(ev[3].elapsed_time(ev[4]))
         nnz_m, nnz_c = lsm.sizes()[1], lsc.sizes()[1]
         r = {"nodes": mesh.num_nodes, "edges": mesh.num_edges, "nnz_momentum": nnz_m, "nnz_continuity": nnz_c,
+             "face_ips_open": len(ipn_o), "face_ips_symmetry": len(ipn_s),
              "producers_ms": round(float(np.mean(prod)), 4),
-             "momentum_ms": round(float(np.mean(mom)), 4), "continuity_ms": round(float(np.mean(con)), 4)}
+             "momentum_ms": round(float(np.mean(mom)), 4), "continuity_ms": round(float(np.mean(con)), 4),
+             "boundary_ms": round(float(np.mean(bnd)), 4)}
         r["assembly_gnnz_s"] = round((nnz_m + nnz_c) / ((r["momentum_ms"] + r["continuity_ms"]) * 1e-3) / 1e9, 3)
         nr = lsc.sizes()[0]
         for vname, learned, cfg in (
@@ -593,10 +622,11 @@ def implicit_step(nw, stream, args) -> dict:
             r[vname] = {"ms": round(rep.solve_ms, 2), "iterations": rep.iterations,
                         "rel_residual_fp64": rep.final_abs_residual / rep.rhs_norm,
                         "converged": bool(rep.converged), "fallback": bool(rep.fallback)}
-        asm = r["producers_ms"] + r["momentum_ms"] + r["continuity_ms"]
+        asm = r["producers_ms"] + r["momentum_ms"] + r["continuity_ms"] + r["boundary_ms"]
         r["step_ms_learned_mixed"] = round(asm + r["learned_mixed_fgmres30"]["ms"], 2)
         r["step_ms_plain_fp64"] = round(asm + r["plain_fp64_gmres50_jacobi"]["ms"], 2)
         res[name] = r
+        del ss_oc, ss_om, ss_s
         del lsm, lsc, d
         torch.cuda.empty_cache()
     return res
@@ -678,6 +708,8 @@ def main():
     ap.add_argument("--heldout", type=int, default=2, help="held-out 128^3 Poisson systems to solve")
     ap.add_argument("--step-n", type=int, default=127, help="hexes per side of the tet-mesh block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--train-epochs", type=int, default=100, help="training epochs of the Poisson network")
+    ap.add_argument("--train-lr", type=float, default=1e-3, help="Adam learning rate of the Poisson network")
     args = ap.parse_args()
     args.shape = tuple(args.shape)
     args.poisson_shape = tuple(args.poisson_shape)
