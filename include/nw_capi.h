@@ -49,7 +49,10 @@ enum {
   NW_PC_NONE = 0,
   NW_PC_JACOBI = 1, /* "jacobi" / "default": Ifpack2 Jacobi, 1 sweep */
   NW_PC_SGS = 2,    /* "sgs": symmetric Gauss-Seidel, 1 sweep, multicolour order */
-  NW_PC_LEARNED = 3 /* learned edge message-passing preconditioner (FGMRES) */
+  NW_PC_LEARNED = 3, /* learned edge message-passing preconditioner (FGMRES) */
+  NW_PC_SGS2 = 4     /* "sgs2": two-stage symmetric Gauss-Seidel, 1 sweep, row
+                        order, sgs2_inner_sweeps Jacobi-Richardson corrections
+                        per triangular solve */
 };
 /* Arithmetic of the solve. */
 enum {
@@ -70,6 +73,7 @@ typedef struct nw_solver_cfg {
   double final_tolerance; /* "final_tolerance", default = tolerance */
   int inner_kspace;       /* mixed: inner restart length */
   double inner_tolerance; /* mixed: relative reduction per inner solve */
+  int sgs2_inner_sweeps;  /* "inner_iterations" of sgs2, default 1 (values < 1 mean 1) */
 } nw_solver_cfg;
 
 /* Per-solve report: LinearSystem::linearSolveIterations / linearResidual /

@@ -23,7 +23,7 @@ NW_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "CUDA_ERROR", 3: "NOT_FINALIZED", 4: "NAN_DETECTED",
                 5: "NOT_CONVERGED", 6: "BREAKDOWN", 7: "TIMEOUT", 8: "NO_DEVICE", 9: "INTERNAL"}
 GMRES, CG, FGMRES, BICGSTAB, TFQMR = 0, 1, 2, 3, 4
-PC_NONE, PC_JACOBI, PC_SGS, PC_LEARNED = 0, 1, 2, 3
+PC_NONE, PC_JACOBI, PC_SGS, PC_LEARNED, PC_SGS2 = 0, 1, 2, 3, 4
 PREC_FP64, PREC_MIXED, PREC_MIXED_BF16 = 0, 1, 2
 
 
@@ -37,7 +37,7 @@ class SolverCfg(C.Structure):
     _fields_ = [("method", C.c_int), ("preconditioner", C.c_int), ("precision", C.c_int),
                 ("kspace", C.c_int), ("max_iterations", C.c_int), ("tolerance", C.c_double),
                 ("final_tolerance", C.c_double), ("inner_kspace", C.c_int),
-                ("inner_tolerance", C.c_double)]
+                ("inner_tolerance", C.c_double), ("sgs2_inner_sweeps", C.c_int)]
 
 
 class SolveReport(C.Structure):
@@ -272,11 +272,11 @@ def dptr(x) -> int:
 
 def solver_cfg(method=GMRES, preconditioner=PC_JACOBI, precision=PREC_FP64, kspace=50,
                max_iterations=50, tolerance=1e-4, final_tolerance=None, inner_kspace=0,
-               inner_tolerance=0.0) -> SolverCfg:
+               inner_tolerance=0.0, sgs2_inner_sweeps=1) -> SolverCfg:
     """TpetraLinearSolverConfig::load defaults (src/LinearSolverConfig.C:37-52)."""
     return SolverCfg(method, preconditioner, precision, kspace, max_iterations, tolerance,
                      tolerance if final_tolerance is None else final_tolerance, inner_kspace,
-                     inner_tolerance)
+                     inner_tolerance, sgs2_inner_sweeps)
 
 
 class LinearSystem:

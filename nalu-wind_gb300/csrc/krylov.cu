@@ -61,6 +61,49 @@ __global__ void __launch_bounds__(kBlock)
   if (lane == 0) y[row] = b ? XT(ACC(b[row]) - acc) : XT(acc);
 }
 
+// Two-stage Gauss-Seidel step: g_out = D^-1 (r - T g_in), T the strictly
+// lower (UPPER false) or upper part of each row in column order. LANES
+// threads per row.
+template <int LANES, bool UPPER, typename VT, typename T>
+__global__ void __launch_bounds__(kBlock)
+    ts_tri_k(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+             const VT* __restrict__ v, const T* __restrict__ rd, const T* __restrict__ r,
+             const T* __restrict__ gin, T* __restrict__ gout) {
+  const int64_t gt = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t row = gt / LANES;
+  const int lane = threadIdx.x % LANES;
+  if (row >= n) return;
+  T acc = 0;
+  for (int64_t p = rp[row] + lane; p < rp[row + 1]; p += LANES) {
+    const int64_t c = ci[p];
+    if (UPPER ? c > row : c < row) acc += T(v[p]) * gin[c];
+  }
+#pragma unroll
+  for (int off = LANES / 2; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off, LANES);
+  if (lane == 0) gout[row] = rd[row] * (r[row] - acc);
+}
+
+template <bool UPPER, typename VT, typename T>
+void ts_tri_launch(int lanes, int64_t n, const int64_t* rp, const int32_t* ci, const VT* v,
+                   const T* rd, const T* r, const T* gin, T* gout, cudaStream_t s) {
+  if (n == 0) return;
+  const unsigned grid = unsigned((n * lanes + kBlock - 1) / kBlock);
+  switch (lanes) {
+    case 4:
+      ts_tri_k<4, UPPER, VT, T><<<grid, kBlock, 0, s>>>(n, rp, ci, v, rd, r, gin, gout);
+      break;
+    case 8:
+      ts_tri_k<8, UPPER, VT, T><<<grid, kBlock, 0, s>>>(n, rp, ci, v, rd, r, gin, gout);
+      break;
+    case 16:
+      ts_tri_k<16, UPPER, VT, T><<<grid, kBlock, 0, s>>>(n, rp, ci, v, rd, r, gin, gout);
+      break;
+    default:
+      ts_tri_k<32, UPPER, VT, T><<<grid, kBlock, 0, s>>>(n, rp, ci, v, rd, r, gin, gout);
+      break;
+  }
+}
+
 template <typename VT, typename XT, typename ACC>
 void spmv_launch(int lanes, int64_t n, const int64_t* rp, const int32_t* ci,
                  const VT* v, const XT* x, const XT* b, XT* y,
@@ -534,6 +577,12 @@ __global__ void add_f32_k(int64_t n, const float* __restrict__ y,
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) x[i] += double(y[i]);
 }
+// y += x
+template <typename T>
+__global__ void axpy_t_k(int64_t n, const T* __restrict__ x, T* __restrict__ y) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += x[i];
+}
 // out = a x + b y (out may alias x or y)
 __global__ void lincomb_k(int64_t n, double a, const double* x, double b, const double* y, double* out) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -894,9 +943,45 @@ void KrylovSolver::learned_presmooth32(const float* x, float* y, cudaStream_t s)
 // sweep left a residual on), ec = Net(R r1), z2 = z1 + alpha P ec with the
 // energy-optimal alpha, then the post-smoothing z = z2 + SGS(x - A z2),
 // evaluated as one symmetric sweep starting from z2.
+// Two-stage symmetric Gauss-Seidel ("sgs2", Ifpack2 "Two-stage Symmetric
+// Gauss-Seidel", src/LinearSolverConfig.C:97-104), one sweep from zero:
+// y1 = (D + L)^-1 x and y = y1 + (D + U)^-1 (x - A y1), each triangular
+// solve replaced by g = D^-1 r followed by `inner` Jacobi-Richardson
+// corrections g <- D^-1 (r - T g) (Berger-Vergiat et al. 2021). Every pass
+// is a row-parallel CSR sweep; no colouring, no row dependences.
+template <typename VT, typename T>
+void KrylovSolver::sgs2(const VT* vals, const T* rd, const T* x, T* y, int inner, T* scratch,
+                        cudaStream_t s) const {
+  const int64_t n = A_.n;
+  T* g[2] = {scratch, scratch + n};
+  T* r1 = scratch + 2 * n;
+  auto tri = [&](bool upper, const T* r, T* out) {
+    jacobi_k<T><<<grid1(n), kBlock, 0, s>>>(n, rd, r, g[0]);
+    int cur = 0;
+    for (int k = 0; k < inner; ++k) {
+      if (upper)
+        ts_tri_launch<true, VT, T>(A_.lanes, n, A_.row_ptr, A_.col_idx, vals, rd, r, g[cur], g[1 - cur], s);
+      else
+        ts_tri_launch<false, VT, T>(A_.lanes, n, A_.row_ptr, A_.col_idx, vals, rd, r, g[cur], g[1 - cur], s);
+      cur = 1 - cur;
+    }
+    NW_CUDA(cudaMemcpyAsync(out, g[cur], n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  };
+  tri(false, x, y);
+  spmv_launch<VT, T, T>(A_.lanes, n, A_.row_ptr, A_.col_idx, vals, y, x, r1, s);  // r1 = x - A y
+  tri(true, r1, r1);
+  axpy_t_k<T><<<grid1(n), kBlock, 0, s>>>(n, r1, y);
+  NW_CUDA(cudaGetLastError());
+}
+
 void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
                              cudaStream_t s) {
   const int64_t n = A_.n;
+  if (pc.kind == NW_PC_SGS2) {
+    sgs2_32_.resize(size_t(3) * n);
+    sgs2<float, float>(vals32_.p, rdiag32_.p, x, y, pc.inner_sweeps, sgs2_32_.p, s);
+    return;
+  }
   if (pc.kind == NW_PC_SGS) {
     if (gs_bf16_)
       sgs<__nv_bfloat16, float>(gs_vals16_.p, rdiag32_.p, x, y, s);
@@ -951,6 +1036,11 @@ void KrylovSolver::apply_precond(const Precond& pc, const double* x, double* y,
   }
   if (pc.kind == NW_PC_SGS) {
     sgs<double, double>(gs_vals_.p, rdiag_.p, x, y, s);
+    return;
+  }
+  if (pc.kind == NW_PC_SGS2) {
+    sgs2_64_.resize(size_t(3) * A_.n);
+    sgs2<double, double>(A_.values, rdiag_.p, x, y, pc.inner_sweeps, sgs2_64_.p, s);
     return;
   }
   precond_apply_t<double, double>(pc, A_.n, A_.row_ptr, A_.col_idx, A_.values,

@@ -32,6 +32,7 @@ struct DevCsr {
 // Preconditioner applied inside the solver (right preconditioning).
 struct Precond {
   int kind = NW_PC_JACOBI;
+  int inner_sweeps = 1;  // NW_PC_SGS2: Jacobi-Richardson corrections per triangular solve
   // multicolour SGS: rows grouped by colour
   const int32_t* color_rows = nullptr;   // nrows, rows of colour 0, 1, ...
   std::vector<int64_t> color_ptr;        // host, ncolors + 1
@@ -140,6 +141,12 @@ class KrylovSolver {
   template <typename VT, typename T>
   void sgs(const VT* vals, const T* rd, const T* x, T* y, cudaStream_t s,
            bool from_guess = false, int sweep = 0) const;
+  // two-stage symmetric Gauss-Seidel (CSR, row order), scratch 3 n
+  template <typename VT, typename T>
+  void sgs2(const VT* vals, const T* rd, const T* x, T* y, int inner, T* scratch,
+            cudaStream_t s) const;
+  DeviceArray<double> sgs2_64_;
+  DeviceArray<float> sgs2_32_;
   void sgs_residual32(const float* x, const float* y, float* r, cudaStream_t s, int last) const;
   DeviceArray<float> diag32_;   // FP32 diagonal
   // FP32 copies for the inner solve of the mixed method

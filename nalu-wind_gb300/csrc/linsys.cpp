@@ -107,6 +107,7 @@ nw_solver_cfg default_cfg() {
   c.final_tolerance = 1e-4;
   c.inner_kspace = 0;
   c.inner_tolerance = 0;
+  c.sgs2_inner_sweeps = 1;
   return c;
 }
 
@@ -115,7 +116,7 @@ void check_cfg(const nw_solver_cfg& c) {
   if (c.max_iterations < 0) fail(NW_INVALID_ARG, "max_iterations < 0");
   if (!(c.tolerance >= 0.0)) fail(NW_INVALID_ARG, "tolerance < 0");
   if (c.method < NW_GMRES || c.method > NW_TFQMR) fail(NW_INVALID_ARG, "bad method");
-  if (c.preconditioner < NW_PC_NONE || c.preconditioner > NW_PC_LEARNED)
+  if (c.preconditioner < NW_PC_NONE || c.preconditioner > NW_PC_SGS2)
     fail(NW_INVALID_ARG, "bad preconditioner");
 }
 
@@ -599,6 +600,7 @@ nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
       fail(NW_INVALID_ARG, "NW_PC_LEARNED needs nw_linsys_attach_learned");
     ls->solver.refresh(ls->stream);
     ls->pc.kind = ls->cfg.preconditioner;
+    ls->pc.inner_sweeps = ls->cfg.sgs2_inner_sweeps > 0 ? ls->cfg.sgs2_inner_sweeps : 1;
     const double tol = final_iter ? ls->cfg.final_tolerance : ls->cfg.tolerance;
     cudaEvent_t a, b;
     NW_CUDA(cudaEventCreate(&a));
@@ -1054,12 +1056,14 @@ nw_status nw_linsys_precond_apply(nw_linsys* ls, int preconditioner,
   return guard([&] {
     need_finalized(ls);
     if (!x || !y) fail(NW_INVALID_ARG, "null vector");
-    if (preconditioner < NW_PC_NONE || preconditioner > NW_PC_SGS)
-      fail(NW_INVALID_ARG, "preconditioner must be none, jacobi or sgs");
+    if (preconditioner < NW_PC_NONE || preconditioner > NW_PC_SGS2 ||
+        preconditioner == NW_PC_LEARNED)
+      fail(NW_INVALID_ARG, "preconditioner must be none, jacobi, sgs or sgs2");
     materialize_zero(ls);
     ls->solver.refresh(ls->stream);
     Precond pc = ls->pc;
     pc.kind = preconditioner;
+    pc.inner_sweeps = ls->cfg.sgs2_inner_sweeps > 0 ? ls->cfg.sgs2_inner_sweeps : 1;
     ls->solver.apply_precond(pc, x, y, ls->stream);
   });
 }

@@ -990,6 +990,7 @@ struct Ctx {
   int nthreads;
   std::vector<double> diag;
   std::vector<int64_t> order;
+  int inner = 1;  // two-stage Gauss-Seidel: Jacobi-Richardson corrections
 };
 
 double dot(const Ctx& c, const double* a, const double* b) {
@@ -1001,10 +1002,43 @@ double dot(const Ctx& c, const double* a, const double* b) {
   return s;
 }
 
+// Two-stage triangular solve: g ~= (D + T)^-1 r with T the strictly lower
+// (upper = false) or upper part in row order, by `inner` Jacobi-Richardson
+// corrections g <- D^-1 (r - T g) of g = D^-1 r.
+void two_stage_tri(const Ctx& c, bool upper, const double* r, double* g) {
+  const int64_t n = c.n;
+  std::vector<double> prev(n);
+  for (int64_t i = 0; i < n; ++i) g[i] = r[i] / c.diag[i];
+  for (int k = 0; k < c.inner; ++k) {
+    std::copy(g, g + n, prev.begin());
+    for (int64_t i = 0; i < n; ++i) {
+      double s = r[i];
+      for (int64_t p = c.rp[i]; p < c.rp[i + 1]; ++p)
+        if (upper ? c.ci[p] > i : c.ci[p] < i) s -= c.v[p] * prev[c.ci[p]];
+      g[i] = s / c.diag[i];
+    }
+  }
+}
+
 // Ifpack2 Relaxation, 1 sweep, zero starting solution: Jacobi y = D^-1 x;
-// symmetric Gauss-Seidel = forward sweep then backward sweep over `order`.
+// symmetric Gauss-Seidel = forward sweep then backward sweep over `order`;
+// kind 4, two-stage symmetric Gauss-Seidel ("sgs2",
+// src/LinearSolverConfig.C:97-104): the forward sweep x1 = (D + L)^-1 b
+// and the backward correction x = x1 + (D + U)^-1 (b - A x1), each
+// triangular solve replaced by the two-stage approximation above
+// (Berger-Vergiat et al., "Two-stage Gauss-Seidel preconditioners and
+// smoothers for Krylov solvers on a GPU cluster", 2021).
 void precond(const Ctx& c, int kind, const double* x, double* y) {
   const int64_t n = c.n;
+  if (kind == 4) {
+    std::vector<double> r(n), h(n);
+    two_stage_tri(c, false, x, y);
+    or_spmv(n, c.rp, c.ci, c.v, y, r.data(), 1);
+    for (int64_t i = 0; i < n; ++i) r[i] = x[i] - r[i];
+    two_stage_tri(c, true, r.data(), h.data());
+    for (int64_t i = 0; i < n; ++i) y[i] += h[i];
+    return;
+  }
   if (kind == 0) {
     std::copy(x, x + n, y);
   } else if (kind == 1) {
@@ -1029,8 +1063,9 @@ extern "C" {
 
 void or_precond_apply(int64_t n, const int64_t* rp, const int32_t* ci,
                       const double* v, int kind, const int64_t* order,
-                      const double* x, double* y) {
+                      const double* x, double* y, int inner_sweeps) {
   Ctx c{n, rp, ci, v, 1, {}, {}};
+  c.inner = inner_sweeps;
   c.diag.assign(n, 0.0);
   for (int64_t i = 0; i < n; ++i)
     for (int64_t p = rp[i]; p < rp[i + 1]; ++p)
@@ -1047,8 +1082,10 @@ void or_precond_apply(int64_t n, const int64_t* rp, const int32_t* ci,
 int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
              const double* b, double* x, int method, int pc,
              const int64_t* order, int m, int maxit, double tol,
-             double* history, or_solve_report* rep, int nthreads) {
+             double* history, or_solve_report* rep, int nthreads,
+             int inner_sweeps) {
   Ctx c{n, rp, ci, v, nthreads > 0 ? nthreads : 1, {}, {}};
+  c.inner = inner_sweeps;
   c.diag.assign(n, 0.0);
   for (int64_t i = 0; i < n; ++i)
     for (int64_t p = rp[i]; p < rp[i + 1]; ++p)

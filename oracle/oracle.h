@@ -215,7 +215,9 @@ typedef struct or_solve_report {
 } or_solve_report;
 
 /* precond: 0 none, 1 Jacobi, 2 symmetric Gauss-Seidel in the row order
- * given by `order` (NULL = natural order). method: 0 GMRES(kspace), 1 CG,
+ * given by `order` (NULL = natural order), 4 two-stage symmetric
+ * Gauss-Seidel with inner_sweeps Jacobi-Richardson corrections per
+ * triangular solve (row order). method: 0 GMRES(kspace), 1 CG,
  * 3 BiCGStab, 4 TFQMR (Belos "bicgstab" / "tfqmr", the strings
  * src/LinearSolver.C:114 passes to the Belos factory; right preconditioned).
  * history (optional, capacity max_iters+1) gets ||r_k||/||r_0|| (TFQMR:
@@ -224,12 +226,13 @@ int or_solve(int64_t nrows, const int64_t* row_ptr, const int32_t* col_idx,
              const double* vals, const double* b, double* x, int method,
              int precond, const int64_t* order, int kspace, int max_iters,
              double tol, double* history, or_solve_report* rep,
-             int nthreads);
+             int nthreads, int inner_sweeps);
 
 /* Preconditioner application alone (for unit tests). */
 void or_precond_apply(int64_t nrows, const int64_t* row_ptr,
                       const int32_t* col_idx, const double* vals, int precond,
-                      const int64_t* order, const double* x, double* y);
+                      const int64_t* order, const double* x, double* y,
+                      int inner_sweeps);
 
 /* ---- input producers ---- */
 /* Unit-test mass flow rate 0.5 (rhoL uL + rhoR uR) . A. */

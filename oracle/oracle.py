@@ -228,7 +228,7 @@ def spmv(row_ptr, col_idx, vals, x, nthreads=1):
 
 
 def solve(row_ptr, col_idx, vals, b, method=0, precond=1, order=None, kspace=50, max_iters=50,
-          tol=1e-8, nthreads=1):
+          tol=1e-8, nthreads=1, inner_sweeps=1):
     row_ptr, vals, b = _i64(row_ptr), _f64(vals), _f64(b)
     col_idx = np.ascontiguousarray(col_idx, np.int32)
     n = b.shape[0]
@@ -238,18 +238,18 @@ def solve(row_ptr, col_idx, vals, b, method=0, precond=1, order=None, kspace=50,
     od = None if order is None else _i64(order)
     lib().or_solve(C.c_int64(n), _p(row_ptr, C.c_int64), _p(col_idx, C.c_int32), _p(vals, C.c_double),
                    _p(b, C.c_double), _p(x, C.c_double), method, precond, _p(od, C.c_int64), kspace,
-                   max_iters, C.c_double(tol), _p(hist, C.c_double), C.byref(rep), nthreads)
+                   max_iters, C.c_double(tol), _p(hist, C.c_double), C.byref(rep), nthreads, inner_sweeps)
     return x, hist[:rep.iterations + 1].copy(), rep
 
 
-def precond_apply(row_ptr, col_idx, vals, kind, x, order=None):
+def precond_apply(row_ptr, col_idx, vals, kind, x, order=None, inner_sweeps=1):
     row_ptr, vals, x = _i64(row_ptr), _f64(vals), _f64(x)
     col_idx = np.ascontiguousarray(col_idx, np.int32)
     y = np.zeros_like(x)
     od = None if order is None else _i64(order)
     lib().or_precond_apply(C.c_int64(x.shape[0]), _p(row_ptr, C.c_int64), _p(col_idx, C.c_int32),
                            _p(vals, C.c_double), kind, _p(od, C.c_int64), _p(x, C.c_double),
-                           _p(y, C.c_double))
+                           _p(y, C.c_double), inner_sweeps)
     return y
 
 

@@ -276,3 +276,25 @@ def test_open_mdot_unit_cube(orc, golds):
     md = orc.mdot_open(ipn, m["coords"], np.full((N, 3), g["velocity"]), np.zeros((N, 3)), np.full(N, g["density"]),
                        np.zeros(N), np.zeros(N), np.ones(N), area, None, noc_fac=1.0, pstab_fac=g["pstab_fac"])
     assert abs(md.sum() - g["mdot_open"]) <= 1e-15
+
+
+def test_oracle_two_stage_sgs_limits(orc):
+    """Two-stage SGS ("sgs2"): with many inner sweeps it is the exact
+    natural-order symmetric Gauss-Seidel; with one it is a preconditioner
+    between Jacobi and SGS in strength."""
+    import scipy.sparse as sp
+    n = 20
+    T = sp.diags([-1.3, 4.0, -0.7], [-1, 0, 1], shape=(n, n))
+    A = (sp.kron(sp.eye(n), T) + sp.kron(sp.diags([-1.1, 0.0, -0.9], [-1, 0, 1], shape=(n, n)), sp.eye(n))).tocsr()
+    A.sort_indices()
+    b = np.random.default_rng(1).normal(size=n * n)
+    y_sgs = orc.precond_apply(A.indptr, A.indices, A.data, 2, b)
+    y_ts = orc.precond_apply(A.indptr, A.indices, A.data, 4, b, inner_sweeps=300)
+    assert np.abs(y_sgs - y_ts).max() <= 1e-13 * np.abs(y_sgs).max()
+    its = {}
+    for pc, inner in ((1, 1), (4, 1), (2, 1)):
+        x, h, rep = orc.solve(A.indptr, A.indices, A.data, b, method=0, precond=pc, kspace=30, max_iters=500,
+                              tol=1e-10, inner_sweeps=inner)
+        assert rep.converged == 1 and np.linalg.norm(b - A @ x) <= 1.01e-10 * np.linalg.norm(b)
+        its[pc] = rep.iterations
+    assert its[2] <= its[4] <= its[1]
