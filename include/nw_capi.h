@@ -553,6 +553,23 @@ nw_status nw_compute_open_mdot(nw_linsys* ls, const nw_sideset* s,
 nw_status nw_correct_open_mdot(nw_linsys* ls, const nw_sideset* s, double correction,
                                double* mdot, double* total);
 
+/* ---- momentum_diag (the Udiag time scale of the pressure projection) ---- */
+/* NGPApplyCoeff::extract_diagonal (src/SolverAlgorithm.C:89-104), enabled
+ * by MomentumEquationSystem::assemble_and_solve when tscaleType is
+ * TSCALE_UDIAGINV (src/LowMachEquationSystem.C:2729-2760): every local
+ * system's lhs(ix, ix) (first dof of each node) summed per node. Here it is
+ * read from the assembled matrix: diag (device, one value per caller node;
+ * periodic slaves get their master's) = the diagonal entry of dof `dof` of
+ * the node's row, which holds the sum of every kernel assembled so far.
+ * Call after the assembly and before nw_linsys_apply_dirichlet. */
+nw_status nw_linsys_extract_diagonal(nw_linsys* ls, int dof, double* diag);
+/* The post-processing that follows the momentum solve (src/
+ * LowMachEquationSystem.C:2760-2790): udiag = (udiag / (rho V) - gamma1/dt)
+ * relax + gamma1/dt, per node (device arrays of the handle's node count,
+ * relax = the velocity relaxation factor). */
+nw_status nw_udiag_postprocess(nw_linsys* ls, const double* density, const double* dual_volume,
+                               double dt, double gamma1, double relax, double* udiag);
+
 /* ---- MatrixMarket export / import ---- */
 /* TpetraLinearSystem::writeToFile (src/TpetraLinearSystem.C:2017-2045):
  * writes <base>-O-<count>.mm.1 (coordinate real general, 1-based global dof

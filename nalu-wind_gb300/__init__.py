@@ -146,6 +146,9 @@ SIGNATURES = {
     "nw_linsys_create": (C.c_int, [C.c_int, C.POINTER(SolverCfg), C.POINTER(C.c_void_p)]),
     "nw_linsys_destroy": (C.c_int, [C.c_void_p]),
     "nw_linsys_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "nw_linsys_extract_diagonal": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "nw_udiag_postprocess": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                       C.c_void_p]),
     "nw_linsys_set_solver_cfg": (C.c_int, [C.c_void_p, C.POINTER(SolverCfg)]),
     "nw_linsys_build_edge_graph": (C.c_int, [C.c_void_p, C.c_int64, _I64P, _I64P, C.c_int64, _I64P]),
     "nw_linsys_finalize": (C.c_int, [C.c_void_p]),
@@ -451,6 +454,14 @@ class LinearSystem:
               "continuity": self.lib.nw_assemble_continuity_mass_bdf,
               "momentum": self.lib.nw_assemble_momentum_mass_bdf}[kind]
         check(fn(self.h, C.byref(f), C.byref(o)))
+
+    # -- momentum_diag (Udiag) of the pressure projection
+    def extract_diagonal(self, diag_dev, dof=0) -> None:
+        check(self.lib.nw_linsys_extract_diagonal(self.h, dof, dptr(diag_dev)))
+
+    def udiag_postprocess(self, density_dev, dual_volume_dev, udiag_dev, dt, gamma1=1.0, relax=1.0) -> None:
+        check(self.lib.nw_udiag_postprocess(self.h, dptr(density_dev), dptr(dual_volume_dev), dt, gamma1, relax,
+                                            dptr(udiag_dev)))
 
     # -- boundary face kernels (add to the assembled system)
     def sideset(self, ip_nodes) -> "SideSet":

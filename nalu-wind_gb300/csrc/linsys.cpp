@@ -996,6 +996,31 @@ nw_status nw_assemble_scalar_open(nw_linsys* ls, const nw_sideset* s,
   });
 }
 
+nw_status nw_linsys_extract_diagonal(nw_linsys* ls, int dof, double* diag) {
+  return guard([&] {
+    need_finalized(ls);
+    if (dof < 0 || dof >= ls->num_dof) fail(NW_INVALID_ARG, "dof out of range");
+    if (ls->g.num_nodes > 0) check_ptr(diag, "diag");
+    materialize_zero(ls);
+    launch_extract_diagonal(ls->stream, plan_view(ls), dof, ls->values.p, diag);
+  });
+}
+
+nw_status nw_udiag_postprocess(nw_linsys* ls, const double* density, const double* dual_volume,
+                               double dt, double gamma1, double relax, double* udiag) {
+  return guard([&] {
+    need_finalized(ls);
+    if (ls->g.num_nodes > 0) {
+      check_ptr(density, "density");
+      check_ptr(dual_volume, "dual_volume");
+      check_ptr(udiag, "udiag");
+    }
+    if (!(dt != 0.0)) fail(NW_INVALID_ARG, "dt is zero");
+    launch_udiag_postprocess(ls->stream, ls->g.num_nodes, density, dual_volume, gamma1 / dt, relax,
+                             udiag);
+  });
+}
+
 nw_status nw_assemble_scalar_mass_bdf(nw_linsys* ls, const nw_mass_bdf_fields* f,
                                       const nw_bdf_opts* o) {
   return mass_bdf(ls, 0, f, o);
@@ -1117,6 +1142,7 @@ PlanView plan_view(const nw_linsys* ls) {
   v.num_nodes = ls->g.num_nodes;
   v.row_nodes_ptr = ls->row_nodes_ptr.p;
   v.row_nodes = ls->row_nodes.p;
+  v.node_lid = ls->node_lid.p;
   return v;
 }
 }  // namespace nw

@@ -63,9 +63,53 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// NGPApplyCoeff::extract_diagonal (src/SolverAlgorithm.C:89-104) adds
+// lhs(ix, ix), the first dof's diagonal of each entity's block, of every
+// local system into momentum_diag as the systems are summed in. The
+// assembled CSR diagonal of that dof holds exactly the sum of those terms
+// (of every kernel assembled so far), so it is read back once per node:
+// call after the assembly and before Dirichlet rows are applied.
+__global__ void extract_diag_k(int64_t N, const int64_t* __restrict__ node_lid, int nd, int dof,
+                               const int32_t* __restrict__ diag_pos,
+                               const int64_t* __restrict__ row_ptr,
+                               const double* __restrict__ values, double* __restrict__ out) {
+  const int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int64_t row0 = node_lid[n];
+  const int dp = diag_pos[row0 / nd];
+  out[n] = dp >= 0 ? values[row_ptr[row0 + dof] + int64_t(nd) * dp + dof] : 0.0;
+}
+
+// MomentumEquationSystem::assemble_and_solve post-processing of the
+// extracted diagonal (src/LowMachEquationSystem.C:2760-2790): divide by
+// rho V, then remove the momentum relaxation factor about gamma1 / dt.
+__global__ void udiag_post_k(int64_t n, const double* __restrict__ rho,
+                             const double* __restrict__ dvol, double pts, double alpha,
+                             double* __restrict__ udiag) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double u = udiag[i] / (rho[i] * dvol[i]);
+  udiag[i] = (u - pts) * alpha + pts;
+}
+
 inline unsigned grid_for(int64_t n) { return unsigned((n + kThreads - 1) / kThreads); }
 
 }  // namespace
+
+void launch_extract_diagonal(cudaStream_t s, const PlanView& v, int dof, const double* values,
+                             double* diag) {
+  if (v.num_nodes == 0) return;
+  extract_diag_k<<<grid_for(v.num_nodes), kThreads, 0, s>>>(v.num_nodes, v.node_lid, v.num_dof, dof,
+                                                             v.diag_pos, v.row_ptr, values, diag);
+  NW_CUDA(cudaGetLastError());
+}
+
+void launch_udiag_postprocess(cudaStream_t s, int64_t n, const double* rho, const double* dvol,
+                              double pts, double alpha, double* udiag) {
+  if (n == 0) return;
+  udiag_post_k<<<grid_for(n), kThreads, 0, s>>>(n, rho, dvol, pts, alpha, udiag);
+  NW_CUDA(cudaGetLastError());
+}
 
 void launch_mass_bdf(cudaStream_t s, int kind, const PlanView& v, const nw_mass_bdf_fields& f,
                      const nw_bdf_opts& o, double* values, double* rhs) {

@@ -12,4 +12,12 @@ namespace nw {
 void launch_mass_bdf(cudaStream_t s, int kind, const PlanView& v, const nw_mass_bdf_fields& f,
                      const nw_bdf_opts& o, double* values, double* rhs);
 
+// diag[n] = the assembled diagonal entry of dof `dof` of node n's row (its
+// master's), 0 where the row has no diagonal entry.
+void launch_extract_diagonal(cudaStream_t s, const PlanView& v, int dof, const double* values,
+                             double* diag);
+// udiag = (udiag / (rho V) - pts) alpha + pts
+void launch_udiag_postprocess(cudaStream_t s, int64_t n, const double* rho, const double* dvol,
+                              double pts, double alpha, double* udiag);
+
 }  // namespace nw

@@ -106,6 +106,7 @@ struct PlanView {
   int64_t num_nodes = 0;
   const int64_t* row_nodes_ptr = nullptr;  // node row -> its nodes (master first)
   const int32_t* row_nodes = nullptr;
+  const int64_t* node_lid = nullptr;       // per node: first CSR row of its master
 };
 // Throws Error unless the handle is finalized.
 PlanView plan_view(const nw_linsys* ls);

@@ -360,3 +360,16 @@ def mdot_open(ipn, coords, vel, dpdx, density, pressure, pressure_bc, udiag, are
     lib().or_mdot_open(C.c_int64(ipn.shape[0]), _p(ipn, C.c_int64), *[_p(a, C.c_double) for a in keep],
                        C.c_double(noc_fac), C.c_double(pstab_fac), _p(out, C.c_double))
     return out
+
+
+def extract_diagonal(pairs, lhs, num_dof, num_nodes):
+    """NGPApplyCoeff::extract_diagonal (src/SolverAlgorithm.C:89-104): every
+    two-node local system (edge, or face IP as (R, L)) adds lhs(ix, ix),
+    ix = node * num_dof, to its node's momentum_diag entry."""
+    pairs = _i64(pairs)
+    nl = 2 * num_dof
+    out = np.zeros(num_nodes)
+    for a in range(2):
+        ix = a * num_dof
+        np.add.at(out, pairs[:, a], lhs[:, ix * nl + ix])
+    return out

@@ -311,3 +311,47 @@ def test_open_mdot_golds_on_the_gpu(nw, golds):
     ss5 = ls.sideset(ipn5)
     md5 = torch.zeros(len(ipn5), dtype=torch.float64, device="cuda")
     assert abs(ls.correct_open_mdot(ss5, corr, md5) - c["post"]) <= 1e-15
+
+
+def test_extract_diagonal_and_udiag_postprocess(nw, orc):
+    """momentum_diag from the assembled momentum system (interior edges plus
+    a symmetry boundary) against the oracle's per-local-system extraction,
+    then the LowMach post-processing against its formula."""
+    import torch
+    case = nw.workload.lowmach_case(14, 12, 10, seed=4)
+    mesh = case.mesh
+    nd = case.node
+    host = dict(coords=mesh.coords, velocity=nd["velocity"], dudx=nd["dudx"], viscosity=nd["viscosity"],
+                density=nd["density"], mask=nd["mask"], area=mesh.area, mdot=case.edge["mdot"],
+                pecfac=case.edge["pecfac"])
+    d = {k: dev(v) for k, v in host.items()}
+    mo = nw.MomentumOpts(alpha=0.2, alpha_upw=0.9, upw_factor=1.0, relax=0.7, include_div_u=1.0, use_limiter=0)
+    ls = _system(nw, mesh, 3)
+    ls.assemble_momentum(nw.MomentumFields(*(d[k].data_ptr() for k in (
+        "coords", "velocity", "dudx", "viscosity", "density", "mask", "area", "mdot", "pecfac"))), mo)
+    ipn, area = mesh.face_ips(("y-", "z+"))
+    ss = ls.sideset(ipn)
+    fa = dev(area)
+    so = dict(include_div_u=1.0, penalty_factor=1.5)
+    ls.assemble_momentum_symmetry(ss, nw.MomentumSymmetryFields(d["coords"].data_ptr(), d["velocity"].data_ptr(),
+                                                                d["dudx"].data_ptr(), d["viscosity"].data_ptr(),
+                                                                fa.data_ptr()), nw.MomentumSymmetryOpts(**so))
+    N = mesh.num_nodes
+    ud = torch.zeros(N, dtype=torch.float64, device="cuda")
+    ls.extract_diagonal(ud, dof=0)
+    om = orc.MomentumOpts(**{k: getattr(mo, k) for k, _ in mo._fields_})
+    eargs = (mesh.edges, mesh.coords, nd["velocity"], nd["velocity"], nd["dudx"], nd["viscosity"], nd["density"],
+             nd["mask"], mesh.area, case.edge["mdot"], case.edge["pecfac"], om)
+    sargs = (ipn, mesh.coords, nd["velocity"], nd["dudx"], nd["viscosity"], area, orc.MomentumSymmetryOpts(**so))
+    ref = orc.extract_diagonal(mesh.edges, orc.momentum_local(*eargs)[0], 3, N) + \
+        orc.extract_diagonal(ipn, orc.momentum_symmetry_local(*sargs)[0], 3, N)
+    S = orc.extract_diagonal(mesh.edges, orc.momentum_local(*eargs, mag=True)[0], 3, N) + \
+        orc.extract_diagonal(ipn, orc.momentum_symmetry_local(*sargs, mag=True)[0], 3, N)
+    check_close(ud.cpu().numpy(), ref, S, "momentum_diag")
+    rng = np.random.default_rng(7)
+    rho, vol = rng.uniform(0.8, 1.2, N), mesh.dualvol
+    dt, g1, relax = 0.05, 1.5, 0.7
+    ls.udiag_postprocess(dev(rho), dev(vol), ud, dt=dt, gamma1=g1, relax=relax)
+    exp = (ref / (rho * vol) - g1 / dt) * relax + g1 / dt
+    scale = (S / (rho * vol) + g1 / dt) * relax + g1 / dt
+    check_close(ud.cpu().numpy(), exp, scale, "post-processed momentum_diag")
