@@ -267,7 +267,8 @@ __global__ void __launch_bounds__(kBlock)
 // FP32 basis with a padded leading dimension (ld a multiple of 32 floats):
 // the multi-dot and multi-axpy below move four consecutive elements per
 // thread with 16-byte loads. Elements in [n, ld) are padding and never
-// enter a result.
+// enter a result. The multi-dot forms each group of four products with FP32
+// FMAs and adds the group into a compensated (two-float) running sum.
 __global__ void __launch_bounds__(kBlock)
     mdot4_k(int64_t n, int nv, const float* __restrict__ V, int64_t ld,
             const float* __restrict__ w, double* __restrict__ partial) {
@@ -300,10 +301,11 @@ __global__ void __launch_bounds__(kBlock)
             if (i0 + 2 >= n) a.z = 0.f;
             if (i0 + 3 >= n) a.w = 0.f;
           }
-          acc_prod(a.x, wv.x, s[k], c[k]);
-          acc_prod(a.y, wv.y, s[k], c[k]);
-          acc_prod(a.z, wv.z, s[k], c[k]);
-          acc_prod(a.w, wv.w, s[k], c[k]);
+          // the group's four products in FP32 (fused), the running sum
+          // compensated: the error is a few ulps of the group's |terms|,
+          // not of the whole length-n sum
+          const float pg = fmaf(a.x, wv.x, fmaf(a.y, wv.y, fmaf(a.z, wv.z, a.w * wv.w)));
+          two_sum_acc(s[k], c[k], pg);
         }
     }
 #pragma unroll
