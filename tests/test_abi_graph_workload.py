@@ -131,7 +131,7 @@ def test_tet_geometry_closed_and_consistent(nw, renumber):
     assert deg.max() == 14
 
 
-def test_mesh_sizes_match_survey_counts(nw):
+def test_mesh_sizes_match_expected_counts(nw):
     mesh = nw.Mesh(32, 32, 32, periodic_x=True, periodic_y=True)
     assert mesh.num_nodes == 35937
     assert mesh.num_edges == 104544
