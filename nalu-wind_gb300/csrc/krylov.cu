@@ -662,6 +662,11 @@ void KrylovSolver::setup(const DevCsr& A, int m, cudaStream_t s) {
   int sms = 0;
   NW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   red_blocks_ = int(std::max<int64_t>(1, std::min<int64_t>(8 * sms, (n + 2 * kBlock - 1) / (2 * kBlock))));
+  // the FP32 multi-dot holds 16 accumulators per thread: size its grid to
+  // the blocks that are resident at once (one wave of its grid-stride loop)
+  int occ = 0;
+  NW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mdot4_k, kBlock, 0));
+  mdot4_blocks_ = std::max(1, std::min(red_blocks_, std::max(1, occ) * sms));
   rdiag_.resize(n);
   V_.resize(size_t(m_ + 1) * n);
   Z_.release();
@@ -1501,8 +1506,8 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
       // cycle and the FP64 outer loop recomputes the true residual, so the
       // second pass of the FP64 method is not needed here (same iteration
       // counts on the Poisson systems measured)
-      mdot4_k<<<red_blocks_, kBlock, 0, s>>>(n, j + 1, V, ld, w32_.p, partial_.p);
-      reduce_partials_k<<<j + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, hs, 0, nullptr);
+      mdot4_k<<<mdot4_blocks_, kBlock, 0, s>>>(n, j + 1, V, ld, w32_.p, partial_.p);
+      reduce_partials_k<<<j + 1, kBlock, 0, s>>>(mdot4_blocks_, partial_.p, hs, 0, nullptr);
       maxpy4_k<<<g4, kBlock, 0, s>>>(n, j + 1, V, ld, hs, w32_.p, partial_.p);
       reduce_partials_k<<<1, kBlock, 0, s>>>(int(g4), partial_.p, h2, 0, nullptr);
       sqrt_scalar_k<<<1, 1, 0, s>>>(h2);

@@ -154,6 +154,7 @@ class KrylovSolver {
   int64_t ld32_ = 0;  // leading dimension of the FP32 basis (n rounded up to 32)
   bool f32_valid_ = false;
   int red_blocks_ = 0;
+  int mdot4_blocks_ = 0;  // grid of the FP32 multi-dot (one resident wave)
 };
 
 }  // namespace nw
