@@ -523,6 +523,31 @@ nw_status nw_assemble_momentum_symmetry(nw_linsys* ls, const nw_sideset* s,
                                         const nw_momentum_symmetry_fields* f,
                                         const nw_momentum_symmetry_opts* o);
 
+typedef struct nw_abl_wall_fields {
+  const double* velocity;               /* N x 3 (state np1) */
+  const double* wall_velocity_bc;       /* N x 3 */
+  const double* density;                /* N */
+  const double* heat_flux_bc;           /* N */
+  const double* specific_heat;          /* N */
+  const double* exposed_area;           /* num_ips x 3 */
+  const double* wall_friction_velocity; /* num_ips (wall_friction_velocity_bip) */
+  const double* wall_normal_distance;   /* num_ips (wall_normal_distance_bip) */
+} nw_abl_wall_fields;
+typedef struct nw_abl_wall_opts {
+  double gravity; /* m/s^2 */
+  double z0;      /* roughness height */
+  double Tref;    /* reference temperature */
+  double kappa;   /* von Karman constant (0.41) */
+  double beta_m;  /* stable Monin-Obukhov coefficient (5) */
+  double gamma_m; /* unstable Monin-Obukhov coefficient (16) */
+} nw_abl_wall_opts;
+/* MomentumABLWallFuncEdgeKernel::execute (src/edge_kernels/
+ * MomentumABLWallFuncEdgeKernel.C:80-158) with the Monin-Obukhov functions
+ * of include/wind_energy/MoninObukhov.h: the wall shear on the tangential
+ * velocity of each face node (its rows and columns only). num_dof 3. */
+nw_status nw_assemble_momentum_abl_wall(nw_linsys* ls, const nw_sideset* s,
+                                        const nw_abl_wall_fields* f, const nw_abl_wall_opts* o);
+
 typedef struct nw_scalar_open_fields {
   const double* q;                   /* N (state np1) */
   const double* q_bc;                /* N (entrained value) */

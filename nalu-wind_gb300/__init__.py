@@ -107,6 +107,17 @@ class MomentumSymmetryOpts(C.Structure):
     _fields_ = [("include_div_u", C.c_double), ("penalty_factor", C.c_double)]
 
 
+class AblWallFields(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("velocity", "wall_velocity_bc", "density", "heat_flux_bc",
+                                           "specific_heat", "exposed_area", "wall_friction_velocity",
+                                           "wall_normal_distance")]
+
+
+class AblWallOpts(C.Structure):
+    _fields_ = [("gravity", C.c_double), ("z0", C.c_double), ("Tref", C.c_double), ("kappa", C.c_double),
+                ("beta_m", C.c_double), ("gamma_m", C.c_double)]
+
+
 class ScalarOpenFields(C.Structure):
     _fields_ = [(k, C.c_void_p) for k in ("q", "q_bc", "open_mass_flow_rate")]
 
@@ -219,6 +230,8 @@ SIGNATURES = {
     "nw_assemble_momentum_symmetry": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(MomentumSymmetryFields),
                                                 C.POINTER(MomentumSymmetryOpts)]),
     "nw_assemble_scalar_open": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ScalarOpenFields), C.c_double]),
+    "nw_assemble_momentum_abl_wall": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(AblWallFields),
+                                                C.POINTER(AblWallOpts)]),
     "nw_compute_open_mdot": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ContinuityOpenFields), C.c_double,
                                        C.c_double, C.c_void_p, C.POINTER(C.c_double)]),
     "nw_correct_open_mdot": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
@@ -477,6 +490,9 @@ class LinearSystem:
     def assemble_momentum_symmetry(self, ss: "SideSet", fields: MomentumSymmetryFields,
                                    opts: MomentumSymmetryOpts) -> None:
         check(self.lib.nw_assemble_momentum_symmetry(self.h, ss.h, C.byref(fields), C.byref(opts)))
+
+    def assemble_momentum_abl_wall(self, ss: "SideSet", fields: AblWallFields, opts: AblWallOpts) -> None:
+        check(self.lib.nw_assemble_momentum_abl_wall(self.h, ss.h, C.byref(fields), C.byref(opts)))
 
     def assemble_scalar_open(self, ss: "SideSet", fields: ScalarOpenFields, relax=1.0) -> None:
         check(self.lib.nw_assemble_scalar_open(self.h, ss.h, C.byref(fields), relax))

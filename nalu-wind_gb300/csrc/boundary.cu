@@ -286,6 +286,73 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Monin-Obukhov stability function for momentum (include/wind_energy/
+// MoninObukhov.h:26-55, van der Laan et al. 2017), by stratification.
+__device__ double abl_psim(double Tflux, double zeta, double beta_m, double gamma_m) {
+  const double eps = 1.0e-8;
+  if (Tflux < -eps) return -beta_m * zeta;  // stable
+  if (Tflux > eps) {                        // unstable
+    const double half_pi = 1.5707963267948966;
+    const double phim = pow(1.0 - gamma_m * zeta, 0.25);
+    const double t2 = 1.0 + phim;
+    return log(0.125 * (1.0 + phim * phim) * (t2 * t2)) - 2.0 * atan(phim) + half_pi;
+  }
+  return 0.0;  // neutral
+}
+
+// MomentumABLWallFuncEdgeKernel::execute (src/edge_kernels/
+// MomentumABLWallFuncEdgeKernel.C:80-158)
+__global__ void __launch_bounds__(kThreads)
+    abl_wall_k(SideView v, nw_abl_wall_fields f, nw_abl_wall_opts o, double* __restrict__ values,
+               double* __restrict__ rhs) {
+  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= v.nb) return;
+  const int row = v.brow[b];
+  const int dp = v.diag_pos[row];
+  const double eps = 1.0e-8, Lmax = 1.0e8;
+  for (int p = v.bptr[b]; p < v.bptr[b + 1]; ++p) {
+    const int4 q = v.ips[p];
+    const int ip = q.x, R = q.y;
+    double av[3], nx[3], amag = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      av[d] = f.exposed_area[3 * ip + d];
+      amag += av[d] * av[d];
+    }
+    amag = sqrt(amag);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) nx[d] = av[d] / amag;
+    const double zh = f.wall_normal_distance[ip], ustar = f.wall_friction_velocity[ip];
+    const double rho = f.density[R];
+    const double Tflux = f.heat_flux_bc[R] / (rho * f.specific_heat[R]);
+    const double Lfac = fabs(Tflux) < eps ? Lmax : (-o.Tref / (o.kappa * o.gravity * Tflux));
+    double moLen = ustar * ustar * ustar * Lfac;
+    moLen = (Tflux < 0.0 ? 1.0 : -1.0) * fmax(1.0e-10, fabs(moLen));
+    const double psim = abl_psim(Tflux, zh / moLen, o.beta_m, o.gamma_m);
+    const double lambda = (rho * o.kappa * ustar / (log(zh / o.z0) - psim)) * amag;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const int64_t base = v.row_ptr[3 * row + i] + 3 * int64_t(dp);
+      double uTan = 0.0, uBcTan = 0.0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const double ninj = nx[i] * nx[j];
+        if (i == j) {
+          const double om = 1.0 - ninj;
+          uTan += om * f.velocity[3 * R + j];
+          uBcTan += om * f.wall_velocity_bc[3 * R + j];
+          values[base + j] += lambda * om;
+        } else {
+          uTan -= ninj * f.velocity[3 * R + j];
+          uBcTan -= ninj * f.wall_velocity_bc[3 * R + j];
+          values[base + j] -= lambda * ninj;
+        }
+      }
+      rhs[3 * row + i] -= lambda * (uTan - uBcTan);
+    }
+  }
+}
+
 // ScalarOpenEdgeKernel::execute (src/edge_kernels/ScalarOpenEdgeKernel.C:
 // 49-72)
 __global__ void __launch_bounds__(kThreads)
@@ -390,6 +457,12 @@ void launch_momentum_symmetry(cudaStream_t s, const SideView& v, const nw_moment
                               const nw_momentum_symmetry_opts& o, double* values, double* rhs) {
   if (v.nb == 0) return;
   momentum_symmetry_k<<<blocks(v.nb), kThreads, 0, s>>>(v, f, o, values, rhs);
+  NW_CUDA(cudaGetLastError());
+}
+void launch_abl_wall(cudaStream_t s, const SideView& v, const nw_abl_wall_fields& f,
+                     const nw_abl_wall_opts& o, double* values, double* rhs) {
+  if (v.nb == 0) return;
+  abl_wall_k<<<blocks(v.nb), kThreads, 0, s>>>(v, f, o, values, rhs);
   NW_CUDA(cudaGetLastError());
 }
 void launch_scalar_open(cudaStream_t s, const SideView& v, const nw_scalar_open_fields& f, double relax,

@@ -27,6 +27,8 @@ void launch_momentum_open(cudaStream_t s, const SideView& v, const nw_momentum_o
                           const nw_momentum_open_opts& o, double* values, double* rhs);
 void launch_momentum_symmetry(cudaStream_t s, const SideView& v, const nw_momentum_symmetry_fields& f,
                               const nw_momentum_symmetry_opts& o, double* values, double* rhs);
+void launch_abl_wall(cudaStream_t s, const SideView& v, const nw_abl_wall_fields& f,
+                     const nw_abl_wall_opts& o, double* values, double* rhs);
 void launch_scalar_open(cudaStream_t s, const SideView& v, const nw_scalar_open_fields& f, double relax,
                         double* values, double* rhs);
 

@@ -945,6 +945,27 @@ nw_status nw_assemble_momentum_symmetry(nw_linsys* ls, const nw_sideset* s,
   });
 }
 
+nw_status nw_assemble_momentum_abl_wall(nw_linsys* ls, const nw_sideset* s,
+                                        const nw_abl_wall_fields* f, const nw_abl_wall_opts* o) {
+  return guard([&] {
+    const SideView v = side_view(ls, s);
+    need_dof(ls, 3, "ABL wall function");
+    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+    check_ptr(f->velocity, "velocity");
+    check_ptr(f->wall_velocity_bc, "wall_velocity_bc");
+    check_ptr(f->density, "density");
+    check_ptr(f->heat_flux_bc, "heat_flux_bc");
+    check_ptr(f->specific_heat, "specific_heat");
+    check_ptr(f->exposed_area, "exposed_area");
+    check_ptr(f->wall_friction_velocity, "wall_friction_velocity");
+    check_ptr(f->wall_normal_distance, "wall_normal_distance");
+    if (!(o->z0 > 0.0) || !(o->kappa > 0.0) || !(o->gravity != 0.0))
+      fail(NW_INVALID_ARG, "z0 and kappa must be positive, gravity non-zero");
+    materialize_zero(ls);
+    launch_abl_wall(ls->stream, v, *f, *o, ls->values.p, ls->rhs.p);
+  });
+}
+
 nw_status nw_compute_open_mdot(nw_linsys* ls, const nw_sideset* s,
                                const nw_continuity_open_fields* f, double noc_fac,
                                double pstab_fac, double* mdot, double* total) {

@@ -1669,6 +1669,74 @@ void scalar_open_ip(int64_t ip, const int64_t* ipn, const double* q,
   if (md > 0.0) A[0] += md / T(relax);
 }
 
+inline double tlog(double x) { return std::log(x); }
+inline Mag tlog(Mag x) { return {std::log(x.v), std::abs(std::log(x.v))}; }
+
+// Monin-Obukhov stability functions (include/wind_energy/MoninObukhov.h:
+// 26-55, van der Laan et al. 2017).
+inline double psim_stable(double zeta, double beta) { return -beta * zeta; }
+inline double psim_unstable(double zeta, double gamma) {
+  const double half_pi = 1.5707963267948966;
+  const double phim = std::pow(1.0 - gamma * zeta, 0.25);
+  const double term1 = 1.0 + phim * phim;
+  const double term2 = 1.0 + phim;
+  const double term3 = term2 * term2;
+  return std::log(0.125 * term1 * term3) - 2.0 * std::atan(phim) + half_pi;
+}
+
+// MomentumABLWallFuncEdgeKernel::execute (src/edge_kernels/
+// MomentumABLWallFuncEdgeKernel.C:80-158), one face IP: the wall-function
+// shear on the tangential velocity of the face node R (no L coupling).
+template <typename T>
+void abl_wall_ip(int64_t ip, const int64_t* ipn, const double* vel, const double* bcvel,
+                 const double* density, const double* heatflux, const double* cp,
+                 const double* areav, const double* ustarF, const double* zhF,
+                 const or_abl_wall_opts* o, T* A, T* b) {
+  const int64_t R = ipn[2 * ip];
+  auto lhs = [&](int r, int c) -> T& { return A[6 * r + c]; };
+  for (int k = 0; k < 36; ++k) A[k] = T(0.0);
+  for (int k = 0; k < 6; ++k) b[k] = T(0.0);
+  const double eps = 1.0e-8, Lmax = 1.0e8;
+  T av[3], nx[3];
+  T amag = T(0.0);
+  for (int d = 0; d < 3; ++d) {
+    av[d] = T(areav[3 * ip + d]);
+    amag += av[d] * av[d];
+  }
+  amag = tsqrt(amag);
+  for (int d = 0; d < 3; ++d) nx[d] = av[d] / amag;
+  // the stability correction enters through a logarithm's argument; it is
+  // evaluated in FP64 (its rounding is far below the tolerance scale)
+  const double zh = zhF[ip], ustar = ustarF[ip];
+  const double rho = density[R];
+  const double Tflux = heatflux[R] / (rho * cp[R]);
+  const double Lfac = std::abs(Tflux) < eps ? Lmax : (-o->Tref / (o->kappa * o->gravity * Tflux));
+  double moLen = ustar * ustar * ustar * Lfac;
+  const double sign = Tflux < 0.0 ? 1.0 : -1.0;
+  moLen = sign * std::max(1.0e-10, std::abs(moLen));
+  const double zeta = zh / moLen;
+  const double psim = Tflux < -eps ? psim_stable(zeta, o->beta_m)
+                      : (Tflux > eps ? psim_unstable(zeta, o->gamma_m) : 0.0);
+  const T lambda = (T(rho) * T(o->kappa) * T(ustar) / T(std::log(zh / o->z0) - psim)) * amag;
+  for (int i = 0; i < 3; ++i) {
+    T uiTan = T(0.0), uiBcTan = T(0.0);
+    for (int j = 0; j < 3; ++j) {
+      const T ninj = nx[i] * nx[j];
+      if (i == j) {
+        const T om = T(1.0) - ninj;
+        uiTan += om * T(vel[3 * R + j]);
+        uiBcTan += om * T(bcvel[3 * R + j]);
+        lhs(i, i) += lambda * om;
+      } else {
+        uiTan -= ninj * T(vel[3 * R + j]);
+        uiBcTan -= ninj * T(bcvel[3 * R + j]);
+        lhs(i, j) -= lambda * ninj;
+      }
+    }
+    b[i] -= lambda * (uiTan - uiBcTan);
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1702,6 +1770,15 @@ NW_OR_BOTH(or_momentum_open_local, 6,
       const or_momentum_symmetry_opts *o, double *lhs, double *rhs
 NW_OR_BOTH(or_momentum_symmetry_local, 6,
            momentum_symmetry_ip(ip, ipn, coords, vel, dudx, viscosity, areav, o, A, b))
+#undef OR_ARGS
+
+#define OR_ARGS                                                                          \
+  int64_t nip, const int64_t *ipn, const double *vel, const double *bcvel,                \
+      const double *density, const double *heatflux, const double *cp,                   \
+      const double *areav, const double *ustar, const double *zh,                        \
+      const or_abl_wall_opts *o, double *lhs, double *rhs
+NW_OR_BOTH(or_abl_wall_local, 6,
+           abl_wall_ip(ip, ipn, vel, bcvel, density, heatflux, cp, areav, ustar, zh, o, A, b))
 #undef OR_ARGS
 
 #define OR_ARGS                                                                          \

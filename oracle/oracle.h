@@ -116,6 +116,15 @@ void or_momentum_symmetry_local(int64_t nip, const int64_t* ipn, const double* c
                                 const double* velocity, const double* dudx,
                                 const double* viscosity, const double* areav,
                                 const or_momentum_symmetry_opts* o, double* lhs, double* rhs);
+typedef struct or_abl_wall_opts {
+  double gravity, z0, Tref, kappa, beta_m, gamma_m;
+} or_abl_wall_opts;
+/* MomentumABLWallFuncEdgeKernel.C:80-158 (ustar, zh: per face IP) */
+void or_abl_wall_local(int64_t nip, const int64_t* ipn, const double* velocity,
+                       const double* wall_velocity_bc, const double* density,
+                       const double* heat_flux_bc, const double* specific_heat,
+                       const double* areav, const double* ustar, const double* zh,
+                       const or_abl_wall_opts* o, double* lhs, double* rhs);
 /* ScalarOpenEdgeKernel.C:49-72 / ScalarEdgeOpenSolverAlg.C:64-104 */
 void or_scalar_open_local(int64_t nip, const int64_t* ipn, const double* q,
                           const double* q_bc, const double* mdot, double relax,

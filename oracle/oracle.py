@@ -49,6 +49,11 @@ class MomentumSymmetryOpts(C.Structure):
     _fields_ = [("include_div_u", C.c_double), ("penalty_factor", C.c_double)]
 
 
+class AblWallOpts(C.Structure):
+    _fields_ = [("gravity", C.c_double), ("z0", C.c_double), ("Tref", C.c_double), ("kappa", C.c_double),
+                ("beta_m", C.c_double), ("gamma_m", C.c_double)]
+
+
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("final_rel_implicit", C.c_double),
                 ("final_abs_explicit", C.c_double), ("rhs_norm", C.c_double)]
@@ -373,3 +378,9 @@ def extract_diagonal(pairs, lhs, num_dof, num_nodes):
         ix = a * num_dof
         np.add.at(out, pairs[:, a], lhs[:, ix * nl + ix])
     return out
+
+
+def abl_wall_local(ipn, vel, bcvel, density, heatflux, cp, areav, ustar, zh, opts: AblWallOpts, mag=False):
+    """Face-IP local systems (node order R, L) of MomentumABLWallFuncEdgeKernel."""
+    fn = lib().or_abl_wall_local_mag if mag else lib().or_abl_wall_local
+    return _face_local(fn, 6, ipn, (vel, bcvel, density, heatflux, cp, areav, ustar, zh), [C.byref(opts)])

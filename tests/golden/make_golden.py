@@ -25,6 +25,9 @@ Sources (paths within the nalu-wind tree):
       relaxation 0.5 and mt19937-drawn inputs (closed-form expectation)
   unit_tests/ngp_algorithms/UnitTestMdotAlg.C           open mass flow rate on the
       z+ side and the open mass-flow correction
+  unit_tests/edge_kernels/UnitTestMomentumABLWallFuncEdge.C ABL wall function on
+      the z- side (fixture constants of MomentumABLKernelHex8Mesh,
+      unit_tests/kernels/UnitTestKernelUtils.h), closed-form expectation
 """
 from __future__ import annotations
 
@@ -140,6 +143,18 @@ def main(ref: Path, out: Path) -> None:
         assert frag in blk, frag
     g["mdot_open_correction_hex8"] = {"inflow": -124.0, "open": 100.0, "ip_count": 24, "side_ips": 4,
                                       "correction": -1.0, "post": 4.0}
+    aw = (ek / "UnitTestMomentumABLWallFuncEdge.C").read_text()
+    kf = (ref / "unit_tests/kernels/UnitTestKernelUtils.h").read_text()
+    for frag in ('get_part("surface_5")', "ustar_ * kappa_ / std::log(zh_ / z0_) * 0.25",
+                 "{-ustar_ * ustar_ * 0.25, 0.0, 0.0}"):
+        assert frag in aw, frag
+    for frag in ("z0_{0.1}", "zh_{0.25}", "uh_{0.15}", "kappa_{0.41}", "gravity_{9.81}", "Tref_{300.0}",
+                 "const double vel[3] = {uh_, 0.0, 0.0};", "field_fill(0.0, *bcHeatFlux_)",
+                 "field_fill(1000.0, *specificHeat_)", "ustar_(kappa_ * uh_ / std::log(zh_ / z0_))"):
+        assert frag in kf, frag
+    g["abl_wall_function_quad4_zminus"] = {"z0": 0.1, "zh": 0.25, "uh": 0.15, "kappa": 0.41, "gravity": 9.81,
+                                          "Tref": 300.0, "heat_flux": 0.0, "specific_heat": 1000.0,
+                                          "density": 1.0, "ip_area": 0.25}
     g["scalar_open_quad4"] = {"draws": [[1.0, 2.0], [1.0, 2.0], [-1.0, 1.0]], "relax": 0.5, "nodes": 4}
 
     assert len(g["continuity_hex8"]["lhs"]) == 64 and len(g["momentum_hex8"]["lhs"]) == 576

@@ -355,3 +355,52 @@ def test_extract_diagonal_and_udiag_postprocess(nw, orc):
     exp = (ref / (rho * vol) - g1 / dt) * relax + g1 / dt
     scale = (S / (rho * vol) + g1 / dt) * relax + g1 / dt
     check_close(ud.cpu().numpy(), exp, scale, "post-processed momentum_diag")
+
+
+@pytest.mark.parametrize("kind", ["hex", "tets"])
+def test_abl_wall_function_matches_oracle(nw, orc, kind):
+    """Stable, unstable and neutral nodes (heat flux of both signs and zero)
+    on the z- side."""
+    mesh = _mesh(nw, kind)
+    rng = np.random.default_rng(17)
+    N = mesh.num_nodes
+    ipn, area = mesh.face_ips(("z-",))
+    n = len(ipn)
+    hf = rng.choice([-1.0, 0.0, 1.0], N) * rng.uniform(0.01, 0.2, N)
+    host = dict(vel=rng.normal(0, 1, (N, 3)), bcvel=rng.normal(0, 0.1, (N, 3)), rho=rng.uniform(0.9, 1.3, N),
+                hf=hf, cp=rng.uniform(900, 1100, N), area=area, ustar=rng.uniform(0.1, 0.6, n),
+                zh=rng.uniform(0.5, 3.0, n))
+    d = {k: dev(v) for k, v in host.items()}
+    oo = dict(gravity=9.81, z0=0.05, Tref=300.0, kappa=0.41, beta_m=5.0, gamma_m=16.0)
+    ls = _system(nw, mesh, 3)
+    ss = ls.sideset(ipn)
+    ls.assemble_momentum_abl_wall(ss, nw.AblWallFields(*(d[k].data_ptr() for k in (
+        "vel", "bcvel", "rho", "hf", "cp", "area", "ustar", "zh"))), nw.AblWallOpts(**oo))
+    vals, rhs = ls.to_host()
+    args = (ipn, host["vel"], host["bcvel"], host["rho"], host["hf"], host["cp"], area, host["ustar"], host["zh"],
+            orc.AblWallOpts(**oo))
+    ref = _oracle_sum(orc, mesh, 3, ipn, *orc.abl_wall_local(*args), *orc.abl_wall_local(*args, mag=True))
+    check_close(vals, ref[0], ref[2], "values")
+    check_close(rhs, ref[1], ref[3], "rhs")
+
+
+def test_abl_wall_function_gold_on_the_gpu(nw, golds):
+    g = golds["abl_wall_function_quad4_zminus"]
+    ustar = g["kappa"] * g["uh"] / np.log(g["zh"] / g["z0"])
+    mesh = nw.Mesh(1, 1, 1)
+    ipn, area = mesh.face_ips(("z-",))
+    N = 8
+    d = {k: dev(v) for k, v in dict(vel=np.tile([g["uh"], 0.0, 0.0], (N, 1)), bcvel=np.zeros((N, 3)),
+                                     rho=np.full(N, g["density"]), hf=np.full(N, g["heat_flux"]),
+                                     cp=np.full(N, g["specific_heat"]), area=area, ustar=np.full(4, ustar),
+                                     zh=np.full(4, g["zh"])).items()}
+    ls = _system(nw, mesh, 3)
+    ls.assemble_momentum_abl_wall(ls.sideset(ipn), nw.AblWallFields(*(d[k].data_ptr() for k in (
+        "vel", "bcvel", "rho", "hf", "cp", "area", "ustar", "zh"))),
+        nw.AblWallOpts(g["gravity"], g["z0"], g["Tref"], g["kappa"], 5.0, 16.0))
+    A, b = _dense(nw, ls, 3, N)
+    lexact = ustar * g["kappa"] / np.log(g["zh"] / g["z0"]) * 0.25
+    for node in range(4):
+        np.testing.assert_allclose(np.diag(A)[3 * node:3 * node + 3], [lexact, lexact, 0.0], rtol=0, atol=1e-12)
+        np.testing.assert_allclose(b[3 * node:3 * node + 3], [-ustar * ustar * 0.25, 0.0, 0.0], rtol=0, atol=1e-12)
+    assert np.abs(A - np.diag(np.diag(A))).max() <= 1e-12 and np.all(b[12:] == 0.0)

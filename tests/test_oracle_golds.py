@@ -298,3 +298,29 @@ def test_oracle_two_stage_sgs_limits(orc):
         assert rep.converged == 1 and np.linalg.norm(b - A @ x) <= 1.01e-10 * np.linalg.norm(b)
         its[pc] = rep.iterations
     assert its[2] <= its[4] <= its[1]
+
+
+def test_abl_wall_function(orc, golds):
+    """MomentumABLWallFuncEdgeKernel on the z- side of the unit cube, neutral
+    (zero heat flux): lhs = u* kappa / ln(zh / z0) * 0.25 on the two
+    tangential components, 0 on the normal one; rhs = (-u*^2 0.25, 0, 0)."""
+    g = golds["abl_wall_function_quad4_zminus"]
+    ustar = g["kappa"] * g["uh"] / np.log(g["zh"] / g["z0"])
+    # z- side of the cube: ids (0, 2, 3, 1), opposed along z by (4, 6, 7, 5)
+    ipn = np.array([[0, 4], [2, 6], [3, 7], [1, 5]], np.int64)
+    area = np.tile([0.0, 0.0, -g["ip_area"]], (4, 1))
+    N = 8
+    vel = np.tile([g["uh"], 0.0, 0.0], (N, 1))
+    o = orc.AblWallOpts(gravity=g["gravity"], z0=g["z0"], Tref=g["Tref"], kappa=g["kappa"], beta_m=5.0,
+                        gamma_m=16.0)
+    lhs, rhs = orc.abl_wall_local(ipn, vel, np.zeros((N, 3)), np.full(N, g["density"]), np.full(N, g["heat_flux"]),
+                                  np.full(N, g["specific_heat"]), area, np.full(4, ustar), np.full(4, g["zh"]), o)
+    L, B = kat.dense_accumulate(ipn, lhs, rhs, 3, N)
+    lexact = ustar * g["kappa"] / np.log(g["zh"] / g["z0"]) * 0.25
+    for node in range(4):  # the bottom nodes 0..3 carry one IP each
+        for d, e in enumerate((lexact, lexact, 0.0)):
+            assert abs(L[3 * node + d, 3 * node + d] - e) <= 1e-12
+        np.testing.assert_allclose(B[3 * node:3 * node + 3], [-ustar * ustar * 0.25, 0.0, 0.0], rtol=0, atol=1e-12)
+    off = L - np.diag(np.diag(L))
+    assert np.abs(off).max() <= 1e-12
+    assert np.all(B[12:] == 0.0)
