@@ -548,6 +548,14 @@ typedef struct nw_abl_wall_opts {
 nw_status nw_assemble_momentum_abl_wall(nw_linsys* ls, const nw_sideset* s,
                                         const nw_abl_wall_fields* f, const nw_abl_wall_opts* o);
 
+/* MomentumABLWallShearStressEdgeKernel::execute (src/edge_kernels/
+ * MomentumABLWallShearStressEdgeKernel.C:49-88): rhs += wall_shear_stress
+ * (num_ips x 3) times |exposed_area| on the rows of the face node (slip != 0)
+ * or of the opposing node (slip == 0). num_dof 3. */
+nw_status nw_assemble_momentum_abl_wall_shear_stress(nw_linsys* ls, const nw_sideset* s,
+                                                     const double* exposed_area,
+                                                     const double* wall_shear_stress, int slip);
+
 typedef struct nw_scalar_open_fields {
   const double* q;                   /* N (state np1) */
   const double* q_bc;                /* N (entrained value) */

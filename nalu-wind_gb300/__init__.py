@@ -232,6 +232,8 @@ SIGNATURES = {
     "nw_assemble_scalar_open": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ScalarOpenFields), C.c_double]),
     "nw_assemble_momentum_abl_wall": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(AblWallFields),
                                                 C.POINTER(AblWallOpts)]),
+    "nw_assemble_momentum_abl_wall_shear_stress": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                             C.c_int]),
     "nw_compute_open_mdot": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ContinuityOpenFields), C.c_double,
                                        C.c_double, C.c_void_p, C.POINTER(C.c_double)]),
     "nw_correct_open_mdot": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
@@ -493,6 +495,10 @@ class LinearSystem:
 
     def assemble_momentum_abl_wall(self, ss: "SideSet", fields: AblWallFields, opts: AblWallOpts) -> None:
         check(self.lib.nw_assemble_momentum_abl_wall(self.h, ss.h, C.byref(fields), C.byref(opts)))
+
+    def assemble_momentum_abl_wall_shear_stress(self, ss: "SideSet", area_dev, tau_dev, slip=False) -> None:
+        check(self.lib.nw_assemble_momentum_abl_wall_shear_stress(self.h, ss.h, dptr(area_dev), dptr(tau_dev),
+                                                                  int(bool(slip))))
 
     def assemble_scalar_open(self, ss: "SideSet", fields: ScalarOpenFields, relax=1.0) -> None:
         check(self.lib.nw_assemble_scalar_open(self.h, ss.h, C.byref(fields), relax))

@@ -353,6 +353,26 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// MomentumABLWallShearStressEdgeKernel::execute (src/edge_kernels/
+// MomentumABLWallShearStressEdgeKernel.C:49-88): rhs += tau_w |A| on the
+// face node's rows (slip) or the opposing node's rows (no slip); one thread
+// per receiving node row.
+__global__ void __launch_bounds__(kThreads)
+    abl_shear_k(int64_t nrows, const int32_t* __restrict__ rows, const int32_t* __restrict__ ptr,
+                const int4* __restrict__ ips, const double* __restrict__ area,
+                const double* __restrict__ tau, double* __restrict__ rhs) {
+  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= nrows) return;
+  const int row = rows[b];
+  for (int p = ptr[b]; p < ptr[b + 1]; ++p) {
+    const int ip = ips[p].x;
+    const double a0 = area[3 * ip], a1 = area[3 * ip + 1], a2 = area[3 * ip + 2];
+    const double amag = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) rhs[3 * row + i] += tau[3 * ip + i] * amag;
+  }
+}
+
 // ScalarOpenEdgeKernel::execute (src/edge_kernels/ScalarOpenEdgeKernel.C:
 // 49-72)
 __global__ void __launch_bounds__(kThreads)
@@ -463,6 +483,14 @@ void launch_abl_wall(cudaStream_t s, const SideView& v, const nw_abl_wall_fields
                      const nw_abl_wall_opts& o, double* values, double* rhs) {
   if (v.nb == 0) return;
   abl_wall_k<<<blocks(v.nb), kThreads, 0, s>>>(v, f, o, values, rhs);
+  NW_CUDA(cudaGetLastError());
+}
+void launch_abl_shear(cudaStream_t s, const SideView& v, const double* area, const double* tau,
+                      int slip, double* rhs) {
+  const int64_t n = slip ? v.nb : v.nl;
+  if (n == 0) return;
+  abl_shear_k<<<blocks(n), kThreads, 0, s>>>(n, slip ? v.brow : v.lrow, slip ? v.bptr : v.lptr,
+                                             slip ? v.ips : v.lips, area, tau, rhs);
   NW_CUDA(cudaGetLastError());
 }
 void launch_scalar_open(cudaStream_t s, const SideView& v, const nw_scalar_open_fields& f, double relax,

@@ -19,6 +19,12 @@ struct SideView {
   const int4* ips = nullptr;
   const int64_t* row_ptr = nullptr;
   const int32_t* diag_pos = nullptr;
+  // the same IPs grouped by the node row of their opposing node L (for
+  // kernels that add to L's rows): lips[p] = (ip index, R, L, unused)
+  int64_t nl = 0;
+  const int32_t* lrow = nullptr;
+  const int32_t* lptr = nullptr;
+  const int4* lips = nullptr;
 };
 
 void launch_continuity_open(cudaStream_t s, const SideView& v, const nw_continuity_open_fields& f,
@@ -29,6 +35,8 @@ void launch_momentum_symmetry(cudaStream_t s, const SideView& v, const nw_moment
                               const nw_momentum_symmetry_opts& o, double* values, double* rhs);
 void launch_abl_wall(cudaStream_t s, const SideView& v, const nw_abl_wall_fields& f,
                      const nw_abl_wall_opts& o, double* values, double* rhs);
+void launch_abl_shear(cudaStream_t s, const SideView& v, const double* area, const double* tau,
+                      int slip, double* rhs);
 void launch_scalar_open(cudaStream_t s, const SideView& v, const nw_scalar_open_fields& f, double relax,
                         double* values, double* rhs);
 

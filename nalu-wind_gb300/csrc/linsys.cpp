@@ -792,6 +792,9 @@ struct nw_sideset {
   int64_t nb = 0;
   DeviceArray<int32_t> brow, bptr;
   DeviceArray<int4> ips;
+  int64_t nl = 0;  // the IPs grouped by the opposing node's row
+  DeviceArray<int32_t> lrow, lptr;
+  DeviceArray<int4> lips;
   DeviceArray<double> total;  // device sum of the open mass flow rates
 };
 
@@ -809,6 +812,10 @@ SideView side_view(const nw_linsys* ls, const nw_sideset* s) {
   v.ips = s->ips.p;
   v.row_ptr = ls->row_ptr.p;
   v.diag_pos = ls->diag_pos.p;
+  v.nl = s->nl;
+  v.lrow = s->lrow.p;
+  v.lptr = s->lptr.p;
+  v.lips = s->lips.p;
   return v;
 }
 
@@ -859,6 +866,23 @@ nw_status nw_sideset_create(nw_linsys* ls, int64_t num_ips, const int64_t* ip_no
       ips[k] = make_int4(v[k].ip, v[k].R, v[k].L, v[k].kL);
     }
     if (!v.empty()) bptr.push_back(int32_t(v.size()));
+    // the same IPs by the opposing node's row (IP order within a row)
+    std::vector<std::pair<int32_t, int32_t>> byl(v.size());  // (row of L, position in v)
+    for (size_t k = 0; k < v.size(); ++k) byl[k] = {int32_t(g.node_lid[v[k].L] / nd), int32_t(k)};
+    std::stable_sort(byl.begin(), byl.end(), [&](const auto& a, const auto& b) {
+      return a.first != b.first ? a.first < b.first : v[a.second].ip < v[b.second].ip;
+    });
+    std::vector<int32_t> lrow, lptr{0};
+    std::vector<int4> lips(v.size());
+    for (size_t k = 0; k < byl.size(); ++k) {
+      if (k == 0 || byl[k].first != byl[k - 1].first) {
+        if (k) lptr.push_back(int32_t(k));
+        lrow.push_back(byl[k].first);
+      }
+      const Ip& q = v[size_t(byl[k].second)];
+      lips[k] = make_int4(q.ip, q.R, q.L, 0);
+    }
+    if (!byl.empty()) lptr.push_back(int32_t(byl.size()));
     auto s = std::make_unique<nw_sideset>();
     s->ls = ls;
     s->num_ips = num_ips;
@@ -867,6 +891,10 @@ nw_status nw_sideset_create(nw_linsys* ls, int64_t num_ips, const int64_t* ip_no
     s->brow.upload(brow, ls->stream);
     s->bptr.upload(bptr, ls->stream);
     s->ips.upload(ips, ls->stream);
+    s->nl = int64_t(lrow.size());
+    s->lrow.upload(lrow, ls->stream);
+    s->lptr.upload(lptr, ls->stream);
+    s->lips.upload(lips, ls->stream);
     s->total.resize(1);
     NW_CUDA(cudaStreamSynchronize(ls->stream));
     *out = s.release();
@@ -963,6 +991,21 @@ nw_status nw_assemble_momentum_abl_wall(nw_linsys* ls, const nw_sideset* s,
       fail(NW_INVALID_ARG, "z0 and kappa must be positive, gravity non-zero");
     materialize_zero(ls);
     launch_abl_wall(ls->stream, v, *f, *o, ls->values.p, ls->rhs.p);
+  });
+}
+
+nw_status nw_assemble_momentum_abl_wall_shear_stress(nw_linsys* ls, const nw_sideset* s,
+                                                     const double* exposed_area,
+                                                     const double* wall_shear_stress, int slip) {
+  return guard([&] {
+    const SideView v = side_view(ls, s);
+    need_dof(ls, 3, "ABL wall shear stress");
+    if (v.nip > 0) {
+      check_ptr(exposed_area, "exposed_area");
+      check_ptr(wall_shear_stress, "wall_shear_stress");
+    }
+    materialize_zero(ls);
+    launch_abl_shear(ls->stream, v, exposed_area, wall_shear_stress, slip ? 1 : 0, ls->rhs.p);
   });
 }
 

@@ -1737,6 +1737,21 @@ void abl_wall_ip(int64_t ip, const int64_t* ipn, const double* vel, const double
   }
 }
 
+// MomentumABLWallShearStressEdgeKernel::execute (src/edge_kernels/
+// MomentumABLWallShearStressEdgeKernel.C:49-88), one face IP: the given
+// wall shear stress times |A| added to the rhs of the face node (slip) or
+// of the opposing node (no slip).
+template <typename T>
+void abl_shear_ip(int64_t ip, const double* areav, const double* tau, int slip, T* A, T* b) {
+  for (int k = 0; k < 36; ++k) A[k] = T(0.0);
+  for (int k = 0; k < 6; ++k) b[k] = T(0.0);
+  T amag = T(0.0);
+  for (int d = 0; d < 3; ++d) amag += T(areav[3 * ip + d]) * T(areav[3 * ip + d]);
+  amag = tsqrt(amag);
+  const int base = slip ? 0 : 3;  // local node order (R, L)
+  for (int i = 0; i < 3; ++i) b[base + i] += T(tau[3 * ip + i]) * amag;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1779,6 +1794,12 @@ NW_OR_BOTH(or_momentum_symmetry_local, 6,
       const or_abl_wall_opts *o, double *lhs, double *rhs
 NW_OR_BOTH(or_abl_wall_local, 6,
            abl_wall_ip(ip, ipn, vel, bcvel, density, heatflux, cp, areav, ustar, zh, o, A, b))
+#undef OR_ARGS
+
+#define OR_ARGS                                                                          \
+  int64_t nip, const int64_t *ipn, const double *areav, const double *tau, int slip,      \
+      double *lhs, double *rhs
+NW_OR_BOTH(or_abl_shear_local, 6, ((void)ipn, abl_shear_ip(ip, areav, tau, slip, A, b)))
 #undef OR_ARGS
 
 #define OR_ARGS                                                                          \

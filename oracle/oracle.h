@@ -125,6 +125,9 @@ void or_abl_wall_local(int64_t nip, const int64_t* ipn, const double* velocity,
                        const double* heat_flux_bc, const double* specific_heat,
                        const double* areav, const double* ustar, const double* zh,
                        const or_abl_wall_opts* o, double* lhs, double* rhs);
+/* MomentumABLWallShearStressEdgeKernel.C:49-88 (tau: per face IP x 3) */
+void or_abl_shear_local(int64_t nip, const int64_t* ipn, const double* areav,
+                        const double* tau, int slip, double* lhs, double* rhs);
 /* ScalarOpenEdgeKernel.C:49-72 / ScalarEdgeOpenSolverAlg.C:64-104 */
 void or_scalar_open_local(int64_t nip, const int64_t* ipn, const double* q,
                           const double* q_bc, const double* mdot, double relax,

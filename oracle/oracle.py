@@ -384,3 +384,9 @@ def abl_wall_local(ipn, vel, bcvel, density, heatflux, cp, areav, ustar, zh, opt
     """Face-IP local systems (node order R, L) of MomentumABLWallFuncEdgeKernel."""
     fn = lib().or_abl_wall_local_mag if mag else lib().or_abl_wall_local
     return _face_local(fn, 6, ipn, (vel, bcvel, density, heatflux, cp, areav, ustar, zh), [C.byref(opts)])
+
+
+def abl_shear_local(ipn, areav, tau, slip, mag=False):
+    """Face-IP local systems (node order R, L) of MomentumABLWallShearStressEdgeKernel."""
+    fn = lib().or_abl_shear_local_mag if mag else lib().or_abl_shear_local
+    return _face_local(fn, 6, ipn, (areav, tau), [C.c_int(int(slip))])

@@ -404,3 +404,22 @@ def test_abl_wall_function_gold_on_the_gpu(nw, golds):
         np.testing.assert_allclose(np.diag(A)[3 * node:3 * node + 3], [lexact, lexact, 0.0], rtol=0, atol=1e-12)
         np.testing.assert_allclose(b[3 * node:3 * node + 3], [-ustar * ustar * 0.25, 0.0, 0.0], rtol=0, atol=1e-12)
     assert np.abs(A - np.diag(np.diag(A))).max() <= 1e-12 and np.all(b[12:] == 0.0)
+
+
+@pytest.mark.parametrize("slip", [True, False])
+@pytest.mark.parametrize("kind", ["hex", "tets", "periodic"])
+def test_abl_wall_shear_stress_matches_oracle(nw, orc, kind, slip):
+    """rhs-only wall stress on the face nodes (slip) or their opposing nodes
+    (no slip; on tets three face IPs share one opposing node)."""
+    mesh = _mesh(nw, kind)
+    rng = np.random.default_rng(18)
+    ipn, area = mesh.face_ips(("z-",))
+    tau = rng.normal(0, 1, (len(ipn), 3))
+    ls = _system(nw, mesh, 3)
+    ss = ls.sideset(ipn)
+    ls.assemble_momentum_abl_wall_shear_stress(ss, dev(area), dev(tau), slip=slip)
+    vals, rhs = ls.to_host()
+    ref = _oracle_sum(orc, mesh, 3, ipn, *orc.abl_shear_local(ipn, area, tau, slip),
+                      *orc.abl_shear_local(ipn, area, tau, slip, mag=True))
+    check_close(rhs, ref[1], ref[3], "rhs")
+    assert np.all(vals == 0.0)
