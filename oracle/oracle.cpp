@@ -1042,6 +1042,9 @@ void precond(const Ctx& c, int kind, const double* x, double* y) {
   if (kind == 0) {
     std::copy(x, x + n, y);
   } else if (kind == 1) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
     for (int64_t i = 0; i < n; ++i) y[i] = x[i] / c.diag[i];
   } else {
     std::fill(y, y + n, 0.0);
@@ -1087,6 +1090,9 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
   Ctx c{n, rp, ci, v, nthreads > 0 ? nthreads : 1, {}, {}};
   c.inner = inner_sweeps;
   c.diag.assign(n, 0.0);
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
   for (int64_t i = 0; i < n; ++i)
     for (int64_t p = rp[i]; p < rp[i + 1]; ++p)
       if (ci[p] == i) c.diag[i] = v[p];
@@ -1112,6 +1118,9 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
     while (its < maxit) {
       or_spmv(n, rp, ci, v, p.data(), q.data(), c.nthreads);
       const double alpha = rz / dot(c, p.data(), q.data());
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) {
         x[i] += alpha * p[i];
         res[i] -= alpha * q[i];
@@ -1124,6 +1133,9 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
       const double rzn = dot(c, res.data(), z.data());
       const double beta = rzn / rz;
       rz = rzn;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
     }
   } else if (method == 3) {  // BiCGStab
@@ -1137,17 +1149,26 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
       if (rho_n == 0.0 || omega == 0.0) { broke = true; break; }
       const double beta = (rho_n / rho) * (alpha / omega);
       rho = rho_n;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) p[i] = res[i] + beta * (p[i] - omega * vv[i]);
       precond(c, pc, p.data(), ph.data());
       or_spmv(n, rp, ci, v, ph.data(), vv.data(), c.nthreads);
       const double rv = dot(c, rh.data(), vv.data());
       if (rv == 0.0) { broke = true; break; }
       alpha = rho / rv;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) sv[i] = res[i] - alpha * vv[i];
       precond(c, pc, sv.data(), sh.data());
       or_spmv(n, rp, ci, v, sh.data(), t.data(), c.nthreads);
       const double tt = dot(c, t.data(), t.data());
       omega = tt > 0.0 ? dot(c, t.data(), sv.data()) / tt : 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) {
         x[i] += alpha * ph[i] + omega * sh[i];
         res[i] = sv[i] - omega * t[i];
@@ -1178,6 +1199,9 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
         alpha = rho / vr;
       }
       const double coef = alpha != 0.0 ? theta * theta / alpha * eta : 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) {
         wv[i] -= alpha * Au[i];
         dh[i] = uh[i] + coef * dh[i];
@@ -1186,8 +1210,14 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
       const double cc = 1.0 / std::sqrt(1.0 + theta * theta);
       tau = tau * theta * cc;
       eta = cc * cc * alpha;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) x[i] += eta * dh[i];
       if (mm % 2 == 0) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
         for (int64_t i = 0; i < n; ++i) u[i] -= alpha * vv[i];
         precond(c, pc, u.data(), uh.data());
         or_spmv(n, rp, ci, v, uh.data(), Au_n.data(), c.nthreads);
@@ -1201,10 +1231,16 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
         if (rho == 0.0) break;
         const double beta = rho_n / rho;
         rho = rho_n;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
         for (int64_t i = 0; i < n; ++i) u[i] = wv[i] + beta * u[i];
         precond(c, pc, u.data(), uh.data());
         // Au holds A M^-1 u_m; Au_n gets A M^-1 u_{m+1}
         or_spmv(n, rp, ci, v, uh.data(), Au_n.data(), c.nthreads);
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
         for (int64_t i = 0; i < n; ++i) vv[i] = Au_n[i] + beta * (Au[i] + beta * vv[i]);
         std::swap(Au, Au_n);
       }
@@ -1216,6 +1252,9 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
     double beta = bnorm;
     bool done = false;
     while (!done && its < maxit) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) V[i] = res[i] / beta;
       std::fill(g.begin(), g.end(), 0.0);
       g[0] = beta;
@@ -1231,6 +1270,9 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
             h2[k] = dot(c, V.data() + size_t(n) * k, w.data());
           for (int k = 0; k <= j; ++k) {
             const double* vk = V.data() + size_t(n) * k;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
             for (int64_t i = 0; i < n; ++i) w[i] -= h2[k] * vk[i];
             h[k] += h2[k];
           }
@@ -1239,6 +1281,9 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
         for (int k = 0; k <= j; ++k) H[size_t(k) * m + j] = h[k];
         H[size_t(j + 1) * m + j] = hn;
         if (hn != 0.0)
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
           for (int64_t i = 0; i < n; ++i) vn[i] = w[i] / hn;
         for (int k = 0; k < j; ++k) {
           const double a = H[size_t(k) * m + j], bb = H[size_t(k + 1) * m + j];
@@ -1272,18 +1317,30 @@ int or_solve(int64_t n, const int64_t* rp, const int32_t* ci, const double* v,
       std::fill(w.begin(), w.end(), 0.0);
       for (int l = 0; l < kk; ++l) {
         const double* vl = V.data() + size_t(n) * l;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
         for (int64_t i = 0; i < n; ++i) w[i] += y[l] * vl[i];
       }
       precond(c, pc, w.data(), z.data());
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) x[i] += z[i];
       if (done || its >= maxit) break;
       or_spmv(n, rp, ci, v, x, w.data(), c.nthreads);
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
       for (int64_t i = 0; i < n; ++i) res[i] = b[i] - w[i];
       beta = std::sqrt(dot(c, res.data(), res.data()));
       if (beta == 0.0) break;
     }
   }
   or_spmv(n, rp, ci, v, x, w.data(), c.nthreads);
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(c.nthreads) schedule(static)
+#endif
   for (int64_t i = 0; i < n; ++i) w[i] = b[i] - w[i];
   r.final_abs_explicit = std::sqrt(dot(c, w.data(), w.data()));
   r.final_rel_implicit = rel;
@@ -1841,6 +1898,16 @@ void or_mdot_open(int64_t nip, const int64_t* ipn, const double* coords,
     }
     mdot[ip] = tmdot;
   }
+}
+
+// Threads of the OpenMP loops that take no explicit count (the per-edge
+// local systems); 0 leaves the runtime default.
+void or_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
 }
 
 // The uniform(lo, hi) draws of one default-seeded std::mt19937 with

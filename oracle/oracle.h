@@ -138,6 +138,8 @@ void or_mdot_open(int64_t nip, const int64_t* ipn, const double* coords,
                   const double* pressure, const double* pressure_bc, const double* udiag,
                   const double* areav, const double* dynp, double noc_fac,
                   double pstab_fac, double* mdot);
+/* threads of the OpenMP loops without an explicit count (0: default) */
+void or_set_threads(int n);
 /* default-seeded std::mt19937 uniform(lo[i], hi[i]) draws, in order */
 void or_mt19937_uniform(int n, const double* lo, const double* hi, double* out);
 

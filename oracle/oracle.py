@@ -390,3 +390,8 @@ def abl_shear_local(ipn, areav, tau, slip, mag=False):
     """Face-IP local systems (node order R, L) of MomentumABLWallShearStressEdgeKernel."""
     fn = lib().or_abl_shear_local_mag if mag else lib().or_abl_shear_local
     return _face_local(fn, 6, ipn, (areav, tau), [C.c_int(int(slip))])
+
+
+def set_threads(n):
+    """Threads of the oracle's OpenMP loops without an explicit count."""
+    lib().or_set_threads(C.c_int(int(n)))
