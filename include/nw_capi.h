@@ -358,7 +358,9 @@ nw_status nw_learned_forward(nw_learned* net, nw_linsys* ls, const float* rc,
  *         (64 x 128); kind 1: out_f32[m x 128] = a_bf16[m x 64] b^T, b
  *         row-major 128 x 64; kind 2: out_f32[128 x 64] = a_bf16[m x 128]^T
  *         b_bf16[m x 64]; kind 3: kind 0 on the tcgen05 tensor cores (TMEM
- *         accumulator), NW_TIMEOUT if one of its bounded waits gave up. */
+ *         accumulator), NW_TIMEOUT if one of its bounded waits gave up;
+ *         kind 4: kind 3 with the tiles loaded by TMA (cp.async.bulk.tensor,
+ *         128-byte swizzle). */
 nw_status nw_gemm_bf16(int kind, int64_t m, const void* a, const void* b,
                        void* out);
 

@@ -839,7 +839,7 @@ void LearnedNet::forward(const CoarseLevel& cl, const float* wgt, const float* d
   for (int l = 0; l < 3; ++l) {
     agg_fwd_k<<<gw, kB, 0, s>>>(nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, wgt, xcs[l]);
     uint16_t* out = l < 2 ? xcs[l + 1] : work.h3.p;
-    launch_gemm_fwd_tc(xcs[l], wtbf.p + size_t(l) * kIn2 * kHid, out, nc, l < 2 ? 128 : 64, s);
+    launch_gemm_fwd_tma(xcs[l], wtbf.p + size_t(l) * kIn2 * kHid, out, nc, l < 2 ? 128 : 64, s);
   }
   output_k<<<gw, kB, 0, s>>>(nc, work.h3.p, params.p + kOffWout, work.scal.p, work.y.p, ec);
   NW_CUDA(cudaGetLastError());

@@ -124,6 +124,10 @@ void load_params(const std::string& path, std::vector<float>& p);
 void launch_gemm_fwd_tc(const uint16_t* a, const uint16_t* wt, uint16_t* out, int64_t m,
                         int ldo, cudaStream_t s);
 int tc_status(cudaStream_t s);
+// The same GEMM with the tiles loaded by TMA (cp.async.bulk.tensor,
+// 128-byte swizzle).
+void launch_gemm_fwd_tma(const uint16_t* a, const uint16_t* wt, uint16_t* out, int64_t m,
+                         int ldo, cudaStream_t s);
 void launch_gemm_fwd(const uint16_t* a, const uint16_t* wt, uint16_t* out,
                      int64_t m, int ldo, cudaStream_t s);
 void launch_gemm_dx(const uint16_t* dz, const uint16_t* w, float* dx, int64_t m,

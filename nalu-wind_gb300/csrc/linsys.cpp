@@ -1573,8 +1573,11 @@ nw_status nw_gemm_bf16(int kind, int64_t m, const void* a, const void* b, void* 
       launch_gemm_fwd(ah, bh, static_cast<uint16_t*>(out), m, 64, nullptr);
     } else if (kind == 1) {
       launch_gemm_dx(ah, bh, static_cast<float*>(out), m, nullptr);
-    } else if (kind == 3) {
-      launch_gemm_fwd_tc(ah, bh, static_cast<uint16_t*>(out), m, 64, nullptr);
+    } else if (kind == 3 || kind == 4) {
+      if (kind == 3)
+        launch_gemm_fwd_tc(ah, bh, static_cast<uint16_t*>(out), m, 64, nullptr);
+      else
+        launch_gemm_fwd_tma(ah, bh, static_cast<uint16_t*>(out), m, 64, nullptr);
       if (tc_status(nullptr)) fail(NW_TIMEOUT, "tensor-core GEMM wait timed out");
     } else if (kind == 2) {
       DeviceArray<float> part;
@@ -1583,7 +1586,7 @@ nw_status nw_gemm_bf16(int kind, int64_t m, const void* a, const void* b, void* 
       launch_gemm_wgrad(ah, bh, part.p, static_cast<float*>(out), m, nullptr);
       NW_CUDA(cudaStreamSynchronize(nullptr));
     } else {
-      fail(NW_INVALID_ARG, "GEMM kind must be 0, 1, 2 or 3");
+      fail(NW_INVALID_ARG, "GEMM kind must be 0 to 4");
     }
     NW_CUDA(cudaGetLastError());
     NW_CUDA(cudaStreamSynchronize(nullptr));

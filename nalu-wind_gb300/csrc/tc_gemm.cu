@@ -14,6 +14,7 @@
 // with tcgen05.ld, applies the ReLU and stores BF16 rows. Every wait is
 // bounded: on a timeout the kernel records an error, waits once more
 // (bounded) for its MMAs, stops, frees its TMEM and returns.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -233,6 +234,187 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same layer with the tiles brought in by the Tensor Memory Accelerator:
+// cp.async.bulk.tensor copies 128-row x 64-element (128-byte) panels of A
+// and W into shared memory with the 128-byte swizzle, which is the layout
+// the UMMA descriptors read as SWIZZLE_128B K-major (8-row groups 1024 bytes
+// apart; a K step of 16 advances the start address by 32 bytes inside the
+// swizzle atom). One thread issues the copies against an mbarrier's
+// transaction count; the next tile streams into the other buffer while the
+// current one computes. Rows past m are zero-filled by the copy engine.
+constexpr int kPanelA = kTileM * 128;  // 16 KiB: 128 rows x 128 bytes
+constexpr int kPanelB = kN * 128;      // 8 KiB
+constexpr int kSmemTma = 2 * kPanelB + 2 * 2 * kPanelA + 1024 + 64;
+
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = uint64_t((addr >> 4) & 0x3FFFu);
+  d |= uint64_t(1) << 16;                     // leading byte offset (unused for swizzled K-major)
+  d |= uint64_t((1024 >> 4) & 0x3FFFu) << 32;  // 8-row groups 1024 bytes apart
+  d |= uint64_t(1) << 46;                     // descriptor version
+  d |= uint64_t(2) << 61;                     // SWIZZLE_128B
+  return d;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(128)
+    gemm_fwd_tma_k(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_w,
+                   uint16_t* __restrict__ out, int64_t m, int ldo) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint8_t* sB = base;                    // 2 panels of W
+  uint8_t* sA = base + 2 * kPanelB;      // 2 buffers x 2 panels of A
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sA + 4 * kPanelA);  // full[2], w, mma
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t ntiles = (m + kTileM - 1) / kTileM;
+  const uint32_t b0 = smem_u32(sB), a0 = smem_u32(sA);
+  const uint32_t full0 = smem_u32(bars), wbar = smem_u32(bars + 2), mbar = smem_u32(bars + 3);
+
+  if (tid == 0) {
+    for (int i = 0; i < 4; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bars + i)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    expect_tx(wbar, 2 * kPanelB);
+    tma_load_2d(b0, &map_w, 0, 0, wbar);
+    tma_load_2d(b0 + kPanelB, &map_w, 64, 0, wbar);
+    if (blockIdx.x < ntiles) {
+      const int y = int(int64_t(blockIdx.x) * kTileM);
+      expect_tx(full0, 2 * kPanelA);
+      tma_load_2d(a0, &map_a, 0, y, full0);
+      tma_load_2d(a0 + kPanelA, &map_a, 64, y, full0);
+    }
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  bool ok = mbar_wait(wbar, 0);
+  int it = 0;
+  for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++it) {
+    const int bsel = it & 1;
+    const uint32_t abuf = a0 + uint32_t(bsel) * 2 * kPanelA;
+    const int64_t tn = t + gridDim.x;
+    if (tid == 0 && tn < ntiles) {
+      // the other buffer was read by the previous tile's MMAs, which completed
+      const uint32_t nb = a0 + uint32_t(1 - bsel) * 2 * kPanelA;
+      const uint32_t fb = full0 + uint32_t(1 - bsel) * 8;
+      const int y = int(tn * kTileM);
+      expect_tx(fb, 2 * kPanelA);
+      tma_load_2d(nb, &map_a, 0, y, fb);
+      tma_load_2d(nb + kPanelA, &map_a, 64, y, fb);
+    }
+    ok = mbar_wait(full0 + uint32_t(bsel) * 8, uint32_t((it >> 1) & 1));
+    if (!__syncthreads_and(ok)) break;
+    if (tid == 0) {
+#pragma unroll
+      for (int k = 0; k < kK / 16; ++k) {
+        // panel k / 4, 32-byte step k % 4 inside the 128-byte swizzle atom
+        const uint32_t off = uint32_t(k >> 2) * kPanelA + uint32_t(k & 3) * 32;
+        const uint32_t offb = uint32_t(k >> 2) * kPanelB + uint32_t(k & 3) * 32;
+        const uint64_t da = smem_desc_sw128(abuf + off);
+        const uint64_t db = smem_desc_sw128(b0 + offb);
+        const uint32_t acc = k > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+          : "memory");
+    }
+    ok = mbar_wait(mbar, uint32_t(it & 1));
+    if (!ok) {
+      atomicExch(&g_tc_status, 1);
+      ok = mbar_wait(mbar, uint32_t(it & 1));
+    }
+    if (!__syncthreads_and(ok)) break;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    uint32_t v[64];
+    const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16);
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+          "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+          "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+          "=r"(v[31])
+        : "r"(taddr));
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]),
+          "=r"(v[38]), "=r"(v[39]), "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]),
+          "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]), "=r"(v[48]), "=r"(v[49]),
+          "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]),
+          "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]),
+          "=r"(v[62]), "=r"(v[63])
+        : "r"(taddr + 32u));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    const int64_t r = t * kTileM + warp * 32 + lane;
+    if (r < m) {
+      uint4* dst = reinterpret_cast<uint4*>(out + r * ldo);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        uint4 o;
+        o.x = pack_bf16_relu(__uint_as_float(v[8 * c + 0]), __uint_as_float(v[8 * c + 1]));
+        o.y = pack_bf16_relu(__uint_as_float(v[8 * c + 2]), __uint_as_float(v[8 * c + 3]));
+        o.z = pack_bf16_relu(__uint_as_float(v[8 * c + 4]), __uint_as_float(v[8 * c + 5]));
+        o.w = pack_bf16_relu(__uint_as_float(v[8 * c + 6]), __uint_as_float(v[8 * c + 7]));
+        dst[c] = o;
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (!ok) atomicExch(&g_tc_status, 1);
+  // copies still in flight (a prefetched tile after an early stop) land
+  // before the shared memory is released: wait for both buffers (bounded)
+  if (tid == 0 && !ok) {
+    mbar_wait(full0, uint32_t(((it + 1) >> 1) & 1));
+    mbar_wait(full0 + 8, uint32_t((it >> 1) & 1));
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
 }  // namespace
 
 void launch_gemm_fwd_tc(const uint16_t* a, const uint16_t* wt, uint16_t* out, int64_t m,
@@ -254,6 +436,65 @@ void launch_gemm_fwd_tc(const uint16_t* a, const uint16_t* wt, uint16_t* out, in
   const int64_t tiles = (m + kTileM - 1) / kTileM;
   const unsigned grid = unsigned(tiles < ctas ? tiles : ctas);
   gemm_fwd_tc_k<<<grid, 128, kSmem, s>>>(a, wt, out, m, ldo);
+  NW_CUDA(cudaGetLastError());
+}
+
+// Tensor maps of the TMA variant (cuTensorMapEncodeTiled through the
+// runtime's driver entry point: no link against the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    NW_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) fail(NW_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+// rows x 128 BF16 (row stride 256 bytes), boxes of 128 bytes x box_rows
+static CUtensorMap make_map(const uint16_t* base, int64_t rows, uint32_t box_rows) {
+  CUtensorMap map;
+  const cuuint64_t dims[2] = {cuuint64_t(kK), cuuint64_t(rows)};
+  const cuuint64_t strides[1] = {cuuint64_t(kK) * 2};
+  const cuuint32_t box[2] = {64, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                                 const_cast<uint16_t*>(base), dims, strides, box, estr,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(NW_INVALID_ARG, "tensor map encoding failed");
+  return map;
+}
+
+void launch_gemm_fwd_tma(const uint16_t* a, const uint16_t* wt, uint16_t* out, int64_t m, int ldo,
+                         cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    NW_CUDA(cudaFuncSetAttribute(gemm_fwd_tma_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kSmemTma));
+    attr = true;
+  }
+  static int ctas = 0;
+  if (!ctas) {
+    int dev = 0, sms = 0;
+    NW_CUDA(cudaGetDevice(&dev));
+    NW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    ctas = 2 * sms;
+  }
+  if (m <= 0) return;
+  if ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(wt)) & 15u)
+    fail(NW_INVALID_ARG, "TMA operands must be 16-byte aligned");
+  const CUtensorMap ma = make_map(a, m, kTileM);
+  const CUtensorMap mw = make_map(wt, kN, kN);
+  const int64_t tiles = (m + kTileM - 1) / kTileM;
+  const unsigned grid = unsigned(tiles < ctas ? tiles : ctas);
+  gemm_fwd_tma_k<<<grid, 128, kSmemTma, s>>>(ma, mw, out, m, ldo);
   NW_CUDA(cudaGetLastError());
 }
 

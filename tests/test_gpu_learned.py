@@ -52,18 +52,20 @@ def test_bf16_gemms_match_torch(nw, m):
     assert bool(((dw - ref).abs() <= 1e-5 * (a.float().abs().T @ dz.float().abs()) + 1e-30).all())
 
 
+@pytest.mark.parametrize("kind", [3, 4])
 @pytest.mark.parametrize("m", [1, 127, 128, 129, 5003, 65553])
-def test_tcgen05_forward_gemm_matches_torch_and_mma_sync(nw, m):
-    """The tensor-core (tcgen05, TMEM accumulator) forward layer GEMM: within
-    BF16 rounding of torch's FP32 product, on full and ragged 128-row tiles;
-    and against the mma.sync kernel, which differs at most by the BF16
-    rounding of FP32 sums taken in another order."""
+def test_tcgen05_forward_gemm_matches_torch_and_mma_sync(nw, m, kind):
+    """The tensor-core (tcgen05, TMEM accumulator) forward layer GEMM, tiles
+    staged by cp.async (kind 3) or by TMA with the 128-byte swizzle (kind 4):
+    within BF16 rounding of torch's FP32 product, on full and ragged 128-row
+    tiles; and against the mma.sync kernel, which differs at most by the
+    BF16 rounding of FP32 sums taken in another order."""
     import torch
     rng = np.random.default_rng(100 + m)
     a = _bf16_tensor(rng.normal(size=(m, 128)))
     wt = _bf16_tensor(rng.normal(size=(64, 128)) * 0.1)
     out = torch.full((m, 64), 7.0, dtype=torch.bfloat16, device="cuda")
-    nw.gemm_bf16(3, m, a, wt, out)
+    nw.gemm_bf16(kind, m, a, wt, out)
     ref = a.float() @ wt.float().T
     scale = a.float().abs() @ wt.float().abs().T
     err = (out.float() - torch.relu(ref)).abs()
