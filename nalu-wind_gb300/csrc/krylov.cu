@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kBlock)
 // thread with 16-byte loads. Elements in [n, ld) are padding and never
 // enter a result. The multi-dot forms each group of four products with FP32
 // FMAs and adds the group into a compensated (two-float) running sum.
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 6)
     mdot4_k(int64_t n, int nv, const float* __restrict__ V, int64_t ld,
             const float* __restrict__ w, double* __restrict__ partial) {
   __shared__ double red[kTile][kBlock / 32];
