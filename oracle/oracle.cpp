@@ -172,6 +172,29 @@ extern "C" {
 
 int or_version(void) { return 1; }
 
+// Replays insertIndices calls on a LocalGraphArrays of the given row
+// lengths (op k inserts op_n[k] columns of op_cols into row op_row[k]);
+// writes rowPointers (nrows + 1) and colIndices. Returns 0, or 1 when a
+// row overflows.
+int or_local_graph_replay(int nrows, const int64_t* row_lengths, int nops,
+                          const int32_t* op_row, const int32_t* op_n,
+                          const int32_t* op_cols, int num_dof,
+                          int64_t* row_ptr, int32_t* col_idx) {
+  try {
+    LocalGraphArrays g(std::vector<int64_t>(row_lengths, row_lengths + nrows));
+    const int32_t* c = op_cols;
+    for (int k = 0; k < nops; ++k) {
+      g.insertIndices(op_row[k], size_t(op_n[k]), c, num_dof);
+      c += op_n[k];
+    }
+    std::copy(g.rowPointers.begin(), g.rowPointers.end(), row_ptr);
+    std::copy(g.colIndices.begin(), g.colIndices.end(), col_idx);
+    return 0;
+  } catch (const std::exception&) {
+    return 1;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // STK "generated:NXxNYxNZ" numbering: node ids run x fastest, then y, then z,
 // from 1; coordinates are the integer lattice (unit spacing).

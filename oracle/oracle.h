@@ -61,6 +61,13 @@ void or_hex8_geometry(int64_t nnodes, const double* coords, int64_t nelem,
  * Pass 1 (row_ptr==NULL): returns nrows and *nnz_out. Pass 2 fills
  * row_ptr (nrows+1), col_idx (nnz), node_lid (nnodes, first row of the node's
  * master). */
+/* LocalGraphArrays (include/LinearSolver.h:80-151) replay: row lengths,
+ * then insertIndices(op_row[k], op_n[k], next op_n[k] of op_cols, num_dof)
+ * in order; returns 1 on row overflow. */
+int or_local_graph_replay(int nrows, const int64_t* row_lengths, int nops,
+                          const int32_t* op_row, const int32_t* op_n,
+                          const int32_t* op_cols, int num_dof,
+                          int64_t* row_ptr, int32_t* col_idx);
 int64_t or_build_graph(int64_t nnodes, const int64_t* nalu_id, int64_t nedges,
                        const int64_t* edges, int num_dof, int64_t* nnz_out,
                        int64_t* row_ptr, int32_t* col_idx, int64_t* node_lid);

@@ -395,3 +395,19 @@ def abl_shear_local(ipn, areav, tau, slip, mag=False):
 def set_threads(n):
     """Threads of the oracle's OpenMP loops without an explicit count."""
     lib().or_set_threads(C.c_int(int(n)))
+
+
+def local_graph_replay(row_lengths, ops, num_dof=1):
+    """LocalGraphArrays: pre-sized rows, then insertIndices(row, cols, numDof)
+    for each (row, cols) in ops. Returns (rowPointers, colIndices) or None on
+    row overflow."""
+    rl = np.asarray(row_lengths, np.int64)
+    rows = np.array([r for r, _ in ops], np.int32)
+    ns = np.array([len(c) for _, c in ops], np.int32)
+    cols = np.array([x for _, c in ops for x in c], np.int32)
+    rp = np.zeros(len(rl) + 1, np.int64)
+    ci = np.zeros(int(rl.sum()), np.int32)
+    rc = lib().or_local_graph_replay(C.c_int(len(rl)), _p(rl, C.c_int64), C.c_int(len(ops)), _p(rows, C.c_int32),
+                                     _p(ns, C.c_int32), _p(cols, C.c_int32), C.c_int(num_dof), _p(rp, C.c_int64),
+                                     _p(ci, C.c_int32))
+    return None if rc else (rp, ci)

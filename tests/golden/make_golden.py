@@ -25,6 +25,8 @@ Sources (paths within the nalu-wind tree):
       relaxation 0.5 and mt19937-drawn inputs (closed-form expectation)
   unit_tests/ngp_algorithms/UnitTestMdotAlg.C           open mass flow rate on the
       z+ side and the open mass-flow correction
+  unit_tests/UnitTestLocalGraphArrays.C                 sorted, deduplicated
+      insertion with numDof expansion (numDof 1 and 3)
   unit_tests/edge_kernels/UnitTestMomentumABLWallFuncEdge.C ABL wall function on
       the z- side (fixture constants of MomentumABLKernelHex8Mesh,
       unit_tests/kernels/UnitTestKernelUtils.h), closed-form expectation
@@ -155,6 +157,17 @@ def main(ref: Path, out: Path) -> None:
     g["abl_wall_function_quad4_zminus"] = {"z0": 0.1, "zh": 0.25, "uh": 0.15, "kappa": 0.41, "gravity": 9.81,
                                           "Tref": 300.0, "heat_flux": 0.0, "specific_heat": 1000.0,
                                           "density": 1.0, "ip_area": 0.25}
+    lg = (ref / "unit_tests/UnitTestLocalGraphArrays.C").read_text()
+    for frag in ("create_graph({2, 3, 4})", "cols = {7, 8, 6, 5};", "create_graph({6, 9, 12})",
+                 "cols = {21, 18, 24, 15};", "EXPECT_EQ(27u, csg->colIndices.size());",
+                 "EXPECT_EQ((int)i, csg->colIndices[i]);"):
+        assert frag in lg, frag
+    g["local_graph_arrays"] = {
+        "num_dof_1": {"row_lengths": [2, 3, 4], "ops": [[0, [0, 1]], [1, [2, 3, 4]], [2, [7, 8, 6, 5]],
+                                                        [0, [0, 1]], [1, [2, 3, 4]]]},
+        "num_dof_3": {"row_lengths": [6, 9, 12], "ops": [[0, [0, 3]], [1, [6, 9, 12]], [2, [21, 18, 24, 15]],
+                                                         [0, [0, 3]], [1, [6, 9, 12]]]},
+        "expect": "colIndices[i] == i for every i"}
     g["scalar_open_quad4"] = {"draws": [[1.0, 2.0], [1.0, 2.0], [-1.0, 1.0]], "relax": 0.5, "nodes": 4}
 
     assert len(g["continuity_hex8"]["lhs"]) == 64 and len(g["momentum_hex8"]["lhs"]) == 576

@@ -324,3 +324,19 @@ def test_abl_wall_function(orc, golds):
     off = L - np.diag(np.diag(L))
     assert np.abs(off).max() <= 1e-12
     assert np.all(B[12:] == 0.0)
+
+
+@pytest.mark.parametrize("case", ["num_dof_1", "num_dof_3"])
+def test_local_graph_arrays_insertion(orc, golds, case):
+    """LocalGraphArrays (unit_tests/UnitTestLocalGraphArrays.C): unsorted
+    inserts land sorted, numDof-expanded, and repeated inserts change
+    nothing; every row is then full and colIndices[i] == i."""
+    g = golds["local_graph_arrays"][case]
+    nd = 3 if case == "num_dof_3" else 1
+    out = orc.local_graph_replay(g["row_lengths"], [(r, c) for r, c in g["ops"]], num_dof=nd)
+    assert out is not None
+    rp, ci = out
+    assert rp[-1] == sum(g["row_lengths"]) and np.array_equal(np.diff(rp), g["row_lengths"])
+    assert np.array_equal(ci, np.arange(len(ci)))
+    # one column too many overflows the pre-sized row
+    assert orc.local_graph_replay([2], [(0, [0, 1, 2])], num_dof=1) is None
