@@ -172,6 +172,47 @@ extern "C" {
 
 int or_version(void) { return 1; }
 
+// Exposed-face sub-control-surface area vectors, one per face node:
+// Quad3DSCS::determinant_scs (src/master_element/Quad43DCVFEM.C:84-124;
+// sub-face of node i = (node i, mid edge i->i+1, centroid, mid edge i-1->i)
+// by quad_area_by_triangulation) for nn = 4, Tri3DSCS::determinant_scs
+// (src/master_element/Tri33DCVFEM.C:56-129; half the cross product of the
+// sub-face's diagonals) for nn = 3. faces: nfaces x nn node indices.
+void or_face_scs_areas(int64_t nfaces, int nn, const int64_t* faces,
+                       const double* coords, double* areav) {
+  for (int64_t f = 0; f < nfaces; ++f) {
+    double p[4][3], e[4][3], c[3] = {0, 0, 0};
+    for (int k = 0; k < nn; ++k)
+      for (int d = 0; d < 3; ++d) p[k][d] = coords[3 * faces[nn * f + k] + d];
+    for (int k = 0; k < nn; ++k)
+      for (int d = 0; d < 3; ++d) {
+        e[k][d] = 0.5 * (p[k][d] + p[(k + 1) % nn][d]);
+        c[d] += p[k][d];
+      }
+    for (int d = 0; d < 3; ++d) c[d] /= nn;
+    for (int k = 0; k < nn; ++k) {
+      double* a = areav + 3 * (nn * f + k);
+      const int km = (k + nn - 1) % nn;
+      if (nn == 4) {
+        double q[4][3];
+        for (int d = 0; d < 3; ++d) {
+          q[0][d] = p[k][d];
+          q[1][d] = e[k][d];
+          q[2][d] = c[d];
+          q[3][d] = e[km][d];
+        }
+        quad_area(q, a);
+      } else {
+        const double d13[3] = {c[0] - p[k][0], c[1] - p[k][1], c[2] - p[k][2]};
+        const double d24[3] = {e[km][0] - e[k][0], e[km][1] - e[k][1], e[km][2] - e[k][2]};
+        a[0] = 0.5 * (d24[2] * d13[1] - d13[2] * d24[1]);
+        a[1] = 0.5 * (d24[0] * d13[2] - d13[0] * d24[2]);
+        a[2] = 0.5 * (d24[1] * d13[0] - d13[1] * d24[0]);
+      }
+    }
+  }
+}
+
 // Replays insertIndices calls on a LocalGraphArrays of the given row
 // lengths (op k inserts op_n[k] columns of op_cols into row op_row[k]);
 // writes rowPointers (nrows + 1) and colIndices. Returns 0, or 1 when a

@@ -68,6 +68,10 @@ int or_local_graph_replay(int nrows, const int64_t* row_lengths, int nops,
                           const int32_t* op_row, const int32_t* op_n,
                           const int32_t* op_cols, int num_dof,
                           int64_t* row_ptr, int32_t* col_idx);
+/* Face-IP area vectors of quad (nn 4, Quad3DSCS) or triangle (nn 3,
+ * Tri3DSCS) faces; faces: nfaces x nn node ids; areav: nfaces x nn x 3. */
+void or_face_scs_areas(int64_t nfaces, int nn, const int64_t* faces,
+                       const double* coords, double* areav);
 int64_t or_build_graph(int64_t nnodes, const int64_t* nalu_id, int64_t nedges,
                        const int64_t* edges, int num_dof, int64_t* nnz_out,
                        int64_t* row_ptr, int32_t* col_idx, int64_t* node_lid);

@@ -411,3 +411,14 @@ def local_graph_replay(row_lengths, ops, num_dof=1):
                                      _p(ns, C.c_int32), _p(cols, C.c_int32), C.c_int(num_dof), _p(rp, C.c_int64),
                                      _p(ci, C.c_int32))
     return None if rc else (rp, ci)
+
+
+def face_scs_areas(faces, coords):
+    """Sub-face area vectors of quad (Quad3DSCS) or triangle (Tri3DSCS)
+    faces, one per face node: (nfaces * nn, 3)."""
+    faces = _i64(faces)
+    nf, nn = faces.shape
+    out = np.zeros((nf * nn, 3))
+    lib().or_face_scs_areas(C.c_int64(nf), C.c_int(nn), _p(faces, C.c_int64), _p(_f64(coords), C.c_double),
+                            _p(out, C.c_double))
+    return out

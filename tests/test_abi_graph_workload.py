@@ -188,3 +188,16 @@ def test_periodic_sides_have_no_face_ips(nw):
     for side in ("x-", "x+", "y-", "y+"):
         assert len(m.face_ips((side,))[0]) == 0
     assert len(m.face_ips(("z-", "z+"))[0]) == 2 * 4 * 16
+
+
+@pytest.mark.parametrize("tets", [False, True])
+def test_face_ip_areas_match_the_master_element_formulas(nw, orc, tets):
+    """The generator's face-IP area vectors against the oracle's restatement
+    of Quad3DSCS / Tri3DSCS on the same (outward-ordered) faces, on a
+    jittered, stretched block."""
+    m = nw.Mesh(4, 3, 3, stretch_z=1.2, jitter=0.2, seed=9, tets=tets)
+    ipn, area = m.face_ips()
+    nn = 3 if tets else 4
+    faces = ipn[:, 0].reshape(-1, nn)
+    ref = orc.face_scs_areas(faces, m.coords)
+    np.testing.assert_allclose(area, ref, rtol=0, atol=1e-14 * np.abs(ref).max())
