@@ -25,6 +25,8 @@ Sources (paths within the nalu-wind tree):
       relaxation 0.5 and mt19937-drawn inputs (closed-form expectation)
   unit_tests/ngp_algorithms/UnitTestMdotAlg.C           open mass flow rate on the
       z+ side and the open mass-flow correction
+  unit_tests/ngp_algorithms/UnitTestNodalGradAlg.C      interior edge nodal
+      gradients of linear fields (scalar and vector)
   unit_tests/UnitTestLocalGraphArrays.C                 sorted, deduplicated
       insertion with numDof expansion (numDof 1 and 3)
   unit_tests/edge_kernels/UnitTestMomentumABLWallFuncEdge.C ABL wall function on
@@ -168,6 +170,16 @@ def main(ref: Path, out: Path) -> None:
         "num_dof_3": {"row_lengths": [6, 9, 12], "ops": [[0, [0, 3]], [1, [6, 9, 12]], [2, [21, 18, 24, 15]],
                                                          [0, [0, 3]], [1, [6, 9, 12]]]},
         "expect": "colIndices[i] == i for every i"}
+    ng = (ref / "unit_tests/ngp_algorithms/UnitTestNodalGradAlg.C").read_text()
+    ua = (ref / "unit_tests/ngp_algorithms/UnitTestNgpAlgUtils.C").read_text()
+    assert "coordsData[0] * xCoeff + coordsData[1] * yCoeff" in ua and "fieldData[0] = coordsData[0] * xCoeff;" in ua
+    s0 = ng[ng.index("NGP_nodal_grad_edge)"):]
+    s1 = ng[ng.index("NGP_nodal_grad_edge_vec)"):]
+    for s_ in (s0, s1):
+        assert "const double xCoeff = 2.0;" in s_[:600] and "zCoeff = 2.0;" in s_[:700]
+    g["nodal_grad_edge_hex8"] = {"coeff": [2.0, 2.0, 2.0],
+                                 "scalar": _nums(_block(s0, "expectedValues")),
+                                 "vector_diagonal": _nums(_block(s1, "expectedValues"))}
     g["scalar_open_quad4"] = {"draws": [[1.0, 2.0], [1.0, 2.0], [-1.0, 1.0]], "relax": 0.5, "nodes": 4}
 
     assert len(g["continuity_hex8"]["lhs"]) == 64 and len(g["momentum_hex8"]["lhs"]) == 576

@@ -340,3 +340,19 @@ def test_local_graph_arrays_insertion(orc, golds, case):
     assert np.array_equal(ci, np.arange(len(ci)))
     # one column too many overflows the pre-sized row
     assert orc.local_graph_replay([2], [(0, [0, 1, 2])], num_dof=1) is None
+
+
+def test_nodal_grad_edge_linear_fields(orc, golds):
+    """NodalGradEdgeAlg on the unit cube (interior edges only, divided by the
+    dual volume) for phi = 2x + 2y + 2z and for u = (2x, 2y, 2z)."""
+    g = golds["nodal_grad_edge_hex8"]
+    m = kat.hex1(orc)
+    x, y, z = m["coords"].T
+    cx, cy, cz = g["coeff"]
+    phi = (cx * x + cy * y + cz * z)[:, None]
+    grad = orc.nodal_grad_edge(m["edges"], phi, m["area"], m["dualvol"], dim1=1)
+    np.testing.assert_allclose(grad.ravel(), g["scalar"], rtol=0, atol=1e-15)
+    u = np.stack([cx * x, cy * y, cz * z], 1)
+    gu = orc.nodal_grad_edge(m["edges"], u, m["area"], m["dualvol"], dim1=3).reshape(8, 3, 3)
+    diag = np.stack([gu[:, i, i] for i in range(3)], 1).ravel()
+    np.testing.assert_allclose(diag, g["vector_diagonal"], rtol=0, atol=1e-15)
