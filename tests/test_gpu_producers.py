@@ -127,3 +127,25 @@ def test_peclet_factor_matches_oracle(nw, orc, tanh_form):
     Spe = (0.5 * (np.abs(x[R]) + np.abs(x[L])) * (np.abs(u[R]) + np.abs(u[L]))).sum(1) / (diff + 1e-16) + pe
     check_close(pecnum.cpu().numpy(), pe, Spe, "peclet number")
     check_close(pecfac.cpu().numpy(), f, fp * Spe + np.abs(f) + 1e-3, "peclet factor")
+
+
+def test_nodal_gradient_golds_on_the_gpu(nw, orc, golds):
+    """The reference's interior edge-gradient golds (unit cube, linear
+    fields) through the C ABI, without the boundary closure."""
+    import torch
+    import kat
+    g = golds["nodal_grad_edge_hex8"]
+    m = kat.hex1(orc)
+    mesh = nw.Mesh(1, 1, 1)
+    assert np.array_equal(mesh.edges, m["edges"])
+    x, y, z = mesh.coords.T
+    cx, cy, cz = g["coeff"]
+    ls = _handle(nw, mesh)
+    grad = torch.zeros((8, 3), dtype=torch.float64, device="cuda")
+    ls.nodal_gradient(dev((cx * x + cy * y + cz * z)[:, None]), dev(mesh.area), dev(mesh.dualvol), grad, dim1=1)
+    np.testing.assert_allclose(grad.cpu().numpy().ravel(), g["scalar"], rtol=0, atol=1e-14)
+    gu = torch.zeros((8, 9), dtype=torch.float64, device="cuda")
+    ls.nodal_gradient(dev(np.stack([cx * x, cy * y, cz * z], 1)), dev(mesh.area), dev(mesh.dualvol), gu, dim1=3)
+    d = gu.cpu().numpy().reshape(8, 3, 3)
+    np.testing.assert_allclose(np.stack([d[:, i, i] for i in range(3)], 1).ravel(), g["vector_diagonal"], rtol=0,
+                               atol=1e-14)
