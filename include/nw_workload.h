@@ -16,8 +16,10 @@
  *     GeometryInteriorAlg.C:70-225, with the Hex8/Tet4 sub-control-surface
  *     geometry of src/master_element/Hex8CVFEM.C:565-591 and
  *     Tet4CVFEM.C),
- *   - lumped exposed-face area vectors per node for Green-Gauss boundary
- *     closure.
+ *   - lumped exposed-face area vectors per node for the Green-Gauss
+ *     boundary closure (the sum of the node's face-IP sub-face area vectors:
+ *     NodalGradBndryElemAlg with the shifted operator, src/ngp_algorithms/
+ *     NodalGradBndryElemAlg.C:130-152), and the face IPs themselves.
  * All arrays are host arrays.
  */
 #ifndef NW_WORKLOAD_H

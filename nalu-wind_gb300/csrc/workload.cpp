@@ -569,38 +569,14 @@ void build(nw_mesh& m, int nx, int ny, int nz, const nw_box_opts& o) {
     for (int ip = 0; ip < nscv; ++ip)
       dualvol[conn[npe * e + ip]] += escv[size_t(e) * nscv + ip];
   }
-  // lumped exposed area vectors on the non-periodic box faces; boundary
-  // nodes of the block are the ones on the original lattice boundary.
+  // lumped exposed area vectors: the sum of the sub-face area vectors of
+  // the face IPs at each node (the shifted boundary closure of the nodal
+  // gradient, NodalGradBndryElemAlg with useShifted); periodic sides have
+  // no face IPs
   std::vector<double> bnd(3 * N, 0.0);
-  if (!o.renumber) {
-    auto addq = [&](int64_t n0, int64_t n1, int64_t n2, int64_t n3) {
-      // outward-oriented quad (n0..n3 counter-clockwise seen from outside)
-      double q[4][3];
-      const int64_t ns[4] = {n0, n1, n2, n3};
-      for (int k = 0; k < 4; ++k)
-        for (int d = 0; d < 3; ++d) q[k][d] = coords[3 * ns[k] + d];
-      double a[3];
-      quad_area(q, a);
-      for (int k = 0; k < 4; ++k)
-        for (int d = 0; d < 3; ++d) bnd[3 * ns[k] + d] += 0.25 * a[d];
-    };
-    for (int64_t j = 0; j < ny; ++j)
-      for (int64_t i = 0; i < nx; ++i) {
-        addq(nid(i, j, 0), nid(i, j + 1, 0), nid(i + 1, j + 1, 0), nid(i + 1, j, 0));
-        addq(nid(i, j, nz), nid(i + 1, j, nz), nid(i + 1, j + 1, nz), nid(i, j + 1, nz));
-      }
-    if (!o.periodic_x)
-      for (int64_t k = 0; k < nz; ++k)
-        for (int64_t j = 0; j < ny; ++j) {
-          addq(nid(0, j, k), nid(0, j, k + 1), nid(0, j + 1, k + 1), nid(0, j + 1, k));
-          addq(nid(nx, j, k), nid(nx, j + 1, k), nid(nx, j + 1, k + 1), nid(nx, j, k + 1));
-        }
-    if (!o.periodic_y)
-      for (int64_t k = 0; k < nz; ++k)
-        for (int64_t i = 0; i < nx; ++i) {
-          addq(nid(i, 0, k), nid(i + 1, 0, k), nid(i + 1, 0, k + 1), nid(i, 0, k + 1));
-          addq(nid(i, ny, k), nid(i, ny, k + 1), nid(i + 1, ny, k + 1), nid(i + 1, ny, k));
-        }
+  for (size_t ip = 0; ip < fips.side.size(); ++ip) {
+    const int64_t R = fips.nodes[2 * ip];
+    for (int d = 0; d < 3; ++d) bnd[3 * R + d] += fips.area[3 * ip + d];
   }
   // periodic sums of nodal quantities: master and slaves hold the total
   for (int64_t n = 0; n < N; ++n)

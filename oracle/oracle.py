@@ -422,3 +422,30 @@ def face_scs_areas(faces, coords):
     lib().or_face_scs_areas(C.c_int64(nf), C.c_int(nn), _p(faces, C.c_int64), _p(_f64(coords), C.c_double),
                             _p(out, C.c_double))
     return out
+
+
+def nodal_grad_bndry(faces, area, phi, dualvol, shifted=True):
+    """NodalGradBndryElemAlg (src/ngp_algorithms/NodalGradBndryElemAlg.C:
+    130-152) on quad faces: each face IP adds q_ip A_ip / V to its node's
+    gradient, q_ip = the IP node's value (shifted) or the quad's bilinear
+    interpolation at the sub-control-volume centre (weights 9/16 own node,
+    3/16 face neighbours, 1/16 opposite). faces: (nf, 4) node ids in IP
+    order; area: (nf * 4, 3); phi: (N, dim1). Returns (N, 3 * dim1)."""
+    faces = _i64(faces)
+    phi = np.asarray(phi, np.float64).reshape(len(dualvol), -1)
+    dim1 = phi.shape[1]
+    out = np.zeros((len(dualvol), 3 * dim1))
+    nf, nn = faces.shape
+    for f in range(nf):
+        for ip in range(nn):
+            if shifted:
+                q = phi[faces[f, ip]]
+            else:
+                w = np.zeros(nn)
+                w[ip] = 9 / 16
+                w[(ip + 1) % nn] = w[(ip + 3) % nn] = 3 / 16
+                w[(ip + 2) % nn] = 1 / 16
+                q = w @ phi[faces[f]]
+            node = faces[f, ip]
+            out[node] += (q[:, None] * area[nn * f + ip][None, :]).ravel() / dualvol[node]
+    return out

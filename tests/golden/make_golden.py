@@ -177,6 +177,13 @@ def main(ref: Path, out: Path) -> None:
     s1 = ng[ng.index("NGP_nodal_grad_edge_vec)"):]
     for s_ in (s0, s1):
         assert "const double xCoeff = 2.0;" in s_[:600] and "zCoeff = 2.0;" in s_[:700]
+    sb = ng[ng.index("NGP_nodal_grad_bndry)"):]
+    ss = ng[ng.index("NGP_nodal_grad_bndry_shifted)"):]
+    assert 'get_part("surface_5")' in sb[:1500] and "const bool useShifted = false;" in sb[:1500]
+    assert "const bool useShifted = true;" in ss[:1500]
+    g["nodal_grad_bndry_hex8_zminus"] = {"coeff": [2.0, 2.0, 2.0],
+                                         "unshifted": _nums(_block(sb, "expectedValues")),
+                                         "shifted": _nums(_block(ss, "expectedValues"))}
     g["nodal_grad_edge_hex8"] = {"coeff": [2.0, 2.0, 2.0],
                                  "scalar": _nums(_block(s0, "expectedValues")),
                                  "vector_diagonal": _nums(_block(s1, "expectedValues"))}

@@ -201,3 +201,15 @@ def test_face_ip_areas_match_the_master_element_formulas(nw, orc, tets):
     faces = ipn[:, 0].reshape(-1, nn)
     ref = orc.face_scs_areas(faces, m.coords)
     np.testing.assert_allclose(area, ref, rtol=0, atol=1e-14 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("tets,periodic", [(False, False), (True, False), (False, True)])
+def test_lumped_boundary_area_is_the_shifted_closure(nw, orc, tets, periodic):
+    """bnd_area equals the sum of each node's face-IP sub-face areas (the
+    shifted NodalGradBndryElemAlg closure), periodic pairs summed."""
+    m = nw.Mesh(4, 3, 3, stretch_z=1.1, jitter=0.1, seed=2, tets=tets, periodic_x=periodic, periodic_y=periodic)
+    ipn, area = m.face_ips()
+    ref = np.zeros((m.num_nodes, 3))
+    np.add.at(ref, ipn[:, 0], area)
+    ref = nw.workload.periodic_sum(m, ref)
+    np.testing.assert_allclose(m.bnd_area, ref, rtol=0, atol=1e-15)

@@ -149,3 +149,23 @@ def test_nodal_gradient_golds_on_the_gpu(nw, orc, golds):
     d = gu.cpu().numpy().reshape(8, 3, 3)
     np.testing.assert_allclose(np.stack([d[:, i, i] for i in range(3)], 1).ravel(), g["vector_diagonal"], rtol=0,
                                atol=1e-14)
+
+
+def test_nodal_gradient_boundary_closure_gold_on_the_gpu(nw, golds):
+    """Interior edges plus the shifted closure of the z- side (bnd_area from
+    that side's face IPs): on the side's nodes the z component is the
+    interior gold plus the reference's shifted boundary gold."""
+    import torch
+    gi = golds["nodal_grad_edge_hex8"]["scalar"]
+    gb = golds["nodal_grad_bndry_hex8_zminus"]["shifted"]
+    mesh = nw.Mesh(1, 1, 1)
+    ipn, area = mesh.face_ips(("z-",))
+    bnd = np.zeros((8, 3))
+    np.add.at(bnd, ipn[:, 0], area)
+    x, y, z = mesh.coords.T
+    ls = _handle(nw, mesh)
+    grad = torch.zeros((8, 3), dtype=torch.float64, device="cuda")
+    ls.nodal_gradient(dev((2 * x + 2 * y + 2 * z)[:, None]), dev(mesh.area), dev(mesh.dualvol), grad,
+                      bnd_area_dev=dev(bnd), dim1=1)
+    gz = grad.cpu().numpy()[:4, 2]
+    np.testing.assert_allclose(gz, np.array(gi).reshape(8, 3)[:4, 2] + np.array(gb), rtol=0, atol=1e-14)

@@ -356,3 +356,20 @@ def test_nodal_grad_edge_linear_fields(orc, golds):
     gu = orc.nodal_grad_edge(m["edges"], u, m["area"], m["dualvol"], dim1=3).reshape(8, 3, 3)
     diag = np.stack([gu[:, i, i] for i in range(3)], 1).ravel()
     np.testing.assert_allclose(diag, g["vector_diagonal"], rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("shifted", [False, True])
+def test_nodal_grad_boundary_closure(orc, golds, shifted):
+    """NodalGradBndryElemAlg on the unit cube's z- side for phi = 2x + 2y +
+    2z: only the z component is non-zero, {-2, -4, -4, -6} interpolated and
+    {0, -4, -4, -8} shifted at the side's nodes (ids 0..3)."""
+    g = golds["nodal_grad_bndry_hex8_zminus"]
+    m = kat.hex1(orc)
+    x, y, z = m["coords"].T
+    phi = (2 * x + 2 * y + 2 * z)[:, None]
+    faces = np.array([[0, 2, 3, 1]], np.int64)  # z- side, outward (IP order)
+    area = np.tile([0.0, 0.0, -0.25], (4, 1))
+    grad = orc.nodal_grad_bndry(faces, area, phi, m["dualvol"], shifted=shifted)
+    exp = g["shifted" if shifted else "unshifted"]
+    np.testing.assert_allclose(grad[:4, 2], exp, rtol=0, atol=1e-15)
+    assert np.all(grad[:4, :2] == 0.0) and np.all(grad[4:] == 0.0)
