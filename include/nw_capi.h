@@ -206,15 +206,20 @@ nw_status nw_assemble_continuity_edges(nw_linsys* ls,
                                        const nw_continuity_opts* o);
 /* No counterpart in the reference. The continuity assembly above for
  * callers that cannot allocate device memory when they assemble (a host
- * code whose device memory all comes from its own pool, or a step being
- * recorded into a CUDA graph): per-edge scratch lives in a fixed 8 MiB
- * device array inside the library, and the assembled values (nnz) and rhs
- * (nrows) go to the caller's device arrays, overwritten (the result equals
- * nw_linsys_zero + nw_assemble_continuity_edges). Allocates nothing.
- * Meshes above 524,288 edges are rejected with NW_INVALID_ARG. The first
- * call on a device looks up the array's address: make it before any stream
- * capture. All calls share the array, so calls that overlap on the GPU race.
- * The handle's own values and rhs are not touched. */
+ * code whose device memory all comes from its own pool allocator, sized up
+ * front): per-edge scratch lives in a fixed 8 MiB device array inside the
+ * library, and the assembled values (nnz) and rhs (nrows) go to the
+ * caller's device arrays, overwritten. The result equals
+ * nw_linsys_zero + nw_assemble_continuity_edges within rounding: this path
+ * always evaluates the general continuity edge kernel, which rounds
+ * differently from the node pre-pass form the regular entry point takes
+ * with the reference's default options. Allocates nothing. Meshes above
+ * 524,288 edges are rejected with NW_INVALID_ARG. The handle's device must
+ * be the current device (else NW_INVALID_ARG). The first call on a device
+ * looks up the array's address with that device current and keeps it for
+ * the life of the process: a cudaDeviceReset afterwards is not supported.
+ * All calls share the array, so calls that overlap on the GPU race. The
+ * handle's own values and rhs are not touched. */
 nw_status nw_assemble_continuity_edges_noalloc(const nw_linsys* ls,
                                                const nw_continuity_fields* f,
                                                const nw_continuity_opts* o,

@@ -2,9 +2,8 @@
 //
 // Some callers cannot call cudaMalloc at the point where they assemble: a
 // host code whose device memory is owned by its own pool allocator (every
-// byte accounted for up front), a time step being recorded into a CUDA
-// graph, or a coupling layer that is only allowed to launch work on memory
-// it was handed. nw_assemble_continuity_edges keeps its per-edge
+// byte accounted for up front), or a coupling layer that is only allowed to
+// launch work on memory it was handed. nw_assemble_continuity_edges keeps its per-edge
 // coefficients in a buffer the handle owns; this variant keeps them in a
 // fixed array that lives in this file instead, and writes the assembled
 // matrix into arrays the caller passes. It allocates nothing and calls no
@@ -13,7 +12,12 @@
 // The scratch array is a file-scope __device__ array: every GPU that loads
 // the library holds it (8 MiB) until the process exits. The first call on a
 // device looks up the array's device address (cudaGetSymbolAddress) with
-// that device current; make that first call before any stream capture.
+// that device current and keeps it for the life of the process, so a
+// cudaDeviceReset after that first call is not supported. The handle's
+// device must be the current device when the entry point is called.
+// This path always evaluates the general continuity edge kernel (it has no
+// room for the node pre-pass buffer), so its result equals the regular
+// entry point's within rounding, not bit for bit.
 // All calls share the one array and it keeps the last call's contents;
 // nothing in it needs to start at zero, because the edge kernel writes
 // every entry the row kernel reads. Calls whose work overlaps on the GPU
@@ -80,6 +84,11 @@ extern "C" nw_status nw_assemble_continuity_edges_noalloc(
                    " edges; the no-allocation path holds at most " +
                    std::to_string(kMaxEdges) +
                    " (use nw_assemble_continuity_edges)");
+    int cur = -1;
+    NW_CUDA(cudaGetDevice(&cur));
+    if (cur != v.device)
+      nw::fail(NW_INVALID_ARG, "the handle's device (" + std::to_string(v.device) +
+                                   ") is not the current device (" + std::to_string(cur) + ")");
     double* scratch = scratch_on(v.device);
     nw::launch_continuity_edges(v.stream, v.num_edges, v.edges, *f, *o, scratch);
     nw::launch_rows(v.stream, 1, v.node_rows, v.inc_ptr, v.inc, v.diag_pos,

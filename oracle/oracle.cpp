@@ -273,6 +273,49 @@ void or_hex_box(int nx, int ny, int nz, double* coords, int64_t* conn) {
       }
 }
 
+// Seeded synthetic box coordinates (the benchmark workloads' definition,
+// not reference code): x = lx i / nx, y = ly j / ny, z geometrically
+// stretched from z = 0 with growth ratio `stretch`; every node draws three
+// splitmix64 uniforms in node order, and interior nodes move by
+// jitter (2u - 1) times the local spacing (z: the smaller neighbouring
+// layer). Same numbering as or_hex_box.
+static uint64_t or_splitmix64(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+void or_box_coords(int nx, int ny, int nz, double lx, double ly, double lz,
+                   double stretch, double jitter, uint64_t seed, double* coords) {
+  std::vector<double> zc(nz + 1);
+  const double r = stretch > 0 ? stretch : 1.0;
+  for (int k = 0; k <= nz; ++k)
+    zc[k] = (std::abs(r - 1.0) < 1e-14)
+                ? lz * double(k) / nz
+                : lz * (std::pow(r, double(k)) - 1.0) / (std::pow(r, double(nz)) - 1.0);
+  uint64_t s = seed;
+  auto u01 = [&]() { return double(or_splitmix64(s) >> 11) * 0x1.0p-53; };
+  for (int k = 0; k <= nz; ++k)
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        const int64_t n = int64_t(i) + int64_t(nx + 1) * (j + int64_t(ny + 1) * k);
+        double x = lx * double(i) / nx, y = ly * double(j) / ny, z = zc[k];
+        if (jitter > 0) {
+          const double ux = u01(), uy = u01(), uz = u01();
+          if (i > 0 && i < nx && j > 0 && j < ny && k > 0 && k < nz) {
+            const double hz = std::min(zc[k + 1] - zc[k], zc[k] - zc[k - 1]);
+            x += jitter * (2 * ux - 1) * lx / nx;
+            y += jitter * (2 * uy - 1) * ly / ny;
+            z += jitter * (2 * uz - 1) * hz;
+          }
+        }
+        coords[3 * n] = x;
+        coords[3 * n + 1] = y;
+        coords[3 * n + 2] = z;
+      }
+}
+
 // STK create_edges: each element's edges by ordinal, created once; node[0]
 // is the lower id (lexicographically smallest permutation). The sign rule
 // of GeometryInteriorAlg.C:209-213 and the unit-test mdot of +2.5 for a

@@ -41,6 +41,12 @@ int64_t or_hex_box_num_elems(int nx, int ny, int nz);
 /* Unit-cube coordinates (N x 3) and exodus-ordered Hex8 connectivity
  * (nelem x 8, 0-based node indices). */
 void or_hex_box(int nx, int ny, int nz, double* coords, int64_t* conn);
+/* Seeded synthetic box coordinates (N x 3, or_hex_box numbering): z
+ * stretched from z = 0 by `stretch`, interior nodes jittered by
+ * jitter x local spacing from splitmix64(seed) draws, three per node in node
+ * order. The benchmark workloads' definition, not reference code. */
+void or_box_coords(int nx, int ny, int nz, double lx, double ly, double lz,
+                   double stretch, double jitter, uint64_t seed, double* coords);
 /* STK create_edges restatement for Hex8: edges in order of first creation
  * (elements in order, hex edge ordinals 0..11), node[0] = lower id.
  * Returns E; writes up to cap edges (E x 2). elem_edges (nelem x 12) gets the

@@ -102,6 +102,16 @@ def hex_box(nx, ny, nz):
     return coords, conn
 
 
+def box_coords(nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, stretch=1.0, jitter=0.0, seed=0):
+    """Seeded stretched / jittered box coordinates (or_box_coords)."""
+    L = lib()
+    N = L.or_hex_box_num_nodes(nx, ny, nz)
+    coords = np.zeros((N, 3))
+    L.or_box_coords(nx, ny, nz, C.c_double(lx), C.c_double(ly), C.c_double(lz), C.c_double(stretch),
+                    C.c_double(jitter), C.c_uint64(seed), _p(coords, C.c_double))
+    return coords
+
+
 def hex8_edges(conn, nnodes):
     L = lib()
     conn = _i64(conn)

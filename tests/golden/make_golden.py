@@ -196,5 +196,6 @@ def main(ref: Path, out: Path) -> None:
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
-    main(ref, Path(__file__).resolve().parent / "reference_golds.json")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/nalu-wind")
+    main(Path(sys.argv[1]), Path(__file__).resolve().parent / "reference_golds.json")

@@ -63,3 +63,25 @@ def test_reference_arm_under_torchrun_prints_one_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+    assert d["steps"] == 1 and d["warmup"] == 1
+
+
+_REF_MAPS = r"""
+import json, sys
+sys.path.insert(0, sys.argv[1])
+import bench
+args = bench.argparse.Namespace(shape=(10, 8, 6), steps=3, warmup=2)
+out = bench.run_reference(args, 0, 1)
+maps = open("/proc/self/maps").read()
+print(json.dumps({"steps": out["steps"], "warmup": out["warmup"], "sample": out["cpu_baseline"]["sample"],
+                  "product_lib": "libnw_gb300" in maps, "oracle_lib": "liboracle" in maps}))
+"""
+
+
+def test_reference_arm_runs_the_given_steps_without_the_product_library():
+    r = subprocess.run([sys.executable, "-c", _REF_MAPS, str(ROOT)], capture_output=True, text=True,
+                       timeout=600, env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d["steps"] == 3 and d["warmup"] == 2 and "3 runs" in d["sample"]
+    assert d["oracle_lib"] and not d["product_lib"]

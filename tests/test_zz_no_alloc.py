@@ -2,7 +2,7 @@
 
 This entry point is for callers that cannot allocate device memory when they
 assemble, such as a host code that hands out all device memory from its own
-pool, or a time step being recorded into a CUDA graph. It keeps its per-edge
+pool allocator, sized up front. It keeps its per-edge
 scratch in a fixed array inside the library and writes into the caller's
 arrays. The test calls it through the C ABI twice in a row, with different
 inputs, and checks each result against the regular entry point
