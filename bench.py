@@ -437,10 +437,7 @@ def poisson_solves(nw, stream, args) -> dict:
                                                   stream=stream.cuda_stream)
     res["training"] = info
     res["_net"] = net
-    without = nw.Learned(seed=0)
-    p0 = without.params()
-    p0[-64:] = 0.0  # zero output layer: the same cycle with no coarse correction
-    without.set_params(p0)
+    controls = learned_controls(nw)
     maxit = args.poisson_maxit
     variants = [
         ("plain_fp64_gmres50_jacobi", None,
@@ -448,9 +445,10 @@ def poisson_solves(nw, stream, args) -> dict:
         ("mixed_gmres50_sgs", None,
          nw.solver_cfg(kspace=50, max_iterations=maxit, tolerance=1e-8, precision=nw.PREC_MIXED_BF16,
                        inner_kspace=50, inner_tolerance=1e-4, preconditioner=nw.PC_SGS)),
-        ("mixed_fgmres30_two_level_no_network", without,
-         nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=maxit, tolerance=1e-8,
-                       precision=nw.PREC_MIXED_BF16, inner_kspace=30, preconditioner=nw.PC_LEARNED)),
+        *[(f"mixed_fgmres30_two_level_{cname}", cnet,
+           nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=maxit, tolerance=1e-8,
+                         precision=nw.PREC_MIXED_BF16, inner_kspace=30, preconditioner=nw.PC_LEARNED))
+          for cname, cnet in controls.items()],
         ("learned_mixed_fgmres30", net,
          nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=maxit, tolerance=1e-8,
                        precision=nw.PREC_MIXED_BF16, inner_kspace=30, preconditioner=nw.PC_LEARNED)),
@@ -512,6 +510,26 @@ def poisson_solves(nw, stream, args) -> dict:
     return res
 
 
+def learned_controls(nw) -> dict:
+    """The learned preconditioner's cycle without the trained network, to
+    measure what training adds: the same network untrained (random
+    initialisation, seed 0), the non-learned coarse directions D_c^-1 r_c and
+    two Jacobi sweeps on the Galerkin operator (each with the same
+    energy-optimal scaling), and no coarse correction (output layer zeroed:
+    the two Gauss-Seidel sweeps alone)."""
+    untrained = nw.Learned(seed=0)
+    jac1 = nw.Learned(seed=0)
+    jac1.set_coarse_direction(1)
+    jac2 = nw.Learned(seed=0)
+    jac2.set_coarse_direction(2)
+    none = nw.Learned(seed=0)
+    p0 = none.params()
+    p0[-64:] = 0.0
+    none.set_params(p0)
+    return {"untrained_network": untrained, "jacobi_coarse_direction": jac1, "two_jacobi_coarse_sweeps": jac2,
+            "no_coarse_correction": none}
+
+
 def heldout_poisson(nw, stream, args, net) -> dict:
     """The learned preconditioner on held-out seeds of the training family's
     distribution at 128^3 nodes (127^3 hexes; stretch ratio from U[1.0, 1.15],
@@ -521,20 +539,23 @@ def heldout_poisson(nw, stream, args, net) -> dict:
     import torch
     rng = np.random.default_rng(1000)
     out = {"workload": "held-out 128^3-node Poisson systems", "systems": []}
+    controls = learned_controls(nw)
     for k in range(args.heldout):
         stretch, jitter = float(rng.uniform(1.0, 1.15)), float(rng.uniform(0.0, 0.1))
         ls = nw.workload.poisson_system((127, 127, 127), seed=1000 + k, stretch=stretch, jitter=jitter,
                                         stream=stream.cuda_stream)
         nr = ls.sizes()[0]
         r = {"seed": 1000 + k, "stretch": round(stretch, 4), "jitter": round(jitter, 4)}
-        ls.attach_learned(net)
-        for name, cfg in (
-                ("plain_fp64_gmres30_jacobi", nw.solver_cfg(kspace=30, max_iterations=args.poisson_maxit,
-                                                            tolerance=1e-8)),
-                ("learned_mixed_fgmres30", nw.solver_cfg(method=nw.FGMRES, kspace=30, inner_kspace=30,
-                                                         max_iterations=args.poisson_maxit, tolerance=1e-8,
-                                                         precision=nw.PREC_MIXED_BF16,
-                                                         preconditioner=nw.PC_LEARNED))):
+        lcfg = nw.solver_cfg(method=nw.FGMRES, kspace=30, inner_kspace=30, max_iterations=args.poisson_maxit,
+                             tolerance=1e-8, precision=nw.PREC_MIXED_BF16, preconditioner=nw.PC_LEARNED)
+        runs = [("plain_fp64_gmres30_jacobi", None, nw.solver_cfg(kspace=30, max_iterations=args.poisson_maxit,
+                                                                   tolerance=1e-8)),
+                ("learned_mixed_fgmres30", net, lcfg)]
+        runs += [(f"mixed_fgmres30_two_level_{c}", cn, lcfg) for c, cn in controls.items()
+                 if c in ("untrained_network", "jacobi_coarse_direction")]
+        for name, lnet, cfg in runs:
+            if lnet is not None:
+                ls.attach_learned(lnet)
             ls.set_solver_cfg(cfg)
             x = torch.zeros(nr, dtype=torch.float64, device="cuda")
             rep = ls.solve(x)

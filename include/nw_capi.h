@@ -44,15 +44,23 @@ typedef enum nw_status {
  * src/LinearSolver.C:114) and preconditioners (src/LinearSolverConfig.C:
  * 89-121). CG, BiCGStab and TFQMR run in FP64; with a NW_PREC_MIXED*
  * precision or NW_PC_LEARNED the solve is (F)GMRES whatever the method. */
-enum { NW_GMRES = 0, NW_CG = 1, NW_FGMRES = 2, NW_BICGSTAB = 3, NW_TFQMR = 4 };
+enum { NW_GMRES = 0, NW_CG = 1, NW_FGMRES = 2, NW_BICGSTAB = 3, NW_TFQMR = 4,
+       NW_SSTEP_GMRES = 5 /* "sstep_gmres": s-step GMRES with CholeskyQR2 */ };
 enum {
   NW_PC_NONE = 0,
   NW_PC_JACOBI = 1, /* "jacobi" / "default": Ifpack2 Jacobi, 1 sweep */
-  NW_PC_SGS = 2,    /* "sgs": symmetric Gauss-Seidel, 1 sweep, multicolour order */
+  NW_PC_SGS = 2,    /* "mt_sgs": symmetric Gauss-Seidel, 1 sweep, multicolour
+                       order (rows colour class by colour class) */
   NW_PC_LEARNED = 3, /* learned edge message-passing preconditioner (FGMRES) */
-  NW_PC_SGS2 = 4     /* "sgs2": two-stage symmetric Gauss-Seidel, 1 sweep, row
+  NW_PC_SGS2 = 4,    /* "sgs2": two-stage symmetric Gauss-Seidel, 1 sweep, row
                         order, sgs2_inner_sweeps Jacobi-Richardson corrections
                         per triangular solve */
+  NW_PC_SGS_NATURAL = 5, /* "sgs": Ifpack2 symmetric Gauss-Seidel, 1 sweep,
+                            natural row order (forward then backward), run
+                            as level-scheduled sweeps */
+  NW_PC_RILUK = 6    /* "riluk": Ifpack2 RILUK at its default level of fill 0,
+                        i.e. ILU(0) on the matrix's own pattern; level-scheduled
+                        factorization and triangular solves */
 };
 /* Arithmetic of the solve. */
 enum {
@@ -61,6 +69,16 @@ enum {
   NW_PREC_MIXED_BF16 = 2  /* as NW_PREC_MIXED, with the Gauss-Seidel sweeps
                              reading BF16 matrix values (FP32 accumulation) */
 };
+
+/* The reference's string options as TpetraLinearSolverConfig::load reads
+ * them (src/LinearSolverConfig.C:37-140): method "gmres", "cg",
+ * "sstep_gmres", "tfqmr", "bicgstab" and preconditioner "jacobi" /
+ * "default", "sgs", "mt_sgs", "sgs2", "riluk". Sets cfg->method and
+ * cfg->preconditioner and leaves the other fields as they are.
+ * "ilut" and "muelu" are rejected with NW_INVALID_ARG (not built: see the
+ * library's design notes). */
+nw_status nw_solver_cfg_from_strings(const char* method, const char* preconditioner,
+                                     struct nw_solver_cfg* cfg);
 
 /* TpetraLinearSolverConfig::load keys (src/LinearSolverConfig.C:37-140). */
 typedef struct nw_solver_cfg {
@@ -294,6 +312,11 @@ nw_status nw_linsys_precond_apply(nw_linsys* ls, int preconditioner,
 /* Row order used by the multicolour SGS (host, nrows): rows of colour 0 in
  * ascending order, then colour 1, ... */
 nw_status nw_linsys_sgs_order(nw_linsys* ls, int64_t* order, int* ncolors);
+/* Boundaries of the colour classes in that order (host, ncolors + 1): class
+ * c is order[class_ptr[c] .. class_ptr[c + 1]). Ifpack2's MT-SGS has the
+ * same notion (a colour set per sweep); there is no single reference call
+ * to cite. */
+nw_status nw_linsys_sgs_classes(nw_linsys* ls, int64_t* class_ptr);
 
 /* ---- learned preconditioner (NW_PC_LEARNED). No counterpart in the
  * reference: nalu-wind's preconditioners are Ifpack2 relaxations and MueLu
@@ -326,6 +349,11 @@ nw_status nw_learned_params(nw_learned* net, float* out, const float* in,
 nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes, int smoother);
 /* Build the aggregation / coarse level of this system's graph (num_dof 1)
  * and use `net` for NW_PC_LEARNED solves of this handle. */
+/* Coarse direction of the two-level cycle: 0 (default) the network; 1 the
+ * Jacobi direction D_c^-1 r_c and 2 two Jacobi sweeps on the Galerkin coarse
+ * operator, each with the same energy-optimal scaling. Modes 1 and 2 are
+ * the cycle without the network, kept to measure what the network adds. */
+nw_status nw_learned_set_coarse_direction(nw_learned* net, int mode);
 nw_status nw_linsys_attach_learned(nw_linsys* ls, nw_learned* net);
 /* Coarse level of an attached handle, refreshed from the current values
  * (host arrays; NULL entries skipped). */

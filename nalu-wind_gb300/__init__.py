@@ -22,8 +22,9 @@ LIB_PATH = PKG_DIR / "libnw_gb300.so"
 NW_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "CUDA_ERROR", 3: "NOT_FINALIZED", 4: "NAN_DETECTED",
                 5: "NOT_CONVERGED", 6: "BREAKDOWN", 7: "TIMEOUT", 8: "NO_DEVICE", 9: "INTERNAL"}
-GMRES, CG, FGMRES, BICGSTAB, TFQMR = 0, 1, 2, 3, 4
-PC_NONE, PC_JACOBI, PC_SGS, PC_LEARNED, PC_SGS2 = 0, 1, 2, 3, 4
+GMRES, CG, FGMRES, BICGSTAB, TFQMR, SSTEP_GMRES = 0, 1, 2, 3, 4, 5
+PC_NONE, PC_JACOBI, PC_SGS, PC_LEARNED, PC_SGS2, PC_SGS_NATURAL, PC_RILUK = 0, 1, 2, 3, 4, 5, 6
+PC_MT_SGS = PC_SGS  # "mt_sgs": multicolour order
 PREC_FP64, PREC_MIXED, PREC_MIXED_BF16 = 0, 1, 2
 
 
@@ -174,6 +175,9 @@ SIGNATURES = {
     "nw_assemble_momentum_edge_range": (C.c_int, [C.c_void_p, C.POINTER(MomentumFields), C.POINTER(MomentumOpts),
                                                   C.c_int64, C.c_int64]),
     "nw_assemble_momentum_rows": (C.c_int, [C.c_void_p, C.POINTER(MomentumOpts)]),
+    "nw_linsys_sgs_classes": (C.c_int, [C.c_void_p, _I64P]),
+    "nw_solver_cfg_from_strings": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(SolverCfg)]),
+    "nw_learned_set_coarse_direction": (C.c_int, [C.c_void_p, C.c_int]),
     "nw_assemble_continuity_edges_noalloc": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
                                                        C.POINTER(ContinuityOpts), C.c_void_p, C.c_void_p]),
     "nw_linsys_sum_into": (C.c_int, [C.c_void_p, C.c_int, _I64P, _DP, _DP]),
@@ -295,6 +299,15 @@ def solver_cfg(method=GMRES, preconditioner=PC_JACOBI, precision=PREC_FP64, kspa
     return SolverCfg(method, preconditioner, precision, kspace, max_iterations, tolerance,
                      tolerance if final_tolerance is None else final_tolerance, inner_kspace,
                      inner_tolerance, sgs2_inner_sweeps)
+
+
+def solver_cfg_from_strings(method: str, preconditioner: str, **kw) -> SolverCfg:
+    """The reference's YAML strings ("gmres", "cg", "tfqmr", "bicgstab";
+    "jacobi" / "default", "sgs", "mt_sgs", "sgs2", "riluk") mapped by the
+    library (nw_solver_cfg_from_strings), other fields as solver_cfg."""
+    cfg = solver_cfg(**kw)
+    check(load().nw_solver_cfg_from_strings(method.encode(), preconditioner.encode(), C.byref(cfg)))
+    return cfg
 
 
 class LinearSystem:
@@ -444,6 +457,13 @@ class LinearSystem:
         check(self.lib.nw_linsys_sgs_order(self.h, _ptr(order, C.c_int64), C.byref(nc)))
         return order, nc.value
 
+    def sgs_classes(self) -> np.ndarray:
+        """Colour-class boundaries of sgs_order() (ncolors + 1)."""
+        _, nc = self.sgs_order()
+        cp = np.zeros(nc + 1, np.int64)
+        check(self.lib.nw_linsys_sgs_classes(self.h, _ptr(cp, C.c_int64)))
+        return cp
+
     def sync(self) -> None:
         check(self.lib.nw_linsys_sync(self.h))
 
@@ -587,6 +607,11 @@ class Learned:
 
     def configure(self, post_smooth: bool = True, agg_passes: int = 2, smoother: int = 0) -> None:
         check(self.lib.nw_learned_configure(self.h, int(post_smooth), int(agg_passes), int(smoother)))
+
+    def set_coarse_direction(self, mode: int) -> None:
+        """0: the network; 1: D_c^-1 r_c; 2: two Jacobi sweeps on Ac (controls
+        without the network, same cycle and scaling)."""
+        check(self.lib.nw_learned_set_coarse_direction(self.h, int(mode)))
 
     def save(self, path) -> None:
         check(self.lib.nw_learned_save(self.h, str(path).encode()))

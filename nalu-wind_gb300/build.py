@@ -3,7 +3,9 @@
 Usage: python nalu-wind_gb300/build.py [--force]
 Compiles every csrc/*.cu with nvcc (-gencode arch=compute_103a,code=sm_103a)
 and every csrc/*.cpp with g++, in parallel, then links one shared library
-next to this file. Object files go to _build/ (not committed).
+next to this file. Object files go to _build/ (not committed). Host code is
+compiled with -ffp-contract=off, so its floating-point results are the same
+on x86_64 and aarch64 hosts (device code uses explicit fma where it fuses).
 """
 from __future__ import annotations
 
@@ -56,9 +58,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         obj = BUILD / (src.name + ".o")
         if src.suffix == ".cu":
             cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
-                   "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", *inc, "-c", str(src), "-o", str(obj)]
+                   "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off", *inc, "-c", str(src), "-o", str(obj)]
         else:
-            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", *inc, "-c", str(src), "-o", str(obj)]
+            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", *inc, "-c", str(src), "-o", str(obj)]
         jobs.append((cmd, obj))
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         futs = [ex.submit(_run, c) for c, _ in jobs]

@@ -170,7 +170,8 @@ __global__ void __launch_bounds__(kThreads)
 // Fast form (rho u and rho_Ip u_Ip interpolated together, incompressible
 // scaling off: the reference defaults): the node phase stores per node
 //   n = (1/udiag, rho u_x, rho u_y, rho u_z, g_x, g_y, g_z, p),
-//   g = (grad p) / udiag,
+//   g = (grad p) / udiag (the edge phase forms p_R - p_L from the FP64
+//   pressures, like the coordinate differences),
 // so that tmdot = -0.5 (n0_L + n0_R) (p_R - p_L) w
 //               + sum_d [0.5 (m_R + m_L) + 0.5 (g_R + g_L)]_d A_d
 //               - noc sum_d k_d 0.5 (g_R + g_L)_d,
@@ -208,6 +209,7 @@ __global__ void __launch_bounds__(kThreads)
     continuity_edge_fast_k(int64_t E, const int2* __restrict__ edges,
                            const double* __restrict__ coords,
                            const dd* __restrict__ nodebuf,
+                           const double* __restrict__ pressure,
                            const double* __restrict__ area, dd noc,
                            dd inv_tau, dd* __restrict__ buf) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     av[d] = ldd(area + 3 * e + d);
-    dx[d] = ldd(coords + 3 * R + d) - ldd(coords + 3 * L + d);
+    dx[d] = dd_from_double(coords[3 * R + d] - coords[3 * L + d]);
   }
   const dd asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
   const dd axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
@@ -245,7 +247,7 @@ __global__ void __launch_bounds__(kThreads)
     flux = (m + g) * av[d] + flux;
     corr = (av[d] - w * dx[d]) * g + corr;
   }
-  dd tmdot = -(projTimeScale * (nr[7] - nl[7]) * w);
+  dd tmdot = -(projTimeScale * dd_from_double(pressure[R] - pressure[L]) * w);
   tmdot = (tmdot + scale2(flux - noc * corr, 0.5f)) * inv_tau;
   const dd f = -(w * projTimeScale * inv_tau);
   reinterpret_cast<float4*>(buf)[e] = make_float4(f.hi, f.lo, tmdot.hi, tmdot.lo);
@@ -279,12 +281,12 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     av[d] = ldd(area + 3 * e + d);
-    dx[d] = ldd(coords + 3 * R + d) - ldd(coords + 3 * L + d);
+    dx[d] = dd_from_double(coords[3 * R + d] - coords[3 * L + d]);
   }
   const dd asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
   const dd axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
   const dd w = asq * dd_rcp(axdx);
-  dd tmdot = -(projTimeScale * (ldd(pressure + R) - ldd(pressure + L)) * w);
+  dd tmdot = -(projTimeScale * dd_from_double(pressure[R] - pressure[L]) * w);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const dd kxj = av[d] - w * dx[d];
@@ -313,36 +315,52 @@ __device__ __forceinline__ dd van_leer_dd(dd dqm, dd dqp, dd eps) {
 //   LL = cLL I - N/relax,  LR = cLR I + N,  RL = cRL I + N,
 //   RR = cRR I - N/relax,  N_ij = -viscIp A_i A_j / (A.dx)
 // because the advective and diffusive factors do not depend on the
-// component; the rhs is (-tf, +tf). Output per edge (13 SoA arrays of
-// float pairs): cLL, cLR, cRL, cRR, N00, N01, N02, N11, N12, N22, tf0, tf1,
-// tf2.
+// component; the rhs is (-tf, +tf). In float-float arithmetic negation is
+// exact and addition and multiplication are odd, so cLL = -cRL / relax and
+// cRR = -cLR / relax hold bit for bit: the row phase derives the diagonal
+// constants and the edge phase stores 11 SoA arrays of float pairs per
+// edge: cLR, cRL, N00, N01, N02, N11, N12, N22, tf0, tf1, tf2.
 struct MomentumDD {
   dd alpha, alpha_upw, om_alpha, om_alpha_upw, upw, divu_fac, irelax, eps;
 };
 
+struct MomentumIn {
+  const int2* __restrict__ edges;
+  const double* __restrict__ coords;
+  const double* __restrict__ vel;
+  const double* __restrict__ dudx;
+  const double* __restrict__ viscosity;
+  const double* __restrict__ mask;
+  const double* __restrict__ area;
+  const double* __restrict__ mdot;
+  const double* __restrict__ pec;
+};
+
 template <bool LIMITER, bool DIVU>
-__global__ void __launch_bounds__(kThreads, 4)
-    momentum_edge_k(int64_t E, int64_t e0, int64_t e1, const int2* __restrict__ edges,
-                    const double* __restrict__ coords,
-                    const double* __restrict__ vel,
-                    const double* __restrict__ dudx,
-                    const double* __restrict__ viscosity,
-                    const double* __restrict__ mask,
-                    const double* __restrict__ area,
-                    const double* __restrict__ mdotA,
-                    const double* __restrict__ pecA, MomentumDD c,
-                    dd* __restrict__ buf) {
-  const int64_t e = e0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= e1) return;
+__device__ __forceinline__ void momentum_edge(int64_t e, int64_t E, const MomentumIn& in,
+                                              const MomentumDD& c, dd* __restrict__ buf) {
+  const int2* __restrict__ edges = in.edges;
+  const double* __restrict__ coords = in.coords;
+  const double* __restrict__ vel = in.vel;
+  const double* __restrict__ dudx = in.dudx;
+  const double* __restrict__ viscosity = in.viscosity;
+  const double* __restrict__ mask = in.mask;
+  const double* __restrict__ area = in.area;
+  const double* __restrict__ mdotA = in.mdot;
+  const double* __restrict__ pecA = in.pec;
   const int2 lr = edges[e];
   const int64_t L = lr.x, R = lr.y;
-  dd av[3], dx[3], uL[3], uR[3];
+  // coordinate and velocity differences are formed in FP64 and split once:
+  // splitting each operand to a float pair first would keep only 48 bits of
+  // each, and the difference of nearby values would lose the rest
+  dd av[3], dx[3], uL[3], uR[3], du[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     av[d] = ldd(area + 3 * e + d);
-    dx[d] = ldd(coords + 3 * R + d) - ldd(coords + 3 * L + d);
+    dx[d] = dd_from_double(coords[3 * R + d] - coords[3 * L + d]);
     uL[d] = ldd(vel + 3 * L + d);
     uR[d] = ldd(vel + 3 * R + d);
+    du[d] = dd_from_double(vel[3 * R + d] - vel[3 * L + d]);
   }
   const dd mdot = ldd(mdotA + e);
   const dd viscIp = scale2(ldd(viscosity + L) + ldd(viscosity + R), 0.5f);
@@ -354,7 +372,8 @@ __global__ void __launch_bounds__(kThreads, 4)
   for (int d = 0; d < 3; ++d) hdx[d] = scale2(dx[d], 0.5f);
   // duidxj with the over-relaxed non-orthogonal correction (gj holds the
   // sum, not the mean, of the two nodal gradients); duL / duR are the
-  // extrapolation increments 0.5 dx . grad u of each side
+  // extrapolation increments 0.5 dx . grad u of each side, and their sum is
+  // the correction's 0.5 dx . (grad u_L + grad u_R)
   dd duidxj[3][3], duL[3], duR[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -367,8 +386,8 @@ __global__ void __launch_bounds__(kThreads, 4)
     }
     duL[i] = hdx[0] * gl[0] + hdx[1] * gl[1] + hdx[2] * gl[2];
     duR[i] = hdx[0] * gr[0] + hdx[1] * gr[1] + hdx[2] * gr[2];
-    const dd gjuidx = hdx[0] * gj[0] + hdx[1] * gj[1] + hdx[2] * gj[2];
-    const dd corr = ((uR[i] - uL[i]) - gjuidx) * inv_axdx;
+    const dd gjuidx = duL[i] + duR[i];
+    const dd corr = (du[i] - gjuidx) * inv_axdx;
 #pragma unroll
     for (int j = 0; j < 3; ++j) duidxj[i][j] = corr * av[j] + scale2(gj[j], 0.5f);
   }
@@ -376,9 +395,8 @@ __global__ void __launch_bounds__(kThreads, 4)
   if (LIMITER) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const dd du = uR[d] - uL[d];
-      limitL[d] = van_leer_dd(scale2(duL[d], 4.0f) - du, du, c.eps);
-      limitR[d] = van_leer_dd(scale2(duR[d], 4.0f) - du, du, c.eps);
+      limitL[d] = van_leer_dd(scale2(duL[d], 4.0f) - du[d], du[d], c.eps);
+      limitR[d] = van_leer_dd(scale2(duR[d], 4.0f) - du[d], du[d], c.eps);
     }
   }
   const dd pecfac = ldd(pecA + e);
@@ -412,19 +430,26 @@ __global__ void __launch_bounds__(kThreads, 4)
   const dd dlhsfac = t * asq;
   const dd ta0 = t * av[0], ta1 = t * av[1], ta2 = t * av[2];
   dd* b = buf + e;
-  b[0] = ((aUL + aC) - dlhsfac) * c.irelax;
-  b[E] = (aUR + aC) + dlhsfac;
-  b[2 * E] = (-aUL - aC) + dlhsfac;
-  b[3 * E] = ((-aUR - aC) - dlhsfac) * c.irelax;
-  b[4 * E] = ta0 * av[0];
-  b[5 * E] = ta0 * av[1];
-  b[6 * E] = ta0 * av[2];
-  b[7 * E] = ta1 * av[1];
-  b[8 * E] = ta1 * av[2];
-  b[9 * E] = ta2 * av[2];
-  b[10 * E] = tf[0];
-  b[11 * E] = tf[1];
-  b[12 * E] = tf[2];
+  b[0] = (aUR + aC) + dlhsfac;
+  b[E] = (-aUL - aC) + dlhsfac;
+  b[2 * E] = ta0 * av[0];
+  b[3 * E] = ta0 * av[1];
+  b[4 * E] = ta0 * av[2];
+  b[5 * E] = ta1 * av[1];
+  b[6 * E] = ta1 * av[2];
+  b[7 * E] = ta2 * av[2];
+  b[8 * E] = tf[0];
+  b[9 * E] = tf[1];
+  b[10 * E] = tf[2];
+}
+
+template <bool LIMITER, bool DIVU>
+__global__ void __launch_bounds__(kThreads, 4)
+    momentum_edge_k(int64_t E, int64_t e0, int64_t e1, MomentumIn in, MomentumDD c,
+                    dd* __restrict__ buf) {
+  const int64_t e = e0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= e1) return;
+  momentum_edge<LIMITER, DIVU>(e, E, in, c, buf);
 }
 
 // ---------------------------------------------------------------------------
@@ -438,7 +463,7 @@ __global__ void __launch_bounds__(kThreads, 4)
 // (f, tmdot as float pairs). Incident entries come in column order; bit 31
 // marks a repeat of the previous column (periodic duplicates).
 __device__ __forceinline__ double to_f64(double v) { return v; }
-__device__ __forceinline__ double to_f64(dd v) { return dd_to_double(v); }
+__device__ __forceinline__ double to_f64(dd v) { return dd_to_double_int(v); }
 
 template <int KIND>
 __global__ void __launch_bounds__(kRow1Threads)
@@ -515,56 +540,67 @@ __global__ void __launch_bounds__(kRow1Threads)
 
 // 3-dof momentum, one thread per CSR row (three per node row, dof q =
 // thread % 3): each thread accumulates its row of every 3x3 block from the
-// float-pair coefficients and widens it to FP64; a block of kRow3Nodes node
+// float-pair coefficients and widens it to FP64 with integer operations
+// (dd_to_double_int: no FP64 instruction per entry); a block of kRow3Nodes node
 // rows stages their CSR range in shared memory and writes it coalesced.
 // (One thread per node row, with the symmetric blocks widened once, needs
 // a third fewer FP64 adds but ran at a third of the occupancy: the shared
 // staging per node is the same, so measured 0.357 against 0.328 ms.)
+// Off-diagonal block of an incident edge: c_side I + N; diagonal block:
+// -(sum of the other side's constants + sum of N) / relax.
 constexpr int kRow3Nodes = 64;
-__global__ void __launch_bounds__(3 * kRow3Nodes)
-    row3t_k(int64_t R, const int32_t* __restrict__ inc_ptr,
-            const uint32_t* __restrict__ inc, const int32_t* __restrict__ diag_pos,
-            const int64_t* __restrict__ row_ptr, const double* __restrict__ buf,
-            int64_t E, dd irelax, double* __restrict__ values,
-            double* __restrict__ rhs, int accumulate, int smem_bytes) {
-  const dd* cb = reinterpret_cast<const dd*>(buf);
-  extern __shared__ double stage[];
-  const int64_t r0 = int64_t(blockIdx.x) * kRow3Nodes;
-  const int64_t r1 = (r0 + kRow3Nodes < R) ? r0 + kRow3Nodes : R;
-  const int64_t base = row_ptr[3 * r0];
-  const int64_t cnt = row_ptr[3 * r1] - base;
-  const bool staged = cnt * int64_t(sizeof(double)) <= smem_bytes;
+struct Row3Args {
+  int64_t R, E;
+  const int32_t* __restrict__ inc_ptr;
+  const uint32_t* __restrict__ inc;
+  const int32_t* __restrict__ diag_pos;
+  const int64_t* __restrict__ row_ptr;
+  const dd* __restrict__ cb;
+  dd irelax;
+  double* __restrict__ values;
+  double* __restrict__ rhs;
+  int accumulate, smem_bytes;
+};
+
+// One block of kRow3Nodes node rows starting at r0 (blockDim 3 kRow3Nodes).
+__device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double* stage) {
+  const dd* cb = a.cb;
+  const int64_t E = a.E;
+  const int64_t r1 = (r0 + kRow3Nodes < a.R) ? r0 + kRow3Nodes : a.R;
+  const int64_t base = a.row_ptr[3 * r0];
+  const int64_t cnt = a.row_ptr[3 * r1] - base;
+  const bool staged = cnt * int64_t(sizeof(double)) <= a.smem_bytes;
   const int local = threadIdx.x / 3, q = threadIdx.x - 3 * (threadIdx.x / 3);
   const int64_t r = r0 + local;
-  // N slots of row q of the symmetric 3x3 N (N00 N01 N02 N11 N12 N22 at 4..9)
-  const int n0 = q == 0 ? 4 : (q == 1 ? 5 : 6);
-  const int n1 = q == 0 ? 5 : (q == 1 ? 7 : 8);
-  const int n2 = q == 0 ? 6 : (q == 1 ? 8 : 9);
+  // N slots of row q of the symmetric 3x3 N (N00 N01 N02 N11 N12 N22 at 2..7)
+  const int n0 = q == 0 ? 2 : (q == 1 ? 3 : 4);
+  const int n1 = q == 0 ? 3 : (q == 1 ? 5 : 6);
+  const int n2 = q == 0 ? 4 : (q == 1 ? 6 : 7);
   if (r < r1) {
-    const int32_t s = inc_ptr[r], t = inc_ptr[r + 1];
-    const int64_t bq = row_ptr[3 * r + q];
-    double* v = staged ? stage + (bq - base) : values + bq;
-    const bool acc = accumulate && !staged;
+    const int32_t s = a.inc_ptr[r], t = a.inc_ptr[r + 1];
+    const int64_t bq = a.row_ptr[3 * r + q];
+    double* v = staged ? stage + (bq - base) : a.values + bq;
+    const bool acc = a.accumulate && !staged;
     if (s != t) {
-      const int dp = diag_pos[r];
-      dd dgc{}, dN[3] = {}, rr{}, ob[3];
+      const int dp = a.diag_pos[r];
+      dd sother{}, dN[3] = {}, rr{}, ob[3];
       int slot = -1;
       auto put3 = [&](int k, const dd* x) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const double d = dd_to_double(x[c]);
+          const double d = dd_to_double_int(x[c]);
           v[k + c] = acc ? v[k + c] + d : d;
         }
       };
       for (int32_t qi = s; qi < t; ++qi) {
-        const uint32_t w = inc[qi];
+        const uint32_t w = a.inc[qi];
         const bool dup = (w >> 31) != 0;
         const int64_t e = (w & 0x7fffffffu) >> 1;
         const int side = w & 1u;
-        const dd co = cb[(side ? 2 : 1) * E + e];
-        const dd cd = cb[(side ? 3 : 0) * E + e];
+        const dd co = cb[(side ? 1 : 0) * E + e];
+        const dd other = cb[(side ? 0 : 1) * E + e];
         const dd na = cb[n0 * E + e], nb = cb[n1 * E + e], nc = cb[n2 * E + e];
-        const dd f = cb[(10 + q) * E + e];
+        const dd f = cb[(8 + q) * E + e];
         rr = side ? rr + f : rr - f;
         const dd blk[3] = {q == 0 ? na + co : na, q == 1 ? nb + co : nb, q == 2 ? nc + co : nc};
         if (!dup) {
@@ -576,27 +612,33 @@ __global__ void __launch_bounds__(3 * kRow3Nodes)
 #pragma unroll
           for (int c = 0; c < 3; ++c) ob[c] = ob[c] + blk[c];
         }
-        dgc = dgc + cd;
+        sother = sother + other;
         dN[0] = dN[0] + na;
         dN[1] = dN[1] + nb;
         dN[2] = dN[2] + nc;
       }
       put3(3 * (slot < dp ? slot : slot + 1), ob);
-      // diagonal block row q: sum(c) e_q - sum(N)_q / relax
-      const dd m0 = -(dN[0] * irelax), m1 = -(dN[1] * irelax), m2 = -(dN[2] * irelax);
+      // diagonal block row q: -(sum(other) e_q + sum(N)_q) / relax
+      const dd m0 = -(dN[0] * a.irelax), m1 = -(dN[1] * a.irelax), m2 = -(dN[2] * a.irelax);
+      const dd dgc = -(sother * a.irelax);
       const dd db[3] = {q == 0 ? m0 + dgc : m0, q == 1 ? m1 + dgc : m1, q == 2 ? m2 + dgc : m2};
       put3(3 * dp, db);
-      const double d = dd_to_double(rr);
-      rhs[3 * r + q] = accumulate ? rhs[3 * r + q] + d : d;
+      const double d = dd_to_double_int(rr);
+      a.rhs[3 * r + q] = a.accumulate ? a.rhs[3 * r + q] + d : d;
     } else if (!acc) {
-      for (int64_t k = 0; k < row_ptr[3 * r + q + 1] - bq; ++k) v[k] = 0.0;
-      if (!accumulate) rhs[3 * r + q] = 0.0;
+      for (int64_t k = 0; k < a.row_ptr[3 * r + q + 1] - bq; ++k) v[k] = 0.0;
+      if (!a.accumulate) a.rhs[3 * r + q] = 0.0;
     }
   }
   if (!staged) return;
   __syncthreads();
   for (int64_t k = threadIdx.x; k < cnt; k += 3 * kRow3Nodes)
-    values[base + k] = accumulate ? values[base + k] + stage[k] : stage[k];
+    a.values[base + k] = a.accumulate ? a.values[base + k] + stage[k] : stage[k];
+}
+
+__global__ void __launch_bounds__(3 * kRow3Nodes) row3t_k(Row3Args a) {
+  extern __shared__ double stage[];
+  row3_block(int64_t(blockIdx.x) * kRow3Nodes, a, stage);
 }
 
 // applyDirichletBCs / resetRows: identity (or diag_value) rows.
@@ -693,7 +735,7 @@ void launch_continuity_edges(cudaStream_t s, int64_t E, int64_t N,
     continuity_node_k<<<grid_for(N), kThreads, 0, s>>>(
         N, f.velocity, f.dpdx, f.density, f.pressure, f.udiag, nb);
     continuity_edge_fast_k<<<grid_for(E), kThreads, 0, s>>>(
-        E, edges, f.coords, nb, f.area, dd_param(o.noc_fac), dd_param(1.0 / o.tau_scale), b);
+        E, edges, f.coords, nb, f.pressure, f.area, dd_param(o.noc_fac), dd_param(1.0 / o.tau_scale), b);
   } else {
     ContinuityDD c;
     c.noc = dd_param(o.noc_fac);
@@ -714,10 +756,8 @@ void launch_continuity_edges(cudaStream_t s, int64_t E, const int2* edges,
   launch_continuity_edges(s, E, 0, edges, f, o, buf, nullptr);
 }
 
-void launch_momentum_edges(cudaStream_t s, int64_t E, int64_t e0, int64_t e1, const int2* edges,
-                           const nw_momentum_fields& f, const MomentumOpts& o,
-                           double* buf) {
-  if (e1 <= e0) return;
+namespace {
+MomentumDD momentum_dd(const MomentumOpts& o) {
   MomentumDD c;
   c.alpha = dd_param(o.alpha);
   c.alpha_upw = dd_param(o.alpha_upw);
@@ -727,12 +767,29 @@ void launch_momentum_edges(cudaStream_t s, int64_t E, int64_t e0, int64_t e1, co
   c.divu_fac = dd_param(2.0 / 3.0 * o.include_div_u);
   c.irelax = dd_param(1.0 / o.relax);
   c.eps = dd_param(1.0e-16);
+  return c;
+}
+MomentumIn momentum_in(const int2* edges, const nw_momentum_fields& f) {
+  return MomentumIn{edges, f.coords, f.velocity, f.dudx, f.viscosity, f.mask, f.area, f.mdot, f.pecfac};
+}
+Row3Args row3_args(int64_t R, const int32_t* inc_ptr, const uint32_t* inc, const int32_t* diag_pos,
+                   const int64_t* row_ptr, const double* buf, int64_t E, double relax, double* values,
+                   double* rhs, int accumulate, int smem_bytes) {
+  return Row3Args{R, E, inc_ptr, inc, diag_pos, row_ptr, reinterpret_cast<const dd*>(buf),
+                  dd_param(1.0 / relax), values, rhs, accumulate, smem_bytes};
+}
+}  // namespace
+
+void launch_momentum_edges(cudaStream_t s, int64_t E, int64_t e0, int64_t e1, const int2* edges,
+                           const nw_momentum_fields& f, const MomentumOpts& o,
+                           double* buf) {
+  if (e1 <= e0) return;
+  const MomentumDD c = momentum_dd(o);
+  const MomentumIn in = momentum_in(edges, f);
   dd* b = reinterpret_cast<dd*>(buf);
   const bool lim = o.use_limiter != 0, divu = o.include_div_u != 0.0;
-#define NW_MOM(LIM, DIV)                                                     \
-  momentum_edge_k<LIM, DIV><<<grid_for(e1 - e0), kThreads, 0, s>>>(        \
-      E, e0, e1, edges, f.coords, f.velocity, f.dudx, f.viscosity, f.mask, f.area,   \
-      f.mdot, f.pecfac, c, b)
+#define NW_MOM(LIM, DIV) \
+  momentum_edge_k<LIM, DIV><<<grid_for(e1 - e0), kThreads, 0, s>>>(E, e0, e1, in, c, b)
   if (lim && divu) NW_MOM(true, true);
   else if (lim) NW_MOM(true, false);
   else if (divu) NW_MOM(false, true);
@@ -769,9 +826,8 @@ void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
     row1_k<1><<<grid_for(R, kRow1Threads), kRow1Threads, smem_bytes, s>>>(
         R, inc_ptr, inc, diag_pos, row_ptr, buf, E, values, rhs, accumulate, smem_bytes);
   else
-    row3t_k<<<grid_for(R, kRow3Nodes), 3 * kRow3Nodes, smem_bytes, s>>>(
-        R, inc_ptr, inc, diag_pos, row_ptr, buf, E, dd_param(1.0 / relax), values, rhs,
-        accumulate, smem_bytes);
+    row3t_k<<<grid_for(R, kRow3Nodes), 3 * kRow3Nodes, smem_bytes, s>>>(row3_args(
+        R, inc_ptr, inc, diag_pos, row_ptr, buf, E, relax, values, rhs, accumulate, smem_bytes));
 }
 
 void launch_reset_rows(cudaStream_t s, int64_t n, const int64_t* nodes,

@@ -14,10 +14,10 @@ using MomentumOpts = nw_momentum_opts;
 
 // 8-byte coefficient slots per edge written by the edge phase: scalar, six
 // FP64 SoA arrays of E; continuity, one 16-byte record (f, tmdot as float
-// pairs) per edge; momentum, 13 SoA arrays of E float pairs.
+// pairs) per edge; momentum, 11 SoA arrays of E float pairs.
 constexpr int kScalarCoefs = 6;
 constexpr int kContinuityCoefs = 2;
-constexpr int kMomentumCoefs = 13;
+constexpr int kMomentumCoefs = 11;
 
 void launch_scalar_edges(cudaStream_t s, int64_t E, const int2* edges,
                          const nw_scalar_fields& f, const ScalarOpts& o,

@@ -155,6 +155,35 @@ NW_HD double widen(float f) {
 // the same.)
 NW_HD double dd_to_double(dd a) { return widen(a.hi) + widen(a.lo); }
 
+// hi + lo as a double with integer operations only, for the row kernels
+// that widen every CSR entry (GB300 issues FP64 adds at about one lane per
+// SM clock, so one add per entry bounds those kernels). double(hi) is a bit
+// move; lo, at least 24 binades below hi in a normalised pair, is added to
+// that pattern as a count of units in the last place of hi's binade,
+// truncated towards zero (one more binary place when the sum drops below
+// hi's binade, which only a power-of-two hi and a lo of the other sign can
+// do). The low 29 bits of double(hi) are zero and lo is worth less than
+// 2^29 of those units, so the add never carries into the exponent. Result:
+// within one unit in the last place of the correctly rounded hi + lo. Pairs
+// outside that form (zero, subnormal or non-finite hi, non-finite lo, lo
+// fewer than 24 binades below hi) take dd_to_double.
+NW_HD double dd_to_double_int(dd a) {
+  const uint32_t hb = f2u(a.hi), lb = f2u(a.lo);
+  const uint32_t eh = (hb >> 23) & 0xffu, el = (lb >> 23) & 0xffu;
+  if (eh - 1u >= 0xfeu || el == 0xffu) return dd_to_double(a);
+  const uint64_t dh = (uint64_t(hb & 0x80000000u) << 32) | (uint64_t(eh + 896u) << 52) |
+                      (uint64_t(hb & 0x7fffffu) << 29);
+  if ((lb & 0x7fffffffu) == 0) return u2d(dh);
+  // a subnormal lo is its 23 fraction bits at the exponent of el = 1
+  const uint32_t d = eh - (el ? el : 1u);
+  if (d < 24u || d > 255u) return dd_to_double(a);
+  const uint32_t ml = (lb & 0x7fffffu) | (el ? 0x800000u : 0u);
+  const bool neg = ((hb ^ lb) & 0x80000000u) != 0;
+  const int sh = 29 - int(d) + ((neg && (hb & 0x7fffffu) == 0) ? 1 : 0);
+  const uint32_t adj = sh >= 0 ? (ml << sh) : (-sh < 32 ? (ml >> -sh) : 0u);
+  return u2d(neg ? dh - adj : dh + adj);
+}
+
 // Split of a double into hi (top 24 significand bits) + lo (the next 24,
 // rounded), with integer operations for |x| in [2^-62, 2^127); zeros are
 // exact; anything else takes the conversion instructions.

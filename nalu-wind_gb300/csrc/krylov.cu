@@ -13,7 +13,10 @@
 //
 // Sparse kernels use no tensor cores: CSR SpMV assigns a sub-warp to each
 // row; reductions are two-stage over a fixed grid, so every dot product is
-// bitwise reproducible run to run.
+// bitwise reproducible run to run. Every multiply-add of the FP64 solver
+// kernels is an explicit fma and the host-side scalar work is compiled
+// without contraction, so the operation order (and rounding) of the FP64
+// solvers is fixed by the source and can be restated exactly on a CPU.
 //
 // The mixed-precision method keeps FP64 for the outer true residual
 // (iterative refinement), the Gram-Schmidt dot products and the Hessenberg
@@ -53,8 +56,7 @@ __global__ void __launch_bounds__(kBlock)
   if (row >= n) return;
   const int64_t s = rp[row], e = rp[row + 1];
   ACC acc = 0;
-  for (int64_t p = s + lane; p < e; p += LANES)
-    acc += ACC(v[p]) * ACC(x[ci[p]]);
+  for (int64_t p = s + lane; p < e; p += LANES) acc = fma(ACC(v[p]), ACC(x[ci[p]]), acc);
 #pragma unroll
   for (int off = LANES / 2; off > 0; off >>= 1)
     acc += __shfl_down_sync(0xffffffffu, acc, off, LANES);
@@ -76,7 +78,7 @@ __global__ void __launch_bounds__(kBlock)
   T acc = 0;
   for (int64_t p = rp[row] + lane; p < rp[row + 1]; p += LANES) {
     const int64_t c = ci[p];
-    if (UPPER ? c > row : c < row) acc += T(v[p]) * gin[c];
+    if (UPPER ? c > row : c < row) acc = fma(T(v[p]), gin[c], acc);
   }
 #pragma unroll
   for (int off = LANES / 2; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off, LANES);
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(kBlock)
   const int32_t* c = cols + o + lane;
   const VT* vv = v + o + lane;
 #pragma unroll 4
-  for (int k = 0; k < len; ++k) acc += ACC(vv[32 * k]) * ACC(x[c[32 * k]]);
+  for (int k = 0; k < len; ++k) acc = fma(ACC(vv[32 * k]), ACC(x[c[32 * k]]), acc);
   if (row < n) y[row] = b ? XT(ACC(b[row]) - acc) : XT(acc);
 }
 
@@ -430,9 +432,9 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll
       for (int q = 0; q < 8; ++q) a[q] = V[int64_t(k + q) * ld + i];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc -= hs[k + q] * a[q];
+      for (int q = 0; q < 8; ++q) acc = fma(-hs[k + q], a[q], acc);
     }
-    for (; k < nv; ++k) acc -= hs[k] * V[int64_t(k) * ld + i];
+    for (; k < nv; ++k) acc = fma(-hs[k], V[int64_t(k) * ld + i], acc);
     w[i] = acc;
     if (nrm_partial) acc_prod(acc, acc, ss, cc);
   }
@@ -505,7 +507,7 @@ __global__ void __launch_bounds__(kBlock)
     const int n = len[k];
     for (int q = 0; q < n; ++q) {
       const int64_t p = base + 32 * int64_t(q);
-      s -= T(v[p]) * y[cols[p]];
+      s = fma(-T(v[p]), y[cols[p]], s);
     }
   }
   y[i] = s * rd[i];
@@ -571,7 +573,7 @@ __global__ void convert_k(int64_t n, const A* __restrict__ a, B* __restrict__ b)
 __global__ void axpy_k(int64_t n, double alpha, const double* __restrict__ y,
                        double* __restrict__ x) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) x[i] += alpha * y[i];
+  if (i < n) x[i] = fma(alpha, y[i], x[i]);
 }
 // x += y (y FP32), mixed correction
 __global__ void add_f32_k(int64_t n, const float* __restrict__ y,
@@ -588,13 +590,13 @@ __global__ void axpy_t_k(int64_t n, const T* __restrict__ x, T* __restrict__ y) 
 // out = a x + b y (out may alias x or y)
 __global__ void lincomb_k(int64_t n, double a, const double* x, double b, const double* y, double* out) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = a * x[i] + b * y[i];
+  if (i < n) out[i] = fma(a, x[i], b * y[i]);
 }
 // BiCGStab direction: p = r + beta (p - omega v)
 __global__ void bicg_dir_k(int64_t n, const double* __restrict__ r, double beta, double omega,
                            const double* __restrict__ v, double* __restrict__ p) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+  if (i < n) p[i] = fma(beta, fma(-omega, v[i], p[i]), r[i]);
 }
 // BiCGStab update: x += alpha ph + omega sh; r = s - omega t
 __global__ void bicg_upd_k(int64_t n, double alpha, const double* __restrict__ ph, double omega,
@@ -603,8 +605,8 @@ __global__ void bicg_upd_k(int64_t n, double alpha, const double* __restrict__ p
                            double* __restrict__ r) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) {
-    x[i] += alpha * ph[i] + omega * sh[i];
-    r[i] = sv[i] - omega * t[i];
+    x[i] = fma(omega, sh[i], fma(alpha, ph[i], x[i]));
+    r[i] = fma(-omega, t[i], sv[i]);
   }
 }
 // TFQMR half step: w -= alpha Au; dh = uh + coef dh
@@ -613,21 +615,21 @@ __global__ void tfqmr_wd_k(int64_t n, double alpha, const double* __restrict__ A
                            double* __restrict__ dh) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) {
-    w[i] -= alpha * Au[i];
-    dh[i] = uh[i] + coef * dh[i];
+    w[i] = fma(-alpha, Au[i], w[i]);
+    dh[i] = fma(coef, dh[i], uh[i]);
   }
 }
 // TFQMR: v = Aun + beta (Au + beta v)
 __global__ void tfqmr_v_k(int64_t n, const double* __restrict__ Aun, double beta,
                           const double* __restrict__ Au, double* __restrict__ v) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) v[i] = Aun[i] + beta * (Au[i] + beta * v[i]);
+  if (i < n) v[i] = fma(beta, fma(beta, v[i], Au[i]), Aun[i]);
 }
 // p = z + beta p
 __global__ void xpby_k(int64_t n, const double* __restrict__ z, double beta,
                        double* __restrict__ p) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = z[i] + beta * p[i];
+  if (i < n) p[i] = fma(beta, p[i], z[i]);
 }
 // y = sum_k c[k] V[k] (c in a device array), in the vector precision.
 template <typename T>
@@ -640,17 +642,238 @@ __global__ void combine_k(int64_t n, int nv, const T* __restrict__ V,
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   T acc = T(0);
-  for (int k = 0; k < nv; ++k) acc += cs[k] * V[int64_t(k) * ld + i];
+  for (int k = 0; k < nv; ++k) acc = fma(cs[k], V[int64_t(k) * ld + i], acc);
   y[i] = acc;
 }
 
 inline unsigned grid1(int64_t n) { return unsigned((n + kBlock - 1) / kBlock); }
 
+// Explicitly rounded scalar operations (no contraction into fused
+// multiply-adds), so that the level-scheduled sweeps below round exactly as
+// a sequential restatement of the same loops does.
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+
+// One level of the natural-order Gauss-Seidel sweep (Ifpack2 "Symmetric
+// Gauss-Seidel"): y_i = (x_i - sum_{j != i} a_ij y_j) / a_ii over the row's
+// entries in column order. The level schedule guarantees that in the
+// forward sweep every y_j with j > i in the row is still zero and in the
+// backward sweep every y_j with j < i still holds its forward value.
+template <typename VT, typename T>
+__global__ void __launch_bounds__(kBlock)
+    gs_level_k(int64_t cnt, const int32_t* __restrict__ rows, const int64_t* __restrict__ rp,
+               const int32_t* __restrict__ ci, const VT* __restrict__ v,
+               const int64_t* __restrict__ dpos, const T* __restrict__ x, T* __restrict__ y) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= cnt) return;
+  const int64_t i = rows[k];
+  T s = x[i];
+  for (int64_t p = rp[i]; p < rp[i + 1]; ++p) {
+    const int64_t c = ci[p];
+    if (c != i) s = rn_sub(s, rn_mul(T(v[p]), y[c]));
+  }
+  y[i] = rn_div(s, T(v[dpos[i]]));
+}
+
+// ILU(0) factorization of the rows of one forward level (IKJ order, Saad,
+// Iterative Methods for Sparse Linear Systems, Algorithm 10.4): for each
+// entry k < i of row i in column order, l_ik = a_ik / u_kk, then
+// a_ij -= l_ik u_kj for the row's entries j > k present in row k. Rows k < i
+// of the pattern lie on earlier levels and are final.
+__global__ void __launch_bounds__(kBlock)
+    ilu0_level_k(int64_t cnt, const int32_t* __restrict__ rows, const int64_t* __restrict__ rp,
+                 const int32_t* __restrict__ ci, const int64_t* __restrict__ dpos,
+                 double* __restrict__ lu) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= cnt) return;
+  const int64_t i = rows[t];
+  const int64_t e = rp[i + 1];
+  for (int64_t p = rp[i]; p < e; ++p) {
+    const int64_t k = ci[p];
+    if (k >= i) break;
+    const double l = rn_div(lu[p], lu[dpos[k]]);
+    lu[p] = l;
+    int64_t qk = dpos[k] + 1;
+    const int64_t ek = rp[k + 1];
+    for (int64_t q = p + 1; q < e; ++q) {
+      const int64_t j = ci[q];
+      while (qk < ek && ci[qk] < j) ++qk;
+      if (qk < ek && ci[qk] == j) lu[q] = rn_sub(lu[q], rn_mul(l, lu[qk]));
+    }
+  }
+}
+
+// One level of the ILU(0) triangular solves: forward (unit L)
+// y_i = x_i - sum_{k < i} l_ik y_k; backward (U, in place)
+// y_i = (y_i - sum_{j > i} u_ij y_j) / u_ii.
+template <bool UPPER, typename T>
+__global__ void __launch_bounds__(kBlock)
+    ilu0_solve_level_k(int64_t cnt, const int32_t* __restrict__ rows, const int64_t* __restrict__ rp,
+                       const int32_t* __restrict__ ci, const int64_t* __restrict__ dpos,
+                       const T* __restrict__ lu, const T* __restrict__ x, T* __restrict__ y) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= cnt) return;
+  const int64_t i = rows[t];
+  if (!UPPER) {
+    T s = x[i];
+    for (int64_t p = rp[i]; p < dpos[i]; ++p) s = rn_sub(s, rn_mul(lu[p], y[ci[p]]));
+    y[i] = s;
+  } else {
+    T s = y[i];
+    for (int64_t p = dpos[i] + 1; p < rp[i + 1]; ++p) s = rn_sub(s, rn_mul(lu[p], y[ci[p]]));
+    y[i] = rn_div(s, lu[dpos[i]]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GMRES least squares on the device. One thread applies the previous
+// Givens rotations to the new Hessenberg column, forms the next rotation,
+// updates the rotated rhs g and the residual estimate, and records
+// convergence; the host reads the control words one chunk of iterations
+// behind instead of waiting for every column. Every operation is an
+// explicitly rounded FP64 add, multiply, divide or square root (no fused
+// multiply-adds), the same arithmetic as the host restatement of the
+// solver, so iterates and histories do not depend on where it runs.
+struct GivensDev {
+  double *H, *cs, *sn, *g, *hist;
+  int* ctl;  // done, iterations of the cycle, status, basis vectors
+  int m;
+};
+enum { kCtlDone = 0, kCtlIts = 1, kCtlStatus = 2, kCtlBasis = 3 };
+
+__global__ void givens_init_k(GivensDev G, double g0) {
+  if (threadIdx.x != 0) return;
+  for (int k = 0; k <= G.m; ++k) G.g[k] = 0.0;
+  G.g[0] = g0;
+  G.ctl[kCtlDone] = 0;
+  G.ctl[kCtlIts] = 0;
+  G.ctl[kCtlStatus] = NW_OK;
+  G.ctl[kCtlBasis] = 0;
+}
+
+// Column j: h = hs[0..j], hn = ||w||. rel = |g[j+1]| / div; the history
+// entry is rel * hist_mul / hist_div; the cycle stops when rel <= tol or
+// hn == 0 (basis j + 1), on a non-finite estimate (basis j + 1) or when the
+// rotation breaks down (basis j).
+__global__ void givens_step_k(GivensDev G, int j, const double* __restrict__ hs,
+                              const double* __restrict__ hnp, double tol, double div,
+                              double hist_mul, double hist_div) {
+  if (threadIdx.x != 0 || G.ctl[kCtlDone]) return;
+  const int m = G.m;
+  double* H = G.H;
+  const double hn = hnp[0];
+  for (int k = 0; k <= j; ++k) H[size_t(k) * m + j] = hs[k];
+  H[size_t(j + 1) * m + j] = hn;
+  for (int k = 0; k < j; ++k) {
+    const double a = H[size_t(k) * m + j], bb = H[size_t(k + 1) * m + j];
+    H[size_t(k) * m + j] = __dadd_rn(__dmul_rn(G.cs[k], a), __dmul_rn(G.sn[k], bb));
+    H[size_t(k + 1) * m + j] = __dadd_rn(__dmul_rn(-G.sn[k], a), __dmul_rn(G.cs[k], bb));
+  }
+  const double a = H[size_t(j) * m + j], bb = H[size_t(j + 1) * m + j];
+  const double den = __dsqrt_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(bb, bb)));
+  if (!(den > 0.0) || !isfinite(den)) {
+    G.ctl[kCtlStatus] = isfinite(den) ? NW_BREAKDOWN : NW_NAN_DETECTED;
+    G.ctl[kCtlBasis] = j;
+    G.ctl[kCtlDone] = 1;
+    return;
+  }
+  G.cs[j] = __ddiv_rn(a, den);
+  G.sn[j] = __ddiv_rn(bb, den);
+  H[size_t(j) * m + j] = den;
+  H[size_t(j + 1) * m + j] = 0.0;
+  G.g[j + 1] = __dmul_rn(-G.sn[j], G.g[j]);
+  G.g[j] = __dmul_rn(G.cs[j], G.g[j]);
+  G.ctl[kCtlIts] = j + 1;
+  const double rel = __ddiv_rn(fabs(G.g[j + 1]), div);
+  G.hist[j] = __ddiv_rn(__dmul_rn(rel, hist_mul), hist_div);
+  if (!isfinite(rel)) {
+    G.ctl[kCtlStatus] = NW_NAN_DETECTED;
+    G.ctl[kCtlBasis] = j + 1;
+    G.ctl[kCtlDone] = 1;
+  } else if (rel <= tol || hn == 0.0) {
+    G.ctl[kCtlBasis] = j + 1;
+    G.ctl[kCtlDone] = 1;
+  }
+}
+
+// Back substitution H(0:kk, 0:kk) y = g(0:kk), y scaled by yscale, into y.
+__global__ void givens_solve_k(GivensDev G, int kk, double yscale, double* __restrict__ y) {
+  if (threadIdx.x != 0) return;
+  const int m = G.m;
+  for (int i = kk - 1; i >= 0; --i) {
+    double sum = G.g[i];
+    for (int l = i + 1; l < kk; ++l) sum = __dsub_rn(sum, __dmul_rn(G.H[size_t(i) * m + l], y[l]));
+    y[i] = __ddiv_rn(sum, G.H[size_t(i) * m + i]);
+  }
+  if (yscale != 1.0)
+    for (int i = 0; i < kk; ++i) y[i] = __dmul_rn(y[i], yscale);
+}
+
 }  // namespace
+
+template <typename StepFn>
+KrylovSolver::Cycle KrylovSolver::run_cycle(int m, int max_steps, double g0, double tol, double div,
+                                            double hist_mul, double hist_div, StepFn arnoldi,
+                                            const double* hs, const double* hn, cudaStream_t s) {
+  constexpr int kChunk = 2;  // iterations per poll; the host waits one chunk behind
+  GivensDev G{gst_.p,
+              gst_.p + size_t(m_ + 1) * m_,
+              gst_.p + size_t(m_ + 1) * m_ + m_,
+              gst_.p + size_t(m_ + 1) * m_ + 2 * m_,
+              gst_.p + size_t(m_ + 1) * m_ + 3 * m_ + 1,
+              gctl_.p, m_};
+  givens_init_k<<<1, 32, 0, s>>>(G, g0);
+  int launched = 0, pending = -1, slot = 0;
+  bool stop = false;
+  for (int j = 0; j < m && launched < max_steps && !stop; ++j) {
+    arnoldi(j);
+    givens_step_k<<<1, 32, 0, s>>>(G, j, hs, hn, tol, div, hist_mul, hist_div);
+    ++launched;
+    if (launched % kChunk == 0) {
+      NW_CUDA(cudaMemcpyAsync(ctl_pinned_ + 4 * slot, gctl_.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+      NW_CUDA(cudaEventRecord(chunk_ev_[slot], s));
+      if (pending >= 0) {
+        NW_CUDA(cudaEventSynchronize(chunk_ev_[pending]));
+        stop = ctl_pinned_[4 * pending + kCtlDone] != 0;
+      }
+      pending = slot;
+      slot ^= 1;
+    }
+  }
+  NW_CUDA(cudaGetLastError());
+  NW_CUDA(cudaMemcpyAsync(ctl_pinned_ + 8, gctl_.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  NW_CUDA(cudaMemcpyAsync(h_pinned_ + 1024, G.hist, sizeof(double) * std::max(1, launched),
+                          cudaMemcpyDeviceToHost, s));
+  NW_CUDA(cudaStreamSynchronize(s));
+  Cycle c;
+  c.done = ctl_pinned_[8 + kCtlDone] != 0;
+  c.iterations = ctl_pinned_[8 + kCtlIts];
+  c.status = nw_status(ctl_pinned_[8 + kCtlStatus]);
+  c.basis = c.done ? ctl_pinned_[8 + kCtlBasis] : launched;
+  c.hist.assign(h_pinned_ + 1024, h_pinned_ + 1024 + c.iterations);
+  return c;
+}
+
+namespace {
+// y on the device from the cycle's least squares (launch helper)
+void cycle_solution(double* gst, int* gctl, int m, int kk, double yscale, double* y, cudaStream_t s) {
+  GivensDev G{gst, gst + size_t(m + 1) * m, gst + size_t(m + 1) * m + m, gst + size_t(m + 1) * m + 2 * m,
+              gst + size_t(m + 1) * m + 3 * m + 1, gctl, m};
+  givens_solve_k<<<1, 32, 0, s>>>(G, kk, yscale, y);
+}
+}  // namespace
+
 
 // ---------------------------------------------------------------------------
 KrylovSolver::~KrylovSolver() {
   if (h_pinned_) cudaFreeHost(h_pinned_);
+  if (ctl_pinned_) cudaFreeHost(ctl_pinned_);
+  for (cudaEvent_t& e : chunk_ev_)
+    if (e) cudaEventDestroy(e);
 }
 
 void KrylovSolver::setup(const DevCsr& A, int m, cudaStream_t s) {
@@ -676,6 +899,11 @@ void KrylovSolver::setup(const DevCsr& A, int m, cudaStream_t s) {
   partial_.resize(std::max<size_t>(size_t(m_ + 2) * red_blocks_, size_t(grid1(n))));
   scal_.resize(4 * (m_ + 4));
   if (!h_pinned_) NW_CUDA(cudaMallocHost(&h_pinned_, sizeof(double) * 4 * 1024));
+  if (!ctl_pinned_) NW_CUDA(cudaMallocHost(&ctl_pinned_, sizeof(int) * 12));
+  for (cudaEvent_t& e : chunk_ev_)
+    if (!e) NW_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  gst_.resize(size_t(m_ + 1) * m_ + 4 * size_t(m_) + 1);
+  gctl_.resize(4);
   // sliced-ELL layout from the host CSR
   sell_slices_ = 0;
   if (A.row_ptr_host && A.col_idx_host && n > 0) {
@@ -730,6 +958,7 @@ void KrylovSolver::refresh(cudaStream_t s) {
   if (cl_) cl_->refresh(A_.values, s);
   NW_CUDA(cudaGetLastError());
   f32_valid_ = false;
+  ilu_valid_ = false;
   gs_vals16_.release();
 }
 
@@ -981,9 +1210,109 @@ void KrylovSolver::sgs2(const VT* vals, const T* rd, const T* x, T* y, int inner
   NW_CUDA(cudaGetLastError());
 }
 
+void KrylovSolver::setup_levels(cudaStream_t s) {
+  if (levels_ready_) return;
+  const int64_t n = A_.n;
+  if (!A_.row_ptr_host || (!A_.col_idx_host && A_.nnz > 0)) fail(NW_INTERNAL, "host graph needed");
+  const int64_t* rp = A_.row_ptr_host;
+  const int32_t* ci = A_.col_idx_host;
+  std::vector<int32_t> lf(n, 0), lb(n, 0);
+  std::vector<int64_t> dp(n, -1);
+  for (int64_t i = 0; i < n; ++i) {
+    int32_t l = 0;
+    for (int64_t p = rp[i]; p < rp[i + 1]; ++p) {
+      if (ci[p] < i) l = std::max(l, lf[ci[p]] + 1);
+      if (ci[p] == i) dp[i] = p;
+    }
+    if (dp[i] < 0) fail(NW_INVALID_ARG, "a row without a diagonal entry");
+    lf[i] = l;
+  }
+  for (int64_t i = n - 1; i >= 0; --i) {
+    int32_t l = 0;
+    for (int64_t p = rp[i]; p < rp[i + 1]; ++p)
+      if (ci[p] > i) l = std::max(l, lb[ci[p]] + 1);
+    lb[i] = l;
+  }
+  auto group = [&](const std::vector<int32_t>& lev, std::vector<int64_t>& ptr, DeviceArray<int32_t>& rows) {
+    const int32_t nl = n ? *std::max_element(lev.begin(), lev.end()) + 1 : 0;
+    ptr.assign(nl + 1, 0);
+    for (int64_t i = 0; i < n; ++i) ptr[lev[i] + 1]++;
+    for (int32_t l = 0; l < nl; ++l) ptr[l + 1] += ptr[l];
+    std::vector<int32_t> r(n);
+    std::vector<int64_t> pos(ptr.begin(), ptr.end() - 1);
+    for (int64_t i = 0; i < n; ++i) r[pos[lev[i]]++] = int32_t(i);
+    rows.upload(r, s);
+  };
+  group(lf, fl_ptr_, fl_rows_);
+  group(lb, bl_ptr_, bl_rows_);
+  dpos_.upload(dp, s);
+  levels_ready_ = true;
+}
+
+template <typename VT, typename T>
+void KrylovSolver::sgs_natural(const VT* vals, const T* x, T* y, cudaStream_t s) {
+  setup_levels(s);
+  const int64_t n = A_.n;
+  fill_k<T><<<grid1(n), kBlock, 0, s>>>(n, y, T(0));
+  for (int pass = 0; pass < 2; ++pass) {
+    const std::vector<int64_t>& ptr = pass == 0 ? fl_ptr_ : bl_ptr_;
+    const int32_t* rows = pass == 0 ? fl_rows_.p : bl_rows_.p;
+    for (size_t l = 0; l + 1 < ptr.size(); ++l) {
+      const int64_t cnt = ptr[l + 1] - ptr[l];
+      if (cnt)
+        gs_level_k<VT, T><<<grid1(cnt), kBlock, 0, s>>>(cnt, rows + ptr[l], A_.row_ptr, A_.col_idx, vals,
+                                                         dpos_.p, x, y);
+    }
+  }
+  NW_CUDA(cudaGetLastError());
+}
+
+void KrylovSolver::ilu0_factor(cudaStream_t s) {
+  if (ilu_valid_) return;
+  setup_levels(s);
+  lu_.resize(A_.nnz);
+  NW_CUDA(cudaMemcpyAsync(lu_.p, A_.values, A_.nnz * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  for (size_t l = 0; l + 1 < fl_ptr_.size(); ++l) {
+    const int64_t cnt = fl_ptr_[l + 1] - fl_ptr_[l];
+    if (cnt)
+      ilu0_level_k<<<grid1(cnt), kBlock, 0, s>>>(cnt, fl_rows_.p + fl_ptr_[l], A_.row_ptr, A_.col_idx,
+                                                 dpos_.p, lu_.p);
+  }
+  lu32_.resize(A_.nnz);
+  convert_k<double, float><<<grid1(A_.nnz), kBlock, 0, s>>>(A_.nnz, lu_.p, lu32_.p);
+  NW_CUDA(cudaGetLastError());
+  ilu_valid_ = true;
+}
+
+template <typename T>
+void KrylovSolver::ilu0_solve(const T* lu, const T* x, T* y, cudaStream_t s) {
+  for (size_t l = 0; l + 1 < fl_ptr_.size(); ++l) {
+    const int64_t cnt = fl_ptr_[l + 1] - fl_ptr_[l];
+    if (cnt)
+      ilu0_solve_level_k<false, T><<<grid1(cnt), kBlock, 0, s>>>(cnt, fl_rows_.p + fl_ptr_[l], A_.row_ptr,
+                                                                  A_.col_idx, dpos_.p, lu, x, y);
+  }
+  for (size_t l = 0; l + 1 < bl_ptr_.size(); ++l) {
+    const int64_t cnt = bl_ptr_[l + 1] - bl_ptr_[l];
+    if (cnt)
+      ilu0_solve_level_k<true, T><<<grid1(cnt), kBlock, 0, s>>>(cnt, bl_rows_.p + bl_ptr_[l], A_.row_ptr,
+                                                                 A_.col_idx, dpos_.p, lu, y, y);
+  }
+  NW_CUDA(cudaGetLastError());
+}
+
 void KrylovSolver::precond32(const Precond& pc, const float* x, float* y,
                              cudaStream_t s) {
   const int64_t n = A_.n;
+  if (pc.kind == NW_PC_SGS_NATURAL) {
+    sgs_natural<float, float>(vals32_.p, x, y, s);
+    return;
+  }
+  if (pc.kind == NW_PC_RILUK) {
+    ilu0_factor(s);
+    ilu0_solve<float>(lu32_.p, x, y, s);
+    return;
+  }
   if (pc.kind == NW_PC_SGS2) {
     sgs2_32_.resize(size_t(3) * n);
     sgs2<float, float>(vals32_.p, rdiag32_.p, x, y, pc.inner_sweeps, sgs2_32_.p, s);
@@ -1050,6 +1379,15 @@ void KrylovSolver::apply_precond(const Precond& pc, const double* x, double* y,
     sgs2<double, double>(A_.values, rdiag_.p, x, y, pc.inner_sweeps, sgs2_64_.p, s);
     return;
   }
+  if (pc.kind == NW_PC_SGS_NATURAL) {
+    sgs_natural<double, double>(A_.values, x, y, s);
+    return;
+  }
+  if (pc.kind == NW_PC_RILUK) {
+    ilu0_factor(s);
+    ilu0_solve<double>(lu_.p, x, y, s);
+    return;
+  }
   precond_apply_t<double, double>(pc, A_.n, A_.row_ptr, A_.col_idx, A_.values,
                                   rdiag_.p, x, y, s);
 }
@@ -1111,7 +1449,6 @@ SolveResult KrylovSolver::gmres(const nw_solver_cfg& cfg, double tol,
     res.converged = 1;
     return res;
   }
-  std::vector<double> H(size_t(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
   double* V = V_.p;
   double beta = bnorm;
   NW_CUDA(cudaMemcpyAsync(r_.p, b, n * sizeof(double),
@@ -1128,10 +1465,7 @@ SolveResult KrylovSolver::gmres(const nw_solver_cfg& cfg, double tol,
     NW_CUDA(cudaMemcpyAsync(h2, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
     scale_jacobi_k<double><<<grid1(n), kBlock, 0, s>>>(
         n, r_.p, V, h2, fuse_jacobi ? rdiag_.p : nullptr, flexible ? Z_.p : z_.p);
-    std::fill(g.begin(), g.end(), 0.0);
-    g[0] = beta;
-    int j = 0;
-    for (; j < m && its < cfg.max_iterations; ++j) {
+    auto arnoldi = [&](int j) {
       double* vj = V + size_t(j) * n;
       double* zj = flexible ? Z_.p + size_t(j) * n : z_.p;
       if (!fuse_jacobi) apply_precond(pc, vj, zj, s);
@@ -1145,62 +1479,19 @@ SolveResult KrylovSolver::gmres(const nw_solver_cfg& cfg, double tol,
       maxpy_k<double><<<grid1(n), kBlock, 0, s>>>(n, j + 1, V, n, h2 + 1, w_.p, partial_.p);
       reduce_partials_k<<<1, kBlock, 0, s>>>(int(grid1(n)), partial_.p, h2, 0, nullptr);
       sqrt_scalar_k<<<1, 1, 0, s>>>(h2);
-      {
-        double* znext = (j + 1 < m) ? (flexible ? Z_.p + size_t(j + 1) * n : z_.p) : nullptr;
-        scale_jacobi_k<double><<<grid1(n), kBlock, 0, s>>>(
-            n, w_.p, V + size_t(j + 1) * n, h2, (fuse_jacobi && znext) ? rdiag_.p : nullptr, znext);
-      }
-      NW_CUDA(cudaGetLastError());
-      NW_CUDA(cudaMemcpyAsync(h_pinned_, hs, sizeof(double) * (j + 1),
-                              cudaMemcpyDeviceToHost, s));
-      NW_CUDA(cudaMemcpyAsync(h_pinned_ + (j + 1), h2, sizeof(double),
-                              cudaMemcpyDeviceToHost, s));
-      NW_CUDA(cudaStreamSynchronize(s));
-      const double hn = h_pinned_[j + 1];
-      for (int k = 0; k <= j; ++k) H[size_t(k) * m + j] = h_pinned_[k];
-      H[size_t(j + 1) * m + j] = hn;
-      for (int k = 0; k < j; ++k) {
-        const double a = H[size_t(k) * m + j], bb = H[size_t(k + 1) * m + j];
-        H[size_t(k) * m + j] = cs[k] * a + sn[k] * bb;
-        H[size_t(k + 1) * m + j] = -sn[k] * a + cs[k] * bb;
-      }
-      const double a = H[size_t(j) * m + j], bb = H[size_t(j + 1) * m + j];
-      const double den = std::sqrt(a * a + bb * bb);
-      if (!(den > 0.0) || !std::isfinite(den)) {
-        res.status = std::isfinite(den) ? NW_BREAKDOWN : NW_NAN_DETECTED;
-        done = true;
-        break;
-      }
-      cs[j] = a / den;
-      sn[j] = bb / den;
-      H[size_t(j) * m + j] = den;
-      H[size_t(j + 1) * m + j] = 0.0;
-      g[j + 1] = -sn[j] * g[j];
-      g[j] = cs[j] * g[j];
-      ++its;
-      rel = std::abs(g[j + 1]) / bnorm;
-      res.history.push_back(rel);
-      if (!std::isfinite(rel)) {
-        res.status = NW_NAN_DETECTED;
-        done = true;
-        ++j;
-        break;
-      }
-      if (rel <= tol || hn == 0.0) {
-        done = true;
-        ++j;
-        break;
-      }
-    }
-    const int kk = j;
-    for (int i = kk - 1; i >= 0; --i) {
-      double sum = g[i];
-      for (int l = i + 1; l < kk; ++l) sum -= H[size_t(i) * m + l] * y[l];
-      y[i] = sum / H[size_t(i) * m + i];
-    }
+      double* znext = (j + 1 < m) ? (flexible ? Z_.p + size_t(j + 1) * n : z_.p) : nullptr;
+      scale_jacobi_k<double><<<grid1(n), kBlock, 0, s>>>(
+          n, w_.p, V + size_t(j + 1) * n, h2, (fuse_jacobi && znext) ? rdiag_.p : nullptr, znext);
+    };
+    const Cycle c = run_cycle(m, cfg.max_iterations - its, beta, tol, bnorm, 1.0, 1.0, arnoldi, hs, h2, s);
+    its += c.iterations;
+    res.history.insert(res.history.end(), c.hist.begin(), c.hist.end());
+    if (!c.hist.empty()) rel = c.hist.back();
+    if (c.status != NW_OK) res.status = c.status;
+    done = c.done;
+    const int kk = c.basis;
     if (kk > 0) {
-      NW_CUDA(cudaMemcpyAsync(h2, y.data(), sizeof(double) * kk,
-                              cudaMemcpyHostToDevice, s));
+      cycle_solution(gst_.p, gctl_.p, m_, kk, 1.0, h2, s);
       if (flexible) {
         combine_k<double><<<grid1(n), kBlock, 0, s>>>(n, kk, Z_.p, n, h2, w_.p);
         axpy_k<<<grid1(n), kBlock, 0, s>>>(n, 1.0, w_.p, x);
@@ -1474,7 +1765,6 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
     res.converged = 1;
     return res;
   }
-  std::vector<double> H(size_t(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
   const bool fuse_jacobi = pc.kind == NW_PC_JACOBI;
   const bool flexible = pc.kind == NW_PC_LEARNED;
   const int64_t ld = ld32_;
@@ -1493,10 +1783,8 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
     NW_CUDA(cudaMemcpyAsync(h2, &rnorm, sizeof(double), cudaMemcpyHostToDevice, s));
     scale_to_f32_k<<<grid1(n), kBlock, 0, s>>>(n, r_.p, V, h2);
     if (fuse_jacobi) jacobi_k<float><<<grid1(n), kBlock, 0, s>>>(n, rdiag32_.p, V, z32_.p);
-    std::fill(g.begin(), g.end(), 0.0);
-    g[0] = 1.0;  // inner system solved for r / ||r||
-    int j = 0;
-    for (; j < m && its < cfg.max_iterations; ++j) {
+    // inner system solved for r / ||r|| (g0 = 1)
+    auto arnoldi = [&](int j) {
       float* vj = V + size_t(j) * ld;
       float* zj = flexible ? Z32_.p + size_t(j) * ld : z32_.p;
       if (!fuse_jacobi) precond32(pc, vj, zj, s);
@@ -1513,47 +1801,14 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
       sqrt_scalar_k<<<1, 1, 0, s>>>(h2);
       scale_jacobi_k<float><<<grid1(n), kBlock, 0, s>>>(n, w32_.p, V + size_t(j + 1) * ld, h2,
                                                         fuse_jacobi ? rdiag32_.p : nullptr, z32_.p);
-      NW_CUDA(cudaGetLastError());
-      NW_CUDA(cudaMemcpyAsync(h_pinned_, hs, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
-      NW_CUDA(cudaMemcpyAsync(h_pinned_ + (j + 1), h2, sizeof(double), cudaMemcpyDeviceToHost, s));
-      NW_CUDA(cudaStreamSynchronize(s));
-      const double hn = h_pinned_[j + 1];
-      for (int k = 0; k <= j; ++k) H[size_t(k) * m + j] = h_pinned_[k];
-      H[size_t(j + 1) * m + j] = hn;
-      for (int k = 0; k < j; ++k) {
-        const double a = H[size_t(k) * m + j], bb = H[size_t(k + 1) * m + j];
-        H[size_t(k) * m + j] = cs[k] * a + sn[k] * bb;
-        H[size_t(k + 1) * m + j] = -sn[k] * a + cs[k] * bb;
-      }
-      const double a = H[size_t(j) * m + j], bb = H[size_t(j + 1) * m + j];
-      const double den = std::sqrt(a * a + bb * bb);
-      if (!(den > 0.0) || !std::isfinite(den)) {
-        res.status = std::isfinite(den) ? NW_BREAKDOWN : NW_NAN_DETECTED;
-        break;
-      }
-      cs[j] = a / den;
-      sn[j] = bb / den;
-      H[size_t(j) * m + j] = den;
-      H[size_t(j + 1) * m + j] = 0.0;
-      g[j + 1] = -sn[j] * g[j];
-      g[j] = cs[j] * g[j];
-      ++its;
-      const double inner_rel = std::abs(g[j + 1]);
-      res.history.push_back(inner_rel * rnorm / bnorm);
-      if (inner_rel <= itol || hn == 0.0) {
-        ++j;
-        break;
-      }
-    }
-    const int kk = j;
-    for (int i = kk - 1; i >= 0; --i) {
-      double sum = g[i];
-      for (int l = i + 1; l < kk; ++l) sum -= H[size_t(i) * m + l] * y[l];
-      y[i] = sum / H[size_t(i) * m + i] * 1.0;
-    }
+    };
+    const Cycle c = run_cycle(m, cfg.max_iterations - its, 1.0, itol, 1.0, rnorm, bnorm, arnoldi, hs, h2, s);
+    its += c.iterations;
+    res.history.insert(res.history.end(), c.hist.begin(), c.hist.end());
+    if (c.status != NW_OK) res.status = c.status;
+    const int kk = c.basis;
     if (kk > 0) {
-      for (int i = 0; i < kk; ++i) y[i] *= rnorm;
-      NW_CUDA(cudaMemcpyAsync(h2, y.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
+      cycle_solution(gst_.p, gctl_.p, m_, kk, rnorm, h2, s);
       if (flexible) {
         combine_k<float><<<grid1(n), kBlock, 0, s>>>(n, kk, Z32_.p, ld, h2, z32_.p);
       } else {
@@ -1570,7 +1825,7 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
       res.status = NW_NAN_DETECTED;
       break;
     }
-    res.history.back() = rel;
+    if (res.history.size() > 1) res.history.back() = rel;
     if (rel <= tol || res.status != NW_OK) break;
     if (flexible && stalled(stalls, rnorm, prev_rnorm)) {
       res.status = NW_NOT_CONVERGED;

@@ -120,6 +120,27 @@ class KrylovSolver {
   DeviceArray<double> partial_; // deterministic reduction partials
   DeviceArray<double> scal_;    // small device scalars
   double* h_pinned_ = nullptr;  // host mirror of scal_
+  // GMRES least squares on the device (Givens rotations of the Hessenberg
+  // columns, the rotated rhs g, the per-iteration residual estimates, the
+  // back substitution): H (m+1) x m | cs m | sn m | g m+1 | hist m, and the
+  // control words done, iterations of the cycle, status, basis size.
+  DeviceArray<double> gst_;
+  DeviceArray<int> gctl_;
+  int* ctl_pinned_ = nullptr;   // host mirrors of gctl_ (3 slots)
+  cudaEvent_t chunk_ev_[2] = {nullptr, nullptr};
+  struct Cycle {
+    int iterations = 0;  // rotations applied (iterations counted)
+    int basis = 0;       // vectors in the update
+    bool done = false;   // converged, broke down or non-finite
+    nw_status status = NW_OK;
+    std::vector<double> hist;
+  };
+  // One restart cycle's Arnoldi steps (arnoldi(j) launches iteration j's
+  // kernels, ending with the new column in hs[0..j] and its norm at h2[0])
+  // with the Givens update on the device and the host one chunk behind.
+  template <typename StepFn>
+  Cycle run_cycle(int m, int max_steps, double g0, double tol, double div, double hist_mul, double hist_div,
+                  StepFn arnoldi, const double* hs, const double* hn, cudaStream_t s);
   // Sliced ELLPACK copy (slices of 32 rows, column-major within a slice)
   // used by the solver's SpMV: coalesced value/column loads for short rows.
   // sell_map_ holds the CSR index of every slot (-1 for padding).
@@ -147,6 +168,25 @@ class KrylovSolver {
             cudaStream_t s) const;
   DeviceArray<double> sgs2_64_;
   DeviceArray<float> sgs2_32_;
+  // Level schedules of the natural row order (NW_PC_SGS_NATURAL,
+  // NW_PC_RILUK): forward level of row i = 1 + the largest level of the
+  // rows j < i in its pattern, backward the same over j > i; rows of one
+  // level are independent. Built on first use from the host graph.
+  void setup_levels(cudaStream_t s);
+  bool levels_ready_ = false;
+  std::vector<int64_t> fl_ptr_, bl_ptr_;
+  DeviceArray<int32_t> fl_rows_, bl_rows_;
+  DeviceArray<int64_t> dpos_;   // CSR position of each row's diagonal
+  template <typename VT, typename T>
+  void sgs_natural(const VT* vals, const T* x, T* y, cudaStream_t s);
+  // ILU(0) factors on the matrix pattern (L unit lower, U upper), FP64 and
+  // an FP32 copy for the mixed method; refactored after refresh()
+  void ilu0_factor(cudaStream_t s);
+  bool ilu_valid_ = false;
+  DeviceArray<double> lu_;
+  DeviceArray<float> lu32_;
+  template <typename T>
+  void ilu0_solve(const T* lu, const T* x, T* y, cudaStream_t s);
   void sgs_residual32(const float* x, const float* y, float* r, cudaStream_t s, int last) const;
   DeviceArray<float> diag32_;   // FP32 diagonal
   // FP32 copies for the inner solve of the mixed method

@@ -374,6 +374,25 @@ __global__ void __launch_bounds__(kB)
 // Coarse operator applied to the network output, thread per coarse row:
 //   (Ac ec)_I = (ec_I - sum_J w_IJ ec_J) / dinv_I     (Ac = D (I - W))
 // with per-block partial sums of ec' rc and ec' Ac ec (two per block).
+// Jacobi step on the coarse operator, written with w_IJ = -Ac_IJ / Ac_II
+// and dinv = 1 / Ac_II: e_out = dinv r + sum_J w_IJ e_in,J (e_in == nullptr:
+// e_out = dinv r, the step from zero).
+__global__ void coarse_jacobi_k(int64_t nc, const int64_t* __restrict__ cptr,
+                                const int32_t* __restrict__ ccol, const int32_t* __restrict__ cdiag,
+                                const float* __restrict__ wgt, const float* __restrict__ dinv,
+                                const float* __restrict__ rc, const float* __restrict__ ein,
+                                float* __restrict__ eout) {
+  const int64_t I = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (I >= nc) return;
+  float v = dinv[I] * rc[I];
+  if (ein) {
+    const int64_t dpos = cdiag[I];
+    for (int64_t q = cptr[I]; q < cptr[I + 1]; ++q)
+      if (q != dpos) v = fmaf(wgt[q], ein[ccol[q]], v);
+  }
+  eout[I] = v;
+}
+
 __global__ void coarse_apply_k(int64_t nc, const int64_t* __restrict__ cptr,
                                const int32_t* __restrict__ ccol,
                                const int32_t* __restrict__ cdiag,
@@ -847,8 +866,17 @@ void LearnedNet::forward(const CoarseLevel& cl, const float* wgt, const float* d
 
 void LearnedNet::coarse_correction(const CoarseLevel& cl, const float* rc, float* ec,
                                    cudaStream_t s) {
-  forward(cl, cl.wgt.p, cl.dinv.p, rc, ec, s);
   const int nb = int(gridn(cl.nc));
+  if (coarse_mode == 0) {
+    forward(cl, cl.wgt.p, cl.dinv.p, rc, ec, s);
+  } else {
+    work.resize(cl.nc);
+    coarse_jacobi_k<<<nb, kB, 0, s>>>(cl.nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, cl.wgt.p, cl.dinv.p, rc,
+                                      nullptr, coarse_mode == 1 ? ec : work.u.p);
+    if (coarse_mode == 2)
+      coarse_jacobi_k<<<nb, kB, 0, s>>>(cl.nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, cl.wgt.p, cl.dinv.p, rc,
+                                        work.u.p, ec);
+  }
   coarse_apply_k<<<nb, kB, 0, s>>>(cl.nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, cl.wgt.p, cl.dinv.p,
                                    ec, rc, work.aec.p, work.partial.p);
   alpha_k<<<1, kB, 0, s>>>(nb, work.partial.p, work.scal.p);

@@ -86,6 +86,9 @@ struct LearnedNet {
   int post_smooth = 1;  // SGS sweep after the coarse correction
   int agg_passes = 2;   // aggregation passes of the coarse level
   int smoother = 0;     // 0: symmetric GS sweeps around the coarse step; 1: forward / backward
+  // coarse direction: 0 the network; 1 D_c^-1 r_c and 2 two Jacobi sweeps on
+  // Ac (the same cycle and alpha rule without the network, as controls)
+  int coarse_mode = 0;
   // training data (coarse vectors of one aggregation)
   int64_t data_nc = 0, data_nnzc = 0;
   int npairs = 0, nsystems = 0;

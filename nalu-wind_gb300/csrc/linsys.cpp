@@ -116,7 +116,7 @@ void check_cfg(const nw_solver_cfg& c) {
   if (c.max_iterations < 0) fail(NW_INVALID_ARG, "max_iterations < 0");
   if (!(c.tolerance >= 0.0)) fail(NW_INVALID_ARG, "tolerance < 0");
   if (c.method < NW_GMRES || c.method > NW_TFQMR) fail(NW_INVALID_ARG, "bad method");
-  if (c.preconditioner < NW_PC_NONE || c.preconditioner > NW_PC_SGS2)
+  if (c.preconditioner < NW_PC_NONE || c.preconditioner > NW_PC_RILUK)
     fail(NW_INVALID_ARG, "bad preconditioner");
 }
 
@@ -1145,15 +1145,41 @@ nw_status nw_linsys_precond_apply(nw_linsys* ls, int preconditioner,
   return guard([&] {
     need_finalized(ls);
     if (!x || !y) fail(NW_INVALID_ARG, "null vector");
-    if (preconditioner < NW_PC_NONE || preconditioner > NW_PC_SGS2 ||
+    if (preconditioner < NW_PC_NONE || preconditioner > NW_PC_RILUK ||
         preconditioner == NW_PC_LEARNED)
-      fail(NW_INVALID_ARG, "preconditioner must be none, jacobi, sgs or sgs2");
+      fail(NW_INVALID_ARG, "preconditioner must be none, jacobi, mt_sgs, sgs2, sgs or riluk");
     materialize_zero(ls);
     ls->solver.refresh(ls->stream);
     Precond pc = ls->pc;
     pc.kind = preconditioner;
     pc.inner_sweeps = ls->cfg.sgs2_inner_sweeps > 0 ? ls->cfg.sgs2_inner_sweeps : 1;
     ls->solver.apply_precond(pc, x, y, ls->stream);
+  });
+}
+
+nw_status nw_solver_cfg_from_strings(const char* method, const char* preconditioner,
+                                     nw_solver_cfg* cfg) {
+  return guard([&] {
+    if (!method || !preconditioner || !cfg) fail(NW_INVALID_ARG, "null argument");
+    const std::string m(method), p(preconditioner);
+    int mi;
+    if (m == "gmres") mi = NW_GMRES;
+    else if (m == "cg") mi = NW_CG;
+    else if (m == "sstep_gmres") mi = NW_SSTEP_GMRES;
+    else if (m == "tfqmr") mi = NW_TFQMR;
+    else if (m == "bicgstab") mi = NW_BICGSTAB;
+    else fail(NW_INVALID_ARG, "unknown linear solver method '" + m + "'");
+    int pi;
+    if (p == "jacobi" || p == "default") pi = NW_PC_JACOBI;
+    else if (p == "sgs") pi = NW_PC_SGS_NATURAL;
+    else if (p == "mt_sgs") pi = NW_PC_SGS;
+    else if (p == "sgs2") pi = NW_PC_SGS2;
+    else if (p == "riluk") pi = NW_PC_RILUK;
+    else if (p == "ilut" || p == "muelu")
+      fail(NW_INVALID_ARG, "preconditioner '" + p + "' is not built by this library");
+    else fail(NW_INVALID_ARG, "invalid linear solver preconditioner specified: '" + p + "'");
+    cfg->method = mi;
+    cfg->preconditioner = pi;
   });
 }
 
@@ -1164,6 +1190,14 @@ nw_status nw_linsys_sgs_order(nw_linsys* ls, int64_t* order, int* ncolors) {
       for (size_t i = 0; i < ls->color_rows_host.size(); ++i)
         order[i] = ls->color_rows_host[i];
     if (ncolors) *ncolors = int(ls->color_ptr.size()) - 1;
+  });
+}
+
+nw_status nw_linsys_sgs_classes(nw_linsys* ls, int64_t* class_ptr) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!class_ptr) fail(NW_INVALID_ARG, "null class_ptr");
+    for (size_t i = 0; i < ls->color_ptr.size(); ++i) class_ptr[i] = ls->color_ptr[i];
   });
 }
 
@@ -1288,6 +1322,13 @@ nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes,
       fail(NW_INVALID_ARG, "harvested pairs use the current aggregation; clear them first");
     net->net.post_smooth = post_smooth;
     net->net.agg_passes = agg_passes;
+  });
+}
+
+nw_status nw_learned_set_coarse_direction(nw_learned* net, int mode) {
+  return guard([&] {
+    if (!net || mode < 0 || mode > 2) fail(NW_INVALID_ARG, "bad coarse direction mode");
+    net->net.coarse_mode = mode;
   });
 }
 

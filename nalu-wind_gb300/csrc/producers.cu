@@ -45,12 +45,12 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     av[d] = ldd(area + 3 * e + d);
-    dx[d] = ldd(coords + 3 * R + d) - ldd(coords + 3 * L + d);
+    dx[d] = dd_from_double(coords[3 * R + d] - coords[3 * L + d]);
   }
   const dd asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
   const dd axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
   const dd w = asq * dd_rcp(axdx);
-  dd tmdot = -(projTimeScale * (ldd(pressure + R) - ldd(pressure + L)) * w);
+  dd tmdot = -(projTimeScale * dd_from_double(pressure[R] - pressure[L]) * w);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const dd uR = ldd(velocity + 3 * R + d), uL = ldd(velocity + 3 * L + d);
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(kThreads)
   dd udotx = {0.f, 0.f};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const dd dxj = ldd(coords + 3 * R + d) - ldd(coords + 3 * L + d);
+    const dd dxj = dd_from_double(coords[3 * R + d] - coords[3 * L + d]);
     udotx = scale2(dxj, 0.5f) * (ldd(vel + 3 * R + d) + ldd(vel + 3 * L + d)) + udotx;
   }
   const dd pe = dd_abs(udotx) * dd_rcp(diffIp + eps);

@@ -15,12 +15,12 @@ LIB = HERE / "liboracle.so"
 
 
 def build(force: bool = False) -> Path:
-    src = [HERE / "oracle.cpp", HERE / "oracle.h", Path(__file__)]
+    src = [HERE / "oracle.cpp", HERE / "gpu_order.cpp", HERE / "oracle.h", Path(__file__)]
     if not force and LIB.exists() and all(p.stat().st_mtime <= LIB.stat().st_mtime for p in src):
         return LIB
     tmp = LIB.with_suffix(".so.tmp")
     cmd = ["g++", "-O3", "-ffp-contract=off", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
-           "-o", str(tmp), str(HERE / "oracle.cpp")]
+           "-o", str(tmp), str(HERE / "oracle.cpp"), str(HERE / "gpu_order.cpp")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)

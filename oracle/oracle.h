@@ -246,7 +246,8 @@ typedef struct or_solve_report {
 } or_solve_report;
 
 /* precond: 0 none, 1 Jacobi, 2 symmetric Gauss-Seidel in the row order
- * given by `order` (NULL = natural order), 4 two-stage symmetric
+ * given by `order` (NULL = natural order; 5 is the same), 6 ILU(0) (Ifpack2
+ * RILUK at level of fill 0), 4 two-stage symmetric
  * Gauss-Seidel with inner_sweeps Jacobi-Richardson corrections per
  * triangular solve (row order). method: 0 GMRES(kspace), 1 CG,
  * 3 BiCGStab, 4 TFQMR (Belos "bicgstab" / "tfqmr", the strings
@@ -258,6 +259,21 @@ int or_solve(int64_t nrows, const int64_t* row_ptr, const int32_t* col_idx,
              int precond, const int64_t* order, int kspace, int max_iters,
              double tol, double* history, or_solve_report* rep,
              int nthreads, int inner_sweeps);
+
+/* The same solvers (method 0 GMRES, 1 CG, 2 FGMRES, 3 BiCGStab, 4 TFQMR;
+ * precond 0 none, 1 Jacobi, 2 multicolour symmetric Gauss-Seidel over the
+ * colour classes order[class_ptr[c] .. class_ptr[c + 1]), 4 two-stage SGS,
+ * 5 natural-order symmetric Gauss-Seidel, 6 ILU(0))
+ * with every sum in the GPU library's fixed order: reductions over
+ * red_blocks blocks of 256 threads, sliced-ELL SpMV rows, CSR rows over
+ * `lanes` lanes, fused multiply-adds where the GPU kernels use them
+ * (gpu_order.cpp). For parity tests only. Returns 0 or a status. */
+int or_solve_gpu_order(int64_t nrows, const int64_t* row_ptr, const int32_t* col_idx,
+                       const double* vals, const double* b, double* x, int method,
+                       int precond, const int64_t* order, const int64_t* class_ptr,
+                       int nclasses, int kspace, int max_iters, double tol,
+                       double* history, or_solve_report* rep, int inner_sweeps,
+                       int red_blocks, int lanes);
 
 /* Preconditioner application alone (for unit tests). */
 void or_precond_apply(int64_t nrows, const int64_t* row_ptr,

@@ -257,6 +257,34 @@ def solve(row_ptr, col_idx, vals, b, method=0, precond=1, order=None, kspace=50,
     return x, hist[:rep.iterations + 1].copy(), rep
 
 
+def gpu_reduction_blocks(n: int, sms: int) -> int:
+    """Blocks of the GPU library's FP64 reductions for n rows on a device
+    with `sms` multiprocessors (KrylovSolver::setup)."""
+    return max(1, min(8 * sms, (n + 511) // 512))
+
+
+def solve_gpu_order(row_ptr, col_idx, vals, b, method=0, precond=1, order=None, class_ptr=None, kspace=50,
+                    max_iters=50, tol=1e-8, inner_sweeps=1, red_blocks=1, lanes=8):
+    """The FP64 solvers in the GPU library's operation order
+    (or_solve_gpu_order): returns x, history (iterations + 1), report."""
+    row_ptr, vals, b = _i64(row_ptr), _f64(vals), _f64(b)
+    col_idx = np.ascontiguousarray(col_idx, np.int32)
+    n = b.shape[0]
+    x = np.zeros(n)
+    hist = np.zeros(max_iters + 1)
+    rep = SolveReport()
+    od = None if order is None else _i64(order)
+    cp = None if class_ptr is None else _i64(class_ptr)
+    nc = 0 if cp is None else len(cp) - 1
+    st = lib().or_solve_gpu_order(C.c_int64(n), _p(row_ptr, C.c_int64), _p(col_idx, C.c_int32),
+                                  _p(vals, C.c_double), _p(b, C.c_double), _p(x, C.c_double), method, precond,
+                                  _p(od, C.c_int64), _p(cp, C.c_int64), nc, kspace, max_iters, C.c_double(tol),
+                                  _p(hist, C.c_double), C.byref(rep), inner_sweeps, red_blocks, lanes)
+    if st == 1:
+        raise ValueError("or_solve_gpu_order: Gauss-Seidel needs the colour classes")
+    return x, hist[:rep.iterations + 1].copy(), rep
+
+
 def precond_apply(row_ptr, col_idx, vals, kind, x, order=None, inner_sweeps=1):
     row_ptr, vals, x = _i64(row_ptr), _f64(vals), _f64(x)
     col_idx = np.ascontiguousarray(col_idx, np.int32)

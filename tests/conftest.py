@@ -59,3 +59,17 @@ def orc():
 def golds():
     import json
     return json.loads((ROOT / "tests" / "golden" / "reference_golds.json").read_text())
+
+
+def pytest_sessionfinish(session, exitstatus):
+    """With NW_PARITY_REPORT set, write the per-check parity statistics of
+    the assembly comparisons (tests/gpu_util.py) to that JSON file."""
+    import json
+    import os
+    path = os.environ.get("NW_PARITY_REPORT")
+    if not path:
+        return
+    gu = sys.modules.get("gpu_util")
+    if gu is None:
+        return
+    Path(path).write_text(json.dumps(gu.PARITY_STATS, indent=1))

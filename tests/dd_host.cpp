@@ -21,6 +21,10 @@ void dd_back(int64_t n, const float* hi, const float* lo, double* out) {
   for (int64_t i = 0; i < n; ++i) out[i] = nw::dd_to_double(dd{hi[i], lo[i]});
 }
 
+void dd_back_int(int64_t n, const float* hi, const float* lo, double* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = nw::dd_to_double_int(dd{hi[i], lo[i]});
+}
+
 void dd_widen(int64_t n, const float* f, double* out) {
   for (int64_t i = 0; i < n; ++i) out[i] = nw::widen(f[i]);
 }

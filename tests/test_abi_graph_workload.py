@@ -213,3 +213,21 @@ def test_lumped_boundary_area_is_the_shifted_closure(nw, orc, tets, periodic):
     np.add.at(ref, ipn[:, 0], area)
     ref = nw.workload.periodic_sum(m, ref)
     np.testing.assert_allclose(m.bnd_area, ref, rtol=0, atol=1e-15)
+
+
+def test_solver_strings_map_like_the_reference(nw):
+    """TpetraLinearSolverConfig::load's strings (src/LinearSolverConfig.C:
+    37-140) through nw_solver_cfg_from_strings."""
+    m = {"gmres": nw.GMRES, "cg": nw.CG, "tfqmr": nw.TFQMR, "bicgstab": nw.BICGSTAB, "sstep_gmres": nw.SSTEP_GMRES}
+    p = {"jacobi": nw.PC_JACOBI, "default": nw.PC_JACOBI, "sgs": nw.PC_SGS_NATURAL, "mt_sgs": nw.PC_MT_SGS,
+         "sgs2": nw.PC_SGS2, "riluk": nw.PC_RILUK}
+    for ms, mv in m.items():
+        for ps, pv in p.items():
+            cfg = nw.solver_cfg_from_strings(ms, ps, kspace=30)
+            assert (cfg.method, cfg.preconditioner, cfg.kspace) == (mv, pv, 30)
+    for bad in ("ilut", "muelu", "foo"):
+        with pytest.raises(nw.NwError) as e:
+            nw.solver_cfg_from_strings("gmres", bad)
+        assert e.value.status == 1
+    with pytest.raises(nw.NwError):
+        nw.solver_cfg_from_strings("lsqr", "jacobi")

@@ -128,3 +128,34 @@ def test_pair_to_double_is_correctly_rounded(lib):
     for h, l, o in zip(hi.tolist(), lo.tolist(), out.tolist()):
         exact = float(Fraction(h) + Fraction(l))
         assert o == exact, (h, l, o, exact)
+
+
+def test_integer_widening_within_one_ulp(lib):
+    """dd_to_double_int (integer operations only, used by the row kernels):
+    within one unit in the last place of the correctly rounded hi + lo for
+    normalised pairs, including a power-of-two hi with a lo of the other
+    sign (the sum drops below hi's binade); other pairs equal the FP64 path."""
+    from fractions import Fraction
+    import math
+    rng = np.random.default_rng(7)
+    n = 20000
+    hi = (rng.choice([-1, 1], n) * 10.0 ** rng.uniform(-30, 30, n)).astype(np.float32)
+    hi[:500] = (np.sign(rng.normal(size=500)) * 2.0 ** rng.integers(-60, 60, 500)).astype(np.float32)
+    ulp = np.spacing(np.abs(hi)).astype(np.float64)
+    lo = (rng.uniform(-0.5, 0.5, n) * ulp * 2.0 ** -rng.integers(0, 40, n)).astype(np.float32)
+    lo[:250] = -np.sign(hi[:250]) * np.abs(lo[:250])  # power of two hi, lo of the other sign
+    lo[250:260] = 0.0
+    extra_hi = np.array([0.0, -0.0, 1e-40, np.inf, 1.0, 1.0], np.float32)
+    extra_lo = np.array([0.0, 1e-44, 0.0, 0.0, np.float32(2.0 ** -24), -np.float32(2.0 ** -23)], np.float32)
+    hi = np.concatenate([hi, extra_hi])
+    lo = np.concatenate([lo, extra_lo])
+    out = np.zeros(len(hi))
+    ref = np.zeros(len(hi))
+    lib.dd_back_int(C.c_int64(len(hi)), _p(hi, C.c_float), _p(lo, C.c_float), _p(out, C.c_double))
+    lib.dd_back(C.c_int64(len(hi)), _p(hi, C.c_float), _p(lo, C.c_float), _p(ref, C.c_double))
+    for h, l, o, r in zip(hi.tolist(), lo.tolist(), out.tolist(), ref.tolist()):
+        if not math.isfinite(h):
+            assert o == r or (math.isnan(o) and math.isnan(r))
+            continue
+        exact = Fraction(h) + Fraction(l)
+        assert abs(Fraction(o) - exact) <= Fraction(np.spacing(abs(r))), (h, l, o, r)

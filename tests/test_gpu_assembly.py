@@ -158,6 +158,64 @@ def test_gpu_lowmach_momentum_continuity_parity(nw, orc, shape):
 
 
 @pytest.mark.parametrize("renumber", [1, 2])
+def test_gpu_tet_momentum_continuity_parity_40cube(nw, orc, renumber):
+    """The tet workload of the implicit step at 40^3 hexes x 6 tets (68,921
+    nodes, 5 % jitter), node ids randomly permuted (1) or permuted then
+    RCM-renumbered (2): interior momentum (3 dof) and continuity assembly
+    against the oracle."""
+    case = nw.workload.lowmach_case(40, 40, 40, seed=5, stretch=1.0, jitter=0.05, lz=1.0, tets=True,
+                                    renumber=renumber, renumber_seed=7)
+    mesh, nd = case.mesh, case.node
+    fm = dict(coords=mesh.coords, velocity=nd["velocity"], dudx=nd["dudx"], viscosity=nd["viscosity"],
+              density=nd["density"], mask=nd["mask"], area=mesh.area, mdot=case.edge["mdot"],
+              pecfac=case.edge["pecfac"])
+    fc = dict(coords=mesh.coords, velocity=nd["velocity"], dpdx=nd["dpdx"], density=nd["density"],
+              pressure=nd["pressure"], udiag=nd["udiag"], area=mesh.area)
+    mo, co = case.opts["momentum"], case.opts["continuity"]
+    for opts in (mo, nw.MomentumOpts(alpha=0.2, alpha_upw=0.6, upw_factor=1.0, relax=0.7, include_div_u=1.0,
+                                     use_limiter=1)):
+        mod = {k: getattr(opts, k) for k, _ in opts._fields_}
+        ref = oracle_momentum(orc, mesh.edges, mesh.nalu_id, fm, mod)
+        ls3 = _linsys(nw, 3, mesh.num_nodes, mesh.edges)
+        ls3.zero_system()
+        ls3.assemble_momentum(momentum_fields(nw, to_dev_dict(fm)), opts)
+        vals, rhs = ls3.to_host()
+        np.testing.assert_array_equal(ls3.graph()[1], ref["ci"])
+        check_close(vals, ref["vals"], ref["vabs"], f"tet momentum values (order {renumber})")
+        check_close(rhs, ref["rhs"], ref["rabs"], f"tet momentum rhs (order {renumber})")
+    cod = {k: getattr(co, k) for k, _ in co._fields_}
+    ref = oracle_continuity(orc, mesh.edges, mesh.nalu_id, fc, cod)
+    ls = _linsys(nw, 1, mesh.num_nodes, mesh.edges)
+    ls.zero_system()
+    ls.assemble_continuity(continuity_fields(nw, to_dev_dict(fc)), co)
+    vals, rhs = ls.to_host()
+    check_close(vals, ref["vals"], ref["vabs"], f"tet continuity values (order {renumber})")
+    check_close(rhs, ref["rhs"], ref["rabs"], f"tet continuity rhs (order {renumber})")
+
+
+def test_gpu_poisson_continuity_parity_256x256x128(nw, orc):
+    """The full pressure-Poisson matrix of the solver benchmark (256 x 256 x
+    128 stretched box: 8,520,321 rows, 59,377,537 nnz) against the oracle."""
+    import torch
+    case = nw.workload.poisson_case(256, 256, 128, seed=3, stretch=1.04)
+    mesh, nd = case.mesh, case.node
+    fc = dict(coords=mesh.coords, velocity=nd["velocity"], dpdx=nd["dpdx"], density=nd["density"],
+              pressure=nd["pressure"], udiag=nd["udiag"], area=mesh.area)
+    co = case.opts["continuity"]
+    ref = oracle_continuity(orc, mesh.edges, mesh.nalu_id, fc, {k: getattr(co, k) for k, _ in co._fields_})
+    ls = _linsys(nw, 1, mesh.num_nodes, mesh.edges)
+    ls.zero_system()
+    ls.assemble_continuity(continuity_fields(nw, to_dev_dict(fc)), co)
+    vals, rhs = ls.to_host()
+    assert vals.shape[0] == 59_377_537
+    np.testing.assert_array_equal(ls.graph()[0], ref["rp"])
+    check_close(vals, ref["vals"], ref["vabs"], "poisson 256x256x128 values")
+    check_close(rhs, ref["rhs"], ref["rabs"], "poisson 256x256x128 rhs")
+    del ls
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("renumber", [1, 2])
 def test_gpu_tet_continuity_parity(nw, orc, renumber):
     mesh = nw.Mesh(10, 9, 8, tets=True, jitter=0.05, seed=4, renumber=renumber, renumber_seed=11)
     rng = np.random.default_rng(5)

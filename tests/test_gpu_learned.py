@@ -166,10 +166,12 @@ def _solve(nw, ls, pc, method, tol=1e-8):
 
 def test_training_reduces_loss_and_speeds_up_the_solve(nw):
     """Train on pairs from two systems, then solve a held-out system and
-    right-hand side. The method without the network is the same
-    preconditioner with the network's output layer zeroed (no coarse
-    correction: the two SGS sweeps alone); the trained network must cut the
-    FGMRES iteration count."""
+    right-hand side with the trained network and with the same cycle
+    without it: the same network untrained (random initialisation, seed 0),
+    the non-learned coarse direction D_c^-1 r_c (same energy-optimal
+    scaling), and no coarse correction (output layer zeroed: the two SGS
+    sweeps alone). Training must cut the FGMRES iteration count against the
+    untrained network and against no coarse correction."""
     net = nw.Learned(seed=0)
     train_a = _poisson(nw, (40, 40, 24), seed=3, stretch=1.04)
     train_b = _poisson(nw, (40, 40, 24), seed=4, stretch=1.10, jitter=0.05)
@@ -189,11 +191,21 @@ def test_training_reduces_loss_and_speeds_up_the_solve(nw):
     without.set_params(p0)
     test.attach_learned(without)
     rep_0, rel_0 = _solve(nw, test, nw.PC_LEARNED, nw.FGMRES)
+    untrained = nw.Learned(seed=0)
+    test.attach_learned(untrained)
+    rep_u, rel_u = _solve(nw, test, nw.PC_LEARNED, nw.FGMRES)
+    jac = nw.Learned(seed=0)
+    jac.set_coarse_direction(1)
+    test.attach_learned(jac)
+    rep_j, rel_j = _solve(nw, test, nw.PC_LEARNED, nw.FGMRES)
     test.attach_learned(net)
     rep_l, rel_l = _solve(nw, test, nw.PC_LEARNED, nw.FGMRES)
-    assert rep_0.converged and rep_l.converged and rep_l.fallback == 0 and rep_0.fallback == 0
-    assert rel_0 <= 1.01e-8 and rel_l <= 1.01e-8
-    assert rep_l.iterations < rep_0.iterations, (rep_l.iterations, rep_0.iterations)
+    its = dict(trained=rep_l.iterations, untrained=rep_u.iterations, jacobi_coarse=rep_j.iterations,
+               no_coarse=rep_0.iterations)
+    for r, rel in ((rep_0, rel_0), (rep_u, rel_u), (rep_j, rel_j), (rep_l, rel_l)):
+        assert r.converged and r.fallback == 0 and rel <= 1.01e-8, its
+    assert rep_l.iterations < rep_0.iterations, its
+    assert rep_l.iterations < rep_u.iterations, its
 
 
 def test_broken_network_falls_back_to_sgs(nw):

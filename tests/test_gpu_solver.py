@@ -1,8 +1,15 @@
 """GPU Krylov solves through the C ABI vs the oracle's restated solvers.
 
-Tolerances (FP64 plain method): residual histories agree per iteration to
-1e-10 relative (the GPU reductions sum in a different order, and GMRES
-amplifies that slightly over the iterations), solutions to 1e-9 relative.
+FP64 plain methods, two comparisons:
+  * against the oracle's solvers in the GPU's operation order
+    (or_solve_gpu_order: the same reduction grid, warp and block trees,
+    sliced-ELL rows, fused multiply-adds): the same iteration count, every
+    residual-history entry to 1e-12 relative over the whole solve, and the
+    solution to 1e-12 relative (HIST_RTOL);
+  * against the oracle's solvers in the natural serial order (the
+    reference's order): the same algorithm with sums rounded in another
+    order, which a Krylov method carries forward, so the histories agree to
+    1e-10 and less for BiCGStab (the order alone moves its iterates apart).
 Mixed precision: the FP64 true residual reaches the tolerance, and the
 solution error against the FP64 oracle solve is reported and bounded.
 """
@@ -12,6 +19,35 @@ import pytest
 from gpu_util import dev, scalar_fields, to_dev_dict
 
 pytestmark = pytest.mark.gpu
+
+HIST_RTOL = 1e-12
+
+
+def _gpu_order(orc, ls, method, pc, kspace, max_iters, tol, inner=1, lanes=8):
+    """The oracle's solve of the handle's assembled system in the GPU's
+    operation order."""
+    import torch
+    rp, ci = ls.graph()
+    vals, rhs = ls.to_host()
+    order = cp = None
+    if pc == 2:
+        order = ls.sgs_order()[0]
+        cp = ls.sgs_classes()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    G = orc.gpu_reduction_blocks(len(rhs), sms)
+    return orc.solve_gpu_order(rp, ci, vals, rhs, method=method, precond=pc, order=order, class_ptr=cp,
+                               kspace=kspace, max_iters=max_iters, tol=tol, inner_sweeps=inner, red_blocks=G,
+                               lanes=lanes)
+
+
+def _check_gpu_order(rep, hist, xg, ref, what):
+    xo, ho, orep = ref
+    assert rep.iterations == orep.iterations, (what, rep.iterations, orep.iterations)
+    assert len(hist) == len(ho)
+    worst = float(np.max(np.abs(hist - ho) / np.maximum(np.abs(ho), 1e-300)))
+    assert worst <= HIST_RTOL, f"{what}: history differs by {worst:.3e} relative"
+    assert np.linalg.norm(xg - xo) <= HIST_RTOL * np.linalg.norm(xo), what
+    return worst
 
 
 def _scalar_system(nw, n=32):
@@ -48,7 +84,7 @@ def _poisson_system(nw, shape=(24, 24, 16)):
     return ls, case
 
 
-@pytest.mark.parametrize("pc", [1, 2])
+@pytest.mark.parametrize("pc", [0, 1, 2])
 def test_gmres_matches_oracle_history(nw, orc, pc):
     import torch
     ls, case, d = _scalar_system(nw)
@@ -62,13 +98,21 @@ def test_gmres_matches_oracle_history(nw, orc, pc):
     rp, ci = ls.graph()
     vals, rhs = ls.to_host()
     order = ls.sgs_order()[0] if pc == 2 else None
+    xg = x.cpu().numpy()
+    _check_gpu_order(rep, hist, xg, _gpu_order(orc, ls, 0, pc, 50, 5000, 1e-8), f"gmres pc {pc}")
     xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=0, precond=pc, order=order, kspace=50,
                              max_iters=5000, tol=1e-8)
-    assert rep.iterations == orep.iterations
-    np.testing.assert_allclose(hist, ho, rtol=1e-10, atol=0)
-    xg = x.cpu().numpy()
-    assert np.linalg.norm(xg - xo) <= 1e-9 * np.linalg.norm(xo)
     assert rep.final_abs_residual <= 1e-8 * rep.rhs_norm * 1.01
+    if pc == 0:
+        # without a preconditioner GMRES(50) needs ~2,000 iterations on this
+        # system and nearly stagnates in places: the two orders of summation
+        # take different paths (both converge)
+        assert orep.converged and abs(rep.iterations - orep.iterations) <= 0.1 * orep.iterations
+        return
+    assert abs(rep.iterations - orep.iterations) <= 1
+    k = min(len(hist), len(ho))
+    np.testing.assert_allclose(hist[:k], ho[:k], rtol=1e-9, atol=0)
+    assert np.linalg.norm(xg - xo) <= 1e-8 * np.linalg.norm(xo)
 
 
 def test_cg_and_gmres_on_poisson(nw, orc):
@@ -77,12 +121,16 @@ def test_cg_and_gmres_on_poisson(nw, orc):
     nr, _ = ls.sizes()
     rp, ci = ls.graph()
     vals, rhs = ls.to_host()
-    for method in (nw.CG, nw.GMRES):
+    for method in (nw.CG, nw.GMRES, nw.FGMRES):
         ls.set_solver_cfg(nw.solver_cfg(method=method, preconditioner=nw.PC_JACOBI, kspace=30,
                                         max_iterations=3000, tolerance=1e-8))
         x = torch.zeros(nr, dtype=torch.float64, device="cuda")
         rep = ls.solve(x)
         assert rep.converged == 1
+        _check_gpu_order(rep, ls.residual_history(), x.cpu().numpy(),
+                         _gpu_order(orc, ls, method, 1, 30, 3000, 1e-8), f"method {method}")
+        if method == nw.FGMRES:
+            continue
         xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=method, precond=1, kspace=30, max_iters=3000,
                                  tol=1e-8)
         assert abs(rep.iterations - orep.iterations) <= 1
@@ -182,7 +230,9 @@ def test_bicgstab_and_tfqmr_match_oracle(nw, orc, method, pc):
     order = ls.sgs_order()[0] if pc == 2 else None
     xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=m, precond=pc, order=order, kspace=50,
                              max_iters=3000, tol=1e-9)
-    strict = method == "tfqmr"
+    _check_gpu_order(rep, ls.residual_history(), x.cpu().numpy(),
+                     _gpu_order(orc, ls, m, pc, 50, 3000, 1e-9), f"{method} pc {pc}")
+    strict = method == "tfqmr" and pc != 0
     assert orep.converged == 1
     assert abs(rep.iterations - orep.iterations) <= (1 if strict else 2 + 0.05 * orep.iterations)
     k = min(len(ho), len(ls.residual_history()), 30 if strict else 15)
@@ -210,6 +260,8 @@ def test_bicgstab_and_tfqmr_on_advection_diffusion(nw, orc, method, pc):
     rp, ci = ls.graph()
     vals, rhs = ls.to_host()
     order = ls.sgs_order()[0] if pc == 2 else None
+    _check_gpu_order(rep, ls.residual_history(), x.cpu().numpy(),
+                     _gpu_order(orc, ls, m, pc, 50, 3000, 1e-9), f"{method} pc {pc} advection-diffusion")
     xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=m, precond=pc, order=order, kspace=50,
                              max_iters=3000, tol=1e-9)
     assert orep.converged == 1
@@ -242,6 +294,8 @@ def test_two_stage_sgs_matches_oracle(nw, orc, inner):
     x = torch.zeros(nr, dtype=torch.float64, device="cuda")
     rep = ls.solve(x)
     assert rep.converged == 1 and rep.status == 0
+    _check_gpu_order(rep, ls.residual_history(), x.cpu().numpy(),
+                     _gpu_order(orc, ls, 0, 4, 50, 5000, 1e-8, inner=inner), f"sgs2 inner {inner}")
     xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=0, precond=4, kspace=50, max_iters=5000, tol=1e-8,
                              inner_sweeps=inner)
     assert rep.iterations == orep.iterations
@@ -252,3 +306,65 @@ def test_two_stage_sgs_matches_oracle(nw, orc, inner):
     x2 = torch.zeros(nr, dtype=torch.float64, device="cuda")
     rep2 = ls.solve(x2)
     assert rep2.converged == 1 and rep2.final_abs_residual <= 1.01e-8 * rep2.rhs_norm
+
+
+@pytest.mark.parametrize("shape,iters", [((128, 128, 64), 120), ((256, 256, 128), 40)])
+def test_history_parity_at_benchmark_sizes(nw, orc, shape, iters):
+    """The pressure-Poisson systems of the benchmark boxes (1,081,665 and
+    8,520,321 rows): GMRES(50) + Jacobi and CG + Jacobi for a bounded number
+    of iterations, every history entry and the iterate against the oracle in
+    the GPU's order."""
+    import torch
+    ls = nw.workload.poisson_system(shape, seed=3, stretch=1.04)
+    nr, _ = ls.sizes()
+    for method in (nw.GMRES, nw.CG):
+        ls.set_solver_cfg(nw.solver_cfg(method=method, preconditioner=nw.PC_JACOBI, kspace=50,
+                                        max_iterations=iters, tolerance=1e-12))
+        x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+        rep = ls.solve(x)
+        assert rep.iterations == iters
+        _check_gpu_order(rep, ls.residual_history(), x.cpu().numpy(),
+                         _gpu_order(orc, ls, method, 1, 50, iters, 1e-12), f"{shape} method {method}")
+    del ls
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("pcname,kind", [("sgs", 5), ("riluk", 6)])
+@pytest.mark.parametrize("system", ["scalar", "poisson"])
+def test_natural_sgs_and_riluk_match_oracle(nw, orc, pcname, kind, system):
+    """Ifpack2's natural-order "sgs" and "riluk" (ILU(0)), level-scheduled
+    on the GPU: the preconditioner application equals the oracle's
+    sequential restatement bit for bit, and GMRES(50) matches the oracle in
+    the GPU's order (iterations, every history entry to 1e-12, solution) and
+    in the natural order (1e-9)."""
+    import torch
+    if system == "scalar":
+        ls, case, d = _scalar_system(nw)
+    else:
+        ls, case = _poisson_system(nw)
+    cfg = nw.solver_cfg_from_strings("gmres", pcname, kspace=50, max_iterations=3000, tolerance=1e-8)
+    assert cfg.preconditioner == kind
+    ls.set_solver_cfg(cfg)
+    nr, _ = ls.sizes()
+    rp, ci = ls.graph()
+    vals, rhs = ls.to_host()
+    xv = np.random.default_rng(4).normal(size=nr)
+    y = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    ls.precond_apply(kind, dev(xv), y)
+    yo = orc.precond_apply(rp, ci, vals, kind, xv)
+    np.testing.assert_array_equal(y.cpu().numpy(), yo)
+    x = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    assert rep.converged == 1 and rep.status == 0
+    _check_gpu_order(rep, ls.residual_history(), x.cpu().numpy(),
+                     _gpu_order(orc, ls, 0, kind, 50, 3000, 1e-8), f"{pcname} {system}")
+    xo, ho, orep = orc.solve(rp, ci, vals, rhs, method=0, precond=kind, kspace=50, max_iters=3000, tol=1e-8)
+    assert abs(rep.iterations - orep.iterations) <= 1
+    k = min(len(ho), len(ls.residual_history()))
+    np.testing.assert_allclose(ls.residual_history()[:k], ho[:k], rtol=1e-9, atol=0)
+    # the same preconditioners inside the mixed-precision method
+    ls.set_solver_cfg(nw.solver_cfg(method=nw.GMRES, preconditioner=kind, precision=nw.PREC_MIXED, kspace=50,
+                                    inner_kspace=50, max_iterations=3000, tolerance=1e-10))
+    x2 = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    rep2 = ls.solve(x2)
+    assert rep2.converged == 1 and rep2.final_abs_residual <= 1.01e-10 * rep2.rhs_norm
