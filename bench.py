@@ -582,8 +582,9 @@ def implicit_step(nw, stream, args) -> dict:
     import torch
     n = args.step_n
     res = {"workload": f"{n}^3-hex block, 6 tets per hex, 5 % jitter; random and RCM node orders",
-           "step": "producers (mdot, open mdot, grad u, grad p, Peclet factor) + momentum and continuity "
-                   "assembly + open (x+) and symmetry (y, z sides) boundary kernels + continuity solve to 1e-8"}
+           "step": "producers (edge area vectors and dual volumes, mdot, open mdot, grad u, grad p, Peclet "
+                   "factor) + momentum and continuity assembly + open (x+) and symmetry (y, z sides) "
+                   "boundary kernels + continuity solve to 1e-8"}
 
     def dev_t(a):
         return torch.from_numpy(np.ascontiguousarray(a)).cuda()
@@ -628,18 +629,22 @@ def implicit_step(nw, stream, args) -> dict:
                                     solve_incompressible=co.solve_incompressible)
         omo = nw.MomentumOpenOpts(include_div_u=mo.include_div_u, nf_entrain=0.0, entrainment=nw.ENTRAIN_COMPUTED)
         osy = nw.MomentumSymmetryOpts(include_div_u=mo.include_div_u, penalty_factor=0.0)
-        # input producers: mdot, nodal gradients of u and p, Peclet factor
+        # input producers: edge area vectors and dual volumes (as after a
+        # mesh motion), mdot, nodal gradients of u and p, Peclet factor
         dv, ba = dev_t(mesh.dualvol), dev_t(mesh.bnd_area)
         pec_o = nw.PecletOpts(0, 1.0, 2.0, 4.0, 1e-16)
+        geo = nw.Geometry(mesh.num_nodes, mesh.conn, mesh.edges, mesh.nalu_id)
 
         def producers():
+            geo.compute(d["coords"], d["area"], dv, stream.cuda_stream)
+            ev[5].record(stream)
             lsc.compute_mdot(fc, d["mdot"], noc_fac=co.noc_fac, interp_together=co.interp_together)
             lsc.open_mdot(ss_oc, fco, bd["omdot"], noc_fac=co.noc_fac, pstab_fac=1.0)
             lsc.nodal_gradient(d["velocity"], d["area"], dv, d["dudx"], bnd_area_dev=ba, dim1=3)
             lsc.nodal_gradient(d["pressure"], d["area"], dv, d["dpdx"], bnd_area_dev=ba, dim1=1)
             lsc.peclet_factor(d["coords"], d["density"], d["viscosity"], d["velocity"], d["pecfac"], opts=pec_o)
 
-        prod, mom, con, bnd = [], [], [], []
+        prod, mom, con, bnd, geom = [], [], [], [], []
         for it in range(5):
             ev[0].record(stream)
             producers()
@@ -657,6 +662,7 @@ def implicit_step(nw, stream, args) -> dict:
             torch.cuda.synchronize()
             if it >= 2:
                 prod.append(ev[0].elapsed_time(ev[1]))
+                geom.append(ev[0].elapsed_time(ev[5]))
                 mom.append(ev[1].elapsed_time(ev[2]))
                 con.append(ev[2].elapsed_time(ev[3]))
                 bnd.append(ev[3].elapsed_time(ev[4]))
@@ -664,6 +670,7 @@ def implicit_step(nw, stream, args) -> dict:
         r = {"nodes": mesh.num_nodes, "edges": mesh.num_edges, "nnz_momentum": nnz_m, "nnz_continuity": nnz_c,
              "face_ips_open": len(ipn_o), "face_ips_symmetry": len(ipn_s),
              "producers_ms": round(float(np.mean(prod)), 4),
+             "geometry_ms": round(float(np.mean(geom)), 4),
              "momentum_ms": round(float(np.mean(mom)), 4), "continuity_ms": round(float(np.mean(con)), 4),
              "boundary_ms": round(float(np.mean(bnd)), 4)}
         r["assembly_gnnz_s"] = round((nnz_m + nnz_c) / ((r["momentum_ms"] + r["continuity_ms"]) * 1e-3) / 1e9, 3)
@@ -686,7 +693,7 @@ def implicit_step(nw, stream, args) -> dict:
         r["step_ms_learned_mixed"] = round(asm + r["learned_mixed_fgmres30"]["ms"], 2)
         r["step_ms_plain_fp64"] = round(asm + r["plain_fp64_gmres50_jacobi"]["ms"], 2)
         res[name] = r
-        del ss_oc, ss_om, ss_s
+        del ss_oc, ss_om, ss_s, geo
         del lsm, lsc, d
         torch.cuda.empty_cache()
     return res

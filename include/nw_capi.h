@@ -433,6 +433,30 @@ nw_status nw_compute_peclet_factor(nw_linsys* ls, const double* coords,
                                    const double* velocity, const nw_peclet_opts* o,
                                    double* pecnum, double* pecfac);
 
+/* Edge area vectors and dual nodal volumes on the device
+ * (GeometryInteriorAlg::impl_compute_edge_area_vector and
+ * impl_compute_dual_nodal_volume, src/ngp_algorithms/GeometryInteriorAlg.C:
+ * 70-225, with the Hex8 / Tet4 sub-control surfaces and volumes of
+ * src/master_element/Hex8CVFEM.C:361-405,565-591 and Tet4CVFEM.C), for
+ * meshes whose coordinates change. nw_geometry_create takes the host
+ * element connectivity (num_elems x nodes_per_elem, 8 = Hex8 in Exodus
+ * order, 4 = Tet4), the edge list (num_edges x 2, the order of the area
+ * output; every element edge must be in it) and optionally nalu_id
+ * (1-based periodic master id per node: masters and slaves receive the
+ * summed volume); it builds the element -> edge and element -> node
+ * incidences once. nw_geometry_compute then evaluates, from device
+ * coordinates (N x 3), area (E x 3) and dualvol (N) on the given stream
+ * (NULL: the default stream), with no atomics: the area vectors of an edge
+ * and the volumes of a node are summed in element order, so the results
+ * equal nw_mesh_get's host values bit for bit. */
+typedef struct nw_geometry nw_geometry;
+nw_status nw_geometry_create(int64_t num_nodes, int nodes_per_elem, int64_t num_elems,
+                             const int64_t* conn, int64_t num_edges, const int64_t* edge_nodes,
+                             const int64_t* nalu_id, nw_geometry** out);
+nw_status nw_geometry_compute(nw_geometry* g, const double* coords, double* area,
+                              double* dualvol, void* stream);
+nw_status nw_geometry_destroy(nw_geometry* g);
+
 /* ---- node kernels: lumped-mass BDF time terms, added into the system
  * (like sumInto) after the edge assembly. States Nm1, N, Np1; device
  * pointers of the caller's nodes. The edge graph has no entry at all in

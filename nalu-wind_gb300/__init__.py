@@ -247,6 +247,10 @@ SIGNATURES = {
     "nw_linsys_write_matrix_market": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_void_p]),
     "nw_linsys_read_matrix_market": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
     "nw_mesh_box": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(BoxOpts), C.POINTER(C.c_void_p)]),
+    "nw_geometry_create": (C.c_int, [C.c_int64, C.c_int, C.c_int64, _I64P, C.c_int64, _I64P, _I64P,
+                                     C.POINTER(C.c_void_p)]),
+    "nw_geometry_compute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "nw_geometry_destroy": (C.c_int, [C.c_void_p]),
     "nw_mesh_destroy": (C.c_int, [C.c_void_p]),
     "nw_mesh_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P, _I64P, C.POINTER(C.c_int)]),
     "nw_mesh_get": (C.c_int, [C.c_void_p, _DP, _I64P, _I64P, _I64P, _I64P, _DP, _DP, _DP]),
@@ -650,6 +654,38 @@ class Learned:
 
 def gemm_bf16(kind: int, m: int, a_dev, b_dev, out_dev) -> None:
     check(load().nw_gemm_bf16(kind, m, dptr(a_dev), dptr(b_dev), dptr(out_dev)))
+
+
+class Geometry:
+    """Edge area vectors and dual volumes of a mesh on the device
+    (nw_geometry_*): built once from the connectivity and edge list, then
+    compute(coords_dev, area_dev, dualvol_dev) after every mesh motion."""
+
+    def __init__(self, num_nodes: int, conn: np.ndarray, edges: np.ndarray, nalu_id=None):
+        self.lib = load()
+        conn = np.ascontiguousarray(conn, np.int64)
+        edges = np.ascontiguousarray(edges, np.int64)
+        nid = None if nalu_id is None else np.ascontiguousarray(nalu_id, np.int64)
+        h = C.c_void_p()
+        check(self.lib.nw_geometry_create(num_nodes, conn.shape[1], conn.shape[0], _ptr(conn, C.c_int64),
+                                          edges.shape[0], _ptr(edges, C.c_int64),
+                                          None if nid is None else _ptr(nid, C.c_int64), C.byref(h)))
+        self.h = h
+
+    def compute(self, coords_dev, area_dev, dualvol_dev, stream=None) -> None:
+        check(self.lib.nw_geometry_compute(self.h, dptr(coords_dev), dptr(area_dev), dptr(dualvol_dev),
+                                           C.c_void_p(stream) if stream else None))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nw_geometry_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class SideSet:

@@ -23,6 +23,9 @@ BUILD = PKG / "_build"
 LIB = PKG / "libnw_gb300.so"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# sources whose device arithmetic must round every multiply and add
+# separately (they restate host code compiled with -ffp-contract=off)
+NO_FMAD = {"geometry.cu"}
 
 
 def _nvcc() -> str:
@@ -58,6 +61,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         obj = BUILD / (src.name + ".o")
         if src.suffix == ".cu":
             cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
+                   *(["-fmad=false"] if src.name in NO_FMAD else []),
                    "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off", *inc, "-c", str(src), "-o", str(obj)]
         else:
             cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", *inc, "-c", str(src), "-o", str(obj)]

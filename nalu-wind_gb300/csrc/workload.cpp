@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "geometry.h"
 #include "nw_internal.h"
 #include "nw_workload.h"
 
@@ -32,6 +33,9 @@ namespace {
 
 using nw::Error;
 using nw::fail;
+using nw::hex_geometry;
+using nw::quad_area;
+using nw::tet_geometry;
 
 uint64_t splitmix64(uint64_t& s) {
   uint64_t z = (s += 0x9E3779B97F4A7C15ull);
@@ -40,152 +44,6 @@ uint64_t splitmix64(uint64_t& s) {
   return z ^ (z >> 31);
 }
 double uniform01(uint64_t& s) { return double(splitmix64(s) >> 11) * 0x1.0p-53; }
-
-// Hex8 sub-control geometry, same construction as HexSCS::determinant_scs
-// and HexSCV::determinant_scv (src/master_element/Hex8CVFEM.C:363-389,
-// 565-591; include/master_element/Hex8GeometryFunctions.h).
-void hex_points(const double c[8][3], double v[27][3]) {
-  for (int n = 0; n < 8; ++n)
-    for (int d = 0; d < 3; ++d) v[n][d] = c[n][d];
-  for (int d = 0; d < 3; ++d) {
-    v[8][d] = 0.5 * (c[0][d] + c[1][d]);
-    v[9][d] = 0.5 * (c[1][d] + c[2][d]);
-    v[10][d] = 0.5 * (c[2][d] + c[3][d]);
-    v[11][d] = 0.5 * (c[3][d] + c[0][d]);
-    v[12][d] = 0.25 * (c[0][d] + c[1][d] + c[2][d] + c[3][d]);
-    v[13][d] = 0.5 * (c[4][d] + c[5][d]);
-    v[14][d] = 0.5 * (c[5][d] + c[6][d]);
-    v[15][d] = 0.5 * (c[6][d] + c[7][d]);
-    v[16][d] = 0.5 * (c[7][d] + c[4][d]);
-    v[17][d] = 0.25 * (c[4][d] + c[5][d] + c[6][d] + c[7][d]);
-    v[18][d] = 0.5 * (c[1][d] + c[5][d]);
-    v[19][d] = 0.5 * (c[0][d] + c[4][d]);
-    v[20][d] = 0.25 * (c[0][d] + c[1][d] + c[4][d] + c[5][d]);
-    v[21][d] = 0.5 * (c[3][d] + c[7][d]);
-    v[22][d] = 0.5 * (c[2][d] + c[6][d]);
-    v[23][d] = 0.25 * (c[2][d] + c[3][d] + c[6][d] + c[7][d]);
-    v[24][d] = 0.25 * (c[1][d] + c[2][d] + c[5][d] + c[6][d]);
-    v[25][d] = 0.25 * (c[0][d] + c[3][d] + c[4][d] + c[7][d]);
-    double s = 0.0;
-    for (int n = 0; n < 8; ++n) s += c[n][d];
-    v[26][d] = s * 0.125;
-  }
-}
-
-void quad_area(const double q[4][3], double a[3]) {
-  a[0] = a[1] = a[2] = 0.0;
-  double xm[3];
-  for (int d = 0; d < 3; ++d) xm[d] = 0.25 * (q[0][d] + q[1][d] + q[2][d] + q[3][d]);
-  double r1[3] = {q[0][0] - xm[0], q[0][1] - xm[1], q[0][2] - xm[2]};
-  for (int t = 0; t < 4; ++t) {
-    const int ti = (t + 1) % 4;
-    const double r2[3] = {q[ti][0] - xm[0], q[ti][1] - xm[1], q[ti][2] - xm[2]};
-    a[0] += r1[1] * r2[2] - r2[1] * r1[2];
-    a[1] += r1[2] * r2[0] - r2[2] * r1[0];
-    a[2] += r1[0] * r2[1] - r2[0] * r1[1];
-    for (int d = 0; d < 3; ++d) r1[d] = r2[d];
-  }
-  for (int d = 0; d < 3; ++d) a[d] *= 0.5;
-}
-
-double grandy(const double s[8][3]) {
-  double cv[14][3];
-  for (int n = 0; n < 8; ++n)
-    for (int d = 0; d < 3; ++d) cv[n][d] = s[n][d];
-  static const int fn[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4},
-                               {2, 3, 7, 6}, {1, 2, 6, 5}, {0, 4, 3, 7}};
-  for (int k = 0; k < 6; ++k)
-    for (int d = 0; d < 3; ++d)
-      cv[8 + k][d] = 0.25 * (cv[fn[k][0]][d] + cv[fn[k][1]][d] +
-                             cv[fn[k][2]][d] + cv[fn[k][3]][d]);
-  static const int tf[24][3] = {
-      {0, 8, 1},  {8, 2, 1},  {3, 2, 8},  {3, 8, 0},  {6, 9, 5},  {7, 9, 6},
-      {4, 9, 7},  {4, 5, 9},  {10, 0, 1}, {5, 10, 1}, {4, 10, 5}, {4, 0, 10},
-      {7, 6, 11}, {6, 2, 11}, {2, 3, 11}, {3, 7, 11}, {6, 12, 2}, {5, 12, 6},
-      {5, 1, 12}, {1, 2, 12}, {0, 4, 13}, {4, 7, 13}, {7, 3, 13}, {3, 0, 13}};
-  double vol = 0.0;
-  for (int k = 0; k < 24; ++k) {
-    const int p = tf[k][0], q = tf[k][1], r = tf[k][2];
-    double m[3], dx[3];
-    for (int d = 0; d < 3; ++d) m[d] = cv[p][d] + cv[q][d] + cv[r][d];
-    dx[0] = (cv[q][1] - cv[p][1]) * (cv[r][2] - cv[p][2]) -
-            (cv[r][1] - cv[p][1]) * (cv[q][2] - cv[p][2]);
-    dx[1] = (cv[r][0] - cv[p][0]) * (cv[q][2] - cv[p][2]) -
-            (cv[q][0] - cv[p][0]) * (cv[r][2] - cv[p][2]);
-    dx[2] = (cv[q][0] - cv[p][0]) * (cv[r][1] - cv[p][1]) -
-            (cv[r][0] - cv[p][0]) * (cv[q][1] - cv[p][1]);
-    vol += m[0] * dx[0] + m[1] * dx[1] + m[2] * dx[2];
-  }
-  return vol / 18.0;
-}
-
-void hex_geometry(const double c[8][3], double scs[12][3], double scv[8]) {
-  static const int facet[12][4] = {
-      {20, 8, 12, 26},  {24, 9, 12, 26},  {10, 12, 26, 23}, {11, 25, 26, 12},
-      {13, 20, 26, 17}, {17, 14, 24, 26}, {17, 15, 23, 26}, {16, 17, 26, 25},
-      {19, 20, 26, 25}, {20, 18, 24, 26}, {22, 23, 26, 24}, {21, 25, 26, 23}};
-  static const int sub[8][8] = {
-      {0, 8, 12, 11, 19, 20, 26, 25},  {8, 1, 9, 12, 20, 18, 24, 26},
-      {12, 9, 2, 10, 26, 24, 22, 23},  {11, 12, 10, 3, 25, 26, 23, 21},
-      {19, 20, 26, 25, 4, 13, 17, 16}, {20, 18, 24, 26, 13, 5, 14, 17},
-      {26, 24, 22, 23, 17, 14, 6, 15}, {25, 26, 23, 21, 16, 17, 15, 7}};
-  double v[27][3];
-  hex_points(c, v);
-  for (int ip = 0; ip < 12; ++ip) {
-    double q[4][3];
-    for (int k = 0; k < 4; ++k)
-      for (int d = 0; d < 3; ++d) q[k][d] = v[facet[ip][k]][d];
-    quad_area(q, scs[ip]);
-  }
-  for (int ip = 0; ip < 8; ++ip) {
-    double s[8][3];
-    for (int n = 0; n < 8; ++n)
-      for (int d = 0; d < 3; ++d) s[n][d] = v[sub[ip][n]][d];
-    scv[ip] = grandy(s);
-  }
-}
-
-// Tet4 sub-control geometry (TetSCS::determinant_scs / TetSCV::
-// determinant_scv, src/master_element/Tet4CVFEM.C:243-360, 522-620).
-void tet_geometry(const double c[4][3], double scs[6][3], double scv[4]) {
-  double p[15][3];
-  for (int j = 0; j < 4; ++j)
-    for (int d = 0; d < 3; ++d) p[j][d] = c[j][d];
-  const double h = 0.5, t = 1.0 / 3.0;
-  for (int d = 0; d < 3; ++d) {
-    p[4][d] = h * (c[0][d] + c[1][d]);
-    p[5][d] = h * (c[1][d] + c[2][d]);
-    p[6][d] = h * (c[2][d] + c[0][d]);
-    p[7][d] = t * (c[0][d] + c[1][d] + c[2][d]);
-    p[8][d] = h * (c[2][d] + c[3][d]);
-    p[9][d] = h * (c[3][d] + c[1][d]);
-    p[10][d] = t * (c[1][d] + c[2][d] + c[3][d]);
-    p[11][d] = h * (c[0][d] + c[3][d]);
-    p[12][d] = t * (c[0][d] + c[2][d] + c[3][d]);
-    p[13][d] = t * (c[0][d] + c[1][d] + c[3][d]);
-    p[14][d] = 0.0;
-    for (int j = 0; j < 4; ++j) p[14][d] += 0.25 * c[j][d];
-  }
-  static const int facet[6][4] = {{4, 7, 14, 13},  {7, 14, 10, 5},
-                                  {6, 12, 14, 7},  {11, 13, 14, 12},
-                                  {13, 9, 10, 14}, {10, 8, 12, 14}};
-  for (int ip = 0; ip < 6; ++ip) {
-    double q[4][3];
-    for (int k = 0; k < 4; ++k)
-      for (int d = 0; d < 3; ++d) q[k][d] = p[facet[ip][k]][d];
-    quad_area(q, scs[ip]);
-  }
-  static const int sub[4][8] = {{0, 4, 7, 6, 11, 13, 14, 12},
-                                {1, 5, 7, 4, 9, 10, 14, 13},
-                                {2, 6, 7, 5, 8, 12, 14, 10},
-                                {3, 9, 13, 11, 8, 10, 14, 12}};
-  for (int ip = 0; ip < 4; ++ip) {
-    double s[8][3];
-    for (int n = 0; n < 8; ++n)
-      for (int d = 0; d < 3; ++d) s[n][d] = p[sub[ip][n]][d];
-    scv[ip] = grandy(s);
-  }
-}
 
 const int kHexEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
                              {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
