@@ -92,6 +92,7 @@ typedef struct nw_solver_cfg {
   int inner_kspace;       /* mixed: inner restart length */
   double inner_tolerance; /* mixed: relative reduction per inner solve */
   int sgs2_inner_sweeps;  /* "inner_iterations" of sgs2, default 1 (values < 1 mean 1) */
+  int sstep_size;         /* "krylov_step_size" of sstep_gmres, default 5 (values < 1 mean 5) */
 } nw_solver_cfg;
 
 /* Per-solve report: LinearSystem::linearSolveIterations / linearResidual /
@@ -661,6 +662,20 @@ nw_status nw_linsys_extract_diagonal(nw_linsys* ls, int dof, double* diag);
  * relax = the velocity relaxation factor). */
 nw_status nw_udiag_postprocess(nw_linsys* ls, const double* density, const double* dual_volume,
                                double dt, double gamma1, double relax, double* udiag);
+
+/* ---- checkpoint / resume (raw binary; the reference restarts through
+ * Exodus/STK I/O, src/OutputInfo.C:163-181, and dumps matrices with
+ * writeToFile, src/TpetraLinearSystem.C:2017-2102). save writes the graph
+ * (row_ptr, col_idx), values, rhs, the solver configuration, the last
+ * solve's report and residual history and, when x (device, nrows) is not
+ * NULL, that vector; the file carries an FNV-1a checksum. load restores
+ * values, rhs, configuration, report and history into a finalized handle
+ * with the same graph (NW_INVALID_ARG on a different graph, a truncated or
+ * corrupted file), and x when not NULL; rep (optional) receives the saved
+ * report. ---- */
+nw_status nw_linsys_checkpoint_save(nw_linsys* ls, const char* path, const double* x);
+nw_status nw_linsys_checkpoint_load(nw_linsys* ls, const char* path, double* x,
+                                    nw_solve_report* rep);
 
 /* ---- MatrixMarket export / import ---- */
 /* TpetraLinearSystem::writeToFile (src/TpetraLinearSystem.C:2017-2045):

@@ -54,6 +54,7 @@ struct LinearSolverConfig {
   int max_iterations = 50;
   int kspace = 50;
   int inner_iterations = 1;  // "inner_iterations" of sgs2
+  int krylov_step_size = 5;  // "krylov_step_size" of sstep_gmres
 
   nw_solver_cfg to_c() const {
     nw_solver_cfg c{};
@@ -63,6 +64,7 @@ struct LinearSolverConfig {
     c.tolerance = tolerance;
     c.final_tolerance = final_tolerance < 0.0 ? tolerance : final_tolerance;
     c.sgs2_inner_sweeps = inner_iterations;
+    c.sstep_size = krylov_step_size;
     check_status(nw_solver_cfg_from_strings(method.c_str(), preconditioner.c_str(), &c), "solver options");
     return c;
   }

@@ -38,7 +38,7 @@ class SolverCfg(C.Structure):
     _fields_ = [("method", C.c_int), ("preconditioner", C.c_int), ("precision", C.c_int),
                 ("kspace", C.c_int), ("max_iterations", C.c_int), ("tolerance", C.c_double),
                 ("final_tolerance", C.c_double), ("inner_kspace", C.c_int),
-                ("inner_tolerance", C.c_double), ("sgs2_inner_sweeps", C.c_int)]
+                ("inner_tolerance", C.c_double), ("sgs2_inner_sweeps", C.c_int), ("sstep_size", C.c_int)]
 
 
 class SolveReport(C.Structure):
@@ -176,6 +176,8 @@ SIGNATURES = {
                                                   C.c_int64, C.c_int64]),
     "nw_assemble_momentum_rows": (C.c_int, [C.c_void_p, C.POINTER(MomentumOpts)]),
     "nw_linsys_sgs_classes": (C.c_int, [C.c_void_p, _I64P]),
+    "nw_linsys_checkpoint_save": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
+    "nw_linsys_checkpoint_load": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.POINTER(SolveReport)]),
     "nw_solver_cfg_from_strings": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(SolverCfg)]),
     "nw_learned_set_coarse_direction": (C.c_int, [C.c_void_p, C.c_int]),
     "nw_assemble_continuity_edges_noalloc": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
@@ -298,11 +300,11 @@ def dptr(x) -> int:
 
 def solver_cfg(method=GMRES, preconditioner=PC_JACOBI, precision=PREC_FP64, kspace=50,
                max_iterations=50, tolerance=1e-4, final_tolerance=None, inner_kspace=0,
-               inner_tolerance=0.0, sgs2_inner_sweeps=1) -> SolverCfg:
+               inner_tolerance=0.0, sgs2_inner_sweeps=1, sstep_size=5) -> SolverCfg:
     """TpetraLinearSolverConfig::load defaults (src/LinearSolverConfig.C:37-52)."""
     return SolverCfg(method, preconditioner, precision, kspace, max_iterations, tolerance,
                      tolerance if final_tolerance is None else final_tolerance, inner_kspace,
-                     inner_tolerance, sgs2_inner_sweeps)
+                     inner_tolerance, sgs2_inner_sweeps, sstep_size)
 
 
 def solver_cfg_from_strings(method: str, preconditioner: str, **kw) -> SolverCfg:
@@ -467,6 +469,18 @@ class LinearSystem:
         cp = np.zeros(nc + 1, np.int64)
         check(self.lib.nw_linsys_sgs_classes(self.h, _ptr(cp, C.c_int64)))
         return cp
+
+    def checkpoint_save(self, path, x_dev=None) -> None:
+        """Raw binary checkpoint of the system and solver state (and x)."""
+        check(self.lib.nw_linsys_checkpoint_save(self.h, str(path).encode(),
+                                                 None if x_dev is None else C.c_void_p(dptr(x_dev))))
+
+    def checkpoint_load(self, path, x_dev=None) -> "SolveReport":
+        rep = SolveReport()
+        check(self.lib.nw_linsys_checkpoint_load(self.h, str(path).encode(),
+                                                 None if x_dev is None else C.c_void_p(dptr(x_dev)),
+                                                 C.byref(rep)))
+        return rep
 
     def sync(self) -> None:
         check(self.lib.nw_linsys_sync(self.h))

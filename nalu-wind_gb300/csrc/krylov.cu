@@ -1404,6 +1404,8 @@ SolveResult KrylovSolver::solve(const nw_solver_cfg& cfg, double tol,
     r = bicgstab(cfg, tol, pc, b, x, s);
   else if (cfg.method == NW_TFQMR && pc.kind != NW_PC_LEARNED)
     r = tfqmr(cfg, tol, pc, b, x, s);
+  else if (cfg.method == NW_SSTEP_GMRES && pc.kind != NW_PC_LEARNED)
+    r = sstep_gmres(cfg, tol, pc, b, x, s);
   else
     r = gmres(cfg, tol, pc, b, x, cfg.method == NW_FGMRES || pc.kind == NW_PC_LEARNED, s);
   // The learned preconditioner is judged by the FP64 residual: if the
@@ -1511,6 +1513,250 @@ SolveResult KrylovSolver::gmres(const nw_solver_cfg& cfg, double tol,
       res.status = NW_NOT_CONVERGED;
       break;
     }
+  }
+  spmv64(x, b, r_.p, s);
+  res.final_abs = std::sqrt(dot(r_.p, r_.p, s));
+  res.final_rel = rel;
+  res.iterations = its;
+  res.converged = rel <= tol ? 1 : 0;
+  if (res.status == NW_OK && !res.converged) res.status = NW_NOT_CONVERGED;
+  return res;
+}
+
+// s-step GMRES ("TPETRA GMRES S-STEP", selected by src/LinearSolverConfig.C:
+// 57-69 with "Step Size" = krylov_step_size and CholeskyQR2), right
+// preconditioned, FP64. Within a restart cycle the basis grows by blocks of
+// s vectors: the matrix powers w_k = A M^-1 u_k / sigma (u_0 = the last
+// orthonormal vector, u_{k+1} = w_k; sigma, the size of A M^-1 seen on the
+// previous block, keeps the scaled monomial basis near unit length) run
+// without any reduction, then one block orthogonalisation: two classical
+// block Gram-Schmidt passes against the previous basis (C) and CholeskyQR
+// twice on the block (R), each pass one batch of dot products. The Arnoldi
+// relation of the block follows from the change of basis
+//   A M^-1 [u_0 .. u_{s-1}] = sigma [u_1 .. u_s],  U = V T,
+// so the Hessenberg columns are H(:, j0:j0+s) = (sigma T(:, 1:s+1) -
+// H_old T_old) T_new^-1 with T_new upper triangular; Givens rotations then
+// test convergence column by column as in GMRES. In exact arithmetic the
+// iterates are GMRES's; the host synchronises once per pass of a block
+// instead of once per vector.
+SolveResult KrylovSolver::sstep_gmres(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                                      const double* b, double* x, cudaStream_t s) {
+  const int64_t n = A_.n;
+  const int m = std::min(m_, std::max(1, cfg.kspace));
+  const int sstep = cfg.sstep_size > 0 ? cfg.sstep_size : 5;
+  SolveResult res;
+  fill_k<double><<<grid1(n), kBlock, 0, s>>>(n, x, 0.0);
+  const double bnorm = std::sqrt(dot(b, b, s));
+  res.bnorm = bnorm;
+  res.history.push_back(1.0);
+  if (!std::isfinite(bnorm)) {
+    res.status = NW_NAN_DETECTED;
+    return res;
+  }
+  if (bnorm == 0.0) {
+    res.converged = 1;
+    return res;
+  }
+  const int ldc = m + 1;
+  sst_.resize(size_t(ldc) * sstep + size_t(sstep) * sstep + sstep + 8);
+  double* Cd = sst_.p;                        // column k of C at Cd + k ldc
+  double* Gd = Cd + size_t(ldc) * sstep;      // column k of the Gram matrix at Gd + k sstep
+  double* Rd = Gd + size_t(sstep) * sstep;    // one column of R
+  double* Sd = Rd + sstep;                    // one scalar
+  // Hr: the Arnoldi Hessenberg as the blocks produce it; H: its columns
+  // after the Givens rotations (the triangular factor of the least squares)
+  std::vector<double> Hr(size_t(m + 1) * m), H(size_t(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+  std::vector<double> Ch(size_t(ldc) * sstep), Cp(size_t(ldc) * sstep), Gh(size_t(sstep) * sstep);
+  double* V = V_.p;
+  double* h2 = scal_.p + (m_ + 2);
+  NW_CUDA(cudaMemcpyAsync(r_.p, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  double beta = bnorm, rel = 1.0, sigma = 1.0;
+  int its = 0;
+  bool done = false;
+  auto upload = [&](double* dst, const double* src, size_t cnt) {
+    NW_CUDA(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, s));
+  };
+  auto download = [&](double* dst, const double* src, size_t cnt) {
+    NW_CUDA(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    NW_CUDA(cudaStreamSynchronize(s));
+  };
+  while (!done && its < cfg.max_iterations) {
+    upload(h2, &beta, 1);
+    scale_jacobi_k<double><<<grid1(n), kBlock, 0, s>>>(n, r_.p, V, h2, nullptr, nullptr);
+    std::fill(H.begin(), H.end(), 0.0);
+    std::fill(Hr.begin(), Hr.end(), 0.0);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int j0 = 0, kk = 0;
+    while (j0 < m && its < cfg.max_iterations && !done) {
+      const int sb = std::min(sstep, std::min(m - j0, cfg.max_iterations - its));
+      double* W = V + size_t(j0 + 1) * n;
+      // matrix powers
+      upload(Sd, &sigma, 1);
+      for (int k = 0; k < sb; ++k) {
+        double* w = W + size_t(k) * n;
+        apply_precond(pc, V + size_t(j0 + k) * n, z_.p, s);
+        spmv(z_.p, w, s);
+        scale_jacobi_k<double><<<grid1(n), kBlock, 0, s>>>(n, w, w, Sd, nullptr, nullptr);
+      }
+      // two block classical Gram-Schmidt passes against V(:, 0:j0+1)
+      std::fill(Ch.begin(), Ch.end(), 0.0);
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int k = 0; k < sb; ++k) {
+          mdot_k<double><<<red_blocks_, kBlock, 0, s>>>(n, j0 + 1, V, n, W + size_t(k) * n, partial_.p);
+          reduce_partials_k<<<j0 + 1, kBlock, 0, s>>>(red_blocks_, partial_.p, Cd + size_t(k) * ldc, 0, nullptr);
+        }
+        for (int k = 0; k < sb; ++k)
+          maxpy_k<double><<<grid1(n), kBlock, 0, s>>>(n, j0 + 1, V, n, Cd + size_t(k) * ldc,
+                                                      W + size_t(k) * n, nullptr);
+        download(Cp.data(), Cd, size_t(ldc) * sb);
+        for (int k = 0; k < sb; ++k)
+          for (int i = 0; i <= j0; ++i) Ch[size_t(k) * ldc + i] += Cp[size_t(k) * ldc + i];
+      }
+      // CholeskyQR twice on the block: W = Q Rt
+      std::vector<double> Rt(size_t(sb) * sb, 0.0), Rp(size_t(sb) * sb), tmp(size_t(sb) * sb);
+      for (int k = 0; k < sb; ++k) Rt[size_t(k) * sb + k] = 1.0;  // Rt[i][k] at k sb + i
+      bool broke = false;
+      for (int pass = 0; pass < 2 && !broke; ++pass) {
+        for (int k = 0; k < sb; ++k) {
+          mdot_k<double><<<red_blocks_, kBlock, 0, s>>>(n, sb, W, n, W + size_t(k) * n, partial_.p);
+          reduce_partials_k<<<sb, kBlock, 0, s>>>(red_blocks_, partial_.p, Gd + size_t(k) * sstep, 0, nullptr);
+        }
+        download(Gh.data(), Gd, size_t(sstep) * sb);
+        std::fill(Rp.begin(), Rp.end(), 0.0);
+        for (int k = 0; k < sb && !broke; ++k) {
+          for (int i = 0; i < k; ++i) {
+            double v = Gh[size_t(k) * sstep + i];
+            for (int l = 0; l < i; ++l) v -= Rp[size_t(i) * sb + l] * Rp[size_t(k) * sb + l];
+            Rp[size_t(k) * sb + i] = v / Rp[size_t(i) * sb + i];
+          }
+          double d = Gh[size_t(k) * sstep + k];
+          for (int l = 0; l < k; ++l) d -= Rp[size_t(k) * sb + l] * Rp[size_t(k) * sb + l];
+          if (!(d > 0.0) || !std::isfinite(d)) {
+            broke = true;
+            break;
+          }
+          Rp[size_t(k) * sb + k] = std::sqrt(d);
+        }
+        if (broke) break;
+        for (int k = 0; k < sb; ++k) {
+          double* w = W + size_t(k) * n;
+          if (k > 0) {
+            upload(Rd, &Rp[size_t(k) * sb], size_t(k));
+            maxpy_k<double><<<grid1(n), kBlock, 0, s>>>(n, k, W, n, Rd, w, nullptr);
+          }
+          upload(Sd, &Rp[size_t(k) * sb + k], 1);
+          scale_jacobi_k<double><<<grid1(n), kBlock, 0, s>>>(n, w, w, Sd, nullptr, nullptr);
+        }
+        // Rt = Rp Rt (both upper triangular)
+        for (int k = 0; k < sb; ++k)
+          for (int i = 0; i <= k; ++i) {
+            double v = 0.0;
+            for (int l = i; l <= k; ++l) v += Rp[size_t(l) * sb + i] * Rt[size_t(k) * sb + l];
+            tmp[size_t(k) * sb + i] = v;
+          }
+        for (int k = 0; k < sb; ++k)
+          for (int i = 0; i <= k; ++i) Rt[size_t(k) * sb + i] = tmp[size_t(k) * sb + i];
+      }
+      if (broke) {
+        res.status = NW_BREAKDOWN;
+        done = true;
+        break;
+      }
+      // Hessenberg columns j0 .. j0 + sb - 1: M = sigma T(:, 1:sb+1) - H_old T_old,
+      // then H_new = M T_new^-1 (rows 0 .. j0 + sb)
+      const int rows = j0 + sb + 1;
+      std::vector<double> Mx(size_t(rows) * sb, 0.0), Tn(size_t(sb) * sb, 0.0), Hn(size_t(rows) * sb, 0.0);
+      for (int k = 0; k < sb; ++k) {
+        for (int i = 0; i <= j0; ++i) Mx[size_t(k) * rows + i] = sigma * Ch[size_t(k) * ldc + i];
+        for (int i = 0; i <= k; ++i) Mx[size_t(k) * rows + j0 + 1 + i] = sigma * Rt[size_t(k) * sb + i];
+        // - H_old T_old: column k of T_old is column k - 1 of C (rows 0 .. j0 - 1)
+        if (k > 0)
+          for (int i = 0; i <= j0; ++i) {
+            double v = 0.0;
+            for (int l = 0; l < j0; ++l) v += Hr[size_t(i) * m + l] * Ch[size_t(k - 1) * ldc + l];
+            Mx[size_t(k) * rows + i] -= v;
+          }
+        // T_new: rows v_j0 .. v_{j0+sb-1}
+        if (k == 0) {
+          Tn[0] = 1.0;
+        } else {
+          Tn[size_t(k) * sb + 0] = Ch[size_t(k - 1) * ldc + j0];
+          for (int i = 1; i <= k; ++i) Tn[size_t(k) * sb + i] = Rt[size_t(k - 1) * sb + i - 1];
+        }
+      }
+      for (int k = 0; k < sb; ++k)
+        for (int i = 0; i < rows; ++i) {
+          double v = Mx[size_t(k) * rows + i];
+          for (int l = 0; l < k; ++l) v -= Hn[size_t(l) * rows + i] * Tn[size_t(k) * sb + l];
+          Hn[size_t(k) * rows + i] = v / Tn[size_t(k) * sb + k];
+        }
+      for (int k = 0; k < sb; ++k) {
+        const int j = j0 + k;
+        for (int i = 0; i <= j + 1; ++i) Hr[size_t(i) * m + j] = H[size_t(i) * m + j] = Hn[size_t(k) * rows + i];
+      }
+      // Givens rotations column by column
+      for (int k = 0; k < sb; ++k) {
+        const int j = j0 + k;
+        for (int q = 0; q < j; ++q) {
+          const double a = H[size_t(q) * m + j], bb = H[size_t(q + 1) * m + j];
+          H[size_t(q) * m + j] = cs[q] * a + sn[q] * bb;
+          H[size_t(q + 1) * m + j] = -sn[q] * a + cs[q] * bb;
+        }
+        const double a = H[size_t(j) * m + j], bb = H[size_t(j + 1) * m + j];
+        const double den = std::sqrt(a * a + bb * bb);
+        if (!(den > 0.0) || !std::isfinite(den)) {
+          res.status = std::isfinite(den) ? NW_BREAKDOWN : NW_NAN_DETECTED;
+          done = true;
+          kk = j;
+          break;
+        }
+        cs[j] = a / den;
+        sn[j] = bb / den;
+        H[size_t(j) * m + j] = den;
+        H[size_t(j + 1) * m + j] = 0.0;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        ++its;
+        rel = std::abs(g[j + 1]) / bnorm;
+        res.history.push_back(rel);
+        kk = j + 1;
+        if (!std::isfinite(rel)) {
+          res.status = NW_NAN_DETECTED;
+          done = true;
+          break;
+        }
+        if (rel <= tol) {
+          done = true;
+          break;
+        }
+      }
+      // the next block's scaling: |A M^-1 u_0| of this block
+      {
+        double w0 = 0.0;
+        for (int i = 0; i <= j0; ++i) w0 += Ch[i] * Ch[i];
+        w0 += Rt[0] * Rt[0];
+        const double next = sigma * std::sqrt(w0);
+        if (std::isfinite(next) && next > 0.0) sigma = next;
+      }
+      j0 += sb;
+    }
+    for (int i = kk - 1; i >= 0; --i) {
+      double sum = g[i];
+      for (int l = i + 1; l < kk; ++l) sum -= H[size_t(i) * m + l] * y[l];
+      y[i] = sum / H[size_t(i) * m + i];
+    }
+    if (kk > 0) {
+      upload(h2, y.data(), size_t(kk));
+      combine_k<double><<<grid1(n), kBlock, 0, s>>>(n, kk, V, n, h2, w_.p);
+      apply_precond(pc, w_.p, z_.p, s);
+      axpy_k<<<grid1(n), kBlock, 0, s>>>(n, 1.0, z_.p, x);
+      NW_CUDA(cudaGetLastError());
+    }
+    if (done || its >= cfg.max_iterations) break;
+    spmv64(x, b, r_.p, s);
+    beta = std::sqrt(dot(r_.p, r_.p, s));
+    if (beta == 0.0) break;
   }
   spmv64(x, b, r_.p, s);
   res.final_abs = std::sqrt(dot(r_.p, r_.p, s));

@@ -106,6 +106,9 @@ class KrylovSolver {
                        const double* b, double* x, cudaStream_t s);
   SolveResult tfqmr(const nw_solver_cfg& cfg, double tol, const Precond& pc,
                     const double* b, double* x, cudaStream_t s);
+  SolveResult sstep_gmres(const nw_solver_cfg& cfg, double tol, const Precond& pc,
+                          const double* b, double* x, cudaStream_t s);
+  DeviceArray<double> sst_;     // s-step GMRES block coefficients
   DeviceArray<double> aux_;     // work vectors of BiCGStab / TFQMR
   LearnedNet* net_ = nullptr;
   CoarseLevel* cl_ = nullptr;

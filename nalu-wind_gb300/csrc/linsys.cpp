@@ -65,6 +65,7 @@ struct nw_linsys {
   std::vector<int64_t> color_ptr;
   std::vector<int32_t> color_rows_host;
   std::vector<double> history;
+  nw_solve_report last_report{};  // of the last solve (checkpointed)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false;
   nw_learned* learned = nullptr;
@@ -108,6 +109,7 @@ nw_solver_cfg default_cfg() {
   c.inner_kspace = 0;
   c.inner_tolerance = 0;
   c.sgs2_inner_sweeps = 1;
+  c.sstep_size = 5;
   return c;
 }
 
@@ -115,7 +117,8 @@ void check_cfg(const nw_solver_cfg& c) {
   if (c.kspace < 1 || c.kspace > 1000) fail(NW_INVALID_ARG, "kspace out of range");
   if (c.max_iterations < 0) fail(NW_INVALID_ARG, "max_iterations < 0");
   if (!(c.tolerance >= 0.0)) fail(NW_INVALID_ARG, "tolerance < 0");
-  if (c.method < NW_GMRES || c.method > NW_TFQMR) fail(NW_INVALID_ARG, "bad method");
+  if (c.method < NW_GMRES || c.method > NW_SSTEP_GMRES) fail(NW_INVALID_ARG, "bad method");
+  if (c.sstep_size > 64) fail(NW_INVALID_ARG, "sstep_size above 64");
   if (c.preconditioner < NW_PC_NONE || c.preconditioner > NW_PC_RILUK)
     fail(NW_INVALID_ARG, "bad preconditioner");
 }
@@ -614,18 +617,156 @@ nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     ls->history = r.history;
-    if (rep) {
-      rep->iterations = r.iterations;
-      rep->outer_iterations = r.outer;
-      rep->status = r.status;
-      rep->converged = r.converged;
-      rep->final_rel_residual = r.final_rel;
-      rep->final_abs_residual = r.final_abs;
-      rep->rhs_norm = r.bnorm;
-      rep->solve_ms = ms;
-      rep->fallback = r.fallback;
-    }
+    nw_solve_report out{};
+    out.iterations = r.iterations;
+    out.outer_iterations = r.outer;
+    out.status = r.status;
+    out.converged = r.converged;
+    out.final_rel_residual = r.final_rel;
+    out.final_abs_residual = r.final_abs;
+    out.rhs_norm = r.bnorm;
+    out.solve_ms = ms;
+    out.fallback = r.fallback;
+    ls->last_report = out;
+    if (rep) *rep = out;
     if (r.status == NW_NAN_DETECTED) fail(NW_NAN_DETECTED, "non-finite value in the solve");
+  });
+}
+
+// ---- checkpoint / resume: raw binary file of the system and solver state.
+// Layout (little-endian, native sizes): CkptHeader, then row_ptr (int64,
+// nrows + 1), col_idx (int32, nnz), values (f64, nnz), rhs (f64, nrows),
+// the last residual history (f64, nhist), and x (f64, nrows) when has_x.
+// `checksum` is FNV-1a over every byte after the header.
+namespace {
+struct CkptHeader {
+  char magic[8];
+  uint32_t version;
+  uint32_t num_dof;
+  int64_t nrows, nnz, nhist;
+  int32_t has_x, pad;
+  nw_solver_cfg cfg;
+  nw_solve_report report;
+  uint64_t checksum;
+};
+constexpr char kCkptMagic[8] = {'N', 'W', 'C', 'K', 'P', 'T', '0', '1'};
+
+struct Fnv {
+  uint64_t h = 1469598103934665603ull;
+  void add(const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) {
+      h ^= c[i];
+      h *= 1099511628211ull;
+    }
+  }
+};
+}  // namespace
+
+nw_status nw_linsys_checkpoint_save(nw_linsys* ls, const char* path, const double* x) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!path) fail(NW_INVALID_ARG, "null path");
+    materialize_zero(ls);
+    const HostGraph& g = ls->g;
+    std::vector<double> vals(g.nnz), rhs(g.nrows), xh(x ? g.nrows : 0);
+    NW_CUDA(cudaMemcpyAsync(vals.data(), ls->values.p, g.nnz * sizeof(double), cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaMemcpyAsync(rhs.data(), ls->rhs.p, g.nrows * sizeof(double), cudaMemcpyDeviceToHost, ls->stream));
+    if (x) NW_CUDA(cudaMemcpyAsync(xh.data(), x, g.nrows * sizeof(double), cudaMemcpyDeviceToHost, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    CkptHeader h{};
+    std::memcpy(h.magic, kCkptMagic, 8);
+    h.version = 1;
+    h.num_dof = uint32_t(ls->num_dof);
+    h.nrows = g.nrows;
+    h.nnz = g.nnz;
+    h.nhist = int64_t(ls->history.size());
+    h.has_x = x ? 1 : 0;
+    h.cfg = ls->cfg;
+    h.report = ls->last_report;
+    Fnv f;
+    f.add(g.row_ptr.data(), g.row_ptr.size() * sizeof(int64_t));
+    f.add(g.col_idx.data(), g.col_idx.size() * sizeof(int32_t));
+    f.add(vals.data(), vals.size() * sizeof(double));
+    f.add(rhs.data(), rhs.size() * sizeof(double));
+    f.add(ls->history.data(), ls->history.size() * sizeof(double));
+    f.add(xh.data(), xh.size() * sizeof(double));
+    h.checksum = f.h;
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) fail(NW_INVALID_ARG, std::string("cannot open ") + path);
+    bool ok = std::fwrite(&h, sizeof(h), 1, fp) == 1;
+    auto put = [&](const void* p, size_t n) { ok = ok && (n == 0 || std::fwrite(p, 1, n, fp) == n); };
+    put(g.row_ptr.data(), g.row_ptr.size() * sizeof(int64_t));
+    put(g.col_idx.data(), g.col_idx.size() * sizeof(int32_t));
+    put(vals.data(), vals.size() * sizeof(double));
+    put(rhs.data(), rhs.size() * sizeof(double));
+    put(ls->history.data(), ls->history.size() * sizeof(double));
+    put(xh.data(), xh.size() * sizeof(double));
+    ok = (std::fclose(fp) == 0) && ok;
+    if (!ok) fail(NW_INVALID_ARG, std::string("short write to ") + path);
+  });
+}
+
+nw_status nw_linsys_checkpoint_load(nw_linsys* ls, const char* path, double* x, nw_solve_report* rep) {
+  return guard([&] {
+    need_finalized(ls);
+    if (!path) fail(NW_INVALID_ARG, "null path");
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) fail(NW_INVALID_ARG, std::string("cannot open ") + path);
+    std::unique_ptr<FILE, int (*)(FILE*)> closer(fp, std::fclose);
+    CkptHeader h{};
+    if (std::fread(&h, sizeof(h), 1, fp) != 1 || std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1)
+      fail(NW_INVALID_ARG, "not a checkpoint of this library");
+    const HostGraph& g = ls->g;
+    if (int(h.num_dof) != ls->num_dof || h.nrows != g.nrows || h.nnz != g.nnz || h.nhist < 0 ||
+        h.nhist > (int64_t(1) << 32))
+      fail(NW_INVALID_ARG, "checkpoint sizes differ from this linear system");
+    std::vector<int64_t> rp(g.nrows + 1);
+    std::vector<int32_t> ci(g.nnz);
+    std::vector<double> vals(g.nnz), rhs(g.nrows), hist(h.nhist), xh(h.has_x ? g.nrows : 0);
+    bool ok = true;
+    auto get = [&](void* p, size_t n) { ok = ok && (n == 0 || std::fread(p, 1, n, fp) == n); };
+    get(rp.data(), rp.size() * sizeof(int64_t));
+    get(ci.data(), ci.size() * sizeof(int32_t));
+    get(vals.data(), vals.size() * sizeof(double));
+    get(rhs.data(), rhs.size() * sizeof(double));
+    get(hist.data(), hist.size() * sizeof(double));
+    get(xh.data(), xh.size() * sizeof(double));
+    if (!ok) fail(NW_INVALID_ARG, "truncated checkpoint");
+    Fnv f;
+    f.add(rp.data(), rp.size() * sizeof(int64_t));
+    f.add(ci.data(), ci.size() * sizeof(int32_t));
+    f.add(vals.data(), vals.size() * sizeof(double));
+    f.add(rhs.data(), rhs.size() * sizeof(double));
+    f.add(hist.data(), hist.size() * sizeof(double));
+    f.add(xh.data(), xh.size() * sizeof(double));
+    if (f.h != h.checksum) fail(NW_INVALID_ARG, "checkpoint checksum mismatch");
+    if (rp != g.row_ptr || ci != g.col_idx) fail(NW_INVALID_ARG, "checkpoint graph differs from this linear system");
+    if (x && !h.has_x) fail(NW_INVALID_ARG, "checkpoint holds no solution vector");
+    check_cfg(h.cfg);
+    NW_CUDA(cudaMemcpyAsync(ls->values.p, vals.data(), g.nnz * sizeof(double), cudaMemcpyHostToDevice, ls->stream));
+    NW_CUDA(cudaMemcpyAsync(ls->rhs.p, rhs.data(), g.nrows * sizeof(double), cudaMemcpyHostToDevice, ls->stream));
+    if (x) NW_CUDA(cudaMemcpyAsync(x, xh.data(), g.nrows * sizeof(double), cudaMemcpyHostToDevice, ls->stream));
+    NW_CUDA(cudaStreamSynchronize(ls->stream));
+    ls->pristine = false;
+    const bool grow = h.cfg.kspace > ls->cfg.kspace || h.cfg.inner_kspace > ls->cfg.inner_kspace;
+    ls->cfg = h.cfg;
+    if (grow) {
+      DevCsr A;
+      A.n = g.nrows;
+      A.nnz = g.nnz;
+      A.row_ptr = ls->row_ptr.p;
+      A.col_idx = ls->col_idx.p;
+      A.values = ls->values.p;
+      A.lanes = ls->num_dof == 1 ? 8 : 32;
+      A.row_ptr_host = g.row_ptr.data();
+      A.col_idx_host = g.col_idx.data();
+      ls->solver.setup(A, std::max(ls->cfg.kspace, ls->cfg.inner_kspace), ls->stream);
+      ls->solver.setup_colors(ls->color_rows_host, ls->color_ptr, ls->stream);
+    }
+    ls->history = hist;
+    ls->last_report = h.report;
+    if (rep) *rep = h.report;
   });
 }
 

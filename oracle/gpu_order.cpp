@@ -581,6 +581,193 @@ int tfqmr(Solver& S, const double* b, double* x, int max_iters, double tol, std:
   return status;
 }
 
+// s-step GMRES (method 5): KrylovSolver::sstep_gmres in the GPU's order.
+// Blocks of s vectors by the scaled matrix powers, two block classical
+// Gram-Schmidt passes, CholeskyQR twice, the block's Hessenberg columns
+// from the change of basis, Givens rotations column by column.
+int sstep_gmres(Solver& S, const double* b, double* x, int m, int sstep, int max_iters, double tol,
+                std::vector<double>& hist, or_solve_report* rep) {
+  const int64_t n = S.A.n;
+  std::fill(x, x + n, 0.0);
+  const double bnorm = std::sqrt(S.dot(b, b));
+  hist.assign(1, 1.0);
+  if (!std::isfinite(bnorm)) return 6;
+  if (bnorm == 0.0) {
+    fill_report(rep, 0, 1, 0.0, 0.0, 0.0);
+    return 0;
+  }
+  const int ldc = m + 1;
+  std::vector<double> V(size_t(m + 1) * n), r(b, b + n), z(n), w(n);
+  std::vector<double> Hr(size_t(m + 1) * m), H(size_t(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+  std::vector<double> Ch(size_t(ldc) * sstep), Cp(size_t(ldc) * sstep), Gh(size_t(sstep) * sstep);
+  auto scale = [&](const double* src, double* dst, double nrm) {
+    const double inv = nrm != 0.0 ? 1.0 / nrm : 0.0;
+    for (int64_t i = 0; i < n; ++i) dst[i] = src[i] * inv;
+  };
+  double beta = bnorm, rel = 1.0, sigma = 1.0;
+  int its = 0, status = 0;
+  bool done = false;
+  while (!done && its < max_iters) {
+    scale(r.data(), V.data(), beta);
+    std::fill(H.begin(), H.end(), 0.0);
+    std::fill(Hr.begin(), Hr.end(), 0.0);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int j0 = 0, kk = 0;
+    while (j0 < m && its < max_iters && !done) {
+      const int sb = std::min(sstep, std::min(m - j0, max_iters - its));
+      double* W = V.data() + size_t(j0 + 1) * n;
+      for (int k = 0; k < sb; ++k) {
+        double* wk = W + size_t(k) * n;
+        S.apply(V.data() + size_t(j0 + k) * n, z.data());
+        gspmv(S.A, z.data(), nullptr, wk);
+        scale(wk, wk, sigma);
+      }
+      std::fill(Ch.begin(), Ch.end(), 0.0);
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int k = 0; k < sb; ++k)
+          for (int i = 0; i <= j0; ++i) Cp[size_t(k) * ldc + i] = S.dot(V.data() + size_t(i) * n, W + size_t(k) * n);
+        for (int k = 0; k < sb; ++k) S.maxpy(j0 + 1, V.data(), &Cp[size_t(k) * ldc], W + size_t(k) * n, false);
+        for (int k = 0; k < sb; ++k)
+          for (int i = 0; i <= j0; ++i) Ch[size_t(k) * ldc + i] += Cp[size_t(k) * ldc + i];
+      }
+      std::vector<double> Rt(size_t(sb) * sb, 0.0), Rp(size_t(sb) * sb), tmp(size_t(sb) * sb);
+      for (int k = 0; k < sb; ++k) Rt[size_t(k) * sb + k] = 1.0;
+      bool broke = false;
+      for (int pass = 0; pass < 2 && !broke; ++pass) {
+        for (int k = 0; k < sb; ++k)
+          for (int i = 0; i < sb; ++i) Gh[size_t(k) * sstep + i] = S.dot(W + size_t(i) * n, W + size_t(k) * n);
+        std::fill(Rp.begin(), Rp.end(), 0.0);
+        for (int k = 0; k < sb && !broke; ++k) {
+          for (int i = 0; i < k; ++i) {
+            double v = Gh[size_t(k) * sstep + i];
+            for (int l = 0; l < i; ++l) v -= Rp[size_t(i) * sb + l] * Rp[size_t(k) * sb + l];
+            Rp[size_t(k) * sb + i] = v / Rp[size_t(i) * sb + i];
+          }
+          double d = Gh[size_t(k) * sstep + k];
+          for (int l = 0; l < k; ++l) d -= Rp[size_t(k) * sb + l] * Rp[size_t(k) * sb + l];
+          if (!(d > 0.0) || !std::isfinite(d)) {
+            broke = true;
+            break;
+          }
+          Rp[size_t(k) * sb + k] = std::sqrt(d);
+        }
+        if (broke) break;
+        for (int k = 0; k < sb; ++k) {
+          double* wk = W + size_t(k) * n;
+          if (k > 0) S.maxpy(k, W, &Rp[size_t(k) * sb], wk, false);
+          scale(wk, wk, Rp[size_t(k) * sb + k]);
+        }
+        for (int k = 0; k < sb; ++k)
+          for (int i = 0; i <= k; ++i) {
+            double v = 0.0;
+            for (int l = i; l <= k; ++l) v += Rp[size_t(l) * sb + i] * Rt[size_t(k) * sb + l];
+            tmp[size_t(k) * sb + i] = v;
+          }
+        for (int k = 0; k < sb; ++k)
+          for (int i = 0; i <= k; ++i) Rt[size_t(k) * sb + i] = tmp[size_t(k) * sb + i];
+      }
+      if (broke) {
+        status = 7;
+        done = true;
+        break;
+      }
+      const int rows = j0 + sb + 1;
+      std::vector<double> Mx(size_t(rows) * sb, 0.0), Tn(size_t(sb) * sb, 0.0), Hn(size_t(rows) * sb, 0.0);
+      for (int k = 0; k < sb; ++k) {
+        for (int i = 0; i <= j0; ++i) Mx[size_t(k) * rows + i] = sigma * Ch[size_t(k) * ldc + i];
+        for (int i = 0; i <= k; ++i) Mx[size_t(k) * rows + j0 + 1 + i] = sigma * Rt[size_t(k) * sb + i];
+        if (k > 0)
+          for (int i = 0; i <= j0; ++i) {
+            double v = 0.0;
+            for (int l = 0; l < j0; ++l) v += Hr[size_t(i) * m + l] * Ch[size_t(k - 1) * ldc + l];
+            Mx[size_t(k) * rows + i] -= v;
+          }
+        if (k == 0) {
+          Tn[0] = 1.0;
+        } else {
+          Tn[size_t(k) * sb + 0] = Ch[size_t(k - 1) * ldc + j0];
+          for (int i = 1; i <= k; ++i) Tn[size_t(k) * sb + i] = Rt[size_t(k - 1) * sb + i - 1];
+        }
+      }
+      for (int k = 0; k < sb; ++k)
+        for (int i = 0; i < rows; ++i) {
+          double v = Mx[size_t(k) * rows + i];
+          for (int l = 0; l < k; ++l) v -= Hn[size_t(l) * rows + i] * Tn[size_t(k) * sb + l];
+          Hn[size_t(k) * rows + i] = v / Tn[size_t(k) * sb + k];
+        }
+      for (int k = 0; k < sb; ++k) {
+        const int j = j0 + k;
+        for (int i = 0; i <= j + 1; ++i) Hr[size_t(i) * m + j] = H[size_t(i) * m + j] = Hn[size_t(k) * rows + i];
+      }
+      for (int k = 0; k < sb; ++k) {
+        const int j = j0 + k;
+        for (int q = 0; q < j; ++q) {
+          const double a = H[size_t(q) * m + j], bb = H[size_t(q + 1) * m + j];
+          H[size_t(q) * m + j] = cs[q] * a + sn[q] * bb;
+          H[size_t(q + 1) * m + j] = -sn[q] * a + cs[q] * bb;
+        }
+        const double a = H[size_t(j) * m + j], bb = H[size_t(j + 1) * m + j];
+        const double den = std::sqrt(a * a + bb * bb);
+        if (!(den > 0.0) || !std::isfinite(den)) {
+          status = std::isfinite(den) ? 7 : 6;
+          done = true;
+          kk = j;
+          break;
+        }
+        cs[j] = a / den;
+        sn[j] = bb / den;
+        H[size_t(j) * m + j] = den;
+        H[size_t(j + 1) * m + j] = 0.0;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        ++its;
+        rel = std::abs(g[j + 1]) / bnorm;
+        hist.push_back(rel);
+        kk = j + 1;
+        if (!std::isfinite(rel)) {
+          status = 6;
+          done = true;
+          break;
+        }
+        if (rel <= tol) {
+          done = true;
+          break;
+        }
+      }
+      {
+        double w0 = 0.0;
+        for (int i = 0; i <= j0; ++i) w0 += Ch[i] * Ch[i];
+        w0 += Rt[0] * Rt[0];
+        const double next = sigma * std::sqrt(w0);
+        if (std::isfinite(next) && next > 0.0) sigma = next;
+      }
+      j0 += sb;
+    }
+    for (int i = kk - 1; i >= 0; --i) {
+      double sum = g[i];
+      for (int l = i + 1; l < kk; ++l) sum -= H[size_t(i) * m + l] * y[l];
+      y[i] = sum / H[size_t(i) * m + i];
+    }
+    if (kk > 0) {
+      for (int64_t i = 0; i < n; ++i) {
+        double acc = 0.0;
+        for (int k = 0; k < kk; ++k) acc = std::fma(y[k], V[size_t(k) * n + i], acc);
+        w[i] = acc;
+      }
+      S.apply(w.data(), z.data());
+      for (int64_t i = 0; i < n; ++i) x[i] = std::fma(1.0, z[i], x[i]);
+    }
+    if (done || its >= max_iters) break;
+    gspmv(S.A, x, b, r.data());
+    beta = std::sqrt(S.dot(r.data(), r.data()));
+    if (beta == 0.0) break;
+  }
+  gspmv(S.A, x, b, r.data());
+  fill_report(rep, its, rel <= tol ? 1 : 0, rel, std::sqrt(S.dot(r.data(), r.data())), bnorm);
+  return status;
+}
+
 }  // namespace
 
 extern "C" int or_solve_gpu_order(int64_t nrows, const int64_t* row_ptr, const int32_t* col_idx,
@@ -588,7 +775,7 @@ extern "C" int or_solve_gpu_order(int64_t nrows, const int64_t* row_ptr, const i
                                   int precond, const int64_t* order, const int64_t* class_ptr,
                                   int nclasses, int kspace, int max_iters, double tol,
                                   double* history, or_solve_report* rep, int inner_sweeps,
-                                  int red_blocks, int lanes) {
+                                  int red_blocks, int lanes, int sstep_size) {
   Solver S;
   S.A = {nrows, row_ptr, col_idx, vals};
   S.G = std::max(1, red_blocks);
@@ -618,6 +805,8 @@ extern "C" int or_solve_gpu_order(int64_t nrows, const int64_t* row_ptr, const i
     st = bicgstab(S, b, x, max_iters, tol, hist, rep);
   else if (method == 4)
     st = tfqmr(S, b, x, max_iters, tol, hist, rep);
+  else if (method == 5)
+    st = sstep_gmres(S, b, x, std::max(1, kspace), sstep_size > 0 ? sstep_size : 5, max_iters, tol, hist, rep);
   else
     st = gmres(S, b, x, std::max(1, kspace), max_iters, tol, method == 2, hist, rep);
   if (history)

@@ -260,7 +260,8 @@ int or_solve(int64_t nrows, const int64_t* row_ptr, const int32_t* col_idx,
              double tol, double* history, or_solve_report* rep,
              int nthreads, int inner_sweeps);
 
-/* The same solvers (method 0 GMRES, 1 CG, 2 FGMRES, 3 BiCGStab, 4 TFQMR;
+/* The same solvers (method 0 GMRES, 1 CG, 2 FGMRES, 3 BiCGStab, 4 TFQMR,
+ * 5 s-step GMRES with step sstep_size;
  * precond 0 none, 1 Jacobi, 2 multicolour symmetric Gauss-Seidel over the
  * colour classes order[class_ptr[c] .. class_ptr[c + 1]), 4 two-stage SGS,
  * 5 natural-order symmetric Gauss-Seidel, 6 ILU(0))
@@ -273,7 +274,7 @@ int or_solve_gpu_order(int64_t nrows, const int64_t* row_ptr, const int32_t* col
                        int precond, const int64_t* order, const int64_t* class_ptr,
                        int nclasses, int kspace, int max_iters, double tol,
                        double* history, or_solve_report* rep, int inner_sweeps,
-                       int red_blocks, int lanes);
+                       int red_blocks, int lanes, int sstep_size);
 
 /* Preconditioner application alone (for unit tests). */
 void or_precond_apply(int64_t nrows, const int64_t* row_ptr,

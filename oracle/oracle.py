@@ -264,7 +264,7 @@ def gpu_reduction_blocks(n: int, sms: int) -> int:
 
 
 def solve_gpu_order(row_ptr, col_idx, vals, b, method=0, precond=1, order=None, class_ptr=None, kspace=50,
-                    max_iters=50, tol=1e-8, inner_sweeps=1, red_blocks=1, lanes=8):
+                    max_iters=50, tol=1e-8, inner_sweeps=1, red_blocks=1, lanes=8, sstep_size=5):
     """The FP64 solvers in the GPU library's operation order
     (or_solve_gpu_order): returns x, history (iterations + 1), report."""
     row_ptr, vals, b = _i64(row_ptr), _f64(vals), _f64(b)
@@ -279,7 +279,8 @@ def solve_gpu_order(row_ptr, col_idx, vals, b, method=0, precond=1, order=None, 
     st = lib().or_solve_gpu_order(C.c_int64(n), _p(row_ptr, C.c_int64), _p(col_idx, C.c_int32),
                                   _p(vals, C.c_double), _p(b, C.c_double), _p(x, C.c_double), method, precond,
                                   _p(od, C.c_int64), _p(cp, C.c_int64), nc, kspace, max_iters, C.c_double(tol),
-                                  _p(hist, C.c_double), C.byref(rep), inner_sweeps, red_blocks, lanes)
+                                  _p(hist, C.c_double), C.byref(rep), inner_sweeps, red_blocks, lanes,
+                                  sstep_size)
     if st == 1:
         raise ValueError("or_solve_gpu_order: Gauss-Seidel needs the colour classes")
     return x, hist[:rep.iterations + 1].copy(), rep

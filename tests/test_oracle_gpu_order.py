@@ -59,3 +59,19 @@ def test_gpu_order_reduction_grid_changes_only_rounding(orc):
            for G in (3, 37)]
     assert out[0][2].iterations == out[1][2].iterations
     np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-9)
+
+
+@pytest.mark.parametrize("sstep", [1, 3, 5])
+def test_sstep_gmres_is_gmres_in_exact_arithmetic(orc, sstep):
+    """s-step GMRES builds the same Krylov spaces as GMRES: with step size
+    1 to 5 the histories agree with GMRES(30) to the basis' rounding."""
+    rp, ci, vals, b = _system(orc)
+    G = orc.gpu_reduction_blocks(len(b), 152)
+    _, h1, r1 = orc.solve_gpu_order(rp, ci, vals, b, method=0, precond=1, kspace=30, max_iters=800, tol=1e-8,
+                                    red_blocks=G)
+    x2, h2, r2 = orc.solve_gpu_order(rp, ci, vals, b, method=5, precond=1, kspace=30, max_iters=800, tol=1e-8,
+                                     red_blocks=G, sstep_size=sstep)
+    assert r2.converged and abs(r1.iterations - r2.iterations) <= 2
+    k = min(len(h1), len(h2), 60)
+    np.testing.assert_allclose(h2[:k], h1[:k], rtol=1e-6)
+    assert r2.final_abs_explicit <= 1.01e-8 * r2.rhs_norm
