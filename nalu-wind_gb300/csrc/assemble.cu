@@ -336,7 +336,12 @@ struct MomentumIn {
   const double* __restrict__ pec;
 };
 
-template <bool LIMITER, bool DIVU>
+// DEF: the reference's default advection options alpha = 0, alpha_upw = 1,
+// upw_factor = 1 (SolutionOptions, src/SolutionOptions.C:31-80). The general
+// formulas then multiply by exactly one and add exact zeros, which in
+// float-float arithmetic return their operand unchanged, so the
+// specialisation drops those operations and gives the same bits.
+template <bool LIMITER, bool DIVU, bool DEF>
 __device__ __forceinline__ void momentum_edge(int64_t e, int64_t E, const MomentumIn& in,
                                               const MomentumDD& c, dd* __restrict__ buf) {
   const int2* __restrict__ edges = in.edges;
@@ -364,8 +369,8 @@ __device__ __forceinline__ void momentum_edge(int64_t e, int64_t E, const Moment
   }
   const dd mdot = ldd(mdotA + e);
   const dd viscIp = scale2(ldd(viscosity + L) + ldd(viscosity + R), 0.5f);
-  const dd asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
-  const dd axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
+  const dd asq = dd_dot3(av[0], av[0], av[1], av[1], av[2], av[2]);
+  const dd axdx = dd_dot3(av[0], dx[0], av[1], dx[1], av[2], dx[2]);
   const dd inv_axdx = dd_rcp(axdx);
   dd hdx[3];
 #pragma unroll
@@ -384,8 +389,8 @@ __device__ __forceinline__ void momentum_edge(int64_t e, int64_t E, const Moment
       gr[j] = ldd(dudx + 9 * R + 3 * i + j);
       gj[j] = gr[j] + gl[j];
     }
-    duL[i] = hdx[0] * gl[0] + hdx[1] * gl[1] + hdx[2] * gl[2];
-    duR[i] = hdx[0] * gr[0] + hdx[1] * gr[1] + hdx[2] * gr[2];
+    duL[i] = dd_dot3(hdx[0], gl[0], hdx[1], gl[1], hdx[2], gl[2]);
+    duR[i] = dd_dot3(hdx[0], gr[0], hdx[1], gr[1], hdx[2], gr[2]);
     const dd gjuidx = duL[i] + duR[i];
     const dd corr = (du[i] - gjuidx) * inv_axdx;
 #pragma unroll
@@ -408,24 +413,38 @@ __device__ __forceinline__ void momentum_edge(int64_t e, int64_t E, const Moment
   dd tf[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const dd uIpL = uL[i] + (LIMITER ? duL[i] * c.upw * limitL[i] : duL[i] * c.upw);
-    const dd uIpR = uR[i] - (LIMITER ? duR[i] * c.upw * limitR[i] : duR[i] * c.upw);
     const dd uiIp = scale2(uR[i] + uL[i], 0.5f);
-    const dd uiUpw = c.alpha_upw * (up ? uIpL : uIpR) + c.om_alpha_upw * uiIp;
-    const dd uiCds = scale2(c.alpha * (uIpL + uIpR), 0.5f) + c.om_alpha * uiIp;
-    const dd adv_flux = mdot * (pecfac * uiUpw + om_pecfac * uiCds);
-    const dd sd = (duidxj[i][0] + duidxj[0][i]) * av[0] + (duidxj[i][1] + duidxj[1][i]) * av[1] +
-                  (duidxj[i][2] + duidxj[2][i]) * av[2];
+    dd adv_flux;
+    if (DEF) {
+      const dd uiUpw = up ? uL[i] + (LIMITER ? duL[i] * limitL[i] : duL[i])
+                          : uR[i] - (LIMITER ? duR[i] * limitR[i] : duR[i]);
+      adv_flux = mdot * (pecfac * uiUpw + om_pecfac * uiIp);
+    } else {
+      const dd uIpL = uL[i] + (LIMITER ? duL[i] * c.upw * limitL[i] : duL[i] * c.upw);
+      const dd uIpR = uR[i] - (LIMITER ? duR[i] * c.upw * limitR[i] : duR[i] * c.upw);
+      const dd uiUpw = c.alpha_upw * (up ? uIpL : uIpR) + c.om_alpha_upw * uiIp;
+      const dd uiCds = scale2(c.alpha * (uIpL + uIpR), 0.5f) + c.om_alpha * uiIp;
+      adv_flux = mdot * (pecfac * uiUpw + om_pecfac * uiCds);
+    }
+    const dd sd = dd_dot3(duidxj[i][0] + duidxj[0][i], av[0], duidxj[i][1] + duidxj[1][i], av[1],
+                          duidxj[i][2] + duidxj[2][i], av[2]);
     dd diff_flux = -(viscIp * sd);
     if (DIVU) diff_flux = divU * (c.divu_fac * viscIp * av[i]) + diff_flux;
     tf[i] = diff_flux * maskNode + adv_flux;
   }
   const dd hm = scale2(mdot, 0.5f);
   const dd habs = scale2(dd_abs(mdot), 0.5f);
-  const dd cen = c.alpha * om_pecfac * hm;
-  const dd aUL = (hm + habs) * pecfac * c.alpha_upw + cen;
-  const dd aUR = (hm - habs) * pecfac * c.alpha_upw + cen;
-  const dd aC = hm * (pecfac * c.om_alpha_upw + om_pecfac * c.om_alpha);
+  dd aUL, aUR, aC;
+  if (DEF) {
+    aUL = (hm + habs) * pecfac;
+    aUR = (hm - habs) * pecfac;
+    aC = hm * om_pecfac;
+  } else {
+    const dd cen = c.alpha * om_pecfac * hm;
+    aUL = (hm + habs) * pecfac * c.alpha_upw + cen;
+    aUR = (hm - habs) * pecfac * c.alpha_upw + cen;
+    aC = hm * (pecfac * c.om_alpha_upw + om_pecfac * c.om_alpha);
+  }
   const dd t = -(viscIp * inv_axdx);
   const dd dlhsfac = t * asq;
   const dd ta0 = t * av[0], ta1 = t * av[1], ta2 = t * av[2];
@@ -443,13 +462,13 @@ __device__ __forceinline__ void momentum_edge(int64_t e, int64_t E, const Moment
   b[10 * E] = tf[2];
 }
 
-template <bool LIMITER, bool DIVU>
+template <bool LIMITER, bool DIVU, bool DEF>
 __global__ void __launch_bounds__(kThreads, 4)
     momentum_edge_k(int64_t E, int64_t e0, int64_t e1, MomentumIn in, MomentumDD c,
                     dd* __restrict__ buf) {
   const int64_t e = e0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= e1) return;
-  momentum_edge<LIMITER, DIVU>(e, E, in, c, buf);
+  momentum_edge<LIMITER, DIVU, DEF>(e, E, in, c, buf);
 }
 
 // ---------------------------------------------------------------------------
@@ -592,15 +611,30 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
           v[k + c] = acc ? v[k + c] + d : d;
         }
       };
+      // software-pipelined: the next incidence's word and coefficients are
+      // loaded while the current one is summed (the loop is otherwise a
+      // chain of dependent loads per thread)
+      uint32_t w = a.inc[s];
+      auto fetch = [&](uint32_t ww, dd* x) {
+        const int64_t ee = (ww & 0x7fffffffu) >> 1;
+        const int sd = ww & 1u;
+        x[0] = cb[(sd ? 1 : 0) * E + ee];
+        x[1] = cb[(sd ? 0 : 1) * E + ee];
+        x[2] = cb[n0 * E + ee];
+        x[3] = cb[n1 * E + ee];
+        x[4] = cb[n2 * E + ee];
+        x[5] = cb[(8 + q) * E + ee];
+      };
+      dd cur[6];
+      fetch(w, cur);
+      uint32_t wn = s + 1 < t ? a.inc[s + 1] : w;
       for (int32_t qi = s; qi < t; ++qi) {
-        const uint32_t w = a.inc[qi];
+        dd nxt[6];
+        const uint32_t wnn = qi + 2 < t ? a.inc[qi + 2] : wn;
+        if (qi + 1 < t) fetch(wn, nxt);
         const bool dup = (w >> 31) != 0;
-        const int64_t e = (w & 0x7fffffffu) >> 1;
         const int side = w & 1u;
-        const dd co = cb[(side ? 1 : 0) * E + e];
-        const dd other = cb[(side ? 0 : 1) * E + e];
-        const dd na = cb[n0 * E + e], nb = cb[n1 * E + e], nc = cb[n2 * E + e];
-        const dd f = cb[(8 + q) * E + e];
+        const dd co = cur[0], other = cur[1], na = cur[2], nb = cur[3], nc = cur[4], f = cur[5];
         rr = side ? rr + f : rr - f;
         const dd blk[3] = {q == 0 ? na + co : na, q == 1 ? nb + co : nb, q == 2 ? nc + co : nc};
         if (!dup) {
@@ -616,6 +650,10 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
         dN[0] = dN[0] + na;
         dN[1] = dN[1] + nb;
         dN[2] = dN[2] + nc;
+        w = wn;
+        wn = wnn;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) cur[k] = nxt[k];
       }
       put3(3 * (slot < dp ? slot : slot + 1), ob);
       // diagonal block row q: -(sum(other) e_q + sum(N)_q) / relax
@@ -788,12 +826,17 @@ void launch_momentum_edges(cudaStream_t s, int64_t E, int64_t e0, int64_t e1, co
   const MomentumIn in = momentum_in(edges, f);
   dd* b = reinterpret_cast<dd*>(buf);
   const bool lim = o.use_limiter != 0, divu = o.include_div_u != 0.0;
-#define NW_MOM(LIM, DIV) \
-  momentum_edge_k<LIM, DIV><<<grid_for(e1 - e0), kThreads, 0, s>>>(E, e0, e1, in, c, b)
-  if (lim && divu) NW_MOM(true, true);
-  else if (lim) NW_MOM(true, false);
-  else if (divu) NW_MOM(false, true);
-  else NW_MOM(false, false);
+  const bool def = o.alpha == 0.0 && o.alpha_upw == 1.0 && o.upw_factor == 1.0;
+#define NW_MOM(LIM, DIV, DEF) \
+  momentum_edge_k<LIM, DIV, DEF><<<grid_for(e1 - e0), kThreads, 0, s>>>(E, e0, e1, in, c, b)
+#define NW_MOM2(LIM, DIV) \
+  if (def) NW_MOM(LIM, DIV, true); \
+  else NW_MOM(LIM, DIV, false)
+  if (lim && divu) NW_MOM2(true, true);
+  else if (lim) NW_MOM2(true, false);
+  else if (divu) NW_MOM2(false, true);
+  else NW_MOM2(false, false);
+#undef NW_MOM2
 #undef NW_MOM
 }
 
@@ -816,7 +859,7 @@ void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
                  const uint32_t* inc, const int32_t* diag_pos,
                  const int64_t* row_ptr, const double* buf, int64_t E,
                  double relax, double* values, double* rhs, int accumulate,
-                 int smem_bytes) {
+                 int smem_bytes, int max_inc) {
   if (R == 0) return;
   set_smem_attrs();
   if (kind == 0)

@@ -38,12 +38,14 @@ void launch_momentum_edges(cudaStream_t s, int64_t E, int64_t e0, int64_t e1, co
                            const nw_momentum_fields& f, const MomentumOpts& o,
                            double* buf);
 // kind 0 scalar, 1 continuity, 2 momentum (3 dof). smem_bytes: staging
-// size from row_stage_bytes (0 disables staging).
+// size from row_stage_bytes (0 disables staging). max_inc: the largest
+// number of incidences of a node row (momentum rows of at most 32 take the
+// warp-per-row kernel; 0 = unknown).
 void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
                  const uint32_t* inc, const int32_t* diag_pos,
                  const int64_t* row_ptr, const double* buf, int64_t E,
                  double relax, double* values, double* rhs, int accumulate,
-                 int smem_bytes);
+                 int smem_bytes, int max_inc = 0);
 int row_stage_bytes(int kind, const int64_t* row_ptr_host, int64_t R);
 void launch_reset_rows(cudaStream_t s, int64_t n, const int64_t* nodes,
                        const int64_t* node_lid, int num_dof, int begin,

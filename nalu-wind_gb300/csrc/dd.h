@@ -238,6 +238,23 @@ NW_HD dd scale2(dd a, float p2) { return {fmul(a.hi, p2), fmul(a.lo, p2)}; }
 
 NW_HD dd dd_fma(dd a, dd b, dd c) { return a * b + c; }
 
+// a0 b0 + a1 b1 + a2 b2: the three FMA two-products (head + error), the
+// heads added with two error-free sums, every error term added in float,
+// one final renormalisation. 31 float operations against 43 for three
+// products and two additions; the error stays a few u^2 times the sum of
+// |a_i b_i| (u = 2^-24), as for the separate operations.
+NW_HD dd dd_dot3(dd a0, dd b0, dd a1, dd b1, dd a2, dd b2) {
+  const float p0 = fmul(a0.hi, b0.hi), p1 = fmul(a1.hi, b1.hi), p2 = fmul(a2.hi, b2.hi);
+  float e0 = ffma(a0.hi, b0.hi, -p0), e1 = ffma(a1.hi, b1.hi, -p1), e2 = ffma(a2.hi, b2.hi, -p2);
+  e0 = ffma(a0.lo, b0.hi, ffma(a0.hi, b0.lo, e0));
+  e1 = ffma(a1.lo, b1.hi, ffma(a1.hi, b1.lo, e1));
+  e2 = ffma(a2.lo, b2.hi, ffma(a2.hi, b2.lo, e2));
+  const dd s01 = two_sum(p0, p1);
+  const dd s = two_sum(s01.hi, p2);
+  const float err = fadd(fadd(fadd(e0, e1), e2), fadd(s01.lo, s.lo));
+  return fast_two_sum(s.hi, err);
+}
+
 // 1/x: float seed refined by one Newton step in double-word arithmetic.
 // x == 0 gives inf (as the FP64 reciprocal does); non-finite x its float
 // reciprocal.

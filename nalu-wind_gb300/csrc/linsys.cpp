@@ -57,6 +57,7 @@ struct nw_linsys {
   DeviceArray<int2> edges;
   DeviceArray<double> values, rhs, buf, nodebuf;
   int stage_bytes[3] = {0, 0, 0};  // row-phase staging per kind
+  int max_inc = 0;                 // most incidences of a node row
   DeviceArray<int> err;
   DeviceArray<int64_t> scratch_lid;
   DeviceArray<double> scratch_vals;
@@ -283,6 +284,9 @@ nw_status nw_linsys_finalize(nw_linsys* ls) {
           row_stage_bytes(0, g.row_ptr.data(), g.node_rows);
     } else if (ls->num_dof == 3) {
       ls->stage_bytes[2] = row_stage_bytes(2, g.row_ptr.data(), g.node_rows);
+      ls->max_inc = 0;
+      for (int64_t r = 0; r < g.node_rows; ++r)
+        ls->max_inc = std::max(ls->max_inc, g.inc_ptr[r + 1] - g.inc_ptr[r]);
     }
     NW_CUDA(cudaMemsetAsync(ls->values.p, 0, g.nnz * sizeof(double), s));
     NW_CUDA(cudaMemsetAsync(ls->rhs.p, 0, g.nrows * sizeof(double), s));
@@ -434,7 +438,7 @@ static void check_momentum_args(const nw_linsys* ls, const nw_momentum_fields* f
 static void momentum_rows(nw_linsys* ls, double relax) {
   launch_rows(ls->stream, 2, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
               ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, ls->g.num_edges, relax,
-              ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[2]);
+              ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[2], ls->max_inc);
   NW_CUDA(cudaGetLastError());
   ls->pristine = false;
 }
