@@ -611,30 +611,15 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
           v[k + c] = acc ? v[k + c] + d : d;
         }
       };
-      // software-pipelined: the next incidence's word and coefficients are
-      // loaded while the current one is summed (the loop is otherwise a
-      // chain of dependent loads per thread)
-      uint32_t w = a.inc[s];
-      auto fetch = [&](uint32_t ww, dd* x) {
-        const int64_t ee = (ww & 0x7fffffffu) >> 1;
-        const int sd = ww & 1u;
-        x[0] = cb[(sd ? 1 : 0) * E + ee];
-        x[1] = cb[(sd ? 0 : 1) * E + ee];
-        x[2] = cb[n0 * E + ee];
-        x[3] = cb[n1 * E + ee];
-        x[4] = cb[n2 * E + ee];
-        x[5] = cb[(8 + q) * E + ee];
-      };
-      dd cur[6];
-      fetch(w, cur);
-      uint32_t wn = s + 1 < t ? a.inc[s + 1] : w;
       for (int32_t qi = s; qi < t; ++qi) {
-        dd nxt[6];
-        const uint32_t wnn = qi + 2 < t ? a.inc[qi + 2] : wn;
-        if (qi + 1 < t) fetch(wn, nxt);
+        const uint32_t w = a.inc[qi];
         const bool dup = (w >> 31) != 0;
+        const int64_t e = (w & 0x7fffffffu) >> 1;
         const int side = w & 1u;
-        const dd co = cur[0], other = cur[1], na = cur[2], nb = cur[3], nc = cur[4], f = cur[5];
+        const dd co = cb[(side ? 1 : 0) * E + e];
+        const dd other = cb[(side ? 0 : 1) * E + e];
+        const dd na = cb[n0 * E + e], nb = cb[n1 * E + e], nc = cb[n2 * E + e];
+        const dd f = cb[(8 + q) * E + e];
         rr = side ? rr + f : rr - f;
         const dd blk[3] = {q == 0 ? na + co : na, q == 1 ? nb + co : nb, q == 2 ? nc + co : nc};
         if (!dup) {
@@ -650,10 +635,6 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
         dN[0] = dN[0] + na;
         dN[1] = dN[1] + nb;
         dN[2] = dN[2] + nc;
-        w = wn;
-        wn = wnn;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) cur[k] = nxt[k];
       }
       put3(3 * (slot < dp ? slot : slot + 1), ob);
       // diagonal block row q: -(sum(other) e_q + sum(N)_q) / relax

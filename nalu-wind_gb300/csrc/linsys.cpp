@@ -1557,7 +1557,7 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
     tight.kspace = std::min(50, std::max(ls->cfg.kspace, 30));
     tight.inner_kspace = tight.kspace;
     tight.inner_tolerance = 1e-4;
-    tight.max_iterations = 100000;
+    tight.max_iterations = 20000;
     pc.kind = NW_PC_SGS;
     SolveResult sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
     if (!sr.converged) {
@@ -1566,7 +1566,11 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
       tight.precision = NW_PREC_FP64;
       sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
     }
-    if (!sr.converged) fail(NW_NOT_CONVERGED, "harvest: reference solve did not converge");
+    // FP64 cannot always reach 1e-11 on the most stretched meshes; a
+    // reference at 1e-9 is still far below the errors of the harvested
+    // iterates (restarts of a 1e-8 solve), so it is kept
+    if (!sr.converged && !(sr.final_abs <= 1e-9 * sr.bnorm))
+      fail(NW_NOT_CONVERGED, "harvest: reference solve did not converge");
     // system coarse weights
     const int sys = L.nsystems++;
     auto* w = new DeviceArray<float>();
