@@ -591,10 +591,14 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
   const bool staged = cnt * int64_t(sizeof(double)) <= a.smem_bytes;
   const int local = threadIdx.x / 3, q = threadIdx.x - 3 * (threadIdx.x / 3);
   const int64_t r = r0 + local;
-  // N slots of row q of the symmetric 3x3 N (N00 N01 N02 N11 N12 N22 at 2..7)
-  const int n0 = q == 0 ? 2 : (q == 1 ? 3 : 4);
-  const int n1 = q == 0 ? 3 : (q == 1 ? 5 : 6);
-  const int n2 = q == 0 ? 4 : (q == 1 ? 6 : 7);
+  // row q of the symmetric N (N00 N01 N02 N11 N12 N22 at slots 2..7): its
+  // diagonal N_qq and the off-diagonals of columns c1 < c2 (the two c != q),
+  // so that the block's c_side I term adds to one fixed entry
+  const int c1 = q == 0 ? 1 : 0, c2 = q == 2 ? 1 : 2;
+  const dd* __restrict__ pd = cb + (q == 0 ? 2 : (q == 1 ? 5 : 7)) * E;
+  const dd* __restrict__ p1 = cb + (q == 2 ? 4 : 3) * E;
+  const dd* __restrict__ p2 = cb + (q == 0 ? 4 : 6) * E;
+  const dd* __restrict__ pf = cb + (8 + q) * E;
   if (r < r1) {
     const int32_t s = a.inc_ptr[r], t = a.inc_ptr[r + 1];
     const int64_t bq = a.row_ptr[3 * r + q];
@@ -602,46 +606,46 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
     const bool acc = a.accumulate && !staged;
     if (s != t) {
       const int dp = a.diag_pos[r];
-      dd sother{}, dN[3] = {}, rr{}, ob[3];
+      dd sother{}, sd{}, s1{}, s2{}, rr{}, od{}, o1{}, o2{};
       int slot = -1;
-      auto put3 = [&](int k, const dd* x) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const double d = dd_to_double_int(x[c]);
-          v[k + c] = acc ? v[k + c] + d : d;
-        }
+      auto put3 = [&](int k, dd xd, dd x1, dd x2) {
+        const double d0 = dd_to_double_int(xd), d1 = dd_to_double_int(x1),
+                     d2 = dd_to_double_int(x2);
+        v[k + q] = acc ? v[k + q] + d0 : d0;
+        v[k + c1] = acc ? v[k + c1] + d1 : d1;
+        v[k + c2] = acc ? v[k + c2] + d2 : d2;
       };
       for (int32_t qi = s; qi < t; ++qi) {
         const uint32_t w = a.inc[qi];
         const bool dup = (w >> 31) != 0;
         const int64_t e = (w & 0x7fffffffu) >> 1;
         const int side = w & 1u;
-        const dd co = cb[(side ? 1 : 0) * E + e];
-        const dd other = cb[(side ? 0 : 1) * E + e];
-        const dd na = cb[n0 * E + e], nb = cb[n1 * E + e], nc = cb[n2 * E + e];
-        const dd f = cb[(8 + q) * E + e];
-        rr = side ? rr + f : rr - f;
-        const dd blk[3] = {q == 0 ? na + co : na, q == 1 ? nb + co : nb, q == 2 ? nc + co : nc};
+        const dd c0 = cb[e], c1v = cb[E + e];
+        const dd co = side ? c1v : c0, other = side ? c0 : c1v;
+        const dd nd = pd[e], n1 = p1[e], n2 = p2[e];
+        const dd f = pf[e];
+        rr = rr + (side ? f : -f);
+        const dd bd = nd + co;
         if (!dup) {
-          if (slot >= 0) put3(3 * (slot < dp ? slot : slot + 1), ob);
+          if (slot >= 0) put3(3 * (slot < dp ? slot : slot + 1), od, o1, o2);
           ++slot;
-#pragma unroll
-          for (int c = 0; c < 3; ++c) ob[c] = blk[c];
+          od = bd;
+          o1 = n1;
+          o2 = n2;
         } else {
-#pragma unroll
-          for (int c = 0; c < 3; ++c) ob[c] = ob[c] + blk[c];
+          od = od + bd;
+          o1 = o1 + n1;
+          o2 = o2 + n2;
         }
         sother = sother + other;
-        dN[0] = dN[0] + na;
-        dN[1] = dN[1] + nb;
-        dN[2] = dN[2] + nc;
+        sd = sd + nd;
+        s1 = s1 + n1;
+        s2 = s2 + n2;
       }
-      put3(3 * (slot < dp ? slot : slot + 1), ob);
+      put3(3 * (slot < dp ? slot : slot + 1), od, o1, o2);
       // diagonal block row q: -(sum(other) e_q + sum(N)_q) / relax
-      const dd m0 = -(dN[0] * a.irelax), m1 = -(dN[1] * a.irelax), m2 = -(dN[2] * a.irelax);
       const dd dgc = -(sother * a.irelax);
-      const dd db[3] = {q == 0 ? m0 + dgc : m0, q == 1 ? m1 + dgc : m1, q == 2 ? m2 + dgc : m2};
-      put3(3 * dp, db);
+      put3(3 * dp, -(sd * a.irelax) + dgc, -(s1 * a.irelax), -(s2 * a.irelax));
       const double d = dd_to_double_int(rr);
       a.rhs[3 * r + q] = a.accumulate ? a.rhs[3 * r + q] + d : d;
     } else if (!acc) {

@@ -148,40 +148,45 @@ NW_HD double widen(float f) {
 }
 
 // hi + lo rounded to the nearest double: both halves widen exactly, so the
-// one FP64 add rounds the exact sum once. (An integer-only rounding of the
-// pair was measured slower in the row kernels: its ~40-instruction
-// dependency chain is not hidden at their occupancy, while the add runs on
-// the otherwise idle FP64 pipe. Issuing it as an FMA, hi * 1 + lo, measured
-// the same.)
+// one FP64 add rounds the exact sum once.
 NW_HD double dd_to_double(dd a) { return widen(a.hi) + widen(a.lo); }
 
-// hi + lo as a double with integer operations only, for the row kernels
-// that widen every CSR entry (GB300 issues FP64 adds at about one lane per
-// SM clock, so one add per entry bounds those kernels). double(hi) is a bit
-// move; lo, at least 24 binades below hi in a normalised pair, is added to
-// that pattern as a count of units in the last place of hi's binade,
-// truncated towards zero (one more binary place when the sum drops below
-// hi's binade, which only a power-of-two hi and a lo of the other sign can
-// do). The low 29 bits of double(hi) are zero and lo is worth less than
-// 2^29 of those units, so the add never carries into the exponent. Result:
-// within one unit in the last place of the correctly rounded hi + lo. Pairs
-// outside that form (zero, subnormal or non-finite hi, non-finite lo, lo
-// fewer than 24 binades below hi) take dd_to_double.
+NW_HD int f2i_rn(float x) {
+#ifdef __CUDA_ARCH__
+  return __float2int_rn(x);
+#else
+  return int(std::nearbyint(x));  // the default rounding: to nearest, ties to even
+#endif
+}
+
+// hi + lo as a double without an FP64 instruction, for the row kernels that
+// widen every CSR entry (GB300 issues FP64 adds at about one lane per SM
+// clock, so one add per entry bounds those kernels). double(hi) is a bit
+// move; lo is scaled (exactly, by a power of two) to units in the last
+// place of a double in hi's binade, rounded to an integer and added to the
+// magnitude bits of double(hi) (subtracted when lo has the other sign). When hi is a power of two and lo has the other sign the sum
+// lies one binade lower, where the unit is half as large: lo is scaled by
+// one more factor of two and the subtraction borrows into the exponent
+// field, which is the pattern of the lower binade. The low 29 bits of
+// double(hi) are zero and a normalised lo (|lo| <= ulp(hi) / 2) is worth at
+// most 2^28 of those units, so the add never carries out of hi's binade.
+// Result: hi + lo rounded to the nearest double (ties to even), within one
+// unit in the last place for pairs that are not normalised. Pairs outside
+// that form (hi zero, subnormal, non-finite or below
+// 2^-74; lo non-finite or worth 2^29 units or more) take dd_to_double.
 NW_HD double dd_to_double_int(dd a) {
   const uint32_t hb = f2u(a.hi), lb = f2u(a.lo);
-  const uint32_t eh = (hb >> 23) & 0xffu, el = (lb >> 23) & 0xffu;
-  if (eh - 1u >= 0xfeu || el == 0xffu) return dd_to_double(a);
-  const uint64_t dh = (uint64_t(hb & 0x80000000u) << 32) | (uint64_t(eh + 896u) << 52) |
-                      (uint64_t(hb & 0x7fffffu) << 29);
-  if ((lb & 0x7fffffffu) == 0) return u2d(dh);
-  // a subnormal lo is its 23 fraction bits at the exponent of el = 1
-  const uint32_t d = eh - (el ? el : 1u);
-  if (d < 24u || d > 255u) return dd_to_double(a);
-  const uint32_t ml = (lb & 0x7fffffu) | (el ? 0x800000u : 0u);
-  const bool neg = ((hb ^ lb) & 0x80000000u) != 0;
-  const int sh = 29 - int(d) + ((neg && (hb & 0x7fffffu) == 0) ? 1 : 0);
-  const uint32_t adj = sh >= 0 ? (ml << sh) : (-sh < 32 ? (ml >> -sh) : 0u);
-  return u2d(neg ? dh - adj : dh + adj);
+  const uint32_t eh = (hb >> 23) & 0xffu;
+  if (eh - 53u > 201u || (lb & 0x7f800000u) == 0x7f800000u) return dd_to_double(a);
+  const uint64_t dh = (uint64_t(hb & 0x80000000u) << 32) |
+                      ((uint64_t(hb & 0x7fffffffu) << 29) + (uint64_t(896u) << 52));
+  const bool down = ((hb ^ lb) & 0x80000000u) != 0 && (hb & 0x7fffffu) == 0;
+  // 2^(52 - e) (2^(53 - e) one binade lower), e = eh - 127 the exponent of hi
+  const float scale = u2f((306u - eh + (down ? 1u : 0u)) << 23);
+  // lo's units with the sign taken relative to hi's: the pattern holds |hi|
+  const float t = u2f(f2u(fmul(a.lo, scale)) ^ (hb & 0x80000000u));
+  if (!(fabsf(t) < 536870912.0f)) return dd_to_double(a);  // 2^29
+  return u2d(dh + uint64_t(int64_t(f2i_rn(t))));
 }
 
 // Split of a double into hi (top 24 significand bits) + lo (the next 24,

@@ -130,11 +130,12 @@ def test_pair_to_double_is_correctly_rounded(lib):
         assert o == exact, (h, l, o, exact)
 
 
-def test_integer_widening_within_one_ulp(lib):
-    """dd_to_double_int (integer operations only, used by the row kernels):
-    within one unit in the last place of the correctly rounded hi + lo for
+def test_integer_widening_rounds_like_the_fp64_add(lib):
+    """dd_to_double_int (no FP64 instruction, used by the row kernels): for
     normalised pairs, including a power-of-two hi with a lo of the other
-    sign (the sum drops below hi's binade); other pairs equal the FP64 path."""
+    sign (the sum drops below hi's binade) and half-unit ties, the same bits
+    as the FP64 add of the widened halves (hi + lo correctly rounded); other
+    pairs take that path."""
     from fractions import Fraction
     import math
     rng = np.random.default_rng(7)
@@ -145,6 +146,15 @@ def test_integer_widening_within_one_ulp(lib):
     lo = (rng.uniform(-0.5, 0.5, n) * ulp * 2.0 ** -rng.integers(0, 40, n)).astype(np.float32)
     lo[:250] = -np.sign(hi[:250]) * np.abs(lo[:250])  # power of two hi, lo of the other sign
     lo[250:260] = 0.0
+    # exact ties: odd multiples of half a double unit of hi's binade (a quarter
+    # unit below a power-of-two hi, where the lower binade's unit is half)
+    ud = np.spacing(np.abs(hi[260:600]).astype(np.float64))
+    odd = 2 * rng.integers(0, 4, 340) + 1
+    lo[260:600] = (rng.choice([-1, 1], 340) * ud * odd / 2).astype(np.float32)
+    lo[260:400] = (-np.sign(hi[260:400]) * ud[:140] * odd[:140] / 4).astype(np.float32)
+    hi[260:400] = (np.sign(hi[260:400]) * 2.0 ** rng.integers(-60, 60, 140)).astype(np.float32)
+    lo[260:400] = (-np.sign(hi[260:400]) * np.spacing(np.abs(hi[260:400]).astype(np.float64))
+                   * odd[:140] / 4).astype(np.float32)
     extra_hi = np.array([0.0, -0.0, 1e-40, np.inf, 1.0, 1.0], np.float32)
     extra_lo = np.array([0.0, 1e-44, 0.0, 0.0, np.float32(2.0 ** -24), -np.float32(2.0 ** -23)], np.float32)
     hi = np.concatenate([hi, extra_hi])
@@ -157,5 +167,6 @@ def test_integer_widening_within_one_ulp(lib):
         if not math.isfinite(h):
             assert o == r or (math.isnan(o) and math.isnan(r))
             continue
+        assert o == r, (h, l, o, r)
         exact = Fraction(h) + Fraction(l)
-        assert abs(Fraction(o) - exact) <= Fraction(np.spacing(abs(r))), (h, l, o, r)
+        assert abs(Fraction(o) - exact) <= Fraction(np.spacing(abs(r))) / 2
