@@ -258,6 +258,25 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         mom_ms.append(ev[0].elapsed_time(ev[1]))
         con_ms.append(ev[1].elapsed_time(ev[2]))
+    # the single-kernel form of the momentum assembly (same bits; its edge
+    # coefficients pass through a ring in L2), timed the same way
+    lsm.set_assembly_path(nw.ASSEMBLY_SINGLE_KERNEL)
+    fused_ms = []
+    for i in range(max(3, args.steps) + 1):
+        ev[0].record(stream)
+        lsm.zero_system()
+        lsm.assemble_momentum(fm, mo)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        if i:
+            fused_ms.append(ev[0].elapsed_time(ev[1]))
+    lsm.sync()
+    lsm.set_assembly_path(nw.ASSEMBLY_TWO_KERNELS)
+    f_avg = float(np.mean(fused_ms))
+    ft = traffic_table().get("momentum_single_kernel_128x128x64")
+    B_m0 = algorithmic_bytes("momentum", N, E, nnz_c)
+    single = {"avg_ms": round(f_avg, 4), "frac": round(B_m0 / (f_avg * 1e-3) / 1e9 / peaks()["hbm_gbs"], 4),
+              "traffic": (ft["bytes_per_launch"] if ft else None), "schedule": lsm.assembly_schedule()}
     # e2e: host inputs -> device -> assemble -> rhs back to host
     rhs_m_host = torch.empty(3 * (lsm.sizes()[0] // 3), dtype=torch.float64).pin_memory()
     rhs_c_host = torch.empty(lsc.sizes()[0], dtype=torch.float64).pin_memory()
@@ -368,8 +387,10 @@ def run_ours(args, rank, world):
         "continuity": {"avg_ms": round(con_avg, 4), "algorithmic_bytes": B_c,
                        "achieved_gbs": round(B_c / (con_avg * 1e-3) / 1e9, 1),
                        "gnnz_s": round(nnz_c / (con_avg * 1e-3) / 1e9, 4)},
-        "momentum": {"avg_ms": round(mom_avg, 4), "gnnz_s": round(nnz_m / (mom_avg * 1e-3) / 1e9, 4)},
-        "gpu_launches": 5 * args.steps * reps,  # momentum: edge + row; continuity: node + edge + row
+        "momentum": {"avg_ms": round(mom_avg, 4), "gnnz_s": round(nnz_m / (mom_avg * 1e-3) / 1e9, 4),
+                     "single_kernel": single},
+        # momentum: edge + row kernels; continuity: node + edge + row kernels
+        "gpu_launches": 5 * args.steps * reps,
         "clocks": clocks,
     }
     poisson_csr = None

@@ -262,6 +262,45 @@ nw_status nw_assemble_momentum_edge_range(nw_linsys* ls, const nw_momentum_field
                                           int64_t edge_end);
 nw_status nw_assemble_momentum_rows(nw_linsys* ls, const nw_momentum_opts* o);
 
+/* How nw_assemble_momentum_edges runs on the GPU. TWO_KERNELS (default):
+ * the edge kernel writes every edge's coefficients to a buffer in HBM, then
+ * the row kernel reads them back. SINGLE_KERNEL: one persistent kernel takes
+ * edge chunks and node-row blocks from a fixed work list; the coefficients
+ * pass through a ring of slots sized to stay in L2 (at most 64 MB), so they
+ * never travel to DRAM (about 1.1x the compulsory bytes instead of 1.6x),
+ * but on GB300 it runs slower than the two kernels (both phases are bound by
+ * instruction issue, not by HBM). Both give the same CSR values and rhs, bit
+ * for bit. A wait of the single kernel that times out (it cannot, by the
+ * construction of the work list, but every wait is bounded) is reported as
+ * NW_TIMEOUT by the next nw_linsys_sync, nw_linsys_copy_to_host or
+ * nw_linsys_solve. */
+enum { NW_ASSEMBLY_SINGLE_KERNEL = 0, NW_ASSEMBLY_TWO_KERNELS = 1 };
+nw_status nw_linsys_set_assembly_path(nw_linsys* ls, int path);
+typedef struct {
+  int single_kernel;     /* 1: the single-kernel path is set up */
+  int grid;              /* resident blocks it launches */
+  int chunk_edges;       /* edges per edge chunk */
+  int block_rows;        /* node rows per row block */
+  int64_t edge_chunks, row_blocks;
+  int64_t ring_chunks;   /* ring slots; >= edge_chunks: no reuse */
+  int64_t ring_bytes;    /* 0 when the ring is the whole coefficient buffer */
+  int64_t lag_chunks;    /* chunks between a row block's last input and it */
+} nw_assembly_schedule;
+nw_status nw_linsys_assembly_schedule(const nw_linsys* ls, nw_assembly_schedule* info);
+/* The work list of the single-kernel assembly for a graph given by its edge
+ * list (host only, no GPU: for inspection and tests). edge_rows: E pairs of
+ * node rows (0 .. rows-1); concurrency: resident blocks; max_ring_bytes:
+ * the ring's limit. Sizes go to info (grid = concurrency); with non-null
+ * arrays also: items (edge_chunks + row_blocks entries, 2 c for edge chunk
+ * c, 2 k + 1 for row block k, in ticket order), chunk_lo / chunk_hi
+ * (row_blocks entries: the chunks a block reads) and block_lo / block_hi
+ * (edge_chunks entries: the blocks reading a chunk). */
+nw_status nw_momentum_schedule(int64_t rows, int64_t num_edges, const int64_t* edge_rows,
+                               int64_t concurrency, int64_t max_ring_bytes,
+                               nw_assembly_schedule* info, int32_t* items,
+                               int32_t* chunk_lo, int32_t* chunk_hi, int32_t* block_lo,
+                               int32_t* block_hi);
+
 /* LinearSystem::sumInto, host-vector overload (include/LinearSystem.h:
  * 167-173): one entity block. nodes (host, n_ent) are node indices; rhs
  * (host, n_ent*num_dof) and lhs (host, row-major square of that size). */

@@ -26,6 +26,7 @@ GMRES, CG, FGMRES, BICGSTAB, TFQMR, SSTEP_GMRES = 0, 1, 2, 3, 4, 5
 PC_NONE, PC_JACOBI, PC_SGS, PC_LEARNED, PC_SGS2, PC_SGS_NATURAL, PC_RILUK = 0, 1, 2, 3, 4, 5, 6
 PC_MT_SGS = PC_SGS  # "mt_sgs": multicolour order
 PREC_FP64, PREC_MIXED, PREC_MIXED_BF16 = 0, 1, 2
+ASSEMBLY_SINGLE_KERNEL, ASSEMBLY_TWO_KERNELS = 0, 1
 
 
 class NwError(RuntimeError):
@@ -140,6 +141,15 @@ class MomentumFields(C.Structure):
                                   "area", "mdot", "pecfac")]
 
 
+class AssemblySchedule(C.Structure):
+    _fields_ = [("single_kernel", C.c_int), ("grid", C.c_int), ("chunk_edges", C.c_int),
+                ("block_rows", C.c_int), ("edge_chunks", C.c_int64), ("row_blocks", C.c_int64),
+                ("ring_chunks", C.c_int64), ("ring_bytes", C.c_int64), ("lag_chunks", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class BoxOpts(C.Structure):
     _fields_ = [("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
                 ("stretch_z", C.c_double), ("jitter", C.c_double), ("seed", C.c_uint64),
@@ -176,6 +186,10 @@ SIGNATURES = {
                                                   C.c_int64, C.c_int64]),
     "nw_assemble_momentum_rows": (C.c_int, [C.c_void_p, C.POINTER(MomentumOpts)]),
     "nw_linsys_sgs_classes": (C.c_int, [C.c_void_p, _I64P]),
+    "nw_linsys_set_assembly_path": (C.c_int, [C.c_void_p, C.c_int]),
+    "nw_linsys_assembly_schedule": (C.c_int, [C.c_void_p, C.POINTER(AssemblySchedule)]),
+    "nw_momentum_schedule": (C.c_int, [C.c_int64, C.c_int64, _I64P, C.c_int64, C.c_int64,
+                                       C.POINTER(AssemblySchedule), _I32P, _I32P, _I32P, _I32P, _I32P]),
     "nw_linsys_checkpoint_save": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
     "nw_linsys_checkpoint_load": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.POINTER(SolveReport)]),
     "nw_solver_cfg_from_strings": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(SolverCfg)]),
@@ -305,6 +319,27 @@ def solver_cfg(method=GMRES, preconditioner=PC_JACOBI, precision=PREC_FP64, kspa
     return SolverCfg(method, preconditioner, precision, kspace, max_iterations, tolerance,
                      tolerance if final_tolerance is None else final_tolerance, inner_kspace,
                      inner_tolerance, sgs2_inner_sweeps, sstep_size)
+
+
+def momentum_schedule(rows: int, edge_rows: np.ndarray, concurrency: int,
+                      max_ring_bytes: int = 64 << 20) -> dict:
+    """Work list of the single-kernel momentum assembly for a graph given by
+    its edge list (E x 2 node rows); host only. Returns the sizes plus the
+    arrays items, chunk_lo, chunk_hi, block_lo, block_hi."""
+    lib = load()
+    er = np.ascontiguousarray(edge_rows, np.int64).reshape(-1, 2)
+    info = AssemblySchedule()
+    args = (int(rows), er.shape[0], _ptr(er, C.c_int64), int(concurrency), int(max_ring_bytes),
+            C.byref(info))
+    check(lib.nw_momentum_schedule(*args, None, None, None, None, None))
+    out = info.as_dict()
+    arrs = {k: np.zeros(n, np.int32) for k, n in (
+        ("items", info.edge_chunks + info.row_blocks), ("chunk_lo", info.row_blocks),
+        ("chunk_hi", info.row_blocks), ("block_lo", info.edge_chunks), ("block_hi", info.edge_chunks))}
+    check(lib.nw_momentum_schedule(*args, *(_ptr(arrs[k], C.c_int32) for k in
+                                            ("items", "chunk_lo", "chunk_hi", "block_lo", "block_hi"))))
+    out.update(arrs)
+    return out
 
 
 def solver_cfg_from_strings(method: str, preconditioner: str, **kw) -> SolverCfg:
@@ -484,6 +519,16 @@ class LinearSystem:
 
     def sync(self) -> None:
         check(self.lib.nw_linsys_sync(self.h))
+
+    def set_assembly_path(self, path: int) -> None:
+        """ASSEMBLY_TWO_KERNELS (default) or ASSEMBLY_SINGLE_KERNEL for
+        the momentum assembly; both give the same bits."""
+        check(self.lib.nw_linsys_set_assembly_path(self.h, int(path)))
+
+    def assembly_schedule(self) -> dict:
+        info = AssemblySchedule()
+        check(self.lib.nw_linsys_assembly_schedule(self.h, C.byref(info)))
+        return info.as_dict()
 
     # -- MatrixMarket
     def write_matrix_market(self, base, count: int = 0, x=None) -> None:

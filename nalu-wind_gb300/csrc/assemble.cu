@@ -33,6 +33,7 @@
 #include <type_traits>
 
 #include "assemble.h"
+#include "schedule.h"
 #include "dd.h"
 #include "nw_internal.h"
 
@@ -343,7 +344,7 @@ struct MomentumIn {
 // specialisation drops those operations and gives the same bits.
 template <bool LIMITER, bool DIVU, bool DEF>
 __device__ __forceinline__ void momentum_edge(int64_t e, int64_t E, const MomentumIn& in,
-                                              const MomentumDD& c, dd* __restrict__ buf) {
+                                              const MomentumDD& c, dd* __restrict__ b) {
   const int2* __restrict__ edges = in.edges;
   const double* __restrict__ coords = in.coords;
   const double* __restrict__ vel = in.vel;
@@ -448,7 +449,6 @@ __device__ __forceinline__ void momentum_edge(int64_t e, int64_t E, const Moment
   const dd t = -(viscIp * inv_axdx);
   const dd dlhsfac = t * asq;
   const dd ta0 = t * av[0], ta1 = t * av[1], ta2 = t * av[2];
-  dd* b = buf + e;
   b[0] = (aUR + aC) + dlhsfac;
   b[E] = (-aUL - aC) + dlhsfac;
   b[2 * E] = ta0 * av[0];
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(kThreads, 4)
                     dd* __restrict__ buf) {
   const int64_t e = e0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= e1) return;
-  momentum_edge<LIMITER, DIVU, DEF>(e, E, in, c, buf);
+  momentum_edge<LIMITER, DIVU, DEF>(e, E, in, c, buf + e);
 }
 
 // ---------------------------------------------------------------------------
@@ -569,36 +569,51 @@ __global__ void __launch_bounds__(kRow1Threads)
 // -(sum of the other side's constants + sum of N) / relax.
 constexpr int kRow3Nodes = 64;
 struct Row3Args {
-  int64_t R, E;
+  int64_t R, E;  // node rows; stride of the coefficient arrays
+  int64_t mask;  // edge -> coefficient slot: e & mask
   const int32_t* __restrict__ inc_ptr;
   const uint32_t* __restrict__ inc;
   const int32_t* __restrict__ diag_pos;
   const int64_t* __restrict__ row_ptr;
-  const dd* __restrict__ cb;
+  const dd* cb;  // not restrict: the single-kernel assembly writes it in flight
   dd irelax;
   double* __restrict__ values;
   double* __restrict__ rhs;
   int accumulate, smem_bytes;
 };
 
-// One block of kRow3Nodes node rows starting at r0 (blockDim 3 kRow3Nodes).
+// coefficient loads: through the read-only path when the buffer is not
+// written during the kernel (NC), else plain loads
+template <bool NC>
+__device__ __forceinline__ dd ldc(const dd* p) {
+  if constexpr (NC) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    return {v.x, v.y};
+  } else {
+    return *p;
+  }
+}
+
+// One block of NB node rows starting at r0 (threads 0 .. 3 NB - 1 of the
+// block; any others only take part in the staging copy).
+template <int NB, bool NC>
 __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double* stage) {
   const dd* cb = a.cb;
-  const int64_t E = a.E;
-  const int64_t r1 = (r0 + kRow3Nodes < a.R) ? r0 + kRow3Nodes : a.R;
+  const int64_t E = a.E, mask = a.mask;
+  const int64_t r1 = (r0 + NB < a.R) ? r0 + NB : a.R;
   const int64_t base = a.row_ptr[3 * r0];
   const int64_t cnt = a.row_ptr[3 * r1] - base;
   const bool staged = cnt * int64_t(sizeof(double)) <= a.smem_bytes;
   const int local = threadIdx.x / 3, q = threadIdx.x - 3 * (threadIdx.x / 3);
-  const int64_t r = r0 + local;
+  const int64_t r = local < NB ? r0 + local : r1;
   // row q of the symmetric N (N00 N01 N02 N11 N12 N22 at slots 2..7): its
   // diagonal N_qq and the off-diagonals of columns c1 < c2 (the two c != q),
   // so that the block's c_side I term adds to one fixed entry
   const int c1 = q == 0 ? 1 : 0, c2 = q == 2 ? 1 : 2;
-  const dd* __restrict__ pd = cb + (q == 0 ? 2 : (q == 1 ? 5 : 7)) * E;
-  const dd* __restrict__ p1 = cb + (q == 2 ? 4 : 3) * E;
-  const dd* __restrict__ p2 = cb + (q == 0 ? 4 : 6) * E;
-  const dd* __restrict__ pf = cb + (8 + q) * E;
+  const dd* pd = cb + (q == 0 ? 2 : (q == 1 ? 5 : 7)) * E;
+  const dd* p1 = cb + (q == 2 ? 4 : 3) * E;
+  const dd* p2 = cb + (q == 0 ? 4 : 6) * E;
+  const dd* pf = cb + (8 + q) * E;
   if (r < r1) {
     const int32_t s = a.inc_ptr[r], t = a.inc_ptr[r + 1];
     const int64_t bq = a.row_ptr[3 * r + q];
@@ -618,12 +633,12 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
       for (int32_t qi = s; qi < t; ++qi) {
         const uint32_t w = a.inc[qi];
         const bool dup = (w >> 31) != 0;
-        const int64_t e = (w & 0x7fffffffu) >> 1;
+        const int64_t e = ((w & 0x7fffffffu) >> 1) & mask;
         const int side = w & 1u;
-        const dd c0 = cb[e], c1v = cb[E + e];
+        const dd c0 = ldc<NC>(cb + e), c1v = ldc<NC>(cb + E + e);
         const dd co = side ? c1v : c0, other = side ? c0 : c1v;
-        const dd nd = pd[e], n1 = p1[e], n2 = p2[e];
-        const dd f = pf[e];
+        const dd nd = ldc<NC>(pd + e), n1 = ldc<NC>(p1 + e), n2 = ldc<NC>(p2 + e);
+        const dd f = ldc<NC>(pf + e);
         rr = rr + (side ? f : -f);
         const dd bd = nd + co;
         if (!dup) {
@@ -655,13 +670,116 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
   }
   if (!staged) return;
   __syncthreads();
-  for (int64_t k = threadIdx.x; k < cnt; k += 3 * kRow3Nodes)
+  for (int64_t k = threadIdx.x; k < cnt; k += blockDim.x)
     a.values[base + k] = a.accumulate ? a.values[base + k] + stage[k] : stage[k];
 }
 
 __global__ void __launch_bounds__(3 * kRow3Nodes) row3t_k(Row3Args a) {
   extern __shared__ double stage[];
-  row3_block(int64_t(blockIdx.x) * kRow3Nodes, a, stage);
+  row3_block<kRow3Nodes, true>(int64_t(blockIdx.x) * kRow3Nodes, a, stage);
+}
+
+// ---------------------------------------------------------------------------
+// Single-kernel momentum assembly: a persistent kernel whose blocks take
+// edge chunks and row blocks from the work list of schedule.h in ticket
+// order. Edge chunks write their coefficients into a ring of slots small
+// enough to stay in L2, row blocks read them from there, so the coefficient
+// round trip of the two-kernel form never reaches DRAM. The arithmetic and
+// the summation order are those of momentum_edge_k + row3t_k: the CSR
+// values are the same bits.
+//
+// Dependencies are flags holding the launch's generation number: a chunk's
+// flag is set once its coefficients are written, a row block's once its
+// reads are done. Waits only point to earlier tickets, held by running
+// blocks, so they end; each poll is still bounded (kSpinLimit rounds), after
+// which the block records the timeout in *err, skips its work, sets its own
+// flag and the remaining blocks stop taking tickets.
+struct FusedArgs {
+  const int32_t* __restrict__ items;
+  const int32_t* __restrict__ in_ptr;   // row block k reads chunks in[in_ptr[k] ..]
+  const int32_t* __restrict__ in;
+  const int32_t* __restrict__ out_ptr;  // chunk c is read by blocks out[out_ptr[c] ..]
+  const int32_t* __restrict__ out;
+  int* eflag;
+  int* rflag;
+  int* ticket;
+  int* err;
+  int64_t num_edges, ring_chunks;
+  int nitems, gen;
+};
+
+constexpr int kSpinLimit = 1 << 20;
+
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_volatile(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+// True once flags[list[0 .. n)] all hold gen. Each thread polls a strided
+// share with relaxed loads and, having seen its flags set, issues one
+// acquire fence (the flag was set by a release store after the producer's
+// writes), then the block agrees at a barrier. False in every thread after a
+// timeout, or when another block has reported one.
+__device__ bool wait_flags(const int* flags, const int32_t* list, int n, int gen, int* err) {
+  bool ok = true, polled = false;
+  for (int i = int(threadIdx.x); ok && i < n; i += int(blockDim.x)) {
+    const int* fp = flags + list[i];
+    polled = true;
+    int spins = 0;
+    while (ld_relaxed(fp) != gen) {
+      if (++spins > kSpinLimit || ((spins & 1023) == 0 && ld_volatile(err) != 0)) {
+        ok = false;
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+  if (polled && ok) fence_acq_rel();
+  const bool all = __syncthreads_and(ok) != 0;
+  if (!all && threadIdx.x == 0) atomicExch(err, 1);
+  return all;
+}
+
+template <bool LIMITER, bool DIVU, bool DEF>
+__global__ void __launch_bounds__(kFusedChunk, 4)
+    momentum_fused_k(FusedArgs f, MomentumIn in, MomentumDD c, Row3Args ra, dd* ring) {
+  extern __shared__ double stage[];
+  __shared__ int s_item[2];
+  int next = 0;
+  if (threadIdx.x == 0) next = atomicAdd(f.ticket, 1);
+  for (int p = 0;; p ^= 1) {
+    // double-buffered item word: the barrier of the next round separates
+    // this round's reads from the write two rounds on
+    if (threadIdx.x == 0) s_item[p] = (next < f.nitems && ld_volatile(f.err) == 0) ? f.items[next] : -1;
+    __syncthreads();
+    const int it = s_item[p];
+    if (it < 0) return;
+    // the next ticket is taken now; its latency hides behind this item
+    if (threadIdx.x == 0) next = atomicAdd(f.ticket, 1);
+    const int idx = it >> 1;
+    if (it & 1) {
+      const int b = f.in_ptr[idx];
+      if (wait_flags(f.eflag, f.in + b, f.in_ptr[idx + 1] - b, f.gen, f.err))
+        row3_block<kFusedBlock, false>(int64_t(idx) * kFusedBlock, ra, stage);
+      __syncthreads();
+      if (threadIdx.x == 0) st_release(f.rflag + idx, f.gen);
+    } else {
+      // the slot's previous chunk must have been read by all its row blocks
+      const int64_t prev = int64_t(idx) - f.ring_chunks;
+      const bool ok = prev < 0 || wait_flags(f.rflag, f.out + f.out_ptr[prev],
+                                             f.out_ptr[prev + 1] - f.out_ptr[prev], f.gen, f.err);
+      const int64_t e = int64_t(idx) * kFusedChunk + threadIdx.x;
+      if (ok && e < f.num_edges) momentum_edge<LIMITER, DIVU, DEF>(e, ra.E, in, c, ring + (e & ra.mask));
+      __syncthreads();
+      if (threadIdx.x == 0) st_release(f.eflag + idx, f.gen);
+    }
+  }
 }
 
 // applyDirichletBCs / resetRows: identity (or diag_value) rows.
@@ -727,6 +845,18 @@ void set_smem_attrs() {
   NW_CUDA(cudaFuncSetAttribute(row1_k<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
   NW_CUDA(cudaFuncSetAttribute(row1_k<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
   NW_CUDA(cudaFuncSetAttribute(row3t_k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
+#define NW_FUSED_ATTR(LIM, DIV, DEF)                                                      \
+  NW_CUDA(cudaFuncSetAttribute(momentum_fused_k<LIM, DIV, DEF>,                           \
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem))
+  NW_FUSED_ATTR(false, false, false);
+  NW_FUSED_ATTR(false, false, true);
+  NW_FUSED_ATTR(false, true, false);
+  NW_FUSED_ATTR(false, true, true);
+  NW_FUSED_ATTR(true, false, false);
+  NW_FUSED_ATTR(true, false, true);
+  NW_FUSED_ATTR(true, true, false);
+  NW_FUSED_ATTR(true, true, true);
+#undef NW_FUSED_ATTR
   g_smem_set_device = dev;
 }
 
@@ -798,7 +928,7 @@ MomentumIn momentum_in(const int2* edges, const nw_momentum_fields& f) {
 Row3Args row3_args(int64_t R, const int32_t* inc_ptr, const uint32_t* inc, const int32_t* diag_pos,
                    const int64_t* row_ptr, const double* buf, int64_t E, double relax, double* values,
                    double* rhs, int accumulate, int smem_bytes) {
-  return Row3Args{R, E, inc_ptr, inc, diag_pos, row_ptr, reinterpret_cast<const dd*>(buf),
+  return Row3Args{R, E, int64_t(-1), inc_ptr, inc, diag_pos, row_ptr, reinterpret_cast<const dd*>(buf),
                   dd_param(1.0 / relax), values, rhs, accumulate, smem_bytes};
 }
 }  // namespace
@@ -825,11 +955,47 @@ void launch_momentum_edges(cudaStream_t s, int64_t E, int64_t e0, int64_t e1, co
 #undef NW_MOM
 }
 
-int row_block_nodes(int kind) { return kind == 2 ? kRow3Nodes : kRow1Threads; }
+int fused_blocks_per_sm(int smem_bytes) {
+  set_smem_attrs();
+  int occ = 0;
+  NW_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, momentum_fused_k<false, false, true>,
+                                                        kFusedChunk, smem_bytes));
+  return occ;
+}
+
+void launch_momentum_fused(cudaStream_t s, const FusedLaunch& L, const int2* edges,
+                           const nw_momentum_fields& f, const MomentumOpts& o) {
+  if (L.nitems == 0) return;
+  set_smem_attrs();
+  const MomentumDD c = momentum_dd(o);
+  const MomentumIn in = momentum_in(edges, f);
+  Row3Args ra = row3_args(L.R, L.inc_ptr, L.inc, L.diag_pos, L.row_ptr, L.ring, L.stride, o.relax,
+                          L.values, L.rhs, L.accumulate, L.smem_bytes);
+  ra.mask = L.mask;
+  FusedArgs fa{L.items, L.in_ptr, L.in, L.out_ptr, L.out, L.eflag, L.rflag,
+               L.ticket, L.err, L.num_edges, L.ring_chunks, int(L.nitems), L.gen};
+  dd* ring = reinterpret_cast<dd*>(L.ring);
+  NW_CUDA(cudaMemsetAsync(L.ticket, 0, sizeof(int), s));
+  const bool lim = o.use_limiter != 0, divu = o.include_div_u != 0.0;
+  const bool def = o.alpha == 0.0 && o.alpha_upw == 1.0 && o.upw_factor == 1.0;
+#define NW_FUSED(LIM, DIV, DEF) \
+  momentum_fused_k<LIM, DIV, DEF><<<L.grid, kFusedChunk, L.smem_bytes, s>>>(fa, in, c, ra, ring)
+#define NW_FUSED2(LIM, DIV) \
+  if (def) NW_FUSED(LIM, DIV, true); \
+  else NW_FUSED(LIM, DIV, false)
+  if (lim && divu) NW_FUSED2(true, true);
+  else if (lim) NW_FUSED2(true, false);
+  else if (divu) NW_FUSED2(false, true);
+  else NW_FUSED2(false, false);
+#undef NW_FUSED2
+#undef NW_FUSED
+}
+
+int row_block_nodes(int kind) { return kind == 3 ? kFusedBlock : (kind == 2 ? kRow3Nodes : kRow1Threads); }
 
 int row_stage_bytes(int kind, const int64_t* row_ptr_host, int64_t R) {
   const int nb = row_block_nodes(kind);
-  const int nd = kind == 2 ? 3 : 1;
+  const int nd = kind >= 2 ? 3 : 1;
   int64_t mx = 0;
   for (int64_t r0 = 0; r0 < R; r0 += nb) {
     const int64_t r1 = r0 + nb < R ? r0 + nb : R;

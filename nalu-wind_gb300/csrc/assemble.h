@@ -46,7 +46,40 @@ void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
                  const int64_t* row_ptr, const double* buf, int64_t E,
                  double relax, double* values, double* rhs, int accumulate,
                  int smem_bytes, int max_inc = 0);
+// kind 3: the row blocks of the single-kernel momentum assembly.
 int row_stage_bytes(int kind, const int64_t* row_ptr_host, int64_t R);
+
+// Single-kernel momentum assembly (momentum_fused_k) over the work list of
+// schedule.h. ring: the coefficient slots (stride `stride`, edge e in slot
+// e & mask); eflag / rflag: one flag per edge chunk / row block, never
+// reset (a launch waits for its own generation `gen`); ticket: the work
+// counter (cleared by the launch); err: set to 1 when a wait timed out.
+struct FusedLaunch {
+  const int32_t* items = nullptr;
+  const int32_t* in_ptr = nullptr;   // chunks each row block reads (CSR)
+  const int32_t* in = nullptr;
+  const int32_t* out_ptr = nullptr;  // row blocks reading each chunk (CSR)
+  const int32_t* out = nullptr;
+  int* eflag = nullptr;
+  int* rflag = nullptr;
+  int* ticket = nullptr;
+  int* err = nullptr;
+  double* ring = nullptr;
+  int64_t nitems = 0, num_edges = 0, ring_chunks = 0, stride = 0, mask = -1;
+  int gen = 0, grid = 0, smem_bytes = 0;
+  int64_t R = 0;
+  const int32_t* inc_ptr = nullptr;
+  const uint32_t* inc = nullptr;
+  const int32_t* diag_pos = nullptr;
+  const int64_t* row_ptr = nullptr;
+  double* values = nullptr;
+  double* rhs = nullptr;
+  int accumulate = 0;
+};
+// resident blocks of the kernel per SM with smem_bytes of row staging
+int fused_blocks_per_sm(int smem_bytes);
+void launch_momentum_fused(cudaStream_t s, const FusedLaunch& L, const int2* edges,
+                           const nw_momentum_fields& f, const MomentumOpts& o);
 void launch_reset_rows(cudaStream_t s, int64_t n, const int64_t* nodes,
                        const int64_t* node_lid, int num_dof, int begin,
                        int end, const int64_t* row_ptr, const int32_t* col_idx,

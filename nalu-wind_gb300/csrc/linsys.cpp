@@ -19,6 +19,7 @@
 #include "learned.h"
 #include "node_kernels.h"
 #include "nw_internal.h"
+#include "schedule.h"
 
 namespace nw {
 
@@ -58,6 +59,15 @@ struct nw_linsys {
   DeviceArray<double> values, rhs, buf, nodebuf;
   int stage_bytes[3] = {0, 0, 0};  // row-phase staging per kind
   int max_inc = 0;                 // most incidences of a node row
+  // single-kernel momentum assembly (schedule.h), taken when fused_ok and
+  // assembly_path is NW_ASSEMBLY_SINGLE_KERNEL
+  bool fused_ok = false;
+  int assembly_path = NW_ASSEMBLY_TWO_KERNELS;
+  FusedSchedule fsched;
+  FusedLaunch fl;
+  DeviceArray<int32_t> f_items, f_in_ptr, f_in, f_out_ptr, f_out;
+  DeviceArray<int> f_eflag, f_rflag, f_ticket, f_err;
+  DeviceArray<double> ring;
   DeviceArray<int> err;
   DeviceArray<int64_t> scratch_lid;
   DeviceArray<double> scratch_vals;
@@ -238,6 +248,86 @@ nw_status nw_linsys_build_edge_graph(nw_linsys* ls, int64_t num_nodes,
   });
 }
 
+// Work list, ring and flags of the single-kernel momentum assembly. The
+// ring holds at most 64 MB of coefficient slots (it is meant to stay in
+// L2); a mesh whose rows read edges too far apart for that gets one slot
+// per edge chunk, i.e. the whole coefficient buffer.
+static void setup_fused(nw_linsys* ls) {
+  const HostGraph& g = ls->g;
+  cudaStream_t s = ls->stream;
+  ls->fused_ok = false;
+  if (g.num_edges == 0 || g.node_rows == 0) return;
+  const int smem = row_stage_bytes(3, g.row_ptr.data(), g.node_rows);
+  const int occ = fused_blocks_per_sm(smem);
+  int sms = 0;
+  NW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ls->device));
+  if (occ < 1 || sms < 1) return;
+  const int64_t slot_bytes = int64_t(kFusedChunk) * kMomentumCoefs * int64_t(sizeof(double));
+  build_fused_schedule(g.num_edges, g.node_rows, g.inc_ptr.data(), g.inc.data(),
+                       int64_t(occ) * sms, (int64_t(64) << 20) / slot_bytes, ls->fsched);
+  const FusedSchedule& fs = ls->fsched;
+  ls->f_items.upload(fs.items, s);
+  ls->f_in_ptr.upload(fs.in_ptr, s);
+  ls->f_in.upload(fs.in, s);
+  ls->f_out_ptr.upload(fs.out_ptr, s);
+  ls->f_out.upload(fs.out, s);
+  ls->f_eflag.resize(size_t(fs.chunks));
+  ls->f_rflag.resize(size_t(fs.blocks));
+  ls->f_ticket.resize(1);
+  ls->f_err.resize(1);
+  NW_CUDA(cudaMemsetAsync(ls->f_eflag.p, 0, fs.chunks * sizeof(int), s));
+  NW_CUDA(cudaMemsetAsync(ls->f_rflag.p, 0, fs.blocks * sizeof(int), s));
+  NW_CUDA(cudaMemsetAsync(ls->f_err.p, 0, sizeof(int), s));
+  FusedLaunch& L = ls->fl;
+  L = FusedLaunch();
+  if (fs.ring_chunks < fs.chunks) {
+    L.stride = fs.ring_chunks * kFusedChunk;
+    L.mask = L.stride - 1;
+    ls->ring.resize(size_t(kMomentumCoefs) * size_t(L.stride));
+    L.ring = ls->ring.p;
+  } else {
+    ls->ring.release();
+    L.stride = g.num_edges;
+    L.mask = -1;
+    L.ring = ls->buf.p;
+  }
+  L.items = ls->f_items.p;
+  L.in_ptr = ls->f_in_ptr.p;
+  L.in = ls->f_in.p;
+  L.out_ptr = ls->f_out_ptr.p;
+  L.out = ls->f_out.p;
+  L.eflag = ls->f_eflag.p;
+  L.rflag = ls->f_rflag.p;
+  L.ticket = ls->f_ticket.p;
+  L.err = ls->f_err.p;
+  L.nitems = int64_t(fs.items.size());
+  L.num_edges = g.num_edges;
+  L.ring_chunks = fs.ring_chunks;
+  L.grid = occ * sms;
+  L.smem_bytes = smem;
+  L.R = g.node_rows;
+  L.inc_ptr = ls->inc_ptr.p;
+  L.inc = ls->inc.p;
+  L.diag_pos = ls->diag_pos.p;
+  L.row_ptr = ls->row_ptr.p;
+  L.values = ls->values.p;
+  L.rhs = ls->rhs.p;
+  ls->fused_ok = true;
+}
+
+// Raises if a single-kernel assembly since the last check timed out in a
+// dependency wait (the system's values are then not valid).
+static void check_fused(nw_linsys* ls) {
+  if (!ls->fused_ok || !ls->f_err.p) return;
+  int h = 0;
+  NW_CUDA(cudaMemcpyAsync(&h, ls->f_err.p, sizeof(int), cudaMemcpyDeviceToHost, ls->stream));
+  NW_CUDA(cudaStreamSynchronize(ls->stream));
+  if (h) {
+    NW_CUDA(cudaMemsetAsync(ls->f_err.p, 0, sizeof(int), ls->stream));
+    fail(NW_TIMEOUT, "momentum assembly: a dependency wait of the single-kernel assembly timed out");
+  }
+}
+
 nw_status nw_linsys_finalize(nw_linsys* ls) {
   return guard([&] {
     if (!ls) fail(NW_INVALID_ARG, "null handle");
@@ -287,6 +377,7 @@ nw_status nw_linsys_finalize(nw_linsys* ls) {
       ls->max_inc = 0;
       for (int64_t r = 0; r < g.node_rows; ++r)
         ls->max_inc = std::max(ls->max_inc, g.inc_ptr[r + 1] - g.inc_ptr[r]);
+      setup_fused(ls);
     }
     NW_CUDA(cudaMemsetAsync(ls->values.p, 0, g.nnz * sizeof(double), s));
     NW_CUDA(cudaMemsetAsync(ls->rhs.p, 0, g.nrows * sizeof(double), s));
@@ -449,8 +540,29 @@ nw_status nw_assemble_momentum_edges(nw_linsys* ls, const nw_momentum_fields* f,
     check_momentum_args(ls, f, o);
     begin_timing(ls);
     const int64_t E = ls->g.num_edges;
-    launch_momentum_edges(ls->stream, E, 0, E, ls->edges.p, *f, *o, ls->buf.p);
-    momentum_rows(ls, o->relax);
+    if (ls->fused_ok && ls->assembly_path == NW_ASSEMBLY_SINGLE_KERNEL) {
+      FusedLaunch& L = ls->fl;
+      if (++L.gen == INT32_MAX) {  // flags hold generations: restart them
+        L.gen = 1;
+        NW_CUDA(cudaMemsetAsync(L.eflag, 0, ls->fsched.chunks * sizeof(int), ls->stream));
+        NW_CUDA(cudaMemsetAsync(L.rflag, 0, ls->fsched.blocks * sizeof(int), ls->stream));
+      }
+      L.accumulate = ls->pristine ? 0 : 1;
+      // the system's arrays as they are now
+      L.values = ls->values.p;
+      L.rhs = ls->rhs.p;
+      L.row_ptr = ls->row_ptr.p;
+      L.inc_ptr = ls->inc_ptr.p;
+      L.inc = ls->inc.p;
+      L.diag_pos = ls->diag_pos.p;
+      if (!ls->ring.p) L.ring = ls->buf.p;
+      launch_momentum_fused(ls->stream, L, ls->edges.p, *f, *o);
+      NW_CUDA(cudaGetLastError());
+      ls->pristine = false;
+    } else {
+      launch_momentum_edges(ls->stream, E, 0, E, ls->edges.p, *f, *o, ls->buf.p);
+      momentum_rows(ls, o->relax);
+    }
     end_timing(ls);
   });
 }
@@ -594,6 +706,7 @@ nw_status nw_linsys_copy_from_host(nw_linsys* ls, const double* values,
       NW_CUDA(cudaMemcpyAsync(ls->rhs.p, rhs, ls->rhs.n * sizeof(double),
                               cudaMemcpyHostToDevice, ls->stream));
     NW_CUDA(cudaStreamSynchronize(ls->stream));
+    check_fused(ls);
   });
 }
 
@@ -603,6 +716,7 @@ nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
     need_finalized(ls);
     if (!x) fail(NW_INVALID_ARG, "null solution vector");
     materialize_zero(ls);
+    check_fused(ls);
     if (ls->cfg.preconditioner == NW_PC_LEARNED && !ls->coarse)
       fail(NW_INVALID_ARG, "NW_PC_LEARNED needs nw_linsys_attach_learned");
     ls->solver.refresh(ls->stream);
@@ -1350,6 +1464,83 @@ nw_status nw_linsys_sync(nw_linsys* ls) {
   return guard([&] {
     if (!ls) fail(NW_INVALID_ARG, "null handle");
     NW_CUDA(cudaStreamSynchronize(ls->stream));
+    check_fused(ls);
+  });
+}
+
+nw_status nw_linsys_set_assembly_path(nw_linsys* ls, int path) {
+  return guard([&] {
+    if (!ls) fail(NW_INVALID_ARG, "null handle");
+    if (path != NW_ASSEMBLY_SINGLE_KERNEL && path != NW_ASSEMBLY_TWO_KERNELS)
+      fail(NW_INVALID_ARG, "unknown assembly path");
+    ls->assembly_path = path;
+  });
+}
+
+nw_status nw_momentum_schedule(int64_t rows, int64_t num_edges, const int64_t* edge_rows,
+                               int64_t concurrency, int64_t max_ring_bytes,
+                               nw_assembly_schedule* info, int32_t* items, int32_t* chunk_lo,
+                               int32_t* chunk_hi, int32_t* block_lo, int32_t* block_hi) {
+  return guard([&] {
+    if (!info || (num_edges > 0 && !edge_rows)) fail(NW_INVALID_ARG, "null argument");
+    if (rows < 1 || num_edges < 0 || num_edges >= (int64_t(1) << 30) || concurrency < 1)
+      fail(NW_INVALID_ARG, "size out of range");
+    // incidence lists as the graph builder orders them (by column, then edge)
+    std::vector<int32_t> ptr(size_t(rows) + 1, 0);
+    for (int64_t e = 0; e < num_edges; ++e)
+      for (int sd = 0; sd < 2; ++sd) {
+        const int64_t r = edge_rows[2 * e + sd];
+        if (r < 0 || r >= rows) fail(NW_INVALID_ARG, "edge row out of range");
+        ++ptr[r + 1];
+      }
+    for (int64_t r = 0; r < rows; ++r) ptr[r + 1] += ptr[r];
+    std::vector<uint32_t> inc(size_t(ptr[rows]));
+    std::vector<int32_t> pos(ptr.begin(), ptr.end() - 1);
+    for (int64_t e = 0; e < num_edges; ++e)
+      for (int sd = 0; sd < 2; ++sd) inc[pos[edge_rows[2 * e + sd]]++] = uint32_t(e << 1 | sd);
+    FusedSchedule fs;
+    const int64_t slot_bytes = int64_t(kFusedChunk) * kMomentumCoefs * int64_t(sizeof(double));
+    build_fused_schedule(num_edges, rows, ptr.data(), inc.data(), concurrency,
+                         std::max<int64_t>(0, max_ring_bytes) / slot_bytes, fs);
+    *info = nw_assembly_schedule{};
+    info->single_kernel = 1;
+    info->grid = int(std::min<int64_t>(concurrency, INT32_MAX));
+    info->chunk_edges = kFusedChunk;
+    info->block_rows = kFusedBlock;
+    info->edge_chunks = fs.chunks;
+    info->row_blocks = fs.blocks;
+    info->ring_chunks = fs.ring_chunks;
+    info->ring_bytes = fs.ring_chunks < fs.chunks ? fs.ring_chunks * slot_bytes : 0;
+    info->lag_chunks = fs.lag;
+    auto put = [](int32_t* dst, const std::vector<int32_t>& v) {
+      if (dst) std::copy(v.begin(), v.end(), dst);
+    };
+    put(items, fs.items);
+    put(chunk_lo, fs.chunk_lo);
+    put(chunk_hi, fs.chunk_hi);
+    put(block_lo, fs.block_lo);
+    put(block_hi, fs.block_hi);
+  });
+}
+
+nw_status nw_linsys_assembly_schedule(const nw_linsys* ls, nw_assembly_schedule* info) {
+  return guard([&] {
+    if (!ls || !info) fail(NW_INVALID_ARG, "null argument");
+    need_finalized(ls);
+    *info = nw_assembly_schedule{};
+    info->single_kernel = ls->fused_ok ? 1 : 0;
+    if (!ls->fused_ok) return;
+    const FusedSchedule& fs = ls->fsched;
+    info->edge_chunks = fs.chunks;
+    info->row_blocks = fs.blocks;
+    info->ring_chunks = fs.ring_chunks;
+    info->ring_bytes = fs.ring_chunks < fs.chunks
+                           ? fs.ring_chunks * kFusedChunk * kMomentumCoefs * int64_t(sizeof(double))
+                           : 0;
+    info->lag_chunks = fs.lag;
+    info->grid = ls->fl.grid;
+    info->chunk_edges = kFusedChunk;
+    info->block_rows = kFusedBlock;
   });
 }
 
