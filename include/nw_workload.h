@@ -50,6 +50,16 @@ typedef struct nw_box_opts {
 nw_status nw_mesh_box(int nx, int ny, int nz, const nw_box_opts* opts,
                       nw_mesh** out);
 nw_status nw_mesh_destroy(nw_mesh* m);
+/* Reverse Cuthill-McKee order of a mesh's node graph, for callers whose node
+ * numbering scatters neighbours (the assembly gathers node data per edge and
+ * the row phase reads every incident edge, so locality in the numbering is
+ * locality in memory: on 2.1M-node tets the assembly runs 2.3x faster in
+ * RCM order than in random order). edges: E pairs of node indices;
+ * order[k] = the node to place at position k (breadth-first from a
+ * minimum-degree node of each component, neighbours by ascending degree,
+ * then reversed). Host only. */
+nw_status nw_mesh_rcm_order(int64_t num_nodes, int64_t num_edges, const int64_t* edges,
+                            int64_t* order);
 /* nodes_per_elem: 8 (hex) or 4 (tet). */
 nw_status nw_mesh_sizes(const nw_mesh* m, int64_t* num_nodes,
                         int64_t* num_edges, int64_t* num_elems,

@@ -268,6 +268,7 @@ SIGNATURES = {
     "nw_geometry_compute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "nw_geometry_destroy": (C.c_int, [C.c_void_p]),
     "nw_mesh_destroy": (C.c_int, [C.c_void_p]),
+    "nw_mesh_rcm_order": (C.c_int, [C.c_int64, C.c_int64, _I64P, _I64P]),
     "nw_mesh_sizes": (C.c_int, [C.c_void_p, _I64P, _I64P, _I64P, C.POINTER(C.c_int)]),
     "nw_mesh_get": (C.c_int, [C.c_void_p, _DP, _I64P, _I64P, _I64P, _I64P, _DP, _DP, _DP]),
     "nw_mesh_face_ips": (C.c_int, [C.c_void_p, C.c_int, _I64P, _I64P, _DP, C.POINTER(C.c_int32)]),
@@ -319,6 +320,15 @@ def solver_cfg(method=GMRES, preconditioner=PC_JACOBI, precision=PREC_FP64, kspa
     return SolverCfg(method, preconditioner, precision, kspace, max_iterations, tolerance,
                      tolerance if final_tolerance is None else final_tolerance, inner_kspace,
                      inner_tolerance, sgs2_inner_sweeps, sstep_size)
+
+
+def rcm_order(num_nodes: int, edges: np.ndarray) -> np.ndarray:
+    """Reverse Cuthill-McKee order of the node graph (nw_mesh_rcm_order):
+    order[k] is the node to place at position k."""
+    e = np.ascontiguousarray(edges, np.int64).reshape(-1, 2)
+    out = np.zeros(int(num_nodes), np.int64)
+    check(load().nw_mesh_rcm_order(int(num_nodes), e.shape[0], _ptr(e, C.c_int64), _ptr(out, C.c_int64)))
+    return out
 
 
 def momentum_schedule(rows: int, edge_rows: np.ndarray, concurrency: int,

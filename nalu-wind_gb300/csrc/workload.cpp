@@ -502,6 +502,38 @@ nw_status nw_mesh_destroy(nw_mesh* m) {
   return NW_OK;
 }
 
+nw_status nw_mesh_rcm_order(int64_t num_nodes, int64_t num_edges, const int64_t* edges,
+                            int64_t* order) {
+  return guard([&] {
+    if (!order || (num_edges > 0 && !edges)) fail(NW_INVALID_ARG, "null argument");
+    if (num_nodes < 1 || num_edges < 0) fail(NW_INVALID_ARG, "size out of range");
+    std::vector<int64_t> ap(size_t(num_nodes) + 1, 0);
+    for (int64_t e = 0; e < 2 * num_edges; ++e) {
+      if (edges[e] < 0 || edges[e] >= num_nodes) fail(NW_INVALID_ARG, "edge node out of range");
+      ++ap[edges[e] + 1];
+    }
+    for (int64_t i = 0; i < num_nodes; ++i) ap[i + 1] += ap[i];
+    std::vector<int64_t> aj(size_t(ap[num_nodes])), pos(ap.begin(), ap.end() - 1);
+    for (int64_t e = 0; e < num_edges; ++e) {
+      const int64_t a = edges[2 * e], b = edges[2 * e + 1];
+      aj[pos[a]++] = b;
+      aj[pos[b]++] = a;
+    }
+    // sorted, duplicate-free neighbour lists (the order then depends on the
+    // graph only, not on the edge order)
+    std::vector<int64_t> ap2(size_t(num_nodes) + 1, 0), aj2;
+    aj2.reserve(aj.size());
+    for (int64_t i = 0; i < num_nodes; ++i) {
+      std::sort(aj.begin() + ap[i], aj.begin() + ap[i + 1]);
+      for (int64_t p = ap[i]; p < ap[i + 1]; ++p)
+        if (aj[p] != i && (p == ap[i] || aj[p] != aj[p - 1])) aj2.push_back(aj[p]);
+      ap2[i + 1] = int64_t(aj2.size());
+    }
+    const std::vector<int64_t> ord = rcm_order(num_nodes, ap2, aj2);
+    std::copy(ord.begin(), ord.end(), order);
+  });
+}
+
 nw_status nw_mesh_sizes(const nw_mesh* m, int64_t* num_nodes,
                         int64_t* num_edges, int64_t* num_elems,
                         int* nodes_per_elem) {

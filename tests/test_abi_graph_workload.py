@@ -231,3 +231,21 @@ def test_solver_strings_map_like_the_reference(nw):
         assert e.value.status == 1
     with pytest.raises(nw.NwError):
         nw.solver_cfg_from_strings("lsqr", "jacobi")
+
+
+def test_rcm_order_restores_locality(nw):
+    """nw_mesh_rcm_order on a randomly numbered tet mesh: a permutation that
+    cuts the bandwidth, and the same order the mesh generator applies for
+    renumber = 2 (random, then RCM) from the same graph."""
+    rnd = nw.Mesh(14, 12, 10, tets=True, renumber=1, renumber_seed=3)
+    N = rnd.num_nodes
+    order = nw.rcm_order(N, rnd.edges)
+    np.testing.assert_array_equal(np.sort(order), np.arange(N))
+    inv = np.empty(N, np.int64)
+    inv[order] = np.arange(N)
+    bw = lambda e: int(np.abs(e[:, 0] - e[:, 1]).max())
+    assert bw(inv[rnd.edges]) * 8 < bw(rnd.edges)
+    rcm = nw.Mesh(14, 12, 10, tets=True, renumber=2, renumber_seed=3)
+    np.testing.assert_array_equal(rcm.coords, rnd.coords[order])
+    with pytest.raises(nw.NwError):
+        nw.rcm_order(3, np.array([[0, 3]]))
