@@ -401,11 +401,14 @@ nw_status nw_linsys_coarse_sizes(nw_linsys* ls, int64_t* nc, int64_t* nnzc);
 nw_status nw_linsys_coarse_graph(nw_linsys* ls, int32_t* agg, int64_t* cptr,
                                  int32_t* ccol, float* wgt, float* dinv);
 /* Harvest (residual, error) pairs from the handle's assembled system:
- * x* from a tight (1e-11) mixed-precision SGS solve, or FP64 SGS-GMRES
- * when FP32 refinement cannot converge, then `restarts` cycles of plain
- * FP64 Jacobi-GMRES(kspace) from x0 = 0, one pair per restart. Stored on
- * the device as the coarse residual R (r - A z1) with the energy norms
- * ||e||_A^2 and ||e - z1||_A^2 of the error e = x* - x. */
+ * x* from a tight (1e-11, at most 5,000 iterations) mixed-precision SGS
+ * solve, or FP64 SGS-GMRES when FP32 refinement cannot converge, then
+ * `restarts` cycles of plain FP64 Jacobi-GMRES(kspace) from x0 = 0, one
+ * pair per restart while the restart's residual is at least 100 times
+ * that of x* (the error target is then accurate to 1 %); NW_NOT_CONVERGED
+ * when x* itself is not below 1e-6 relative. Stored on the device as the
+ * coarse residual R (r - A z1) with the energy norms ||e||_A^2 and
+ * ||e - z1||_A^2 of the error e = x* - x. */
 nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts,
                              int kspace, int* total_pairs);
 nw_status nw_learned_clear_data(nw_learned* net);

@@ -1748,7 +1748,7 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
     tight.kspace = std::min(50, std::max(ls->cfg.kspace, 30));
     tight.inner_kspace = tight.kspace;
     tight.inner_tolerance = 1e-4;
-    tight.max_iterations = 20000;
+    tight.max_iterations = 5000;
     pc.kind = NW_PC_SGS;
     SolveResult sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
     if (!sr.converged) {
@@ -1757,10 +1757,13 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
       tight.precision = NW_PREC_FP64;
       sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
     }
-    // FP64 cannot always reach 1e-11 on the most stretched meshes; a
-    // reference at 1e-9 is still far below the errors of the harvested
-    // iterates (restarts of a 1e-8 solve), so it is kept
-    if (!sr.converged && !(sr.final_abs <= 1e-9 * sr.bnorm))
+    // On strongly stretched meshes (cell growth 1.15 over 127 cells is a
+    // 4e7 ratio of the first to the last z spacing) FP64 GMRES stalls short
+    // of 1e-11. The reference x* is kept at the residual r* it reached, and
+    // a pair (r, e = x* - x) only while |r| >= 100 |r*|: A e = r - r*, so
+    // the target error is then within 1 % of e.
+    const double rstar = sr.final_abs;
+    if (!(rstar <= 1e-6 * sr.bnorm))
       fail(NW_NOT_CONVERGED, "harvest: reference solve did not converge");
     // system coarse weights
     const int sys = L.nsystems++;
@@ -1800,7 +1803,7 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
         h32[i] = float(hr[i]);
         rn += hr[i] * hr[i];
       }
-      if (!(rn > 0.0)) break;
+      if (!(rn > 0.0) || std::sqrt(rn) < 100.0 * rstar) break;
       NW_CUDA(cudaMemcpyAsync(r32.p, h32.data(), n * 4, cudaMemcpyHostToDevice, s));
       // z1 = pre-smoothing sweep of r, r1 = r - A z1, rc = R r1
       ks.learned_presmooth32(r32.p, z1.p, s);
