@@ -401,8 +401,9 @@ nw_status nw_linsys_coarse_sizes(nw_linsys* ls, int64_t* nc, int64_t* nnzc);
 nw_status nw_linsys_coarse_graph(nw_linsys* ls, int32_t* agg, int64_t* cptr,
                                  int32_t* ccol, float* wgt, float* dinv);
 /* Harvest (residual, error) pairs from the handle's assembled system:
- * x* from a tight (1e-11, at most 5,000 iterations) mixed-precision SGS
- * solve, or FP64 SGS-GMRES when FP32 refinement cannot converge, then
+ * x* from a tight (1e-11) FP64 CG + SGS solve (at most 20,000 iterations),
+ * or, when that stops above 1e-9, the better of it and SGS-GMRES(50)
+ * (mixed precision, then FP64; at most 5,000 iterations each), then
  * `restarts` cycles of plain FP64 Jacobi-GMRES(kspace) from x0 = 0, one
  * pair per restart while the restart's residual is at least 100 times
  * that of x* (the error target is then accurate to 1 %); NW_NOT_CONVERGED
@@ -436,7 +437,10 @@ nw_status nw_learned_forward(nw_learned* net, nw_linsys* ls, const float* rc,
  *         b_bf16[m x 64]; kind 3: kind 0 on the tcgen05 tensor cores (TMEM
  *         accumulator), NW_TIMEOUT if one of its bounded waits gave up;
  *         kind 4: kind 3 with the tiles loaded by TMA (cp.async.bulk.tensor,
- *         128-byte swizzle). */
+ *         128-byte swizzle); kind 5: kind 1 on the tcgen05 tensor cores
+ *         (TMA tiles); kind 6: kind 2 on the tcgen05 tensor cores (node
+ *         chunks transposed while staged). The training step uses kinds 4,
+ *         5 and 6. */
 nw_status nw_gemm_bf16(int kind, int64_t m, const void* a, const void* b,
                        void* out);
 

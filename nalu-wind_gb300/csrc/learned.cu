@@ -616,6 +616,12 @@ void launch_gemm_wgrad(const uint16_t* xc, const uint16_t* dz, float* partial,
   gemm_wgrad_k<<<nb, 256, 0, s>>>(xc, dz, partial, m);
   colsum_k<<<gridn(128 * 64), kB, 0, s>>>(nb, 128 * 64, partial, dw, 1);
 }
+void launch_gemm_wgrad_tc(const uint16_t* xc, const uint16_t* dz, float* partial,
+                          float* dw, int64_t m, cudaStream_t s) {
+  const int nb = wgrad_blocks(m);
+  launch_wgrad_partials_tc(xc, dz, partial, m, nb, s);
+  colsum_k<<<gridn(128 * 64), kB, 0, s>>>(nb, 128 * 64, partial, dw, 1);
+}
 
 void launch_restrict(const CoarseLevel& cl, const float* r, float* rc, cudaStream_t s) {
   restrict_k<<<gridn(cl.nc * 32), kB, 0, s>>>(cl.nc, cl.mptr.p, cl.mrows.p, r, rc);
@@ -910,9 +916,9 @@ double LearnedNet::forward_backward(const CoarseLevel& cl, const float* wgt,
   uint16_t* xcs[3] = {work.xc1.p, work.xc2.p, work.xc3.p};
   for (int l = 2; l >= 0; --l) {
     // dW_l += X_l^T dZ_l ; dX_l = dZ_l W_l^T
-    launch_gemm_wgrad(xcs[l], work.dz.p, wpartial.p, grads.p + kOffW1 + size_t(l) * kIn2 * kHid,
-                      nc, s);
-    launch_gemm_dx(work.dz.p, wbf.p + size_t(l) * kIn2 * kHid, work.dxc.p, nc, s);
+    launch_gemm_wgrad_tc(xcs[l], work.dz.p, wpartial.p, grads.p + kOffW1 + size_t(l) * kIn2 * kHid,
+                         nc, s);
+    launch_gemm_dx_tma(work.dz.p, wbf.p + size_t(l) * kIn2 * kHid, work.dxc.p, nc, s);
     agg_bwd_k<<<gw, kB, 0, s>>>(nc, cl.cptr.p, cl.ccol.p, cl.cdiag.p, cl.rev.p, wgt, work.dxc.p,
                                 work.dh.p);
     if (l > 0) mask_k<<<nb64, kB, 0, s>>>(nc, work.dh.p, xcs[l], 128, work.dz.p);

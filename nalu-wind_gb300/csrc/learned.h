@@ -137,6 +137,16 @@ void launch_gemm_dx(const uint16_t* dz, const uint16_t* w, float* dx, int64_t m,
                     cudaStream_t s);
 void launch_gemm_wgrad(const uint16_t* xc, const uint16_t* dz, float* partial,
                        float* dw, int64_t m, cudaStream_t s);
+// The backward GEMMs on the tcgen05 tensor cores (tc_gemm.cu): dX = dZ W^T
+// with TMA-loaded tiles, and the dW partials (one 128 x 64 block per CTA,
+// `blocks` CTAs over 64-node chunks); launch_gemm_wgrad_tc adds the fixed-
+// order column sum into dw. Timeouts go to tc_status.
+void launch_gemm_dx_tma(const uint16_t* dz, const uint16_t* w, float* dx, int64_t m,
+                        cudaStream_t s);
+void launch_wgrad_partials_tc(const uint16_t* xc, const uint16_t* dz, float* partial, int64_t m,
+                              int blocks, cudaStream_t s);
+void launch_gemm_wgrad_tc(const uint16_t* xc, const uint16_t* dz, float* partial,
+                          float* dw, int64_t m, cudaStream_t s);
 
 // Two-level application helpers (FP32).
 void launch_restrict(const CoarseLevel& cl, const float* r, float* rc, cudaStream_t s);

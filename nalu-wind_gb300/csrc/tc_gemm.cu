@@ -415,6 +415,289 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Backward layer GEMMs of the training step on the tcgen05 tensor cores.
+//
+// dX = dZ W^T: dx[r, 0:128] (FP32) = dz[r, 0:64] . w[0:128, 0:64]^T. Both
+// operands are K-major (K = 64 output channels, 128 bytes per row: one
+// swizzle-128B atom wide), loaded by TMA; M 128, N 128, four K16 steps into
+// a 128-column TMEM accumulator; persistent CTAs over 128-row tiles with
+// the next dz tile streaming into the other buffer.
+constexpr int kDxN = 128;
+constexpr int kDxPanel = kTileM * 128;      // 16 KiB: 128 rows x 64 BF16
+constexpr int kSmemDx = 3 * kDxPanel + 1024 + 64;
+constexpr uint32_t kIdescDx = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kDxN >> 3) << 17) |
+                              (uint32_t(kTileM >> 4) << 24);
+
+// 32 columns of this warp's 32 TMEM lanes as FP32
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* f) {
+  uint32_t v[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+        "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+        "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+        "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+        "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) f[i] = __uint_as_float(v[i]);
+}
+
+__global__ void __launch_bounds__(128)
+    gemm_dx_tma_k(const __grid_constant__ CUtensorMap map_dz, const __grid_constant__ CUtensorMap map_w,
+                  float* __restrict__ dx, int64_t m) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint8_t* sW = base;                   // w (128 x 64)
+  uint8_t* sA = base + kDxPanel;        // 2 buffers of dz tiles
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sA + 2 * kDxPanel);  // full[2], w, mma
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t ntiles = (m + kTileM - 1) / kTileM;
+  const uint32_t w0 = smem_u32(sW), a0 = smem_u32(sA);
+  const uint32_t full0 = smem_u32(bars), wbar = smem_u32(bars + 2), mbar = smem_u32(bars + 3);
+  if (tid == 0) {
+    for (int i = 0; i < 4; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bars + i)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    expect_tx(wbar, kDxPanel);
+    tma_load_2d(w0, &map_w, 0, 0, wbar);
+    if (blockIdx.x < ntiles) {
+      expect_tx(full0, kDxPanel);
+      tma_load_2d(a0, &map_dz, 0, int(int64_t(blockIdx.x) * kTileM), full0);
+    }
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(uint32_t(kDxN))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  bool ok = mbar_wait(wbar, 0);
+  int it = 0;
+  for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++it) {
+    const int bsel = it & 1;
+    const uint32_t abuf = a0 + uint32_t(bsel) * kDxPanel;
+    const int64_t tn = t + gridDim.x;
+    if (tid == 0 && tn < ntiles) {
+      // the other buffer was read by the previous tile's MMAs, which completed
+      const uint32_t fb = full0 + uint32_t(1 - bsel) * 8;
+      expect_tx(fb, kDxPanel);
+      tma_load_2d(a0 + uint32_t(1 - bsel) * kDxPanel, &map_dz, 0, int(tn * kTileM), fb);
+    }
+    ok = mbar_wait(full0 + uint32_t(bsel) * 8, uint32_t((it >> 1) & 1));
+    if (!__syncthreads_and(ok)) break;
+    if (tid == 0) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {  // 32-byte K16 steps inside the swizzle atom
+        const uint64_t da = smem_desc_sw128(abuf + uint32_t(k) * 32);
+        const uint64_t db = smem_desc_sw128(w0 + uint32_t(k) * 32);
+        const uint32_t acc = k > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(kIdescDx), "r"(acc)
+            : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+          : "memory");
+    }
+    ok = mbar_wait(mbar, uint32_t(it & 1));
+    if (!ok) {
+      atomicExch(&g_tc_status, 1);
+      ok = mbar_wait(mbar, uint32_t(it & 1));
+    }
+    if (!__syncthreads_and(ok)) break;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int64_t r = t * kTileM + warp * 32 + lane;
+    const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16);
+#pragma unroll
+    for (int h = 0; h < kDxN / 32; ++h) {
+      float f[32];
+      tmem_ld32(taddr + uint32_t(32 * h), f);
+      if (r < m) {
+        float4* dst = reinterpret_cast<float4*>(dx + r * kDxN + 32 * h);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) dst[c] = make_float4(f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (!ok) atomicExch(&g_tc_status, 1);
+  if (tid == 0 && !ok) {
+    mbar_wait(full0, uint32_t(((it + 1) >> 1) & 1));
+    mbar_wait(full0 + 8, uint32_t((it >> 1) & 1));
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(uint32_t(kDxN))
+                 : "memory");
+  }
+}
+
+// dW partials: partial[block][c][o] = sum over this block's nodes of
+// x[node][c] dz[node][o] (c < 128, o < 64). The reduction runs over nodes,
+// which both operands store as rows, so each 64-node chunk is transposed
+// while it is staged: x^T (128 x 64) and dz^T (64 x 64) in the no-swizzle
+// K-major canonical layout (8-row x 16-byte core matrices, K-adjacent cores
+// 128 bytes apart, 8-row groups 1024 bytes apart), built from pairs of
+// node rows so that each shared store is one 32-bit word. Four K16 MMAs (M
+// 128, N 64) per chunk accumulate in TMEM over the block's chunks (grid
+// stride); one commit-and-wait per chunk frees the staging buffer.
+constexpr int kWgChunk = 64;
+constexpr int kWgSbo = (kWgChunk / 8) * 128;  // 1024
+constexpr int kWgABytes = 128 * kWgChunk * 2;  // 16 KiB
+constexpr int kWgBBytes = 64 * kWgChunk * 2;   // 8 KiB
+constexpr int kSmemWg = kWgABytes + kWgBBytes + 128 + 64;
+
+// word offset of the element pair (row, k), (row, k + 1) in a canonical tile
+__device__ __forceinline__ uint32_t wg_off(int row, int k) {
+  return uint32_t((row >> 3) * kWgSbo + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+__global__ void __launch_bounds__(128)
+    gemm_wgrad_tc_k(const uint16_t* __restrict__ xc, const uint16_t* __restrict__ dz,
+                    float* __restrict__ partial, int64_t m) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
+                                             ~uintptr_t(127));
+  uint8_t* sA = base;
+  uint8_t* sB = base + kWgABytes;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sB + kWgBBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB), bar = smem_u32(mbar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  bool ok = true, any = false;
+  int it = 0;
+  // thread -> k pair (lane: nodes 2 kp, 2 kp + 1) and column groups of 8
+  const int kp = lane;
+  for (int64_t c0 = int64_t(blockIdx.x) * kWgChunk; ok && c0 < m;
+       c0 += int64_t(gridDim.x) * kWgChunk, ++it) {
+    const int64_t n0 = c0 + 2 * kp, n1 = n0 + 1;
+    // x: 16 groups of 8 columns, 4 per warp
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int cg = warp + 4 * i;
+      uint4 u0 = make_uint4(0, 0, 0, 0), u1 = u0;
+      if (n0 < m) u0 = *reinterpret_cast<const uint4*>(xc + n0 * 128 + cg * 8);
+      if (n1 < m) u1 = *reinterpret_cast<const uint4*>(xc + n1 * 128 + cg * 8);
+      const uint32_t w0[4] = {u0.x, u0.y, u0.z, u0.w}, w1[4] = {u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        // columns 8 cg + 2 j (low halves) and 8 cg + 2 j + 1 (high halves)
+        const uint32_t lo = (w0[j] & 0xffffu) | (w1[j] << 16);
+        const uint32_t hi = (w0[j] >> 16) | (w1[j] & 0xffff0000u);
+        const int c = 8 * cg + 2 * j;
+        asm volatile("st.shared.b32 [%0], %1;" ::"r"(a0 + wg_off(c, 2 * kp)), "r"(lo) : "memory");
+        asm volatile("st.shared.b32 [%0], %1;" ::"r"(a0 + wg_off(c + 1, 2 * kp)), "r"(hi) : "memory");
+      }
+    }
+    // dz: 8 groups of 8 columns, 2 per warp
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int cg = warp + 4 * i;
+      uint4 u0 = make_uint4(0, 0, 0, 0), u1 = u0;
+      if (n0 < m) u0 = *reinterpret_cast<const uint4*>(dz + n0 * 64 + cg * 8);
+      if (n1 < m) u1 = *reinterpret_cast<const uint4*>(dz + n1 * 64 + cg * 8);
+      const uint32_t w0[4] = {u0.x, u0.y, u0.z, u0.w}, w1[4] = {u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t lo = (w0[j] & 0xffffu) | (w1[j] << 16);
+        const uint32_t hi = (w0[j] >> 16) | (w1[j] & 0xffff0000u);
+        const int c = 8 * cg + 2 * j;
+        asm volatile("st.shared.b32 [%0], %1;" ::"r"(b0 + wg_off(c, 2 * kp)), "r"(lo) : "memory");
+        asm volatile("st.shared.b32 [%0], %1;" ::"r"(b0 + wg_off(c + 1, 2 * kp)), "r"(hi) : "memory");
+      }
+    }
+    // the stores become visible to the tensor cores (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+      for (int k = 0; k < kWgChunk / 16; ++k) {
+        const uint64_t da = smem_desc(a0 + uint32_t(k) * 256, 128, kWgSbo);
+        const uint64_t db = smem_desc(b0 + uint32_t(k) * 256, 128, kWgSbo);
+        const uint32_t acc = (it > 0 || k > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+          : "memory");
+    }
+    // the staging buffer is reused by the next chunk once the MMAs read it
+    ok = mbar_wait(bar, uint32_t(it & 1));
+    if (!ok) {
+      atomicExch(&g_tc_status, 1);
+      ok = mbar_wait(bar, uint32_t(it & 1));
+    }
+    ok = __syncthreads_and(ok) != 0;
+    any = true;
+  }
+  if (!ok) atomicExch(&g_tc_status, 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // rows of D are input channels c (TMEM lanes), columns output channels
+  float* out = partial + int64_t(blockIdx.x) * (128 * 64) + int64_t(warp * 32 + lane) * 64;
+  const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float f[32];
+    tmem_ld32(taddr + uint32_t(32 * h), f);
+    float4* dst = reinterpret_cast<float4*>(out + 32 * h);
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      dst[c] = (any && ok) ? make_float4(f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3])
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
 }  // namespace
 
 void launch_gemm_fwd_tc(const uint16_t* a, const uint16_t* wt, uint16_t* out, int64_t m,
@@ -456,11 +739,11 @@ static EncodeTiledFn encode_fn() {
   }
   return fn;
 }
-// rows x 128 BF16 (row stride 256 bytes), boxes of 128 bytes x box_rows
-static CUtensorMap make_map(const uint16_t* base, int64_t rows, uint32_t box_rows) {
+// rows x cols BF16 (row stride 2 cols bytes), boxes of 128 bytes x box_rows
+static CUtensorMap make_map(const uint16_t* base, int64_t rows, uint32_t box_rows, int cols = kK) {
   CUtensorMap map;
-  const cuuint64_t dims[2] = {cuuint64_t(kK), cuuint64_t(rows)};
-  const cuuint64_t strides[1] = {cuuint64_t(kK) * 2};
+  const cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
+  const cuuint64_t strides[1] = {cuuint64_t(cols) * 2};
   const cuuint32_t box[2] = {64, box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
@@ -495,6 +778,42 @@ void launch_gemm_fwd_tma(const uint16_t* a, const uint16_t* wt, uint16_t* out, i
   const int64_t tiles = (m + kTileM - 1) / kTileM;
   const unsigned grid = unsigned(tiles < ctas ? tiles : ctas);
   gemm_fwd_tma_k<<<grid, 128, kSmemTma, s>>>(ma, mw, out, m, ldo);
+  NW_CUDA(cudaGetLastError());
+}
+
+void launch_gemm_dx_tma(const uint16_t* dz, const uint16_t* w, float* dx, int64_t m,
+                        cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    NW_CUDA(cudaFuncSetAttribute(gemm_dx_tma_k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemDx));
+    attr = true;
+  }
+  static int ctas = 0;
+  if (!ctas) {
+    int dev = 0, sms = 0;
+    NW_CUDA(cudaGetDevice(&dev));
+    NW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    ctas = 2 * sms;
+  }
+  if (m <= 0) return;
+  if ((reinterpret_cast<uintptr_t>(dz) | reinterpret_cast<uintptr_t>(w) |
+       reinterpret_cast<uintptr_t>(dx)) & 15u)
+    fail(NW_INVALID_ARG, "TMA operands must be 16-byte aligned");
+  const CUtensorMap mz = make_map(dz, m, kTileM, 64);
+  const CUtensorMap mw = make_map(w, kDxN, kDxN, 64);
+  const int64_t tiles = (m + kTileM - 1) / kTileM;
+  const unsigned grid = unsigned(tiles < ctas ? tiles : ctas);
+  gemm_dx_tma_k<<<grid, 128, kSmemDx, s>>>(mz, mw, dx, m);
+  NW_CUDA(cudaGetLastError());
+}
+
+void launch_wgrad_partials_tc(const uint16_t* xc, const uint16_t* dz, float* partial, int64_t m,
+                              int blocks, cudaStream_t s) {
+  if (blocks <= 0) return;
+  if ((reinterpret_cast<uintptr_t>(xc) | reinterpret_cast<uintptr_t>(dz) |
+       reinterpret_cast<uintptr_t>(partial)) & 15u)
+    fail(NW_INVALID_ARG, "GEMM operands must be 16-byte aligned");
+  gemm_wgrad_tc_k<<<blocks, 128, kSmemWg, s>>>(xc, dz, partial, m);
   NW_CUDA(cudaGetLastError());
 }
 

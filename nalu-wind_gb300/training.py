@@ -42,6 +42,7 @@ def train_poisson_network(shape=(64, 64, 48), systems=16, restarts=40, kspace=30
     t2 = time.perf_counter()
     net.clear_data()
     info = {"systems": systems, "shape": list(shape), "tets": bool(tets), "pairs": pairs, "epochs": epochs,
+            "updates": epochs * ((pairs + batch - 1) // batch),
             "harvest_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
             "loss_before": round(before, 5), "loss_after": round(after, 5)}
     return net, info

@@ -76,6 +76,36 @@ def test_tcgen05_forward_gemm_matches_torch_and_mma_sync(nw, m, kind):
     assert bool((d <= 2.0 ** -7 * out0.float().abs() + 1e-5 * scale).all())
 
 
+@pytest.mark.parametrize("m", [1, 37, 128, 129, 5003, 65553])
+def test_tcgen05_backward_gemms_match_torch_and_mma_sync(nw, m):
+    """The training step's backward GEMMs on the tcgen05 tensor cores: dX =
+    dZ W^T with TMA tiles (kind 5) and dW = X^T dZ with the node chunks
+    transposed while staged (kind 6), FP32 outputs within 1e-5 of the sum of
+    |products| of torch's FP32 product of the same BF16 operands, and of the
+    mma.sync kernels (kinds 1, 2) they replaced."""
+    import torch
+    rng = np.random.default_rng(300 + m)
+    x = _bf16_tensor(rng.normal(size=(m, 128)))
+    dz = _bf16_tensor(rng.normal(size=(m, 64)))
+    w = _bf16_tensor(rng.normal(size=(128, 64)) * 0.1)
+    dx = torch.full((m, 128), 7.0, dtype=torch.float32, device="cuda")
+    nw.gemm_bf16(5, m, dz, w, dx)
+    ref = dz.float() @ w.float().T
+    scale = dz.float().abs() @ w.float().abs().T
+    assert bool(((dx - ref).abs() <= 1e-5 * scale + 1e-30).all())
+    dx1 = torch.empty_like(dx)
+    nw.gemm_bf16(1, m, dz, w, dx1)
+    assert bool(((dx - dx1).abs() <= 2e-5 * scale + 1e-30).all())
+    dw = torch.full((128, 64), 7.0, dtype=torch.float32, device="cuda")
+    nw.gemm_bf16(6, m, x, dz, dw)
+    ref = x.float().T @ dz.float()
+    scale = x.float().abs().T @ dz.float().abs()
+    assert bool(((dw - ref).abs() <= 1e-5 * scale + 1e-30).all())
+    dw1 = torch.empty_like(dw)
+    nw.gemm_bf16(2, m, x, dz, dw1)
+    assert bool(((dw - dw1).abs() <= 2e-5 * scale + 1e-30).all())
+
+
 def _poisson(nw, shape, seed=3, stretch=1.04, jitter=0.0, rhs_seed=None):
     return nw.workload.poisson_system(shape, seed=seed, stretch=stretch, jitter=jitter, rhs_seed=rhs_seed)
 
