@@ -398,8 +398,9 @@ def run_ours(args, rank, world):
         out["poisson"] = poisson_solves(nw, stream, args)
         poisson_csr = out["poisson"].pop("_csr", None)
         net = out["poisson"].pop("_net")
+        net_run = out["poisson"].pop("_net_run")
         if args.heldout > 0:
-            out["poisson_heldout_128"] = heldout_poisson(nw, stream, args, net)
+            out["poisson_heldout_128"] = heldout_poisson(nw, stream, args, net, net_run)
     if not args.no_step:
         out["implicit_step_tets"] = implicit_step(nw, stream, args)
     if rank == 0 and not args.no_cpu_baseline:
@@ -441,8 +442,10 @@ def poisson_solves(nw, stream, args) -> dict:
     """Pressure Poisson to 1e-8 FP64 relative residual on the 256 x 256 x 128
     stretched box: plain FP64 GMRES(50) + Jacobi against the mixed-precision
     solvers, the headline being learned-preconditioned mixed FGMRES(30).
-    The network is trained first (untimed) on a family of 64 x 64 x 48
-    systems with other seeds. Every solve starts from x = 0. Errors are
+    The network is the one of the 128^3-node training set (weights file
+    made by nalu-wind_gb300/train_poisson.py); a second network is trained
+    in the run (untimed) on a family of 64 x 64 x 48 systems with other
+    seeds, and both are reported. Every solve starts from x = 0. Errors are
     measured against an FP64 reference solution (FP64 GMRES(50) + SGS to
     1e-11; zero-mean parts: the system is singular, its null space the
     constants). The mixed SGS solver is also run to 1e-10, the refinement
@@ -454,10 +457,28 @@ def poisson_solves(nw, stream, args) -> dict:
            "rows": nr, "nnz": nnz, "tol": 1e-8,
            "mixed_precision": "FP64 outer residual / refinement; FP32 inner Krylov, SpMV and network "
                               "coarse step; BF16 Gauss-Seidel matrix values with FP32 accumulation"}
-    net, info = nw.training.train_poisson_network(epochs=args.train_epochs, lr=args.train_lr,
-                                                  stream=stream.cuda_stream)
-    res["training"] = info
+    # the networks are only needed when a learned variant runs
+    need_net = (not args.poisson_variants or args.heldout > 0
+                or any("learned" in v or "two_level" in v for v in args.poisson_variants.split(",")))
+    if not need_net:
+        net_run, info = None, None
+    else:
+        net_run, info = nw.training.train_poisson_network(epochs=args.train_epochs, lr=args.train_lr,
+                                                          stream=stream.cuda_stream)
+    res["training_in_run"] = info
+    # the network of the 128^3-node training set (nalu-wind_gb300/
+    # train_poisson.py), trained once and loaded here; without its weights
+    # file the in-run network takes its place
+    net = net_run
+    wpath = Path(args.weights) if args.weights else None
+    if need_net and wpath is not None and wpath.exists():
+        net, recipe = nw.training.load_poisson_network(wpath)
+        res["training"] = dict(recipe, weights=str(wpath.relative_to(ROOT) if wpath.is_relative_to(ROOT)
+                                                   else wpath))
+    elif need_net:
+        res["training"] = dict(info, weights=None)
     res["_net"] = net
+    res["_net_run"] = net_run if net is not net_run else None
     controls = learned_controls(nw)
     maxit = args.poisson_maxit
     variants = [
@@ -474,6 +495,11 @@ def poisson_solves(nw, stream, args) -> dict:
          nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=maxit, tolerance=1e-8,
                        precision=nw.PREC_MIXED_BF16, inner_kspace=30, preconditioner=nw.PC_LEARNED)),
     ]
+    if net is not net_run:
+        variants.append(("learned_mixed_fgmres30_in_run_network", net_run,
+                         nw.solver_cfg(method=nw.FGMRES, kspace=30, max_iterations=maxit, tolerance=1e-8,
+                                       precision=nw.PREC_MIXED_BF16, inner_kspace=30,
+                                       preconditioner=nw.PC_LEARNED)))
     variants.append(("mixed_gmres50_sgs_to_1e-10", None,
                      nw.solver_cfg(kspace=50, max_iterations=maxit, tolerance=1e-10,
                                    precision=nw.PREC_MIXED_BF16, inner_kspace=50, inner_tolerance=1e-4,
@@ -551,7 +577,7 @@ def learned_controls(nw) -> dict:
             "no_coarse_correction": none}
 
 
-def heldout_poisson(nw, stream, args, net) -> dict:
+def heldout_poisson(nw, stream, args, net, net_run=None) -> dict:
     """The learned preconditioner on held-out seeds of the training family's
     distribution at 128^3 nodes (127^3 hexes; stretch ratio from U[1.0, 1.15],
     interior jitter from U[0, 10 %], seeds 1000 + k): learned mixed FGMRES(30)
@@ -572,6 +598,8 @@ def heldout_poisson(nw, stream, args, net) -> dict:
         runs = [("plain_fp64_gmres30_jacobi", None, nw.solver_cfg(kspace=30, max_iterations=args.poisson_maxit,
                                                                    tolerance=1e-8)),
                 ("learned_mixed_fgmres30", net, lcfg)]
+        if net_run is not None:
+            runs.append(("learned_mixed_fgmres30_in_run_network", net_run, lcfg))
         runs += [(f"mixed_fgmres30_two_level_{c}", cn, lcfg) for c, cn in controls.items()
                  if c in ("untrained_network", "jacobi_coarse_direction")]
         for name, lnet, cfg in runs:
@@ -847,6 +875,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--train-epochs", type=int, default=100, help="training epochs of the Poisson network")
     ap.add_argument("--train-lr", type=float, default=1e-3, help="Adam learning rate of the Poisson network")
+    ap.add_argument("--weights", default=str(PKG / "weights" / "poisson_128cube.nwl"),
+                    help="weights of the 128^3-node recipe (train_poisson.py); '' trains in the run only")
     args = ap.parse_args()
     args.shape = tuple(args.shape)
     args.poisson_shape = tuple(args.poisson_shape)

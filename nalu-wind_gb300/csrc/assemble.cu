@@ -236,18 +236,21 @@ __global__ void __launch_bounds__(kThreads)
     av[d] = ldd(area + 3 * e + d);
     dx[d] = dd_from_double(coords[3 * R + d] - coords[3 * L + d]);
   }
-  const dd asq = av[0] * av[0] + av[1] * av[1] + av[2] * av[2];
-  const dd axdx = av[0] * dx[0] + av[1] * dx[1] + av[2] * dx[2];
+  const dd asq = dd_dot3(av[0], av[0], av[1], av[1], av[2], av[2]);
+  const dd axdx = dd_dot3(av[0], dx[0], av[1], dx[1], av[2], dx[2]);
   const dd w = asq * dd_rcp(axdx);
   const dd projTimeScale = scale2(nl[0] + nr[0], 0.5f);
-  dd flux = {0.f, 0.f}, corr = {0.f, 0.f};
+  dd mg[3], g[3], c[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const dd m = nl[1 + d] + nr[1 + d];
-    const dd g = nl[4 + d] + nr[4 + d];
-    flux = (m + g) * av[d] + flux;
-    corr = (av[d] - w * dx[d]) * g + corr;
+    g[d] = nl[4 + d] + nr[4 + d];
+    mg[d] = (nl[1 + d] + nr[1 + d]) + g[d];
+    c[d] = av[d] - w * dx[d];
   }
+  // sum (rho u + G p / A_p) . A and the non-orthogonal correction
+  // sum (A - w dx) . (G p / A_p), as three-term dots
+  const dd flux = dd_dot3(mg[0], av[0], mg[1], av[1], mg[2], av[2]);
+  const dd corr = dd_dot3(c[0], g[0], c[1], g[1], c[2], g[2]);
   dd tmdot = -(projTimeScale * dd_from_double(pressure[R] - pressure[L]) * w);
   tmdot = (tmdot + scale2(flux - noc * corr, 0.5f)) * inv_tau;
   const dd f = -(w * projTimeScale * inv_tau);

@@ -42,7 +42,23 @@ def train_poisson_network(shape=(64, 64, 48), systems=16, restarts=40, kspace=30
     t2 = time.perf_counter()
     net.clear_data()
     info = {"systems": systems, "shape": list(shape), "tets": bool(tets), "pairs": pairs, "epochs": epochs,
-            "updates": epochs * ((pairs + batch - 1) // batch),
+            "updates": epochs * ((pairs + batch - 1) // batch), "agg_passes": agg_passes, "smoother": smoother,
             "harvest_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
             "loss_before": round(before, 5), "loss_after": round(after, 5)}
+    return net, info
+
+
+def load_poisson_network(path, seed=0):
+    """A network saved by train_poisson.py: the weights (checksummed) and
+    the application settings of its recipe from the .json beside them.
+    Returns (network, recipe)."""
+    import json
+    from pathlib import Path
+
+    path = Path(path)
+    info = json.loads(path.with_suffix(".json").read_text())
+    net = Learned(seed=seed)
+    net.configure(post_smooth=True, agg_passes=int(info.get("agg_passes", 2)),
+                  smoother=int(info.get("smoother", 0)))
+    net.load(path)
     return net, info
