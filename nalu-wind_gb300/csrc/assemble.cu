@@ -624,7 +624,10 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
     const bool acc = a.accumulate && !staged;
     if (s != t) {
       const int dp = a.diag_pos[r];
-      dd sother{}, sd{}, s1{}, s2{}, rr{}, od{}, o1{}, o2{};
+      // sums over the incident edges: the diagonal entry's N_qq + c_other,
+      // the two off-diagonal N sums and the rhs (deferred renormalisation)
+      dd_acc sdg, s1, s2, rr;
+      dd od{}, o1{}, o2{};
       int slot = -1;
       auto put3 = [&](int k, dd xd, dd x1, dd x2) {
         const double d0 = dd_to_double_int(xd), d1 = dd_to_double_int(x1),
@@ -642,7 +645,7 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
         const dd co = side ? c1v : c0, other = side ? c0 : c1v;
         const dd nd = ldc<NC>(pd + e), n1 = ldc<NC>(p1 + e), n2 = ldc<NC>(p2 + e);
         const dd f = ldc<NC>(pf + e);
-        rr = rr + (side ? f : -f);
+        acc_add(rr, side ? f : -f);
         const dd bd = nd + co;
         if (!dup) {
           if (slot >= 0) put3(3 * (slot < dp ? slot : slot + 1), od, o1, o2);
@@ -655,16 +658,16 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
           o1 = o1 + n1;
           o2 = o2 + n2;
         }
-        sother = sother + other;
-        sd = sd + nd;
-        s1 = s1 + n1;
-        s2 = s2 + n2;
+        acc_add(sdg, nd);
+        acc_add(sdg, other);
+        acc_add(s1, n1);
+        acc_add(s2, n2);
       }
       put3(3 * (slot < dp ? slot : slot + 1), od, o1, o2);
       // diagonal block row q: -(sum(other) e_q + sum(N)_q) / relax
-      const dd dgc = -(sother * a.irelax);
-      put3(3 * dp, -(sd * a.irelax) + dgc, -(s1 * a.irelax), -(s2 * a.irelax));
-      const double d = dd_to_double_int(rr);
+      put3(3 * dp, -(acc_value(sdg) * a.irelax), -(acc_value(s1) * a.irelax),
+           -(acc_value(s2) * a.irelax));
+      const double d = dd_to_double_int(acc_value(rr));
       a.rhs[3 * r + q] = a.accumulate ? a.rhs[3 * r + q] + d : d;
     } else if (!acc) {
       for (int64_t k = 0; k < a.row_ptr[3 * r + q + 1] - bq; ++k) v[k] = 0.0;

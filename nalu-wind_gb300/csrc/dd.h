@@ -243,6 +243,21 @@ NW_HD dd scale2(dd a, float p2) { return {fmul(a.hi, p2), fmul(a.lo, p2)}; }
 
 NW_HD dd dd_fma(dd a, dd b, dd c) { return a * b + c; }
 
+// A running sum of float pairs with the renormalisation deferred to the
+// end: s is the two-sum head, c the float sum of the heads' rounding errors
+// and of the low parts (8 operations per term against 11 for the pair
+// addition). After k terms the error is within about k^2 u^2 of the sum of
+// |terms| (u = 2^-24), which the host test checks against long double.
+struct dd_acc {
+  float s = 0.0f, c = 0.0f;
+};
+NW_HD void acc_add(dd_acc& a, dd x) {
+  const dd t = two_sum(a.s, x.hi);
+  a.s = t.hi;
+  a.c = fadd(a.c, fadd(t.lo, x.lo));
+}
+NW_HD dd acc_value(const dd_acc& a) { return fast_two_sum(a.s, a.c); }
+
 // a0 b0 + a1 b1 + a2 b2: the three FMA two-products (head + error), the
 // heads added with two error-free sums, every error term added in float,
 // one final renormalisation. 31 float operations against 43 for three

@@ -47,4 +47,16 @@ void dd_binop(int op, int64_t n, const float* ah, const float* al, const float* 
   }
 }
 
+// sums of k consecutive pairs with the deferred-renormalisation
+// accumulator (dd_acc), one result per group
+void dd_accsum(int64_t groups, int k, const float* hi, const float* lo, float* rh, float* rl) {
+  for (int64_t g = 0; g < groups; ++g) {
+    nw::dd_acc a;
+    for (int j = 0; j < k; ++j) nw::acc_add(a, dd{hi[g * k + j], lo[g * k + j]});
+    const dd r = nw::acc_value(a);
+    rh[g] = r.hi;
+    rl[g] = r.lo;
+  }
+}
+
 }  // extern "C"

@@ -170,3 +170,26 @@ def test_integer_widening_rounds_like_the_fp64_add(lib):
         assert o == r, (h, l, o, r)
         exact = Fraction(h) + Fraction(l)
         assert abs(Fraction(o) - exact) <= Fraction(np.spacing(abs(r))) / 2
+
+
+@pytest.mark.parametrize("k", [2, 7, 30])
+def test_deferred_accumulator_bound(lib, k):
+    """dd_acc (the row kernels' running sums): the sum of k pairs within
+    k^2 u^2 of the sum of |terms|, with mixed signs and heavy cancellation."""
+    rng = np.random.default_rng(11 + k)
+    groups = 4000
+    x = rng.normal(size=groups * k) * 10.0 ** rng.uniform(-3, 3, groups * k)
+    x[: groups * k // 2] *= rng.choice([-1.0, 1.0], groups * k // 2)
+    # every fifth group: terms that cancel to a small remainder
+    for g in range(0, groups, 5):
+        seg = x[g * k:(g + 1) * k]
+        seg[-1] = -np.sum(seg[:-1]) * (1 + 1e-9)
+    hi, lo = _split(lib, x)
+    rh, rl = np.zeros(groups, np.float32), np.zeros(groups, np.float32)
+    lib.dd_accsum(C.c_int64(groups), C.c_int(k), _p(hi, C.c_float), _p(lo, C.c_float),
+                  _p(rh, C.c_float), _p(rl, C.c_float))
+    terms = hi.astype(np.longdouble) + lo.astype(np.longdouble)
+    exact = terms.reshape(groups, k).sum(1)
+    mag = np.abs(terms).reshape(groups, k).sum(1)
+    got = rh.astype(np.longdouble) + rl.astype(np.longdouble)
+    assert np.all(np.abs(got - exact) <= k * k * 2.0 ** -48 * mag)
