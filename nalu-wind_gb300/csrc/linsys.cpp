@@ -1737,13 +1737,14 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
     ks.refresh(s);
     ks.ensure_f32(s);
     Precond pc = ls->pc;
-    // x*: a tight (1e-11) reference solve. The pressure-Poisson matrix is
+    // x*: a tight (1e-10) reference solve. The pressure-Poisson matrix is
     // symmetric, and on strongly stretched meshes (cell growth 1.15 over
     // 127 cells is a 4e7 ratio of the first to the last z spacing)
     // restarted GMRES(50) + SGS stalls near 5e-3 where CG + (symmetric) SGS
-    // reaches 2e-10 in ~15k iterations: CG + SGS in FP64 comes first, then
-    // mixed and FP64 SGS-GMRES(50) for systems it does not solve; the best
-    // of the attempts is kept.
+    // reaches 2e-10 in ~15k iterations: CG + SGS in FP64 comes first (at
+    // most 40,000 iterations); mixed and FP64 SGS-GMRES(50) follow only
+    // when CG fails outright (above 1e-3, or non-finite: a matrix that is
+    // not symmetric), and the best of the attempts is kept.
     DeviceArray<double> xs, x, d, r;
     xs.resize(n);
     x.resize(n);
@@ -1753,9 +1754,9 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
     nw_solver_cfg tight = ls->cfg;
     tight.precision = NW_PREC_FP64;
     tight.method = NW_CG;
-    tight.max_iterations = 20000;
-    SolveResult sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
-    if (!(sr.final_abs <= 1e-9 * sr.bnorm)) {
+    tight.max_iterations = 40000;
+    SolveResult sr = ks.solve(tight, 1e-10, pc, ls->rhs.p, xs.p, s);
+    if (!(sr.final_abs <= 1e-3 * sr.bnorm)) {
       NW_CUDA(cudaMemcpyAsync(x.p, xs.p, n * 8, cudaMemcpyDeviceToDevice, s));  // CG's iterate
       const SolveResult cg_res = sr;
       tight.method = NW_GMRES;
@@ -1764,11 +1765,11 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
       tight.inner_kspace = tight.kspace;
       tight.inner_tolerance = 1e-4;
       tight.max_iterations = 5000;
-      sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
+      sr = ks.solve(tight, 1e-10, pc, ls->rhs.p, xs.p, s);
       if (!sr.converged) {
         // FP32 inner solves cannot refine a system this ill-conditioned
         tight.precision = NW_PREC_FP64;
-        sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
+        sr = ks.solve(tight, 1e-10, pc, ls->rhs.p, xs.p, s);
       }
       if (!(sr.final_abs <= cg_res.final_abs)) {
         sr = cg_res;

@@ -14,7 +14,7 @@ import time
 
 import numpy as np
 
-from . import Learned
+from . import Learned, NwError
 from .workload import poisson_system
 
 
@@ -28,11 +28,20 @@ def train_poisson_network(shape=(64, 64, 48), systems=16, restarts=40, kspace=30
     t0 = time.perf_counter()
     first = None
     pairs = 0
+    skipped = []
     for k in range(systems):
-        ls = poisson_system(shape, seed=100 + k, stretch=float(rng.uniform(1.0, 1.15)),
-                            jitter=float(rng.uniform(0.0, 0.1)), stream=stream, tets=tets)
+        stretch, jitter = float(rng.uniform(1.0, 1.15)), float(rng.uniform(0.0, 0.1))
+        ls = poisson_system(shape, seed=100 + k, stretch=stretch, jitter=jitter, stream=stream, tets=tets)
         ls.attach_learned(net)
-        pairs = net.harvest(ls, restarts=restarts, kspace=kspace)
+        try:
+            pairs = net.harvest(ls, restarts=restarts, kspace=kspace)
+        except NwError as err:
+            # a system whose FP64 reference solve cannot get below 1e-6
+            # (the most stretched draws at 128^3 nodes) gives no pairs
+            if err.status != 5:  # NW_NOT_CONVERGED
+                raise
+            skipped.append({"seed": 100 + k, "stretch": round(stretch, 4)})
+            continue
         if first is None:
             first = ls
     t1 = time.perf_counter()
@@ -43,6 +52,7 @@ def train_poisson_network(shape=(64, 64, 48), systems=16, restarts=40, kspace=30
     net.clear_data()
     info = {"systems": systems, "shape": list(shape), "tets": bool(tets), "pairs": pairs, "epochs": epochs,
             "updates": epochs * ((pairs + batch - 1) // batch), "agg_passes": agg_passes, "smoother": smoother,
+            "systems_without_reference": skipped,
             "harvest_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3),
             "loss_before": round(before, 5), "loss_after": round(after, 5)}
     return net, info
