@@ -245,3 +245,24 @@ def test_broken_network_falls_back_to_sgs(nw):
     net.set_params(np.full(net.num_params, np.nan, np.float32))
     rep, rel = _solve(nw, ls, nw.PC_LEARNED, nw.FGMRES)
     assert rep.fallback == 1 and rep.converged == 1 and rel <= 1.01e-8
+
+
+def test_committed_128cube_network_loads_and_solves(nw):
+    """The network of the 128^3-node training set (nalu-wind_gb300/weights,
+    made by train_poisson.py: 200 systems, ~20k pairs) loads with its
+    checksum and recipe, differs from the untrained initialisation, and
+    preconditions a held-out system's mixed FGMRES to 1e-8."""
+    import torch
+    from pathlib import Path
+    path = Path(nw.__file__).parent / "weights" / "poisson_128cube.nwl"
+    net, info = nw.training.load_poisson_network(path)
+    assert info["systems"] == 200 and info["pairs"] >= 19000 and info["shape"] == [127, 127, 127]
+    assert not np.allclose(net.params(), nw.Learned(seed=0).params())
+    ls = _poisson(nw, (40, 36, 30), seed=77, stretch=1.06, jitter=0.05)
+    ls.attach_learned(net)
+    ls.set_solver_cfg(nw.solver_cfg(method=nw.FGMRES, kspace=30, inner_kspace=30, max_iterations=3000,
+                                    tolerance=1e-8, precision=nw.PREC_MIXED_BF16,
+                                    preconditioner=nw.PC_LEARNED))
+    x = torch.zeros(ls.sizes()[0], dtype=torch.float64, device="cuda")
+    rep = ls.solve(x)
+    assert rep.converged == 1 and not rep.fallback
