@@ -401,7 +401,7 @@ nw_status nw_linsys_coarse_sizes(nw_linsys* ls, int64_t* nc, int64_t* nnzc);
 nw_status nw_linsys_coarse_graph(nw_linsys* ls, int32_t* agg, int64_t* cptr,
                                  int32_t* ccol, float* wgt, float* dinv);
 /* Harvest (residual, error) pairs from the handle's assembled system:
- * x* from a tight (1e-10) FP64 CG + SGS solve (at most 40,000 iterations),
+ * x* from a tight (1e-11) FP64 CG + SGS solve (at most 40,000 iterations),
  * or, when that fails outright (above 1e-3 or non-finite), the better of it
  * and SGS-GMRES(50) (mixed precision, then FP64; at most 5,000 iterations
  * each), then

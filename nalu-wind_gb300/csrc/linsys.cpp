@@ -1737,7 +1737,7 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
     ks.refresh(s);
     ks.ensure_f32(s);
     Precond pc = ls->pc;
-    // x*: a tight (1e-10) reference solve. The pressure-Poisson matrix is
+    // x*: a tight (1e-11) reference solve. The pressure-Poisson matrix is
     // symmetric, and on strongly stretched meshes (cell growth 1.15 over
     // 127 cells is a 4e7 ratio of the first to the last z spacing)
     // restarted GMRES(50) + SGS stalls near 5e-3 where CG + (symmetric) SGS
@@ -1755,7 +1755,7 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
     tight.precision = NW_PREC_FP64;
     tight.method = NW_CG;
     tight.max_iterations = 40000;
-    SolveResult sr = ks.solve(tight, 1e-10, pc, ls->rhs.p, xs.p, s);
+    SolveResult sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
     if (!(sr.final_abs <= 1e-3 * sr.bnorm)) {
       NW_CUDA(cudaMemcpyAsync(x.p, xs.p, n * 8, cudaMemcpyDeviceToDevice, s));  // CG's iterate
       const SolveResult cg_res = sr;
@@ -1765,11 +1765,11 @@ nw_status nw_learned_harvest(nw_learned* net, nw_linsys* ls, int restarts, int k
       tight.inner_kspace = tight.kspace;
       tight.inner_tolerance = 1e-4;
       tight.max_iterations = 5000;
-      sr = ks.solve(tight, 1e-10, pc, ls->rhs.p, xs.p, s);
+      sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
       if (!sr.converged) {
         // FP32 inner solves cannot refine a system this ill-conditioned
         tight.precision = NW_PREC_FP64;
-        sr = ks.solve(tight, 1e-10, pc, ls->rhs.p, xs.p, s);
+        sr = ks.solve(tight, 1e-11, pc, ls->rhs.p, xs.p, s);
       }
       if (!(sr.final_abs <= cg_res.final_abs)) {
         sr = cg_res;
