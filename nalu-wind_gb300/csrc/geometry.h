@@ -40,20 +40,18 @@ NW_HD void hex_points(const double c[8][3], double v[27][3]) {
   }
 }
 
+// Vector area of a quadrilateral sub-control surface q0 q1 q2 q3: half the
+// cross product of its diagonals. The vector area of a closed polygon
+// depends only on its boundary, so this equals, in exact arithmetic, the
+// sum over the four triangles fanned around the face centre that
+// Quad3DSCS / HexSCS::determinant_scs evaluate (planar or not), with one
+// cross product instead of four.
 NW_HD void quad_area(const double q[4][3], double a[3]) {
-  a[0] = a[1] = a[2] = 0.0;
-  double xm[3];
-  for (int d = 0; d < 3; ++d) xm[d] = 0.25 * (q[0][d] + q[1][d] + q[2][d] + q[3][d]);
-  double r1[3] = {q[0][0] - xm[0], q[0][1] - xm[1], q[0][2] - xm[2]};
-  for (int t = 0; t < 4; ++t) {
-    const int ti = (t + 1) % 4;
-    const double r2[3] = {q[ti][0] - xm[0], q[ti][1] - xm[1], q[ti][2] - xm[2]};
-    a[0] += r1[1] * r2[2] - r2[1] * r1[2];
-    a[1] += r1[2] * r2[0] - r2[2] * r1[0];
-    a[2] += r1[0] * r2[1] - r2[0] * r1[1];
-    for (int d = 0; d < 3; ++d) r1[d] = r2[d];
-  }
-  for (int d = 0; d < 3; ++d) a[d] *= 0.5;
+  const double d1[3] = {q[2][0] - q[0][0], q[2][1] - q[0][1], q[2][2] - q[0][2]};
+  const double d2[3] = {q[3][0] - q[1][0], q[3][1] - q[1][1], q[3][2] - q[1][2]};
+  a[0] = 0.5 * (d1[1] * d2[2] - d1[2] * d2[1]);
+  a[1] = 0.5 * (d1[2] * d2[0] - d1[0] * d2[2]);
+  a[2] = 0.5 * (d1[0] * d2[1] - d1[1] * d2[0]);
 }
 
 NW_HD double grandy(const double s[8][3]) {
@@ -143,16 +141,23 @@ NW_HD void tet_geometry(const double c[4][3], double scs[6][3], double scv[4]) {
       for (int d = 0; d < 3; ++d) q[k][d] = p[facet[ip][k]][d];
     quad_area(q, scs[ip]);
   }
-  const int sub[4][8] = {{0, 4, 7, 6, 11, 13, 14, 12},
-                                {1, 5, 7, 4, 9, 10, 14, 13},
-                                {2, 6, 7, 5, 8, 12, 14, 10},
-                                {3, 9, 13, 11, 8, 10, 14, 12}};
-  for (int ip = 0; ip < 4; ++ip) {
-    double s[8][3];
-    for (int n = 0; n < 8; ++n)
-      for (int d = 0; d < 3; ++d) s[n][d] = p[sub[ip][n]][d];
-    scv[ip] = grandy(s);
+  // The four sub-control volumes of a linear tet (node, three edge
+  // midpoints, three face centroids, centroid) are its barycentric
+  // subdivision: equal quarters of the tet's volume (true for a regular
+  // tet by symmetry, and volume ratios are affine invariants). TetSCV
+  // evaluates each with Grandy's hexahedron formula, equal in exact
+  // arithmetic; the signed volume here is taken from edge vectors of node
+  // 0, which also avoids that formula's cancellation far from the origin.
+  double e1[3], e2[3], e3[3];
+  for (int d = 0; d < 3; ++d) {
+    e1[d] = c[1][d] - c[0][d];
+    e2[d] = c[2][d] - c[0][d];
+    e3[d] = c[3][d] - c[0][d];
   }
+  const double det = (e1[1] * e2[2] - e1[2] * e2[1]) * e3[0] + (e1[2] * e2[0] - e1[0] * e2[2]) * e3[1] +
+                     (e1[0] * e2[1] - e1[1] * e2[0]) * e3[2];
+  const double quarter = det / 24.0;
+  for (int ip = 0; ip < 4; ++ip) scv[ip] = quarter;
 }
 
 

@@ -134,6 +134,67 @@ def hex8_geometry(coords, conn, elem_edges, edges):
     return area, vol
 
 
+# TetSCS / TetSCV restated in numpy (src/master_element/Tet4CVFEM.C:243-360,
+# 522-620): the element's points are its nodes, edge midpoints, face
+# centroids and centroid; each sub-control surface is the quad (edge
+# midpoint, face centroid, centroid, face centroid) whose area vector is
+# the triangle fan about the quad centre (Quad3DSCS::determinant_scs), and
+# each sub-control volume the hexahedron (node, midpoints, face centroids,
+# centroid) by Grandy's 24-triangle formula (Hex8GeometryFunctions.h).
+_TET_LR = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]
+_TET_FACET = [(4, 7, 14, 13), (7, 14, 10, 5), (6, 12, 14, 7), (11, 13, 14, 12), (13, 9, 10, 14),
+              (10, 8, 12, 14)]
+_TET_SUB = [(0, 4, 7, 6, 11, 13, 14, 12), (1, 5, 7, 4, 9, 10, 14, 13), (2, 6, 7, 5, 8, 12, 14, 10),
+            (3, 9, 13, 11, 8, 10, 14, 12)]
+_GRANDY_FACES = [(0, 3, 2, 1), (4, 5, 6, 7), (0, 1, 5, 4), (2, 3, 7, 6), (1, 2, 6, 5), (0, 4, 3, 7)]
+_GRANDY_TRI = [(0, 8, 1), (8, 2, 1), (3, 2, 8), (3, 8, 0), (6, 9, 5), (7, 9, 6), (4, 9, 7), (4, 5, 9),
+               (10, 0, 1), (5, 10, 1), (4, 10, 5), (4, 0, 10), (7, 6, 11), (6, 2, 11), (2, 3, 11),
+               (3, 7, 11), (6, 12, 2), (5, 12, 6), (5, 1, 12), (1, 2, 12), (0, 4, 13), (4, 7, 13),
+               (7, 3, 13), (3, 0, 13)]
+
+
+def _fan_area(q):
+    xm = q.mean(axis=1, keepdims=True)
+    r = q - xm
+    return 0.5 * sum(np.cross(r[:, t], r[:, (t + 1) % 4]) for t in range(4))
+
+
+def _grandy(s):
+    cv = np.concatenate([s, np.stack([s[:, list(f)].mean(axis=1) for f in _GRANDY_FACES], axis=1)], axis=1)
+    vol = 0.0
+    for a, b, c in _GRANDY_TRI:
+        p, q, r = cv[:, a], cv[:, b], cv[:, c]
+        vol = vol + np.einsum("md,md->m", p + q + r, np.cross(q - p, r - p))
+    return vol / 18.0
+
+
+def tet4_geometry(coords, conn, edges):
+    """Edge area vectors and dual volumes of a Tet4 mesh (edges: E x 2 with
+    edges[:, 0] < edges[:, 1]; an element edge adds its area vector with
+    the sign of its orientation relative to the edge)."""
+    coords, conn, edges = _f64(coords), _i64(conn), _i64(edges)
+    c = coords[conn]  # M x 4 x 3
+    mid = lambda a, b: 0.5 * (c[:, a] + c[:, b])
+    fc = lambda a, b, d: (c[:, a] + c[:, b] + c[:, d]) / 3.0
+    p = np.stack([c[:, 0], c[:, 1], c[:, 2], c[:, 3], mid(0, 1), mid(1, 2), mid(2, 0), fc(0, 1, 2),
+                  mid(2, 3), mid(3, 1), fc(1, 2, 3), mid(0, 3), fc(0, 2, 3), fc(0, 1, 3),
+                  c.mean(axis=1)], axis=1)
+    N, E = coords.shape[0], edges.shape[0]
+    key = edges[:, 0] * N + edges[:, 1]
+    order = np.argsort(key)
+    area = np.zeros((E, 3))
+    for ip, (a, b) in enumerate(_TET_LR):
+        s = _fan_area(p[:, list(_TET_FACET[ip])])
+        na, nb = conn[:, a], conn[:, b]
+        lo, hi = np.minimum(na, nb), np.maximum(na, nb)
+        e = order[np.searchsorted(key[order], lo * N + hi)]
+        np.add.at(area, e, np.where((na == lo)[:, None], s, -s))
+    vol = np.zeros(N)
+    for j in range(4):
+        np.add.at(vol, conn[:, j], _grandy(p[:, list(_TET_SUB[j])]))
+    return area, vol
+
+
 def build_graph(nalu_id, edges, num_dof=1):
     nalu_id, edges = _i64(nalu_id), _i64(edges)
     N = nalu_id.shape[0]

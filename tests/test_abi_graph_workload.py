@@ -249,3 +249,15 @@ def test_rcm_order_restores_locality(nw):
     np.testing.assert_array_equal(rcm.coords, rnd.coords[order])
     with pytest.raises(nw.NwError):
         nw.rcm_order(3, np.array([[0, 3]]))
+
+
+@pytest.mark.parametrize("renumber", [0, 2])
+def test_tet_geometry_vs_oracle(nw, orc, renumber):
+    """The generator's (and the GPU's) Tet4 geometry: sub-control-surface
+    area vectors as half the cross product of the quad diagonals and the
+    sub-control volumes as quarters of the tet volume, against the oracle's
+    restatement of TetSCS (triangle fans) and TetSCV (Grandy's formula)."""
+    m = nw.Mesh(6, 5, 4, stretch_z=1.2, jitter=0.2, seed=4, tets=True, renumber=renumber, renumber_seed=3)
+    area, vol = orc.tet4_geometry(m.coords, m.conn, m.edges)
+    assert np.abs(m.area - area).max() <= 1e-14 * np.abs(area).max()
+    assert np.abs(m.dualvol - vol).max() <= 1e-14 * vol.max()
