@@ -394,6 +394,13 @@ nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes,
  * operator, each with the same energy-optimal scaling. Modes 1 and 2 are
  * the cycle without the network, kept to measure what the network adds. */
 nw_status nw_learned_set_coarse_direction(nw_learned* net, int mode);
+/* Aggregation of the coarse level: 0 (default) plain aggregation of the
+ * matrix graph; strength in (0, 1): aggregation over strong connections
+ * (|a_ij| >= strength sqrt(|a_ii a_jj|)), each pass on the Galerkin values
+ * of the previous one, so that aggregates follow the dominant couplings
+ * of stretched cells. Takes effect at nw_linsys_attach_learned, which then
+ * reads the assembled values. */
+nw_status nw_learned_set_aggregation(nw_learned* net, double strength);
 nw_status nw_linsys_attach_learned(nw_linsys* ls, nw_learned* net);
 /* Coarse level of an attached handle, refreshed from the current values
  * (host arrays; NULL entries skipped). */

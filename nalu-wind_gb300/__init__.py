@@ -194,6 +194,7 @@ SIGNATURES = {
     "nw_linsys_checkpoint_load": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.POINTER(SolveReport)]),
     "nw_solver_cfg_from_strings": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(SolverCfg)]),
     "nw_learned_set_coarse_direction": (C.c_int, [C.c_void_p, C.c_int]),
+    "nw_learned_set_aggregation": (C.c_int, [C.c_void_p, C.c_double]),
     "nw_assemble_continuity_edges_noalloc": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
                                                        C.POINTER(ContinuityOpts), C.c_void_p, C.c_void_p]),
     "nw_linsys_sum_into": (C.c_int, [C.c_void_p, C.c_int, _I64P, _DP, _DP]),
@@ -680,6 +681,11 @@ class Learned:
 
     def configure(self, post_smooth: bool = True, agg_passes: int = 2, smoother: int = 0) -> None:
         check(self.lib.nw_learned_configure(self.h, int(post_smooth), int(agg_passes), int(smoother)))
+
+    def set_aggregation(self, strength: float) -> None:
+        """0: plain aggregation; in (0, 1): aggregation over strong
+        connections (nw_learned_set_aggregation)."""
+        check(self.lib.nw_learned_set_aggregation(self.h, float(strength)))
 
     def set_coarse_direction(self, mode: int) -> None:
         """0: the network; 1: D_c^-1 r_c; 2: two Jacobi sweeps on Ac (controls

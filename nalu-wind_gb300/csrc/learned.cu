@@ -677,6 +677,62 @@ static int32_t plain_aggregate(int64_t R, const int64_t* ptr, const int32_t* col
   return na;
 }
 
+// The same aggregation over strong connections only: c is a strong
+// neighbour of r when |a_rc| >= theta sqrt(|a_rr| |a_cc|) (the strength
+// measure of smoothed aggregation). On stretched meshes the thin cells'
+// couplings dominate, so the aggregates follow them (semi-coarsening). A
+// row with no strong neighbour does not seed an aggregate; leftover rows
+// join the aggregated neighbour they are most strongly coupled to, or
+// start their own.
+static int32_t strength_aggregate(int64_t R, const int64_t* ptr, const int32_t* col,
+                                  const double* val, double theta, std::vector<int32_t>& agg) {
+  std::vector<double> d(R, 0.0);
+  for (int64_t r = 0; r < R; ++r)
+    for (int64_t p = ptr[r]; p < ptr[r + 1]; ++p)
+      if (col[p] == r) d[r] = std::fabs(val[p]);
+  std::vector<char> strong(size_t(ptr[R]), 0);
+  for (int64_t r = 0; r < R; ++r)
+    for (int64_t p = ptr[r]; p < ptr[r + 1]; ++p)
+      strong[p] = col[p] != r && std::fabs(val[p]) >= theta * std::sqrt(d[r] * d[col[p]]);
+  agg.assign(R, -1);
+  int32_t na = 0;
+  std::vector<int64_t> visit(R);
+  std::iota(visit.begin(), visit.end(), 0);
+  uint64_t st = 0x2545F4914F6CDD1Dull;  // xorshift64, fixed seed (as plain_aggregate)
+  for (int64_t i = R - 1; i > 0; --i) {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    std::swap(visit[i], visit[int64_t(st % uint64_t(i + 1))]);
+  }
+  for (const int64_t r : visit) {
+    if (agg[r] >= 0) continue;
+    int nstrong = 0;
+    bool free_nbrs = true;
+    for (int64_t p = ptr[r]; p < ptr[r + 1] && free_nbrs; ++p)
+      if (strong[p]) {
+        ++nstrong;
+        if (agg[col[p]] >= 0) free_nbrs = false;
+      }
+    if (!free_nbrs || nstrong == 0) continue;
+    for (int64_t p = ptr[r]; p < ptr[r + 1]; ++p)
+      if (strong[p]) agg[col[p]] = na;
+    agg[r] = na++;
+  }
+  for (int64_t r = 0; r < R; ++r) {
+    if (agg[r] >= 0) continue;
+    int64_t best = -1;
+    double bw = -1.0;
+    for (int64_t p = ptr[r]; p < ptr[r + 1]; ++p)
+      if (col[p] != r && agg[col[p]] >= 0 && std::fabs(val[p]) > bw) {
+        bw = std::fabs(val[p]);
+        best = p;
+      }
+    agg[r] = best >= 0 ? agg[col[best]] : na++;
+  }
+  return na;
+}
+
 // Graph of the aggregates (sorted, unique columns) from a fine graph.
 static void aggregate_graph(int64_t R, const int64_t* ptr, const int32_t* col,
                             const std::vector<int32_t>& agg, int64_t nagg,
@@ -698,19 +754,56 @@ static void aggregate_graph(int64_t R, const int64_t* ptr, const int32_t* col,
 
 // Aggregation applied `passes` times (aggregates of aggregates), composed
 // into one fine-row -> aggregate map.
-void CoarseLevel::setup(const HostGraph& g, int npasses, cudaStream_t s) {
+void CoarseLevel::setup(const HostGraph& g, int npasses, cudaStream_t s, const double* values,
+                        double theta) {
   if (g.num_dof != 1) fail(NW_INVALID_ARG, "the learned preconditioner needs num_dof 1");
   if (npasses < 1 || npasses > 4) fail(NW_INVALID_ARG, "aggregation passes must be 1..4");
   passes = npasses;
+  strength = values ? theta : 0.0;
   const int64_t R = g.node_rows;
   nf = R;
-  int32_t na = plain_aggregate(R, g.nrow_ptr.data(), g.ncol.data(), agg_h);
-  for (int pass = 1; pass < npasses; ++pass) {
-    std::vector<int64_t> p1;
-    std::vector<int32_t> c1, agg2;
-    aggregate_graph(R, g.nrow_ptr.data(), g.ncol.data(), agg_h, na, p1, c1);
-    na = plain_aggregate(na, p1.data(), c1.data(), agg2);
-    for (int64_t r = 0; r < R; ++r) agg_h[r] = agg2[agg_h[r]];
+  int32_t na = 0;
+  if (strength > 0.0) {
+    // every pass on the Galerkin values of the previous level
+    std::vector<int64_t> lp(g.nrow_ptr);
+    std::vector<int32_t> lc(g.ncol);
+    std::vector<double> lv(values, values + g.nrow_ptr[R]);
+    std::vector<int32_t> a;
+    int64_t lr = R;
+    for (int pass = 0; pass < npasses; ++pass) {
+      const int32_t n2 = strength_aggregate(lr, lp.data(), lc.data(), lv.data(), strength, a);
+      if (pass == 0) {
+        agg_h = a;
+      } else {
+        for (int64_t r = 0; r < R; ++r) agg_h[r] = a[agg_h[r]];
+      }
+      if (pass + 1 < npasses) {
+        std::vector<int64_t> p1;
+        std::vector<int32_t> c1;
+        aggregate_graph(lr, lp.data(), lc.data(), a, n2, p1, c1);
+        std::vector<double> v1(size_t(p1[n2]), 0.0);
+        for (int64_t r = 0; r < lr; ++r)
+          for (int64_t p = lp[r]; p < lp[r + 1]; ++p) {
+            const int32_t I = a[r], J = a[lc[p]];
+            const auto b = c1.begin() + p1[I], e = c1.begin() + p1[I + 1];
+            v1[size_t(std::lower_bound(b, e, J) - c1.begin())] += lv[p];
+          }
+        lp.swap(p1);
+        lc.swap(c1);
+        lv.swap(v1);
+        lr = n2;
+      }
+      na = n2;
+    }
+  } else {
+    na = plain_aggregate(R, g.nrow_ptr.data(), g.ncol.data(), agg_h);
+    for (int pass = 1; pass < npasses; ++pass) {
+      std::vector<int64_t> p1;
+      std::vector<int32_t> c1, agg2;
+      aggregate_graph(R, g.nrow_ptr.data(), g.ncol.data(), agg_h, na, p1, c1);
+      na = plain_aggregate(na, p1.data(), c1.data(), agg2);
+      for (int64_t r = 0; r < R; ++r) agg_h[r] = agg2[agg_h[r]];
+    }
   }
   nc = na;
   // members

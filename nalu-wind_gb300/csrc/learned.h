@@ -56,6 +56,7 @@ constexpr int kNumParams = kOffWout + kHid;
 struct CoarseLevel {
   int64_t nf = 0, nc = 0, nnzc = 0;
   int passes = 1;                          // aggregation passes
+  double strength = 0.0;                   // strong-connection threshold (0: plain)
   std::vector<int32_t> agg_h;              // fine row -> aggregate
   std::vector<int64_t> cptr_h;             // coarse CSR
   std::vector<int32_t> ccol_h, cdiag_h, rev_h;
@@ -63,7 +64,10 @@ struct CoarseLevel {
   DeviceArray<int64_t> mptr, cptr, gptr;
   DeviceArray<double> ac;                  // Galerkin values
   DeviceArray<float> wgt, dinv;            // edge weights, 1 / Ac_II
-  void setup(const HostGraph& g, int passes, cudaStream_t s);
+  // values (host, aligned with the node graph) and theta > 0: aggregation
+  // over strong connections; otherwise plain aggregation of the graph
+  void setup(const HostGraph& g, int passes, cudaStream_t s, const double* values = nullptr,
+             double theta = 0.0);
   void refresh(const double* fine_values, cudaStream_t s);
 };
 
@@ -85,6 +89,7 @@ struct LearnedNet {
   uint64_t seed = 0;
   int post_smooth = 1;  // SGS sweep after the coarse correction
   int agg_passes = 2;   // aggregation passes of the coarse level
+  double agg_strength = 0.0;  // strong-connection threshold of the aggregation (0: plain)
   int smoother = 0;     // 0: symmetric GS sweeps around the coarse step; 1: forward / backward
   // coarse direction: 0 the network; 1 D_c^-1 r_c and 2 two Jacobi sweeps on
   // Ac (the same cycle and alpha rule without the network, as controls)

@@ -1661,6 +1661,15 @@ nw_status nw_learned_configure(nw_learned* net, int post_smooth, int agg_passes,
   });
 }
 
+nw_status nw_learned_set_aggregation(nw_learned* net, double strength) {
+  return guard([&] {
+    if (!net || !(strength >= 0.0 && strength < 1.0)) fail(NW_INVALID_ARG, "bad aggregation threshold");
+    if (strength != net->net.agg_strength && net->net.npairs > 0)
+      fail(NW_INVALID_ARG, "harvested pairs use the current aggregation; clear them first");
+    net->net.agg_strength = strength;
+  });
+}
+
 nw_status nw_learned_set_coarse_direction(nw_learned* net, int mode) {
   return guard([&] {
     if (!net || mode < 0 || mode > 2) fail(NW_INVALID_ARG, "bad coarse direction mode");
@@ -1673,9 +1682,23 @@ nw_status nw_linsys_attach_learned(nw_linsys* ls, nw_learned* net) {
     need_finalized(ls);
     if (!net) fail(NW_INVALID_ARG, "null network");
     if (ls->num_dof != 1) fail(NW_INVALID_ARG, "the learned preconditioner needs num_dof 1");
-    if (!ls->coarse || ls->coarse->passes != net->net.agg_passes) {
+    const double theta = net->net.agg_strength;
+    if (!ls->coarse || ls->coarse->passes != net->net.agg_passes || ls->coarse->strength != theta ||
+        theta > 0.0) {
       auto cl = std::make_unique<CoarseLevel>();
-      cl->setup(ls->g, net->net.agg_passes, ls->stream);
+      if (theta > 0.0) {
+        // the aggregation reads the assembled values
+        materialize_zero(ls);
+        if (int64_t(ls->values.n) != ls->g.nrow_ptr[ls->g.node_rows])
+          fail(NW_INTERNAL, "node graph and values differ in size");
+        std::vector<double> v(ls->values.n);
+        NW_CUDA(cudaMemcpyAsync(v.data(), ls->values.p, v.size() * sizeof(double),
+                                cudaMemcpyDeviceToHost, ls->stream));
+        NW_CUDA(cudaStreamSynchronize(ls->stream));
+        cl->setup(ls->g, net->net.agg_passes, ls->stream, v.data(), theta);
+      } else {
+        cl->setup(ls->g, net->net.agg_passes, ls->stream);
+      }
       ls->coarse = std::move(cl);
     }
     ls->learned = net;

@@ -266,3 +266,30 @@ def test_committed_128cube_network_loads_and_solves(nw):
     x = torch.zeros(ls.sizes()[0], dtype=torch.float64, device="cuda")
     rep = ls.solve(x)
     assert rep.converged == 1 and not rep.fallback
+
+
+def test_strength_aggregation_option(nw):
+    """nw_learned_set_aggregation: aggregation over strong connections
+    covers every row with more, smaller aggregates than plain aggregation
+    on a stretched box, and the two-level cycle (two Jacobi sweeps on A_c
+    as the coarse direction) still converges to 1e-8 with it."""
+    import torch
+    ls = _poisson(nw, (40, 36, 30), seed=21, stretch=1.12, jitter=0.05)
+    sizes = {}
+    for theta in (0.0, 0.08):
+        net = nw.Learned(seed=0)
+        net.set_aggregation(theta)
+        net.set_coarse_direction(2)
+        ls.attach_learned(net)
+        g = ls.coarse_graph()
+        agg, nc = g["agg"], g["nc"]
+        assert agg.min() == 0 and agg.max() == nc - 1 and len(np.unique(agg)) == nc
+        sizes[theta] = nc
+        ls.set_solver_cfg(nw.solver_cfg(method=nw.FGMRES, kspace=30, inner_kspace=30, max_iterations=6000,
+                                        tolerance=1e-8, precision=nw.PREC_MIXED, preconditioner=nw.PC_LEARNED))
+        x = torch.zeros(ls.sizes()[0], dtype=torch.float64, device="cuda")
+        rep = ls.solve(x)
+        assert rep.converged == 1
+    assert sizes[0.08] > sizes[0.0]
+    with pytest.raises(nw.NwError):
+        nw.Learned(seed=0).set_aggregation(1.5)
