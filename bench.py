@@ -602,6 +602,11 @@ def heldout_poisson(nw, stream, args, net, net_run=None) -> dict:
             runs.append(("learned_mixed_fgmres30_in_run_network", net_run, lcfg))
         runs += [(f"mixed_fgmres30_two_level_{c}", cn, lcfg) for c, cn in controls.items()
                  if c in ("untrained_network", "jacobi_coarse_direction")]
+        # the same non-learned cycle on aggregates of strong connections
+        strong = nw.Learned(seed=0)
+        strong.set_aggregation(0.08)
+        strong.set_coarse_direction(2)
+        runs.append(("mixed_fgmres30_two_level_two_jacobi_coarse_sweeps_strength_aggregation_0.08", strong, lcfg))
         for name, lnet, cfg in runs:
             if lnet is not None:
                 ls.attach_learned(lnet)
