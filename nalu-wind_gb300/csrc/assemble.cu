@@ -358,7 +358,9 @@ __device__ __forceinline__ void momentum_edge(int64_t e, int64_t E, const Moment
   const double* __restrict__ mdotA = in.mdot;
   const double* __restrict__ pecA = in.pec;
   const int2 lr = edges[e];
-  const int64_t L = lr.x, R = lr.y;
+  // 32-bit node offsets (9 N < 2^32 is checked when the system is
+  // finalized): fewer registers than 64-bit ones
+  const uint32_t L = uint32_t(lr.x), R = uint32_t(lr.y);
   // coordinate and velocity differences are formed in FP64 and split once:
   // splitting each operand to a float pair first would keep only 48 bits of
   // each, and the difference of nearby values would lose the rest
@@ -599,10 +601,14 @@ __device__ __forceinline__ dd ldc(const dd* p) {
 
 // One block of NB node rows starting at r0 (threads 0 .. 3 NB - 1 of the
 // block; any others only take part in the staging copy).
-template <int NB, bool NC>
+// IDX: the type of the coefficient offsets (uint32_t when 11 E < 2^31:
+// one register and one wide multiply-add per load instead of a 64-bit
+// pointer per coefficient array).
+template <int NB, bool NC, typename IDX = int64_t>
 __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double* stage) {
   const dd* cb = a.cb;
-  const int64_t E = a.E, mask = a.mask;
+  const IDX E = IDX(a.E);
+  const int64_t mask = a.mask;
   const int64_t r1 = (r0 + NB < a.R) ? r0 + NB : a.R;
   const int64_t base = a.row_ptr[3 * r0];
   const int64_t cnt = a.row_ptr[3 * r1] - base;
@@ -613,10 +619,10 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
   // diagonal N_qq and the off-diagonals of columns c1 < c2 (the two c != q),
   // so that the block's c_side I term adds to one fixed entry
   const int c1 = q == 0 ? 1 : 0, c2 = q == 2 ? 1 : 2;
-  const dd* pd = cb + (q == 0 ? 2 : (q == 1 ? 5 : 7)) * E;
-  const dd* p1 = cb + (q == 2 ? 4 : 3) * E;
-  const dd* p2 = cb + (q == 0 ? 4 : 6) * E;
-  const dd* pf = cb + (8 + q) * E;
+  const IDX xd = IDX(q == 0 ? 2 : (q == 1 ? 5 : 7)) * E;
+  const IDX x1 = IDX(q == 2 ? 4 : 3) * E;
+  const IDX x2 = IDX(q == 0 ? 4 : 6) * E;
+  const IDX xf = IDX(8 + q) * E;
   if (r < r1) {
     const int32_t s = a.inc_ptr[r], t = a.inc_ptr[r + 1];
     const int64_t bq = a.row_ptr[3 * r + q];
@@ -639,12 +645,12 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
       for (int32_t qi = s; qi < t; ++qi) {
         const uint32_t w = a.inc[qi];
         const bool dup = (w >> 31) != 0;
-        const int64_t e = ((w & 0x7fffffffu) >> 1) & mask;
+        const IDX e = IDX(int64_t((w & 0x7fffffffu) >> 1) & mask);
         const int side = w & 1u;
-        const dd c0 = ldc<NC>(cb + e), c1v = ldc<NC>(cb + E + e);
+        const dd c0 = ldc<NC>(cb + e), c1v = ldc<NC>(cb + (E + e));
         const dd co = side ? c1v : c0, other = side ? c0 : c1v;
-        const dd nd = ldc<NC>(pd + e), n1 = ldc<NC>(p1 + e), n2 = ldc<NC>(p2 + e);
-        const dd f = ldc<NC>(pf + e);
+        const dd nd = ldc<NC>(cb + (xd + e)), n1 = ldc<NC>(cb + (x1 + e)), n2 = ldc<NC>(cb + (x2 + e));
+        const dd f = ldc<NC>(cb + (xf + e));
         acc_add(rr, side ? f : -f);
         const dd bd = nd + co;
         if (!dup) {
@@ -680,9 +686,10 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
     a.values[base + k] = a.accumulate ? a.values[base + k] + stage[k] : stage[k];
 }
 
+template <typename IDX>
 __global__ void __launch_bounds__(3 * kRow3Nodes) row3t_k(Row3Args a) {
   extern __shared__ double stage[];
-  row3_block<kRow3Nodes, true>(int64_t(blockIdx.x) * kRow3Nodes, a, stage);
+  row3_block<kRow3Nodes, true, IDX>(int64_t(blockIdx.x) * kRow3Nodes, a, stage);
 }
 
 // ---------------------------------------------------------------------------
@@ -850,7 +857,8 @@ void set_smem_attrs() {
   if (g_smem_set_device == dev) return;
   NW_CUDA(cudaFuncSetAttribute(row1_k<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
   NW_CUDA(cudaFuncSetAttribute(row1_k<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
-  NW_CUDA(cudaFuncSetAttribute(row3t_k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
+  NW_CUDA(cudaFuncSetAttribute(row3t_k<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
+  NW_CUDA(cudaFuncSetAttribute(row3t_k<int64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
 #define NW_FUSED_ATTR(LIM, DIV, DEF)                                                      \
   NW_CUDA(cudaFuncSetAttribute(momentum_fused_k<LIM, DIV, DEF>,                           \
                                cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem))
@@ -1025,8 +1033,11 @@ void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
   else if (kind == 1)
     row1_k<1><<<grid_for(R, kRow1Threads), kRow1Threads, smem_bytes, s>>>(
         R, inc_ptr, inc, diag_pos, row_ptr, buf, E, values, rhs, accumulate, smem_bytes);
+  else if (int64_t(kMomentumCoefs) * E < (int64_t(1) << 31))
+    row3t_k<uint32_t><<<grid_for(R, kRow3Nodes), 3 * kRow3Nodes, smem_bytes, s>>>(row3_args(
+        R, inc_ptr, inc, diag_pos, row_ptr, buf, E, relax, values, rhs, accumulate, smem_bytes));
   else
-    row3t_k<<<grid_for(R, kRow3Nodes), 3 * kRow3Nodes, smem_bytes, s>>>(row3_args(
+    row3t_k<int64_t><<<grid_for(R, kRow3Nodes), 3 * kRow3Nodes, smem_bytes, s>>>(row3_args(
         R, inc_ptr, inc, diag_pos, row_ptr, buf, E, relax, values, rhs, accumulate, smem_bytes));
 }
 

@@ -373,6 +373,9 @@ nw_status nw_linsys_finalize(nw_linsys* ls) {
       ls->stage_bytes[0] = ls->stage_bytes[1] =
           row_stage_bytes(0, g.row_ptr.data(), g.node_rows);
     } else if (ls->num_dof == 3) {
+      // the momentum kernels address node fields with 32-bit offsets (up
+      // to 9 doubles per node); a system that large would not fit in HBM
+      if (9 * g.num_nodes >= (int64_t(1) << 32)) fail(NW_INVALID_ARG, "too many nodes for a 3-dof system");
       ls->stage_bytes[2] = row_stage_bytes(2, g.row_ptr.data(), g.node_rows);
       ls->max_inc = 0;
       for (int64_t r = 0; r < g.node_rows; ++r)
