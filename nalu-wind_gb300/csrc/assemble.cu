@@ -513,6 +513,7 @@ __global__ void __launch_bounds__(kRow1Threads)
     if (s != t) {
       const int dp = diag_pos[r];
       C dg{}, rr{}, off{};
+      dd_acc dga, rra;  // continuity: the diagonal and rhs sums, deferred renormalisation
       int slot = -1;
       for (int32_t qi = s; qi < t; ++qi) {
         const uint32_t w = inc[qi];
@@ -542,8 +543,17 @@ __global__ void __launch_bounds__(kRow1Threads)
         } else {
           off = off + co;
         }
-        dg = dg + cd;
-        rr = rr + cr;
+        if constexpr (KIND == 0) {
+          dg = dg + cd;
+          rr = rr + cr;
+        } else {
+          acc_add(dga, cd);
+          acc_add(rra, cr);
+        }
+      }
+      if constexpr (KIND == 1) {
+        dg = acc_value(dga);
+        rr = acc_value(rra);
       }
       double* p = out + (slot < dp ? slot : slot + 1);
       const double v = to_f64(off), vd = to_f64(dg), vr = to_f64(rr);
