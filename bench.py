@@ -293,7 +293,9 @@ def run_ours(args, rank, world):
     # assembles. Steps do not overlap one another (a solver's next inputs
     # depend on this step's solve).
     # The momentum edge phase runs in edge chunks as the per-edge inputs
-    # (area, mdot, pecfac) arrive, after the node fields.
+    # (area, mdot, pecfac) arrive, after the node fields; after each chunk
+    # the row phase runs over the node rows whose incident edges are all
+    # done (nw_assemble_momentum_rows_range), and their rhs is read back.
     copy_s = torch.cuda.Stream()
     d2h_s = torch.cuda.Stream()
     con_only = ("pressure", "dpdx", "udiag")
@@ -302,6 +304,12 @@ def run_ours(args, rank, world):
     n_chunks = 8
     bounds = [E * c // n_chunks for c in range(n_chunks + 1)]
     ecols = {k: (pinned[k].numel() // E) for k in edge_keys}
+    # node rows complete after each chunk: every incident edge index below
+    # the chunk's end (node rows are the nodes in index order here)
+    maxinc = np.full(N, -1, np.int64)
+    np.maximum.at(maxinc, mesh.edges[:, 0], np.arange(E))
+    np.maximum.at(maxinc, mesh.edges[:, 1], np.arange(E))
+    row_ready = [int(np.searchsorted(np.maximum.accumulate(maxinc), b)) for b in bounds[1:-1]] + [N]
 
     def e2e_step():
         copy_s.wait_stream(stream)
@@ -321,19 +329,23 @@ def run_ours(args, rank, world):
             ev_c = torch.cuda.Event()
             ev_c.record(copy_s)
         lsm.zero_system()
-        for (a, b), ev in zip(zip(bounds[:-1], bounds[1:]), chunk_ev):
+        done = 0
+        for (a, b), ev, r in zip(zip(bounds[:-1], bounds[1:]), chunk_ev, row_ready):
             stream.wait_event(ev)
             lsm.assemble_momentum_range(fm, mo, a, b)
-        lsm.assemble_momentum_rows(mo)
-        ev_mr = torch.cuda.Event()
-        ev_mr.record(stream)
+            if r > done:
+                lsm.assemble_momentum_rows_range(mo, done, r)
+                ev_mr = torch.cuda.Event()
+                ev_mr.record(stream)
+                d2h_s.wait_event(ev_mr)
+                cudart_copy(rhs_m_host.data_ptr() + 24 * done, rm_dev + 24 * done, 24 * (r - done),
+                            d2h_s.cuda_stream)
+                done = r
         stream.wait_event(ev_c)
         lsc.zero_system()
         lsc.assemble_continuity(fc, co)
         ev_cr = torch.cuda.Event()
         ev_cr.record(stream)
-        d2h_s.wait_event(ev_mr)
-        cudart_copy(rhs_m_host.data_ptr(), rm_dev, rhs_m_host.numel() * 8, d2h_s.cuda_stream)
         d2h_s.wait_event(ev_cr)
         cudart_copy(rhs_c_host.data_ptr(), rc_dev, rhs_c_host.numel() * 8, d2h_s.cuda_stream)
         stream.wait_stream(d2h_s)
@@ -357,6 +369,10 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     barrier(world)
     ms_e2e = t0.elapsed_time(t1)
+    # the streamed step's rhs read-backs are the assembled systems' rhs
+    if not (np.array_equal(rhs_m_host.numpy(), lsm.to_host()[1])
+            and np.array_equal(rhs_c_host.numpy(), lsc.to_host()[1])):
+        raise RuntimeError("end-to-end rhs differs from the assembled rhs")
     ms_total = max_over_ranks(ms_total, world)
     ms_e2e = max_over_ranks(ms_e2e, world)
     nnz_step = nnz_m + nnz_c

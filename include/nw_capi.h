@@ -261,6 +261,17 @@ nw_status nw_assemble_momentum_edge_range(nw_linsys* ls, const nw_momentum_field
                                           const nw_momentum_opts* o, int64_t edge_begin,
                                           int64_t edge_end);
 nw_status nw_assemble_momentum_rows(nw_linsys* ls, const nw_momentum_opts* o);
+/* The row phase over node rows [row_begin, row_end) only, so that it can
+ * run as soon as every edge incident to those rows has been through the
+ * edge phase (with edges ordered by their first node, the rows below a
+ * chunk's last first node are then complete). On a system zeroed by
+ * nw_linsys_zero the ranges must follow each other from row 0 (each
+ * overwrites its rows; the system counts as assembled once the last row is
+ * covered, and an operation in between zeroes the rows not yet covered);
+ * otherwise each range adds into its rows. The rows of all ranges together
+ * equal nw_assemble_momentum_rows bit for bit. */
+nw_status nw_assemble_momentum_rows_range(nw_linsys* ls, const nw_momentum_opts* o,
+                                          int64_t row_begin, int64_t row_end);
 
 /* How nw_assemble_momentum_edges runs on the GPU. TWO_KERNELS (default):
  * the edge kernel writes every edge's coefficients to a buffer in HBM, then

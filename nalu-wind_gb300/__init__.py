@@ -185,6 +185,7 @@ SIGNATURES = {
     "nw_assemble_momentum_edge_range": (C.c_int, [C.c_void_p, C.POINTER(MomentumFields), C.POINTER(MomentumOpts),
                                                   C.c_int64, C.c_int64]),
     "nw_assemble_momentum_rows": (C.c_int, [C.c_void_p, C.POINTER(MomentumOpts)]),
+    "nw_assemble_momentum_rows_range": (C.c_int, [C.c_void_p, C.POINTER(MomentumOpts), C.c_int64, C.c_int64]),
     "nw_linsys_sgs_classes": (C.c_int, [C.c_void_p, _I64P]),
     "nw_linsys_set_assembly_path": (C.c_int, [C.c_void_p, C.c_int]),
     "nw_linsys_assembly_schedule": (C.c_int, [C.c_void_p, C.POINTER(AssemblySchedule)]),
@@ -447,6 +448,10 @@ class LinearSystem:
 
     def assemble_momentum_rows(self, opts: "MomentumOpts") -> None:
         check(self.lib.nw_assemble_momentum_rows(self.h, C.byref(opts)))
+
+    def assemble_momentum_rows_range(self, opts: "MomentumOpts", row_begin: int, row_end: int) -> None:
+        """Row phase over node rows [row_begin, row_end)."""
+        check(self.lib.nw_assemble_momentum_rows_range(self.h, C.byref(opts), int(row_begin), int(row_end)))
 
     def sum_into(self, nodes, rhs, lhs) -> None:
         nodes = np.ascontiguousarray(nodes, np.int64)

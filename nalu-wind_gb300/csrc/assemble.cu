@@ -584,7 +584,8 @@ __global__ void __launch_bounds__(kRow1Threads)
 // -(sum of the other side's constants + sum of N) / relax.
 constexpr int kRow3Nodes = 64;
 struct Row3Args {
-  int64_t R, E;  // node rows; stride of the coefficient arrays
+  int64_t R, E;  // end of the node rows; stride of the coefficient arrays
+  int64_t r_begin;  // first node row (the row kernel's blocks start here)
   int64_t mask;  // edge -> coefficient slot: e & mask
   const int32_t* __restrict__ inc_ptr;
   const uint32_t* __restrict__ inc;
@@ -699,7 +700,7 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
 template <typename IDX>
 __global__ void __launch_bounds__(3 * kRow3Nodes) row3t_k(Row3Args a) {
   extern __shared__ double stage[];
-  row3_block<kRow3Nodes, true, IDX>(int64_t(blockIdx.x) * kRow3Nodes, a, stage);
+  row3_block<kRow3Nodes, true, IDX>(a.r_begin + int64_t(blockIdx.x) * kRow3Nodes, a, stage);
 }
 
 // ---------------------------------------------------------------------------
@@ -952,7 +953,7 @@ MomentumIn momentum_in(const int2* edges, const nw_momentum_fields& f) {
 Row3Args row3_args(int64_t R, const int32_t* inc_ptr, const uint32_t* inc, const int32_t* diag_pos,
                    const int64_t* row_ptr, const double* buf, int64_t E, double relax, double* values,
                    double* rhs, int accumulate, int smem_bytes) {
-  return Row3Args{R, E, int64_t(-1), inc_ptr, inc, diag_pos, row_ptr, reinterpret_cast<const dd*>(buf),
+  return Row3Args{R, E, 0, int64_t(-1), inc_ptr, inc, diag_pos, row_ptr, reinterpret_cast<const dd*>(buf),
                   dd_param(1.0 / relax), values, rhs, accumulate, smem_bytes};
 }
 }  // namespace
@@ -1034,8 +1035,8 @@ void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
                  const uint32_t* inc, const int32_t* diag_pos,
                  const int64_t* row_ptr, const double* buf, int64_t E,
                  double relax, double* values, double* rhs, int accumulate,
-                 int smem_bytes, int max_inc) {
-  if (R == 0) return;
+                 int smem_bytes, int max_inc, int64_t row_begin) {
+  if (R <= row_begin) return;
   set_smem_attrs();
   if (kind == 0)
     row1_k<0><<<grid_for(R, kRow1Threads), kRow1Threads, smem_bytes, s>>>(
@@ -1043,12 +1044,16 @@ void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
   else if (kind == 1)
     row1_k<1><<<grid_for(R, kRow1Threads), kRow1Threads, smem_bytes, s>>>(
         R, inc_ptr, inc, diag_pos, row_ptr, buf, E, values, rhs, accumulate, smem_bytes);
-  else if (int64_t(kMomentumCoefs) * E < (int64_t(1) << 31))
-    row3t_k<uint32_t><<<grid_for(R, kRow3Nodes), 3 * kRow3Nodes, smem_bytes, s>>>(row3_args(
-        R, inc_ptr, inc, diag_pos, row_ptr, buf, E, relax, values, rhs, accumulate, smem_bytes));
-  else
-    row3t_k<int64_t><<<grid_for(R, kRow3Nodes), 3 * kRow3Nodes, smem_bytes, s>>>(row3_args(
-        R, inc_ptr, inc, diag_pos, row_ptr, buf, E, relax, values, rhs, accumulate, smem_bytes));
+  else {
+    Row3Args a = row3_args(R, inc_ptr, inc, diag_pos, row_ptr, buf, E, relax, values, rhs,
+                           accumulate, smem_bytes);
+    a.r_begin = row_begin;
+    const unsigned grid = grid_for(R - row_begin, kRow3Nodes);
+    if (int64_t(kMomentumCoefs) * E < (int64_t(1) << 31))
+      row3t_k<uint32_t><<<grid, 3 * kRow3Nodes, smem_bytes, s>>>(a);
+    else
+      row3t_k<int64_t><<<grid, 3 * kRow3Nodes, smem_bytes, s>>>(a);
+  }
 }
 
 void launch_reset_rows(cudaStream_t s, int64_t n, const int64_t* nodes,

@@ -37,15 +37,14 @@ constexpr int kContinuityNodeStride = 8;
 void launch_momentum_edges(cudaStream_t s, int64_t E, int64_t e0, int64_t e1, const int2* edges,
                            const nw_momentum_fields& f, const MomentumOpts& o,
                            double* buf);
-// kind 0 scalar, 1 continuity, 2 momentum (3 dof). smem_bytes: staging
-// size from row_stage_bytes (0 disables staging). max_inc: the largest
-// number of incidences of a node row (momentum rows of at most 32 take the
-// warp-per-row kernel; 0 = unknown).
+// kind 0 scalar, 1 continuity, 2 momentum (3 dof), over node rows
+// [row_begin, R) (row_begin > 0: momentum only). smem_bytes: staging size
+// from row_stage_bytes (0 disables staging). max_inc: unused.
 void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
                  const uint32_t* inc, const int32_t* diag_pos,
                  const int64_t* row_ptr, const double* buf, int64_t E,
                  double relax, double* values, double* rhs, int accumulate,
-                 int smem_bytes, int max_inc = 0);
+                 int smem_bytes, int max_inc = 0, int64_t row_begin = 0);
 // kind 3: the row blocks of the single-kernel momentum assembly.
 int row_stage_bytes(int kind, const int64_t* row_ptr_host, int64_t R);
 

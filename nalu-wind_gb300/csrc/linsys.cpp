@@ -50,6 +50,9 @@ struct nw_linsys {
   bool built = false;
   bool finalized = false;
   bool pristine = false;  // zeroSystem issued, no values written since
+  // with pristine: node rows below this were written by in-order row-range
+  // calls (nw_assemble_momentum_rows_range); the rest are still zero
+  int64_t pristine_from = 0;
   HostGraph g;
   DeviceArray<int64_t> row_ptr, node_lid, row_nodes_ptr;
   DeviceArray<int32_t> row_nodes;
@@ -139,12 +142,23 @@ void need_finalized(const nw_linsys* ls) {
   if (!ls->finalized) fail(NW_NOT_FINALIZED, "linear system not finalized");
 }
 
-// materialise a pending zeroSystem before a partial update
+// materialise a pending zeroSystem before a partial update (the rows that
+// in-order row-range calls already wrote are kept)
 void materialize_zero(nw_linsys* ls) {
   if (!ls->pristine) return;
-  NW_CUDA(cudaMemsetAsync(ls->values.p, 0, ls->values.n * sizeof(double), ls->stream));
-  NW_CUDA(cudaMemsetAsync(ls->rhs.p, 0, ls->rhs.n * sizeof(double), ls->stream));
+  const int64_t r0 = ls->pristine_from * ls->num_dof;
+  const int64_t v0 = ls->g.row_ptr.empty() ? 0 : ls->g.row_ptr[r0];
+  NW_CUDA(cudaMemsetAsync(ls->values.p + v0, 0, (ls->values.n - v0) * sizeof(double), ls->stream));
+  NW_CUDA(cudaMemsetAsync(ls->rhs.p + r0, 0, (ls->rhs.n - r0) * sizeof(double), ls->stream));
   ls->pristine = false;
+  ls->pristine_from = 0;
+}
+
+// accumulate flag of a kernel that writes every row: 0 (overwrite) on a
+// zeroed system, else 1; a partly written zeroed system is materialised
+int write_mode(nw_linsys* ls) {
+  if (ls->pristine && ls->pristine_from > 0) materialize_zero(ls);
+  return ls->pristine ? 0 : 1;
 }
 
 void begin_timing(nw_linsys* ls) {
@@ -454,6 +468,7 @@ nw_status nw_linsys_zero(nw_linsys* ls) {
     need_finalized(ls);
     // zeroSystem is deferred: the next full assembly overwrites every slot
     ls->pristine = true;
+    ls->pristine_from = 0;
   });
 }
 
@@ -477,7 +492,7 @@ nw_status nw_assemble_scalar_edges(nw_linsys* ls, const nw_scalar_fields* f,
     launch_scalar_edges(ls->stream, E, ls->edges.p, *f, *o, ls->buf.p);
     launch_rows(ls->stream, 0, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
                 ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, o->relax,
-                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[0]);
+                ls->values.p, ls->rhs.p, write_mode(ls), ls->stage_bytes[0]);
     NW_CUDA(cudaGetLastError());
     end_timing(ls);
     ls->pristine = false;
@@ -505,7 +520,7 @@ nw_status nw_assemble_continuity_edges(nw_linsys* ls,
                             ls->buf.p, ls->nodebuf.p);
     launch_rows(ls->stream, 1, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
                 ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, 1.0,
-                ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[1]);
+                ls->values.p, ls->rhs.p, write_mode(ls), ls->stage_bytes[1]);
     NW_CUDA(cudaGetLastError());
     end_timing(ls);
     ls->pristine = false;
@@ -532,7 +547,7 @@ static void check_momentum_args(const nw_linsys* ls, const nw_momentum_fields* f
 static void momentum_rows(nw_linsys* ls, double relax) {
   launch_rows(ls->stream, 2, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
               ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, ls->g.num_edges, relax,
-              ls->values.p, ls->rhs.p, ls->pristine ? 0 : 1, ls->stage_bytes[2], ls->max_inc);
+              ls->values.p, ls->rhs.p, write_mode(ls), ls->stage_bytes[2], ls->max_inc);
   NW_CUDA(cudaGetLastError());
   ls->pristine = false;
 }
@@ -550,7 +565,7 @@ nw_status nw_assemble_momentum_edges(nw_linsys* ls, const nw_momentum_fields* f,
         NW_CUDA(cudaMemsetAsync(L.eflag, 0, ls->fsched.chunks * sizeof(int), ls->stream));
         NW_CUDA(cudaMemsetAsync(L.rflag, 0, ls->fsched.blocks * sizeof(int), ls->stream));
       }
-      L.accumulate = ls->pristine ? 0 : 1;
+      L.accumulate = write_mode(ls);
       // the system's arrays as they are now
       L.values = ls->values.p;
       L.rhs = ls->rhs.p;
@@ -580,6 +595,37 @@ nw_status nw_assemble_momentum_edge_range(nw_linsys* ls, const nw_momentum_field
       fail(NW_INVALID_ARG, "edge range out of bounds");
     launch_momentum_edges(ls->stream, E, edge_begin, edge_end, ls->edges.p, *f, *o, ls->buf.p);
     NW_CUDA(cudaGetLastError());
+  });
+}
+
+nw_status nw_assemble_momentum_rows_range(nw_linsys* ls, const nw_momentum_opts* o,
+                                          int64_t row_begin, int64_t row_end) {
+  return guard([&] {
+    need_finalized(ls);
+    if (ls->num_dof != 3) fail(NW_INVALID_ARG, "momentum assembly needs num_dof 3");
+    if (!o) fail(NW_INVALID_ARG, "null argument");
+    if (!(o->relax != 0.0)) fail(NW_INVALID_ARG, "relaxation factor is zero");
+    const int64_t R = ls->g.node_rows;
+    if (row_begin < 0 || row_end > R || row_begin > row_end) fail(NW_INVALID_ARG, "row range out of bounds");
+    if (row_begin == row_end) return;
+    int accumulate = 1;
+    if (ls->pristine) {
+      // on a zeroed system the ranges overwrite, so they must come in order
+      if (row_begin != ls->pristine_from)
+        fail(NW_INVALID_ARG, "after zeroSystem, row ranges must follow each other from row 0");
+      accumulate = 0;
+    }
+    launch_rows(ls->stream, 2, row_end, ls->inc_ptr.p, ls->inc.p, ls->diag_pos.p, ls->row_ptr.p,
+                ls->buf.p, ls->g.num_edges, o->relax, ls->values.p, ls->rhs.p, accumulate,
+                ls->stage_bytes[2], ls->max_inc, row_begin);
+    NW_CUDA(cudaGetLastError());
+    if (ls->pristine) {
+      ls->pristine_from = row_end;
+      if (row_end == R) {
+        ls->pristine = false;
+        ls->pristine_from = 0;
+      }
+    }
   });
 }
 

@@ -149,3 +149,67 @@ def test_momentum_in_edge_ranges_equals_one_call(nw):
                 ls.assemble_momentum_range(fm, mo, 5, mesh.num_edges + 1)
         out.append(ls.to_host())
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_momentum_row_ranges_pipeline_with_edge_ranges(nw):
+    """Edge ranges each followed by the row range their edges complete
+    (rows below the chunk's last first node), as the streamed end-to-end
+    step runs them: bit for bit the one-call assembly. On a zeroed system
+    the row ranges must come in order; stopping part-way and reading the
+    system gives zeros in the rows not yet covered; on an assembled system
+    a range adds into its rows."""
+    case = nw.workload.lowmach_case(20, 16, 12, seed=2)
+    mesh = case.mesh
+    nd = case.node
+    host = dict(coords=mesh.coords, velocity=nd["velocity"], dudx=nd["dudx"], viscosity=nd["viscosity"],
+                density=nd["density"], mask=nd["mask"], area=mesh.area, mdot=case.edge["mdot"],
+                pecfac=case.edge["pecfac"])
+    d = {k: dev(v) for k, v in host.items()}
+    fm = nw.MomentumFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dudx", "viscosity", "density", "mask",
+                                                        "area", "mdot", "pecfac")))
+    mo = case.opts["momentum"]
+    N, E = mesh.num_nodes, mesh.num_edges
+
+    def fresh():
+        ls = nw.LinearSystem(3)
+        ls.build_edge_graph(N, mesh.edges)
+        ls.finalize()
+        ls.zero_system()
+        return ls
+
+    ref = fresh()
+    ref.assemble_momentum(fm, mo)
+    v_ref, r_ref = ref.to_host()
+    # rows complete after edge chunk [.., b): every incident edge index < b
+    maxinc = np.full(N, -1)
+    np.maximum.at(maxinc, mesh.edges[:, 0], np.arange(E))
+    np.maximum.at(maxinc, mesh.edges[:, 1], np.arange(E))
+    ready = lambda b: int(np.searchsorted(np.maximum.accumulate(maxinc), b))  # rows r with prefix max < b
+    ls = fresh()
+    bounds = [0, 1000, 2500, 4000, E]
+    done = 0
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        ls.assemble_momentum_range(fm, mo, a, b)
+        r = ready(b) if b < E else N
+        ls.assemble_momentum_rows_range(mo, done, r)
+        done = r
+    v, rh = ls.to_host()
+    assert np.array_equal(v, v_ref) and np.array_equal(rh, r_ref)
+    # out of order on a zeroed system
+    ls = fresh()
+    ls.assemble_momentum_range(fm, mo, 0, E)
+    with pytest.raises(nw.NwError, match="row ranges"):
+        ls.assemble_momentum_rows_range(mo, 10, 20)
+    # part-way, then read: the rows not covered are zero
+    half = N // 2
+    ls.assemble_momentum_rows_range(mo, 0, half)
+    v, rh = ls.to_host()
+    rp, _ = ls.graph()
+    cut = rp[3 * half]
+    assert np.array_equal(v[:cut], v_ref[:cut]) and not np.any(v[cut:])
+    assert np.array_equal(rh[:3 * half], r_ref[:3 * half]) and not np.any(rh[3 * half:])
+    # on an assembled system a range adds
+    ls.assemble_momentum_rows_range(mo, 0, N)
+    v2, rh2 = ls.to_host()
+    np.testing.assert_array_equal(v2[cut:], v_ref[cut:])
+    np.testing.assert_allclose(v2[:cut], 2 * v_ref[:cut], rtol=1e-15, atol=0)
