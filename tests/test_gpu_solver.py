@@ -215,8 +215,12 @@ def test_bicgstab_and_tfqmr_match_oracle(nw, orc, method, pc):
     history entries to 1e-8 relative, solution to 1e-7 relative. BiCGStab
     amplifies a change of summation order by about 2.5x per iteration (the
     oracle run on 1 and on 7 threads differs by 3e-8 at iteration 25 and by
-    up to 5 iterations in the count), so for it: the first 15 entries to
-    1e-8, the count within 5% + 2, the solution to 1e-5 relative."""
+    up to 5 iterations in the count; a rounding-level change of the mesh
+    geometry moved the Jacobi count from 123 to 133), so for it: the first
+    15 entries to 1e-8, the count within 10% + 2, the solution to 1e-5
+    relative. These bounds are for the natural-order (OpenMP) oracle; the
+    restatement in the GPU's operation order is matched to 1e-12 in every
+    entry and in the iteration count (_check_gpu_order)."""
     import torch
     m = {"bicgstab": nw.BICGSTAB, "tfqmr": nw.TFQMR}[method]
     ls, case = _poisson_system(nw)
@@ -234,7 +238,7 @@ def test_bicgstab_and_tfqmr_match_oracle(nw, orc, method, pc):
                      _gpu_order(orc, ls, m, pc, 50, 3000, 1e-9), f"{method} pc {pc}")
     strict = method == "tfqmr" and pc != 0
     assert orep.converged == 1
-    assert abs(rep.iterations - orep.iterations) <= (1 if strict else 2 + 0.05 * orep.iterations)
+    assert abs(rep.iterations - orep.iterations) <= (1 if strict else 2 + 0.10 * orep.iterations)
     k = min(len(ho), len(ls.residual_history()), 30 if strict else 15)
     np.testing.assert_allclose(ls.residual_history()[:k], ho[:k], rtol=1e-8, atol=0)
     xg = x.cpu().numpy()
