@@ -402,6 +402,7 @@ def run_ours(args, rank, world):
                      "traffic": (tt["bytes_per_launch"] if tt else None)},
         "continuity": {"avg_ms": round(con_avg, 4), "algorithmic_bytes": B_c,
                        "achieved_gbs": round(B_c / (con_avg * 1e-3) / 1e9, 1),
+                       "frac": round(B_c / (con_avg * 1e-3) / 1e9 / pk["hbm_gbs"], 4),
                        "gnnz_s": round(nnz_c / (con_avg * 1e-3) / 1e9, 4)},
         "momentum": {"avg_ms": round(mom_avg, 4), "gnnz_s": round(nnz_m / (mom_avg * 1e-3) / 1e9, 4),
                      "single_kernel": single},
