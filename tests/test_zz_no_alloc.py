@@ -8,8 +8,9 @@ arrays. The test calls it through the C ABI twice in a row, with different
 inputs, and checks each result against the regular entry point
 (nw_assemble_continuity_edges) within the assembly tests' tolerance
 (1e-12 times the oracle's running magnitude of each entry). It also checks
-that the calls leave the device's free memory unchanged and that meshes
-above the stated edge limit are refused.
+that the calls leave the device's free memory unchanged, that meshes
+above the stated edge limit are refused, and that the call captures into a
+CUDA graph whose replays equal eager calls.
 
 Named test_zz_* so pytest collects it last.
 """
@@ -99,3 +100,55 @@ def test_noalloc_rejects_meshes_above_the_limit(nw):
     with pytest.raises(nw.NwError) as e:
         ls.assemble_continuity_noalloc(f, nw.ContinuityOpts(1.0, 1.0, 1.0, 0.0), vals, rhs)
     assert e.value.status == 1 and "524288" in str(e.value)
+
+
+def test_noalloc_call_captures_into_a_cuda_graph(nw):
+    """The call allocates nothing and makes no synchronous call, so it can be
+    captured into a CUDA graph on the handle's stream: captured once after a
+    warm-up call, the graph is replayed with new field values written into
+    the same device buffers, and each replay equals an eager call bit for
+    bit (the same kernels on the same inputs)."""
+    import torch
+    case, f = _inputs(nw, seed=4)
+    mesh = case.mesh
+    co = case.opts["continuity"]
+    ls = nw.LinearSystem(1)
+    ls.build_edge_graph(mesh.num_nodes, mesh.edges)
+    ls.finalize()
+    nr, nnz = ls.sizes()
+    s = torch.cuda.Stream()
+    ls.set_stream(s.cuda_stream)
+    d = to_dev_dict(f)
+    fields = continuity_fields(nw, d)
+    vals = torch.zeros(nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        ls.assemble_continuity_noalloc(fields, co, vals, rhs)  # one-time set-up outside the capture
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        ls.assemble_continuity_noalloc(fields, co, vals, rhs)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(21)
+    prev = None
+    for _ in range(2):
+        d["velocity"].copy_(torch.from_numpy(rng.normal(size=f["velocity"].shape)))
+        d["pressure"].copy_(torch.from_numpy(rng.normal(size=mesh.num_nodes)))
+        d["udiag"].copy_(torch.from_numpy(rng.uniform(1.0, 3.0, mesh.num_nodes)))
+        vals.fill_(7.0)
+        rhs.fill_(-3.0)
+        g.replay()
+        torch.cuda.synchronize()
+        got_v, got_r = vals.cpu().numpy().copy(), rhs.cpu().numpy().copy()
+        ev = torch.full((nnz,), 5.0, dtype=torch.float64, device="cuda")
+        er = torch.full((nr,), 5.0, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        with torch.cuda.stream(s):
+            ls.assemble_continuity_noalloc(fields, co, ev, er)
+        s.synchronize()
+        np.testing.assert_array_equal(got_v, ev.cpu().numpy())
+        np.testing.assert_array_equal(got_r, er.cpu().numpy())
+        if prev is not None:
+            assert not np.array_equal(prev, got_v)
+        prev = got_v
