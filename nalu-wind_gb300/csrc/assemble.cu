@@ -614,10 +614,13 @@ __device__ __forceinline__ dd ldc(const dd* p) {
 // block; any others only take part in the staging copy).
 // IDX: the type of the coefficient offsets (uint32_t when 11 E < 2^31:
 // one register and one wide multiply-add per load instead of a 64-bit
-// pointer per coefficient array).
-template <int NB, bool NC, typename IDX = int64_t>
+// pointer per coefficient array). ACC: 0 overwrite, 1 add to the values
+// present, -1 as a.accumulate says (the write mode as a constant drops the
+// read and select of every store).
+template <int NB, bool NC, typename IDX = int64_t, int ACC = -1>
 __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double* stage) {
   const dd* cb = a.cb;
+  const bool accumulate = ACC < 0 ? a.accumulate != 0 : ACC != 0;
   const IDX E = IDX(a.E);
   const int64_t mask = a.mask;
   const int64_t r1 = (r0 + NB < a.R) ? r0 + NB : a.R;
@@ -638,7 +641,7 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
     const int32_t s = a.inc_ptr[r], t = a.inc_ptr[r + 1];
     const int64_t bq = a.row_ptr[3 * r + q];
     double* v = staged ? stage + (bq - base) : a.values + bq;
-    const bool acc = a.accumulate && !staged;
+    const bool acc = accumulate && !staged;
     if (s != t) {
       const int dp = a.diag_pos[r];
       // sums over the incident edges: the diagonal entry's N_qq + c_other,
@@ -685,22 +688,25 @@ __device__ __forceinline__ void row3_block(int64_t r0, const Row3Args& a, double
       put3(3 * dp, -(acc_value(sdg) * a.irelax), -(acc_value(s1) * a.irelax),
            -(acc_value(s2) * a.irelax));
       const double d = dd_to_double_int(acc_value(rr));
-      a.rhs[3 * r + q] = a.accumulate ? a.rhs[3 * r + q] + d : d;
+      a.rhs[3 * r + q] = accumulate ? a.rhs[3 * r + q] + d : d;
     } else if (!acc) {
       for (int64_t k = 0; k < a.row_ptr[3 * r + q + 1] - bq; ++k) v[k] = 0.0;
-      if (!a.accumulate) a.rhs[3 * r + q] = 0.0;
+      if (!accumulate) a.rhs[3 * r + q] = 0.0;
     }
   }
   if (!staged) return;
   __syncthreads();
-  for (int64_t k = threadIdx.x; k < cnt; k += blockDim.x)
-    a.values[base + k] = a.accumulate ? a.values[base + k] + stage[k] : stage[k];
+  // a staged range fits the shared array: 32-bit counts
+  double* out = a.values + base;
+  const int n = int(cnt);
+  for (int k = int(threadIdx.x); k < n; k += int(blockDim.x))
+    out[k] = accumulate ? out[k] + stage[k] : stage[k];
 }
 
-template <typename IDX>
+template <typename IDX, int ACC>
 __global__ void __launch_bounds__(3 * kRow3Nodes) row3t_k(Row3Args a) {
   extern __shared__ double stage[];
-  row3_block<kRow3Nodes, true, IDX>(a.r_begin + int64_t(blockIdx.x) * kRow3Nodes, a, stage);
+  row3_block<kRow3Nodes, true, IDX, ACC>(a.r_begin + int64_t(blockIdx.x) * kRow3Nodes, a, stage);
 }
 
 // ---------------------------------------------------------------------------
@@ -868,8 +874,10 @@ void set_smem_attrs() {
   if (g_smem_set_device == dev) return;
   NW_CUDA(cudaFuncSetAttribute(row1_k<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
   NW_CUDA(cudaFuncSetAttribute(row1_k<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
-  NW_CUDA(cudaFuncSetAttribute(row3t_k<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
-  NW_CUDA(cudaFuncSetAttribute(row3t_k<int64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
+  NW_CUDA(cudaFuncSetAttribute(row3t_k<uint32_t, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
+  NW_CUDA(cudaFuncSetAttribute(row3t_k<uint32_t, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
+  NW_CUDA(cudaFuncSetAttribute(row3t_k<int64_t, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
+  NW_CUDA(cudaFuncSetAttribute(row3t_k<int64_t, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem));
 #define NW_FUSED_ATTR(LIM, DIV, DEF)                                                      \
   NW_CUDA(cudaFuncSetAttribute(momentum_fused_k<LIM, DIV, DEF>,                           \
                                cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxRowSmem))
@@ -1049,10 +1057,15 @@ void launch_rows(cudaStream_t s, int kind, int64_t R, const int32_t* inc_ptr,
                            accumulate, smem_bytes);
     a.r_begin = row_begin;
     const unsigned grid = grid_for(R - row_begin, kRow3Nodes);
-    if (int64_t(kMomentumCoefs) * E < (int64_t(1) << 31))
-      row3t_k<uint32_t><<<grid, 3 * kRow3Nodes, smem_bytes, s>>>(a);
+    const bool narrow = int64_t(kMomentumCoefs) * E < (int64_t(1) << 31);
+    if (narrow && !accumulate)
+      row3t_k<uint32_t, 0><<<grid, 3 * kRow3Nodes, smem_bytes, s>>>(a);
+    else if (narrow)
+      row3t_k<uint32_t, 1><<<grid, 3 * kRow3Nodes, smem_bytes, s>>>(a);
+    else if (!accumulate)
+      row3t_k<int64_t, 0><<<grid, 3 * kRow3Nodes, smem_bytes, s>>>(a);
     else
-      row3t_k<int64_t><<<grid, 3 * kRow3Nodes, smem_bytes, s>>>(a);
+      row3t_k<int64_t, 1><<<grid, 3 * kRow3Nodes, smem_bytes, s>>>(a);
   }
 }
 
