@@ -105,7 +105,9 @@ typedef struct nw_solve_report {
   double final_rel_residual;  /* last tested relative residual */
   double final_abs_residual;  /* explicit ||b - A x||_2 in FP64 */
   double rhs_norm;            /* ||b||_2 (nonLinearResidual / l2Scaling) */
-  double solve_ms;            /* device time of the solve */
+  double solve_ms;            /* device time of the solve, with the per-solve refresh
+                                 of the solver's value copies (diagonal, sliced
+                                 layouts, coarse operator) */
   int fallback;               /* learned preconditioner failed; SGS result */
 } nw_solve_report;
 

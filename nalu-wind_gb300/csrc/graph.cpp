@@ -159,14 +159,16 @@ void build_graph(HostGraph& g, int num_dof, int64_t num_nodes,
   }
 }
 
-int color_node_graph(const HostGraph& g, std::vector<int32_t>& color) {
-  const int64_t R = g.node_rows;
-  color.assign(R, -1);
-  std::vector<int64_t> mark;
+namespace {
+
+// First-fit colouring of the node rows visited in `order` (every row once).
+int greedy_colors(const HostGraph& g, const std::vector<int32_t>& order, std::vector<int32_t>& color) {
+  color.assign(g.node_rows, -1);
   int ncolors = 0;
-  for (int64_t r = 0; r < R; ++r) {
+  std::vector<int32_t> extra;
+  for (const int32_t r : order) {
     int64_t used = 0;  // bitmask for the first 64 colours
-    std::vector<int32_t> extra;
+    extra.clear();
     for (int64_t p = g.nrow_ptr[r]; p < g.nrow_ptr[r + 1]; ++p) {
       const int32_t c = g.ncol[p];
       if (c == r || color[c] < 0) continue;
@@ -185,6 +187,41 @@ int color_node_graph(const HostGraph& g, std::vector<int32_t>& color) {
     ncolors = std::max(ncolors, k + 1);
   }
   return ncolors;
+}
+
+}  // namespace
+
+// First fit in row order, then Culberson's iterated greedy: recolouring the
+// rows class by class (highest colour first) with first fit never needs more
+// colours than the classes it started from, and repeated passes drain the
+// small last classes of a first-fit colouring of an unstructured mesh in
+// random order (a 2.1M-node tet block: 12 classes, the last three of 19,215,
+// 917 and 3 rows; each class is one launch of every Gauss-Seidel sweep).
+// The result replaces the first-fit colouring only when it has fewer
+// classes, so one that is already minimal (the two classes of a hex box, or
+// an RCM-ordered tet block) stays as it is.
+int color_node_graph(const HostGraph& g, std::vector<int32_t>& color) {
+  constexpr int kPasses = 8;
+  const int64_t R = g.node_rows;
+  std::vector<int32_t> order(R);
+  for (int64_t r = 0; r < R; ++r) order[r] = int32_t(r);
+  const int first = greedy_colors(g, order, color);
+  if (first <= 2) return first;
+  std::vector<int32_t> cur(color), next;
+  int ncolors = first;
+  for (int pass = 0; pass < kPasses; ++pass) {
+    std::vector<int64_t> start(ncolors + 1, 0);
+    for (int64_t r = 0; r < R; ++r) start[ncolors - cur[r]]++;  // class c at position ncolors-1-c
+    for (int c = 0; c < ncolors; ++c) start[c + 1] += start[c];
+    for (int64_t r = 0; r < R; ++r) order[start[ncolors - 1 - cur[r]]++] = int32_t(r);
+    ncolors = greedy_colors(g, order, next);  // never more than before
+    cur.swap(next);
+  }
+  if (ncolors < first) {
+    color.swap(cur);
+    return ncolors;
+  }
+  return first;
 }
 
 }  // namespace nw

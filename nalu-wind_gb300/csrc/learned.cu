@@ -540,15 +540,22 @@ __global__ void to_bf16_k(const float* __restrict__ p, uint16_t* __restrict__ w,
   wt[l * kIn2 * kHid + n * kIn2 + k] = b;
 }
 
-// Galerkin sums Ac[q] = sum of the fine values mapped to coarse slot q
-__global__ void galerkin_k(int64_t nnzc, const int64_t* __restrict__ gptr,
-                           const int32_t* __restrict__ gfine, const double* __restrict__ v,
-                           double* __restrict__ ac) {
-  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+// Galerkin sums Ac[q] = sum of the fine values mapped to coarse slot q:
+// warp per slot, lanes stride the contribution list, fixed-order butterfly
+// sum. (A diagonal slot collects every entry inside its aggregate, ~10^3
+// after two aggregation passes, so a thread per slot serialised the kernel
+// on those few slots.)
+__global__ void __launch_bounds__(kB)
+    galerkin_k(int64_t nnzc, const int64_t* __restrict__ gptr,
+               const int32_t* __restrict__ gfine, const double* __restrict__ v,
+               double* __restrict__ ac) {
+  const int64_t q = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (q >= nnzc) return;
   double s = 0.0;
-  for (int64_t k = gptr[q]; k < gptr[q + 1]; ++k) s += v[gfine[k]];
-  ac[q] = s;
+  for (int64_t k = gptr[q] + lane; k < gptr[q + 1]; k += 32) s += v[gfine[k]];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if (lane == 0) ac[q] = s;
 }
 
 __global__ void coarse_weights_k(int64_t nc, const int64_t* __restrict__ cptr,
@@ -859,7 +866,7 @@ void CoarseLevel::setup(const HostGraph& g, int npasses, cudaStream_t s, const d
 }
 
 void CoarseLevel::refresh(const double* fine_values, cudaStream_t s) {
-  galerkin_k<<<gridn(nnzc), kB, 0, s>>>(nnzc, gptr.p, gfine.p, fine_values, ac.p);
+  galerkin_k<<<gridn(nnzc * 32), kB, 0, s>>>(nnzc, gptr.p, gfine.p, fine_values, ac.p);
   coarse_weights_k<<<gridn(nc), kB, 0, s>>>(nc, cptr.p, cdiag.p, ac.p, wgt.p, dinv.p);
   NW_CUDA(cudaGetLastError());
 }

@@ -768,14 +768,16 @@ nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
     check_fused(ls);
     if (ls->cfg.preconditioner == NW_PC_LEARNED && !ls->coarse)
       fail(NW_INVALID_ARG, "NW_PC_LEARNED needs nw_linsys_attach_learned");
-    ls->solver.refresh(ls->stream);
     ls->pc.kind = ls->cfg.preconditioner;
     ls->pc.inner_sweeps = ls->cfg.sgs2_inner_sweeps > 0 ? ls->cfg.sgs2_inner_sweeps : 1;
     const double tol = final_iter ? ls->cfg.final_tolerance : ls->cfg.tolerance;
     cudaEvent_t a, b;
     NW_CUDA(cudaEventCreate(&a));
     NW_CUDA(cudaEventCreate(&b));
+    // the timed solve includes the per-solve refresh of the solver's copies
+    // of the values (diagonal, sliced layouts, coarse Galerkin operator)
     NW_CUDA(cudaEventRecord(a, ls->stream));
+    ls->solver.refresh(ls->stream);
     SolveResult r = ls->solver.solve(ls->cfg, tol, ls->pc, ls->rhs.p, x, ls->stream);
     NW_CUDA(cudaEventRecord(b, ls->stream));
     NW_CUDA(cudaEventSynchronize(b));
