@@ -818,7 +818,8 @@ __global__ void givens_solve_k(GivensDev G, int kk, double yscale, double* __res
 template <typename StepFn>
 KrylovSolver::Cycle KrylovSolver::run_cycle(int m, int max_steps, double g0, double tol, double div,
                                             double hist_mul, double hist_div, StepFn arnoldi,
-                                            const double* hs, const double* hn, cudaStream_t s) {
+                                            const double* hs, const double* hn, cudaStream_t s,
+                                            bool graph) {
   constexpr int kChunk = 2;  // iterations per poll; the host waits one chunk behind
   GivensDev G{gst_.p,
               gst_.p + size_t(m_ + 1) * m_,
@@ -829,9 +830,49 @@ KrylovSolver::Cycle KrylovSolver::run_cycle(int m, int max_steps, double g0, dou
   givens_init_k<<<1, 32, 0, s>>>(G, g0);
   int launched = 0, pending = -1, slot = 0;
   bool stop = false;
-  for (int j = 0; j < m && launched < max_steps && !stop; ++j) {
+  auto step = [&](int j) {
     arnoldi(j);
     givens_step_k<<<1, 32, 0, s>>>(G, j, hs, hn, tol, div, hist_mul, hist_div);
+  };
+  for (int j = 0; j < m && launched < max_steps && !stop; ++j) {
+    // the first step of a cycle runs as plain launches: any one-time set-up
+    // (buffer growth) happens there, outside a capture. A stream that cannot
+    // be captured (the legacy default stream) keeps plain launches.
+    if (graph && j > 0 && cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      graph = false;
+    }
+    if (graph && j > 0) {
+      cudaGraph_t g = nullptr;
+      try {
+        step(j);
+      } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      NW_CUDA(cudaStreamEndCapture(s, &g));
+      if (iter_exec_) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(iter_exec_, g, &info) != cudaSuccess) {
+          cudaGetLastError();  // a different node layout: instantiate anew
+          cudaGraphExecDestroy(iter_exec_);
+          iter_exec_ = nullptr;
+        }
+      }
+      if (!iter_exec_) {
+        const cudaError_t e = cudaGraphInstantiate(&iter_exec_, g, 0);
+        if (e != cudaSuccess) {
+          cudaGraphDestroy(g);
+          iter_exec_ = nullptr;
+          NW_CUDA(e);
+        }
+      }
+      cudaGraphDestroy(g);
+      NW_CUDA(cudaGraphLaunch(iter_exec_, s));
+    } else {
+      step(j);
+    }
     ++launched;
     if (launched % kChunk == 0) {
       NW_CUDA(cudaMemcpyAsync(ctl_pinned_ + 4 * slot, gctl_.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -870,6 +911,7 @@ void cycle_solution(double* gst, int* gctl, int m, int kk, double yscale, double
 
 // ---------------------------------------------------------------------------
 KrylovSolver::~KrylovSolver() {
+  if (iter_exec_) cudaGraphExecDestroy(iter_exec_);
   if (h_pinned_) cudaFreeHost(h_pinned_);
   if (ctl_pinned_) cudaFreeHost(ctl_pinned_);
   for (cudaEvent_t& e : chunk_ev_)
@@ -2048,7 +2090,8 @@ SolveResult KrylovSolver::mixed(const nw_solver_cfg& cfg, double tol,
       scale_jacobi_k<float><<<grid1(n), kBlock, 0, s>>>(n, w32_.p, V + size_t(j + 1) * ld, h2,
                                                         fuse_jacobi ? rdiag32_.p : nullptr, z32_.p);
     };
-    const Cycle c = run_cycle(m, cfg.max_iterations - its, 1.0, itol, 1.0, rnorm, bnorm, arnoldi, hs, h2, s);
+    const Cycle c = run_cycle(m, cfg.max_iterations - its, 1.0, itol, 1.0, rnorm, bnorm, arnoldi, hs, h2, s,
+                              true);
     its += c.iterations;
     res.history.insert(res.history.end(), c.hist.begin(), c.hist.end());
     if (c.status != NW_OK) res.status = c.status;

@@ -141,9 +141,14 @@ class KrylovSolver {
   // One restart cycle's Arnoldi steps (arnoldi(j) launches iteration j's
   // kernels, ending with the new column in hs[0..j] and its norm at h2[0])
   // with the Givens update on the device and the host one chunk behind.
+  // With `graph`, the steps after the first of the cycle are captured from
+  // the same launches into a CUDA graph each, which updates iter_exec_ in
+  // place and is launched as one unit (the kernels then follow each other
+  // without the per-launch gaps of a stream).
   template <typename StepFn>
   Cycle run_cycle(int m, int max_steps, double g0, double tol, double div, double hist_mul, double hist_div,
-                  StepFn arnoldi, const double* hs, const double* hn, cudaStream_t s);
+                  StepFn arnoldi, const double* hs, const double* hn, cudaStream_t s, bool graph = false);
+  cudaGraphExec_t iter_exec_ = nullptr;
   // Sliced ELLPACK copy (slices of 32 rows, column-major within a slice)
   // used by the solver's SpMV: coalesced value/column loads for short rows.
   // sell_map_ holds the CSR index of every slot (-1 for padding).
