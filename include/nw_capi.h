@@ -225,6 +225,23 @@ nw_status nw_assemble_scalar_edges(nw_linsys* ls, const nw_scalar_fields* f,
 nw_status nw_assemble_continuity_edges(nw_linsys* ls,
                                        const nw_continuity_fields* f,
                                        const nw_continuity_opts* o);
+/* The same assembly in parts, for a caller that streams its inputs to the
+ * device (ContinuityEdgeSolverAlg::execute split at its edge loop):
+ * nw_assemble_continuity_edge_range evaluates the coefficients of edges
+ * [edge_begin, edge_end) into the handle's edge buffer. The ranges of one
+ * assembly come in order from edge 0 (a later range must start where the
+ * previous one ended, else NW_INVALID_ARG). Each range reads the node
+ * fields of nodes 0 .. m only, m the largest node index of edges
+ * 0 .. edge_end - 1 (it also evaluates the per-node quantities of the node
+ * pre-pass form for the nodes that m newly covers), so a caller can copy
+ * the node fields in index order, a slice ahead of each edge range.
+ * nw_assemble_continuity_rows then sums the coefficients into the CSR values
+ * and rhs (NW_INVALID_ARG unless the ranges covered every edge). Together
+ * they equal nw_assemble_continuity_edges bit for bit. */
+nw_status nw_assemble_continuity_edge_range(nw_linsys* ls, const nw_continuity_fields* f,
+                                            const nw_continuity_opts* o, int64_t edge_begin,
+                                            int64_t edge_end);
+nw_status nw_assemble_continuity_rows(nw_linsys* ls);
 /* No counterpart in the reference. The continuity assembly above for
  * callers that cannot allocate device memory when they assemble (a host
  * code whose device memory all comes from its own pool allocator, sized up

@@ -181,6 +181,9 @@ SIGNATURES = {
     "nw_assemble_scalar_edges": (C.c_int, [C.c_void_p, C.POINTER(ScalarFields), C.POINTER(ScalarOpts)]),
     "nw_assemble_continuity_edges": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
                                                C.POINTER(ContinuityOpts)]),
+    "nw_assemble_continuity_edge_range": (C.c_int, [C.c_void_p, C.POINTER(ContinuityFields),
+                                                    C.POINTER(ContinuityOpts), C.c_int64, C.c_int64]),
+    "nw_assemble_continuity_rows": (C.c_int, [C.c_void_p]),
     "nw_assemble_momentum_edges": (C.c_int, [C.c_void_p, C.POINTER(MomentumFields), C.POINTER(MomentumOpts)]),
     "nw_assemble_momentum_edge_range": (C.c_int, [C.c_void_p, C.POINTER(MomentumFields), C.POINTER(MomentumOpts),
                                                   C.c_int64, C.c_int64]),
@@ -430,6 +433,15 @@ class LinearSystem:
 
     def assemble_continuity(self, f: ContinuityFields, o: ContinuityOpts) -> None:
         check(self.lib.nw_assemble_continuity_edges(self.h, C.byref(f), C.byref(o)))
+
+    def assemble_continuity_range(self, f: ContinuityFields, o: ContinuityOpts, edge_begin: int,
+                                  edge_end: int) -> None:
+        """Edge phase over edges [edge_begin, edge_end), ranges in order from
+        edge 0; finish with assemble_continuity_rows."""
+        check(self.lib.nw_assemble_continuity_edge_range(self.h, C.byref(f), C.byref(o), edge_begin, edge_end))
+
+    def assemble_continuity_rows(self) -> None:
+        check(self.lib.nw_assemble_continuity_rows(self.h))
 
     def assemble_continuity_noalloc(self, f: ContinuityFields, o: ContinuityOpts, values_dev, rhs_dev) -> None:
         """Continuity assembly into caller-owned device arrays with no device

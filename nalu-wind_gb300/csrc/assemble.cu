@@ -188,15 +188,16 @@ __device__ __forceinline__ void st4(dd* p, dd a, dd b, dd c, dd d) {
   q[1] = make_float4(c.hi, c.lo, d.hi, d.lo);
 }
 
+// nodes [n0, n1)
 __global__ void __launch_bounds__(kThreads)
-    continuity_node_k(int64_t N, const double* __restrict__ velocity,
+    continuity_node_k(int64_t n0, int64_t n1, const double* __restrict__ velocity,
                       const double* __restrict__ Gpdx,
                       const double* __restrict__ density,
                       const double* __restrict__ pressure,
                       const double* __restrict__ udiag,
                       dd* __restrict__ nodebuf) {
-  const int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (n >= N) return;
+  const int64_t n = n0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= n1) return;
   const dd iu = dd_rcp(ldd(udiag + n));
   const dd rho = ldd(density + n);
   dd* out = nodebuf + kNodeStride * n;
@@ -910,19 +911,24 @@ bool continuity_fast_path(const ContinuityOpts& o) {
 
 dd dd_param(double x) { return dd_from_double(x); }
 
-void launch_continuity_edges(cudaStream_t s, int64_t E, int64_t N,
-                             const int2* edges, const nw_continuity_fields& f,
-                             const ContinuityOpts& o, double* buf,
-                             double* nodebuf) {
-  if (E == 0) return;
-  dd* b = reinterpret_cast<dd*>(buf);
+void launch_continuity_edge_range(cudaStream_t s, int64_t n0, int64_t n1, int64_t e0, int64_t e1,
+                                  const int2* edges, const nw_continuity_fields& f,
+                                  const ContinuityOpts& o, double* buf, double* nodebuf) {
+  // the edge kernels index edges, area vectors and records from 0: shift
+  // the per-edge pointers to the range
+  const int64_t n = e1 > e0 ? e1 - e0 : 0;
+  dd* b = reinterpret_cast<dd*>(buf) + 2 * e0;
+  const int2* er = edges + e0;
+  const double* ar = f.area + 3 * e0;
   if (nodebuf && continuity_fast_path(o)) {
     dd* nb = reinterpret_cast<dd*>(nodebuf);
-    continuity_node_k<<<grid_for(N), kThreads, 0, s>>>(
-        N, f.velocity, f.dpdx, f.density, f.pressure, f.udiag, nb);
-    continuity_edge_fast_k<<<grid_for(E), kThreads, 0, s>>>(
-        E, edges, f.coords, nb, f.pressure, f.area, dd_param(o.noc_fac), dd_param(1.0 / o.tau_scale), b);
-  } else {
+    if (n1 > n0)
+      continuity_node_k<<<grid_for(n1 - n0), kThreads, 0, s>>>(
+          n0, n1, f.velocity, f.dpdx, f.density, f.pressure, f.udiag, nb);
+    if (n)
+      continuity_edge_fast_k<<<grid_for(n), kThreads, 0, s>>>(
+          n, er, f.coords, nb, f.pressure, ar, dd_param(o.noc_fac), dd_param(1.0 / o.tau_scale), b);
+  } else if (n) {
     ContinuityDD c;
     c.noc = dd_param(o.noc_fac);
     c.inv_tau = dd_param(1.0 / o.tau_scale);
@@ -930,10 +936,18 @@ void launch_continuity_edges(cudaStream_t s, int64_t E, int64_t N,
     c.om_interp = dd_param(1.0 - o.interp_together);
     c.incomp = dd_param(o.solve_incompressible);
     c.om_incomp = dd_param(1.0 - o.solve_incompressible);
-    continuity_edge_k<<<grid_for(E), kThreads, 0, s>>>(
-        E, edges, f.coords, f.velocity, f.dpdx, f.density, f.pressure, f.udiag,
-        f.area, c, b);
+    continuity_edge_k<<<grid_for(n), kThreads, 0, s>>>(
+        n, er, f.coords, f.velocity, f.dpdx, f.density, f.pressure, f.udiag,
+        ar, c, b);
   }
+}
+
+void launch_continuity_edges(cudaStream_t s, int64_t E, int64_t N,
+                             const int2* edges, const nw_continuity_fields& f,
+                             const ContinuityOpts& o, double* buf,
+                             double* nodebuf) {
+  if (E == 0) return;
+  launch_continuity_edge_range(s, 0, N, 0, E, edges, f, o, buf, nodebuf);
 }
 
 void launch_continuity_edges(cudaStream_t s, int64_t E, const int2* edges,

@@ -31,6 +31,12 @@ void launch_continuity_edges(cudaStream_t s, int64_t E, int64_t N,
                              const int2* edges, const nw_continuity_fields& f,
                              const ContinuityOpts& o, double* buf,
                              double* nodebuf);
+// The same over edges [e0, e1) of E (one 16-byte record per edge at its
+// index), the node phase of the node-phase route over nodes [n0, n1) first
+// (every node an edge of the range reads must have had its node phase).
+void launch_continuity_edge_range(cudaStream_t s, int64_t n0, int64_t n1, int64_t e0, int64_t e1,
+                                  const int2* edges, const nw_continuity_fields& f,
+                                  const ContinuityOpts& o, double* buf, double* nodebuf);
 constexpr int kContinuityNodeStride = 8;
 // Edge phase of the momentum assembly over edges [e0, e1) of E (the
 // coefficient buffer is laid out with stride E).

@@ -53,6 +53,12 @@ struct nw_linsys {
   // with pristine: node rows below this were written by in-order row-range
   // calls (nw_assemble_momentum_rows_range); the rest are still zero
   int64_t pristine_from = 0;
+  // continuity assembled in edge ranges (nw_assemble_continuity_edge_range):
+  // the end of the ranges evaluated so far, in order from edge 0; -1 none.
+  // edge_node_max[e]: the largest node index of edges 0..e (built on first
+  // use): a range's node pre-pass covers the nodes that become reachable
+  int64_t cont_next = -1;
+  std::vector<int32_t> edge_node_max;
   HostGraph g;
   DeviceArray<int64_t> row_ptr, node_lid, row_nodes_ptr;
   DeviceArray<int32_t> row_nodes;
@@ -499,31 +505,79 @@ nw_status nw_assemble_scalar_edges(nw_linsys* ls, const nw_scalar_fields* f,
   });
 }
 
+static void check_continuity_args(const nw_linsys* ls, const nw_continuity_fields* f,
+                                  const nw_continuity_opts* o) {
+  need_finalized(ls);
+  if (ls->num_dof != 1) fail(NW_INVALID_ARG, "continuity assembly needs num_dof 1");
+  if (!f || !o) fail(NW_INVALID_ARG, "null argument");
+  check_ptr(f->coords, "coords");
+  check_ptr(f->velocity, "velocity");
+  check_ptr(f->dpdx, "dpdx");
+  check_ptr(f->density, "density");
+  check_ptr(f->pressure, "pressure");
+  check_ptr(f->udiag, "udiag");
+  check_ptr(f->area, "area");
+  if (!(o->tau_scale != 0.0)) fail(NW_INVALID_ARG, "tau_scale is zero");
+}
+
+static void continuity_rows(nw_linsys* ls) {
+  launch_rows(ls->stream, 1, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
+              ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, ls->g.num_edges, 1.0,
+              ls->values.p, ls->rhs.p, write_mode(ls), ls->stage_bytes[1]);
+  NW_CUDA(cudaGetLastError());
+  ls->pristine = false;
+}
+
 nw_status nw_assemble_continuity_edges(nw_linsys* ls,
                                        const nw_continuity_fields* f,
                                        const nw_continuity_opts* o) {
   return guard([&] {
-    need_finalized(ls);
-    if (ls->num_dof != 1) fail(NW_INVALID_ARG, "continuity assembly needs num_dof 1");
-    if (!f || !o) fail(NW_INVALID_ARG, "null argument");
-    check_ptr(f->coords, "coords");
-    check_ptr(f->velocity, "velocity");
-    check_ptr(f->dpdx, "dpdx");
-    check_ptr(f->density, "density");
-    check_ptr(f->pressure, "pressure");
-    check_ptr(f->udiag, "udiag");
-    check_ptr(f->area, "area");
-    if (!(o->tau_scale != 0.0)) fail(NW_INVALID_ARG, "tau_scale is zero");
+    check_continuity_args(ls, f, o);
     begin_timing(ls);
     const int64_t E = ls->g.num_edges;
+    ls->cont_next = -1;
     launch_continuity_edges(ls->stream, E, ls->g.num_nodes, ls->edges.p, *f, *o,
                             ls->buf.p, ls->nodebuf.p);
-    launch_rows(ls->stream, 1, ls->g.node_rows, ls->inc_ptr.p, ls->inc.p,
-                ls->diag_pos.p, ls->row_ptr.p, ls->buf.p, E, 1.0,
-                ls->values.p, ls->rhs.p, write_mode(ls), ls->stage_bytes[1]);
-    NW_CUDA(cudaGetLastError());
+    continuity_rows(ls);
     end_timing(ls);
-    ls->pristine = false;
+  });
+}
+
+nw_status nw_assemble_continuity_edge_range(nw_linsys* ls, const nw_continuity_fields* f,
+                                            const nw_continuity_opts* o, int64_t edge_begin,
+                                            int64_t edge_end) {
+  return guard([&] {
+    check_continuity_args(ls, f, o);
+    const int64_t E = ls->g.num_edges;
+    if (edge_begin < 0 || edge_end > E || edge_begin > edge_end)
+      fail(NW_INVALID_ARG, "edge range out of bounds");
+    if (edge_begin != 0 && edge_begin != ls->cont_next)
+      fail(NW_INVALID_ARG, "continuity edge ranges must follow each other from edge 0");
+    std::vector<int32_t>& pm = ls->edge_node_max;
+    if (int64_t(pm.size()) != E) {
+      pm.resize(E);
+      int32_t m = -1;
+      for (int64_t e = 0; e < E; ++e) pm[e] = m = std::max({m, ls->g.edges[2 * e], ls->g.edges[2 * e + 1]});
+    }
+    // node pre-pass over the nodes the range's edges reach beyond the
+    // earlier ranges' (the largest node index so far, plus one)
+    const int64_t n0 = edge_begin == 0 ? 0 : int64_t(pm[edge_begin - 1]) + 1;
+    const int64_t n1 = edge_end == 0 ? 0 : int64_t(pm[edge_end - 1]) + 1;
+    launch_continuity_edge_range(ls->stream, n0, std::max(n0, n1), edge_begin, edge_end, ls->edges.p, *f, *o,
+                                 ls->buf.p, ls->nodebuf.p);
+    NW_CUDA(cudaGetLastError());
+    ls->cont_next = edge_end;
+  });
+}
+
+nw_status nw_assemble_continuity_rows(nw_linsys* ls) {
+  return guard([&] {
+    need_finalized(ls);
+    if (ls->num_dof != 1) fail(NW_INVALID_ARG, "continuity assembly needs num_dof 1");
+    if (ls->cont_next != ls->g.num_edges)
+      fail(NW_INVALID_ARG, "continuity edge ranges do not cover every edge");
+    continuity_rows(ls);
+    ls->cont_next = -1;
   });
 }
 

@@ -213,3 +213,132 @@ def test_momentum_row_ranges_pipeline_with_edge_ranges(nw):
     v2, rh2 = ls.to_host()
     np.testing.assert_array_equal(v2[cut:], v_ref[cut:])
     np.testing.assert_allclose(v2[:cut], 2 * v_ref[:cut], rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("general", [False, True])
+def test_continuity_edge_ranges_equal_the_one_call_assembly(nw, general):
+    """Continuity edge ranges in order from edge 0, then the row phase, as
+    the streamed end-to-end step runs them: bit for bit the one-call
+    assembly, on the node pre-pass route (the reference's default options)
+    and on the general one (interpolated velocity blend, incompressible
+    density scaling). Ranges out of order, and a row phase before the
+    ranges cover every edge, are refused."""
+    case = nw.workload.lowmach_case(20, 16, 12, seed=4)
+    mesh = case.mesh
+    nd = case.node
+    host = dict(coords=mesh.coords, velocity=nd["velocity"], dpdx=nd["dpdx"], density=nd["density"],
+                pressure=nd["pressure"], udiag=nd["udiag"], area=mesh.area)
+    d = {k: dev(v) for k, v in host.items()}
+    fc = nw.ContinuityFields(*(d[k].data_ptr() for k in ("coords", "velocity", "dpdx", "density", "pressure",
+                                                        "udiag", "area")))
+    co = case.opts["continuity"]
+    if general:
+        co = nw.ContinuityOpts(**{k: getattr(co, k) for k, _ in co._fields_})
+        co.interp_together = 0.5
+        co.solve_incompressible = 1.0
+    N, E = mesh.num_nodes, mesh.num_edges
+
+    def fresh():
+        ls = nw.LinearSystem(1)
+        ls.build_edge_graph(N, mesh.edges)
+        ls.finalize()
+        ls.zero_system()
+        return ls
+
+    ref = fresh()
+    ref.assemble_continuity(fc, co)
+    v_ref, r_ref = ref.to_host()
+    ls = fresh()
+    bounds = [0, 0, 1000, 2500, 2500, 4000, E]
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        ls.assemble_continuity_range(fc, co, a, b)
+    ls.assemble_continuity_rows()
+    v, rh = ls.to_host()
+    assert np.array_equal(v, v_ref) and np.array_equal(rh, r_ref)
+    # a second assembly on the same handle: ranges restart at edge 0
+    ls.zero_system()
+    for a, b in ((0, E // 2), (E // 2, E)):
+        ls.assemble_continuity_range(fc, co, a, b)
+    ls.assemble_continuity_rows()
+    v, rh = ls.to_host()
+    assert np.array_equal(v, v_ref) and np.array_equal(rh, r_ref)
+    # refused: a gap, a range past the end, rows before every edge is done,
+    # rows twice without new ranges
+    ls = fresh()
+    ls.assemble_continuity_range(fc, co, 0, 1000)
+    with pytest.raises(nw.NwError, match="follow each other"):
+        ls.assemble_continuity_range(fc, co, 1500, 2000)
+    with pytest.raises(nw.NwError, match="out of bounds"):
+        ls.assemble_continuity_range(fc, co, 1000, E + 1)
+    with pytest.raises(nw.NwError, match="cover every edge"):
+        ls.assemble_continuity_rows()
+    ls.assemble_continuity_range(fc, co, 1000, E)
+    ls.assemble_continuity_rows()
+    with pytest.raises(nw.NwError, match="cover every edge"):
+        ls.assemble_continuity_rows()
+
+
+def test_streamed_step_reads_only_the_node_fields_it_has(nw):
+    """The streamed end-to-end step: node fields arrive in index order, a
+    slice ahead of each edge chunk (up to the largest node index of the
+    edges so far); the rest of every node field is NaN until its slice
+    lands. Momentum and continuity edge ranges, momentum row ranges and the
+    continuity row phase then give the one-call assemblies bit for bit: no
+    range reads a node field it was not given."""
+    import torch
+    case = nw.workload.lowmach_case(20, 16, 12, seed=6)
+    mesh = case.mesh
+    nd = case.node
+    host = dict(coords=mesh.coords, velocity=nd["velocity"], dudx=nd["dudx"], viscosity=nd["viscosity"],
+                density=nd["density"], mask=nd["mask"], pressure=nd["pressure"], dpdx=nd["dpdx"],
+                udiag=nd["udiag"], area=mesh.area, mdot=case.edge["mdot"], pecfac=case.edge["pecfac"])
+    N, E = mesh.num_nodes, mesh.num_edges
+    edge_keys = ("area", "mdot", "pecfac")
+    full = {k: dev(v) for k, v in host.items()}
+    part = {k: (v.clone() if k in edge_keys else torch.full_like(v, float("nan"))) for k, v in full.items()}
+    mo, co = case.opts["momentum"], case.opts["continuity"]
+
+    def fields(d):
+        fm = nw.MomentumFields(*(d[k].data_ptr() for k in (
+            "coords", "velocity", "dudx", "viscosity", "density", "mask", "area", "mdot", "pecfac")))
+        fc = nw.ContinuityFields(*(d[k].data_ptr() for k in (
+            "coords", "velocity", "dpdx", "density", "pressure", "udiag", "area")))
+        return fm, fc
+
+    def fresh(ndof):
+        ls = nw.LinearSystem(ndof)
+        ls.build_edge_graph(N, mesh.edges)
+        ls.finalize()
+        ls.zero_system()
+        return ls
+
+    fm, fc = fields(full)
+    rm, rc = fresh(3), fresh(1)
+    rm.assemble_momentum(fm, mo)
+    rc.assemble_continuity(fc, co)
+    vm_ref, bm_ref = rm.to_host()
+    vc_ref, bc_ref = rc.to_host()
+    fm, fc = fields(part)
+    lsm, lsc = fresh(3), fresh(1)
+    reach = np.maximum.accumulate(mesh.edges.max(axis=1)) + 1  # nodes needed by edges 0..e
+    maxinc = np.full(N, -1)
+    np.maximum.at(maxinc, mesh.edges[:, 0], np.arange(E))
+    np.maximum.at(maxinc, mesh.edges[:, 1], np.arange(E))
+    bounds = [0, 700, 1900, 3100, 4400, E]
+    have = done = 0
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        need = int(reach[b - 1])
+        for k in host:
+            if k not in edge_keys:
+                part[k][have:need] = full[k][have:need]
+        have = need
+        lsm.assemble_momentum_range(fm, mo, a, b)
+        r = int(np.searchsorted(np.maximum.accumulate(maxinc), b)) if b < E else N
+        lsm.assemble_momentum_rows_range(mo, done, r)
+        done = r
+        lsc.assemble_continuity_range(fc, co, a, b)
+    lsc.assemble_continuity_rows()
+    vm, bm = lsm.to_host()
+    vc, bc = lsc.to_host()
+    assert np.array_equal(vm, vm_ref) and np.array_equal(bm, bm_ref)
+    assert np.array_equal(vc, vc_ref) and np.array_equal(bc, bc_ref)
