@@ -87,6 +87,11 @@ struct nw_linsys {
   std::vector<double> history;
   nw_solve_report last_report{};  // of the last solve (checkpointed)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // solves of a handle on the legacy default stream run on this stream
+  // (non-blocking, joined to the caller's stream by events), because the
+  // legacy stream cannot be captured into the solver's CUDA graphs
+  cudaStream_t solve_stream = nullptr;
+  cudaEvent_t solve_in = nullptr, solve_out = nullptr;
   bool timed = false;
   nw_learned* learned = nullptr;
   std::unique_ptr<CoarseLevel> coarse;
@@ -222,6 +227,9 @@ nw_status nw_linsys_destroy(nw_linsys* ls) {
     if (!ls) return;
     if (ls->ev0) cudaEventDestroy(ls->ev0);
     if (ls->ev1) cudaEventDestroy(ls->ev1);
+    if (ls->solve_in) cudaEventDestroy(ls->solve_in);
+    if (ls->solve_out) cudaEventDestroy(ls->solve_out);
+    if (ls->solve_stream) cudaStreamDestroy(ls->solve_stream);
     delete ls;
   });
 }
@@ -831,8 +839,35 @@ nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
     // the timed solve includes the per-solve refresh of the solver's copies
     // of the values (diagonal, sliced layouts, coarse Galerkin operator)
     NW_CUDA(cudaEventRecord(a, ls->stream));
-    ls->solver.refresh(ls->stream);
-    SolveResult r = ls->solver.solve(ls->cfg, tol, ls->pc, ls->rhs.p, x, ls->stream);
+    cudaStream_t s = ls->stream;
+    const bool legacy = s == nullptr || s == cudaStreamLegacy;
+    if (legacy) {
+      if (!ls->solve_stream) {
+        NW_CUDA(cudaStreamCreateWithFlags(&ls->solve_stream, cudaStreamNonBlocking));
+        NW_CUDA(cudaEventCreateWithFlags(&ls->solve_in, cudaEventDisableTiming));
+        NW_CUDA(cudaEventCreateWithFlags(&ls->solve_out, cudaEventDisableTiming));
+      }
+      NW_CUDA(cudaEventRecord(ls->solve_in, ls->stream));
+      NW_CUDA(cudaStreamWaitEvent(ls->solve_stream, ls->solve_in, 0));
+      s = ls->solve_stream;
+    }
+    SolveResult r;
+    try {
+      ls->solver.refresh(s);
+      r = ls->solver.solve(ls->cfg, tol, ls->pc, ls->rhs.p, x, s);
+    } catch (...) {
+      if (legacy) {  // later work on the caller's stream still follows the solve's
+        cudaEventRecord(ls->solve_out, s);
+        cudaStreamWaitEvent(ls->stream, ls->solve_out, 0);
+      }
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      throw;
+    }
+    if (legacy) {
+      NW_CUDA(cudaEventRecord(ls->solve_out, s));
+      NW_CUDA(cudaStreamWaitEvent(ls->stream, ls->solve_out, 0));
+    }
     NW_CUDA(cudaEventRecord(b, ls->stream));
     NW_CUDA(cudaEventSynchronize(b));
     float ms = 0.f;
