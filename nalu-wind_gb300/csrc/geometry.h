@@ -113,49 +113,50 @@ NW_HD void hex_geometry(const double c[8][3], double scs[12][3], double scv[8]) 
 
 // Tet4 sub-control geometry (TetSCS::determinant_scs / TetSCV::
 // determinant_scv, src/master_element/Tet4CVFEM.C:243-360, 522-620).
+//
+// Sub-control surfaces: each is the quadrilateral (edge midpoint, face
+// centroid, element centroid, face centroid) of one edge, and its vector
+// area is half the cross product of its diagonals (quad_area). Both
+// diagonals are fixed combinations of the edge vectors e_k = c_k - c_0 (one
+// runs from a midpoint or face centroid to the centroid or a face centroid:
+// (e_a + e_b - e_c) / 4 or e_k / 3 and the like), so every area is a
+// small-integer combination of the three cross products X = e1 x e2,
+// Y = e2 x e3, Z = e3 x e1, divided by 24. For the facets of edges
+// 0-1, 1-2, 2-0, 0-3, 1-3, 2-3 (the reference's ordering of TetSCS's
+// integration points): X + 2Y + Z, Z - Y, X + Y + 2Z, 2X + Y + Z, X - Y,
+// X - Z. Equal to the reference's four-triangle fans in exact arithmetic,
+// with three cross products instead of twenty-four.
 NW_HD void tet_geometry(const double c[4][3], double scs[6][3], double scv[4]) {
-  double p[15][3];
-  for (int j = 0; j < 4; ++j)
-    for (int d = 0; d < 3; ++d) p[j][d] = c[j][d];
-  const double h = 0.5, t = 1.0 / 3.0;
-  for (int d = 0; d < 3; ++d) {
-    p[4][d] = h * (c[0][d] + c[1][d]);
-    p[5][d] = h * (c[1][d] + c[2][d]);
-    p[6][d] = h * (c[2][d] + c[0][d]);
-    p[7][d] = t * (c[0][d] + c[1][d] + c[2][d]);
-    p[8][d] = h * (c[2][d] + c[3][d]);
-    p[9][d] = h * (c[3][d] + c[1][d]);
-    p[10][d] = t * (c[1][d] + c[2][d] + c[3][d]);
-    p[11][d] = h * (c[0][d] + c[3][d]);
-    p[12][d] = t * (c[0][d] + c[2][d] + c[3][d]);
-    p[13][d] = t * (c[0][d] + c[1][d] + c[3][d]);
-    p[14][d] = 0.0;
-    for (int j = 0; j < 4; ++j) p[14][d] += 0.25 * c[j][d];
-  }
-  const int facet[6][4] = {{4, 7, 14, 13},  {7, 14, 10, 5},
-                                  {6, 12, 14, 7},  {11, 13, 14, 12},
-                                  {13, 9, 10, 14}, {10, 8, 12, 14}};
-  for (int ip = 0; ip < 6; ++ip) {
-    double q[4][3];
-    for (int k = 0; k < 4; ++k)
-      for (int d = 0; d < 3; ++d) q[k][d] = p[facet[ip][k]][d];
-    quad_area(q, scs[ip]);
-  }
-  // The four sub-control volumes of a linear tet (node, three edge
-  // midpoints, three face centroids, centroid) are its barycentric
-  // subdivision: equal quarters of the tet's volume (true for a regular
-  // tet by symmetry, and volume ratios are affine invariants). TetSCV
-  // evaluates each with Grandy's hexahedron formula, equal in exact
-  // arithmetic; the signed volume here is taken from edge vectors of node
-  // 0, which also avoids that formula's cancellation far from the origin.
   double e1[3], e2[3], e3[3];
   for (int d = 0; d < 3; ++d) {
     e1[d] = c[1][d] - c[0][d];
     e2[d] = c[2][d] - c[0][d];
     e3[d] = c[3][d] - c[0][d];
   }
-  const double det = (e1[1] * e2[2] - e1[2] * e2[1]) * e3[0] + (e1[2] * e2[0] - e1[0] * e2[2]) * e3[1] +
-                     (e1[0] * e2[1] - e1[1] * e2[0]) * e3[2];
+  const double X[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                       e1[0] * e2[1] - e1[1] * e2[0]};
+  const double Y[3] = {e2[1] * e3[2] - e2[2] * e3[1], e2[2] * e3[0] - e2[0] * e3[2],
+                       e2[0] * e3[1] - e2[1] * e3[0]};
+  const double Z[3] = {e3[1] * e1[2] - e3[2] * e1[1], e3[2] * e1[0] - e3[0] * e1[2],
+                       e3[0] * e1[1] - e3[1] * e1[0]};
+  const double k = 1.0 / 24.0;
+  for (int d = 0; d < 3; ++d) {
+    scs[0][d] = k * (X[d] + 2.0 * Y[d] + Z[d]);
+    scs[1][d] = k * (Z[d] - Y[d]);
+    scs[2][d] = k * (X[d] + Y[d] + 2.0 * Z[d]);
+    scs[3][d] = k * (2.0 * X[d] + Y[d] + Z[d]);
+    scs[4][d] = k * (X[d] - Y[d]);
+    scs[5][d] = k * (X[d] - Z[d]);
+  }
+  // The four sub-control volumes of a linear tet (node, three edge
+  // midpoints, three face centroids, centroid) are its barycentric
+  // subdivision: equal quarters of the tet's volume (true for a regular
+  // tet by symmetry, and volume ratios are affine invariants). TetSCV
+  // evaluates each with Grandy's hexahedron formula, equal in exact
+  // arithmetic; the signed volume here, (e1 x e2) . e3 / 6, is taken from
+  // the edge vectors, which also avoids that formula's cancellation far
+  // from the origin.
+  const double det = X[0] * e3[0] + X[1] * e3[1] + X[2] * e3[2];
   const double quarter = det / 24.0;
   for (int ip = 0; ip < 4; ++ip) scv[ip] = quarter;
 }

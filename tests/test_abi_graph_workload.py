@@ -254,7 +254,8 @@ def test_rcm_order_restores_locality(nw):
 @pytest.mark.parametrize("renumber", [0, 2])
 def test_tet_geometry_vs_oracle(nw, orc, renumber):
     """The generator's (and the GPU's) Tet4 geometry: sub-control-surface
-    area vectors as half the cross product of the quad diagonals and the
+    area vectors as small-integer combinations of the three edge-vector
+    cross products (half the cross product of each quad's diagonals) and the
     sub-control volumes as quarters of the tet volume, against the oracle's
     restatement of TetSCS (triangle fans) and TetSCV (Grandy's formula)."""
     m = nw.Mesh(6, 5, 4, stretch_z=1.2, jitter=0.2, seed=4, tets=True, renumber=renumber, renumber_seed=3)
