@@ -301,6 +301,10 @@ def run_ours(args, rank, world):
     # copies.)
     copy_s = torch.cuda.Stream()
     d2h_s = torch.cuda.Stream()
+    # the continuity system assembles on its own stream, beside the momentum
+    # kernels of the same chunk
+    con_s = torch.cuda.Stream()
+    lsc.set_stream(con_s.cuda_stream)
     edge_keys = ("area", "mdot", "pecfac")
     node_keys = [k for k in pinned if k not in edge_keys]
     n_chunks = 8
@@ -327,11 +331,14 @@ def run_ours(args, rank, world):
                 ev.record(copy_s)
                 chunk_ev.append(ev)
         lsm.zero_system()
+        con_s.wait_stream(stream)
         lsc.zero_system()
         done = 0
         for (a, b), ev, r in zip(zip(bounds[:-1], bounds[1:]), chunk_ev, row_ready):
             stream.wait_event(ev)
+            con_s.wait_event(ev)
             lsm.assemble_momentum_range(fm, mo, a, b)
+            lsc.assemble_continuity_range(fc, co, a, b)
             if r > done:
                 lsm.assemble_momentum_rows_range(mo, done, r)
                 ev_mr = torch.cuda.Event()
@@ -340,10 +347,9 @@ def run_ours(args, rank, world):
                 cudart_copy(rhs_m_host.data_ptr() + 24 * done, rm_dev + 24 * done, 24 * (r - done),
                             d2h_s.cuda_stream)
                 done = r
-            lsc.assemble_continuity_range(fc, co, a, b)
         lsc.assemble_continuity_rows()
         ev_cr = torch.cuda.Event()
-        ev_cr.record(stream)
+        ev_cr.record(con_s)
         d2h_s.wait_event(ev_cr)
         cudart_copy(rhs_c_host.data_ptr(), rc_dev, rhs_c_host.numel() * 8, d2h_s.cuda_stream)
         stream.wait_stream(d2h_s)
