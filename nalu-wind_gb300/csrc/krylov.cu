@@ -487,6 +487,8 @@ __global__ void scale_jacobi_k(int64_t n, const T* __restrict__ w,
   if (rd) z[i] = vi * rd[i];
 }
 
+constexpr int kGsBatch = 8;
+
 // One colour class of the Gauss-Seidel sweep over the class-ordered sliced
 // copy (off-diagonal entries only, same column order as the CSR row):
 //   y_i = (x_i - sum_{j != i} a_ij y_j) / a_ii
@@ -505,9 +507,24 @@ __global__ void __launch_bounds__(kBlock)
   if (!first) {
     const int64_t base = off[k >> 5] + (k & 31);
     const int n = len[k];
-    for (int q = 0; q < n; ++q) {
-      const int64_t p = base + 32 * int64_t(q);
-      s = fma(-T(v[p]), y[cols[p]], s);
+    // batches of kGsBatch entries: every column and value load of the batch
+    // first, then every y gather, then the multiply-adds in column order
+    // (the same sum as one entry at a time, with the loads in flight
+    // together instead of one dependent pair per entry)
+    for (int q = 0; q < n; q += kGsBatch) {
+      int32_t c[kGsBatch];
+      T a[kGsBatch], yv[kGsBatch];
+#pragma unroll
+      for (int j = 0; j < kGsBatch; ++j) {
+        const int64_t p = base + 32 * int64_t(q + j);
+        c[j] = q + j < n ? cols[p] : i;
+        a[j] = q + j < n ? T(v[p]) : T(0);
+      }
+#pragma unroll
+      for (int j = 0; j < kGsBatch; ++j) yv[j] = q + j < n ? y[c[j]] : T(0);
+#pragma unroll
+      for (int j = 0; j < kGsBatch; ++j)
+        if (q + j < n) s = fma(-a[j], yv[j], s);
     }
   }
   y[i] = s * rd[i];
@@ -526,9 +543,20 @@ __global__ void __launch_bounds__(kBlock)
   float s = fmaf(-diag[i], y[i], x[i]);
   const int64_t base = off[k >> 5] + (k & 31);
   const int n = len[k];
-  for (int q = 0; q < n; ++q) {
-    const int64_t p = base + 32 * int64_t(q);
-    s = fmaf(-v[p], y[cols[p]], s);
+  for (int q = 0; q < n; q += kGsBatch) {  // batched loads as in gs_sell_k
+    int32_t c[kGsBatch];
+    float a[kGsBatch], yv[kGsBatch];
+#pragma unroll
+    for (int j = 0; j < kGsBatch; ++j) {
+      const int64_t p = base + 32 * int64_t(q + j);
+      c[j] = q + j < n ? cols[p] : i;
+      a[j] = q + j < n ? v[p] : 0.f;
+    }
+#pragma unroll
+    for (int j = 0; j < kGsBatch; ++j) yv[j] = q + j < n ? y[c[j]] : 0.f;
+#pragma unroll
+    for (int j = 0; j < kGsBatch; ++j)
+      if (q + j < n) s = fmaf(-a[j], yv[j], s);
   }
   r[i] = s;
 }
