@@ -363,7 +363,12 @@ nw_status nw_linsys_copy_from_host(nw_linsys* ls, const double* values,
 
 /* ---- solve: LinearSystem::solve (src/TpetraLinearSystem.C:1811-1881) ->
  * TpetraLinearSolver::solve (src/LinearSolver.C:209-254). x (device, nrows)
- * receives the solution from x0 = 0; final_iter selects final_tolerance. */
+ * receives the solution from x0 = 0; final_iter selects final_tolerance.
+ * Returns when the solve is done (the report needs its results). The mixed
+ * methods launch their inner iterations as CUDA graphs captured on the
+ * handle's stream; on the legacy default stream, which cannot be captured,
+ * the solve runs on a stream of the handle's own, ordered after earlier
+ * work on the caller's stream and before later work by events. */
 nw_status nw_linsys_solve(nw_linsys* ls, double* x, int final_iter,
                           nw_solve_report* rep);
 /* Residual history of the last solve (relative, first entry 1). */
