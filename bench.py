@@ -864,7 +864,7 @@ def oracle_inputs(shape):
 
 def run_reference(args, rank, world):
     """The restated reference path (CPU oracle, OpenMP on all host cores) on
-    the same workload, with the driver's --steps and --warmup: each step is
+    the same workload, with the --steps and --warmup it is given: each step is
     one full momentum + continuity assembly."""
     if rank != 0:
         return None

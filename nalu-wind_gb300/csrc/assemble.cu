@@ -785,8 +785,8 @@ __global__ void __launch_bounds__(kFusedChunk, 4)
   int next = 0;
   if (threadIdx.x == 0) next = atomicAdd(f.ticket, 1);
   for (int p = 0;; p ^= 1) {
-    // double-buffered item word: the barrier of the next round separates
-    // this round's reads from the write two rounds on
+    // double-buffered item word: the barrier of the next item separates
+    // this item's reads from the write two items on
     if (threadIdx.x == 0) s_item[p] = (next < f.nitems && ld_volatile(f.err) == 0) ? f.items[next] : -1;
     __syncthreads();
     const int it = s_item[p];
